@@ -1,0 +1,1 @@
+/* empty stand-in: nothing from this OpenCV header is used on the CPU path */
