@@ -1,0 +1,346 @@
+"""Benchmark of the DPM detection path (one JSON line on rank 0).
+
+Workload (default): DPM car + person models together on one synthetic
+1280x720 frame, FP32 GPU drop-in (the plain path whose results match the
+reference CPU path bit for bit).  A step is one frame through the whole path:
+resize pyramid, HOG pyramid, root/part convolution, distance transforms,
+score assembly and boxes, accumulated score map, NMS and box regression, for
+both models.
+
+  value  frames/s with the frame already in device memory (geye_detect_device),
+         CUDA events on the library's stream around each step, L2 flushed
+         between steps (a 256 MiB write outside the timed events).
+  e2e    frames/s through the C ABI a caller uses (geye_detect_multi) with host
+         buffers: frame + A_SCORE maps copied in, results + A_SCORE maps copied
+         out inside the timed region; p50/p99 per-frame latency from the same calls.
+  roofline  the dominant kernel (the convolution) from live CUDA events.
+  cpu_baseline  the CPU oracle (this project's restatement of the reference's
+         CPU path) timed on this host's cores on one frame of the same workload.
+
+--impl reference times the CPU oracle alone (all host threads) on the same
+workload and prints the reference arm's line.  Synthetic data: seeded frames
+and random-init models in the reference's CSV format (no dataset is needed).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOADS = {
+    "car+person_1280x720_fp32": dict(w=1280, h=720, models=("car", "person"), conv="fp32"),
+    "car+person_640x480_fp32": dict(w=640, h=480, models=("car", "person"), conv="fp32"),
+    "car_640x480_fp32": dict(w=640, h=480, models=("car",), conv="fp32"),
+}
+DEFAULT_WORKLOAD = "car+person_1280x720_fp32"
+
+
+def _peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return d.get("hbm_gbs", 6800.0), d.get("bf16_tflops", 1897.9), d.get("bf16_tflops_sustained", 1687.2), "measured"
+    return 6800.0, 1900.0, 1700.0, "fallback"
+
+
+def _traffic(kernel_key: str):
+    """Per-launch DRAM bytes of a kernel from a committed ncu summary, if any."""
+    p = os.path.join(ROOT, "profiles", "traffic_per_launch.txt")
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        parts = line.split()
+        if len(parts) >= 2 and parts[0] == kernel_key:
+            try:
+                return float(parts[1])
+            except ValueError:
+                return None
+    return None
+
+
+class ClockSampler:
+    """Samples nvidia-smi clocks and throttle reasons while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def _write_models(spec_names, d):
+    from geye_gb300 import synth
+    specs = {"car": synth.CAR_SPEC, "person": synth.PERSON_SPEC}
+    return [synth.write_model_csv(specs[n], d) for n in spec_names]
+
+
+def cpu_oracle_frames_per_sec(wl, paths, frame, nthreads, n_frames=1):
+    from oracle import oracle as O
+    models = [O.Model(*p) for p in paths]
+    t0 = time.perf_counter()
+    for _ in range(n_frames):
+        for m in models:
+            m.m.ini = 1
+            a = np.full((wl["w"], wl["h"]), -100, np.float32)
+            O.car_detection(m, frame, -0.5, 0.5, a_score=a, nthreads=nthreads)
+    dt = time.perf_counter() - t0
+    return n_frames / dt, dt
+
+
+def dist_info():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def run_reference(args, wl):
+    rank, world, _ = dist_info()
+    if rank != 0:
+        return 0
+    from geye_gb300 import synth
+    from oracle import oracle as O
+    O.build()
+    nthreads = os.cpu_count() or 1
+    with tempfile.TemporaryDirectory() as d:
+        paths = _write_models(wl["models"], d)
+        frame = synth.make_frame(wl["w"], wl["h"], seed=0)
+        for _ in range(args.warmup):
+            cpu_oracle_frames_per_sec(wl, paths, frame, nthreads)
+        times = []
+        for _ in range(args.steps):
+            _, dt = cpu_oracle_frames_per_sec(wl, paths, frame, nthreads)
+            times.append(dt)
+    fps = len(times) / sum(times)
+    line = {
+        "impl": "reference", "metric": "frames_per_sec", "value": fps, "unit": "frames/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * sum(times) / len(times),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": args.workload, "frame": f"{wl['w']}x{wl['h']}", "models": list(wl["models"]),
+                   "thresh": -0.5, "overlap": 0.5},
+        "p50_ms": 1000.0 * float(np.percentile(times, 50)), "p99_ms": 1000.0 * float(np.percentile(times, 99)),
+        "cpu_baseline": {"value": fps, "unit": "frames/s", "cores": nthreads, "kind": "port",
+                         "sample": f"{args.steps} frames of the workload, one at a time"},
+        "e2e": {"value": fps, "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_gpu(args, wl):
+    import torch
+    rank, world, local = dist_info()
+    dev = local if world > 1 else 0
+    torch.cuda.set_device(dev)
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+        pg = dist
+
+    import geye_gb300 as g
+    from geye_gb300 import synth
+
+    stream = torch.cuda.Stream(device=dev)
+    ctx = g.Context(dev, stream=stream.cuda_stream, conv=g.CONV_BF16 if wl["conv"] == "bf16" else g.CONV_FP32)
+    tmp = tempfile.TemporaryDirectory()
+    paths = _write_models(wl["models"], tmp.name)
+    models = [g.Model(ctx, *p) for p in paths]
+    W, H = wl["w"], wl["h"]
+    frame = synth.make_frame(W, H, seed=rank)
+    d_frame = torch.from_numpy(frame).to(f"cuda:{dev}")
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{dev}")
+
+    def dev_step():
+        ctx.detect_device(d_frame.data_ptr(), W, H, models)
+
+    torch.cuda.synchronize()
+    # warm-up (plan build, attribute setup)
+    for _ in range(max(args.warmup, 3)):
+        dev_step()
+        ctx.synchronize()
+    # ---- device-resident timed region
+    ctx.enable_timing(True)
+    stage_acc = {}
+    conv_ms, total_ms = [], []
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    if pg:
+        pg.barrier()
+    torch.cuda.synchronize()
+    launches = 0
+    with ClockSampler(dev) as clk:
+        for i in range(args.steps):
+            with torch.cuda.stream(stream):
+                flush.fill_(float(i))
+                ev[i][0].record(stream)
+            dev_step()
+            with torch.cuda.stream(stream):
+                ev[i][1].record(stream)
+            st = ctx.stage_times()
+            launches += st["launches"]
+            for k, v in st["ms"].items():
+                stage_acc.setdefault(k, []).append(v)
+        torch.cuda.synchronize()
+    if pg:
+        pg.barrier()
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    t_total = sum(step_ms) / 1000.0
+    if pg:
+        t = torch.tensor([t_total], dtype=torch.float64)
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        t_total = float(t.item())
+    value = world * args.steps / t_total
+    st_last = ctx.stage_times()
+    ctx.enable_timing(False)
+
+    # ---- end-to-end through the C ABI with host buffers
+    a_scores = [np.full((W, H), -100, np.float32) for _ in models]
+    for _ in range(max(args.warmup, 3)):
+        for a in a_scores:
+            a.fill(-100)
+        ctx.detect_multi(frame, models, -0.5, 0.5, a_scores)
+    e2e_ms = []
+    kept = None
+    for i in range(args.steps):
+        for a in a_scores:
+            a.fill(-100)
+        t0 = time.perf_counter()
+        kept = ctx.detect_multi(frame, models, -0.5, 0.5, a_scores)
+        e2e_ms.append(1000.0 * (time.perf_counter() - t0))
+    e2e_t = sum(e2e_ms) / 1000.0
+    if pg:
+        t = torch.tensor([e2e_t], dtype=torch.float64)
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        e2e_t = float(t.item())
+    e2e_fps = world * args.steps / e2e_t
+    h2d = frame.nbytes + sum(a.nbytes for a in a_scores)
+    d2h = sum(a.nbytes for a in a_scores) + sum(k["num"] * (4 * 4 + 4 * 4 + 4 + 4 + 4) + 8 for k in kept)
+
+    # ---- roofline of the dominant kernel
+    hbm, bf16, bf16s, peak_src = _peaks()
+    conv_med_ms = statistics.median(stage_acc["conv"])
+    conv_flops = st_last["conv_flops"]
+    achieved_tflops = conv_flops / (conv_med_ms / 1000.0) / 1e12
+    traffic = _traffic("conv_fp32" if wl["conv"] == "fp32" else "conv_bf16")
+    roofline = {"kernel": "conv (root + part filters, k_conv_fp32)" if wl["conv"] == "fp32" else "conv (tcgen05)",
+                "bound": "tensor", "achieved": achieved_tflops, "peak": bf16, "unit": "TFLOP/s",
+                "frac": achieved_tflops / bf16, "traffic": traffic,
+                "note": (f"peak = dense bf16 tensor ({peak_src}); the FP32 drop-in runs this contraction on the "
+                         "FP32 CUDA cores in the reference's summation order"),
+                "flops_per_launch": conv_flops, "ms_per_launch": conv_med_ms}
+    stages = {k: statistics.median(v) for k, v in stage_acc.items()}
+    bytes_ = st_last["bytes"]
+    stage_gbs = {k: (bytes_[k] / (stages[k] / 1000.0) / 1e9 if stages.get(k) and bytes_.get(k) else None)
+                 for k in ("pyramid", "hog", "dt", "score")}
+
+    # ---- CPU baseline (rank 0, N=1 only)
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        from oracle import oracle as O
+        O.build()
+        nthreads = os.cpu_count() or 1
+        fps_cpu, dt = cpu_oracle_frames_per_sec(wl, paths, frame, nthreads, n_frames=1)
+        cpu = {"value": fps_cpu, "unit": "frames/s", "cores": nthreads, "kind": "port",
+               "sample": f"1 frame of the workload ({dt:.2f} s wall, both models, oracle with {nthreads} threads)"}
+
+    clocks = clk.summary()
+    if rank == 0:
+        line = {
+            "metric": "frames_per_sec", "value": value, "unit": "frames/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1000.0 * t_total / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": args.workload, "frame": f"{W}x{H}", "models": list(wl["models"]),
+                       "conv": wl["conv"], "thresh": -0.5, "overlap": 0.5, "parallelism": f"replicas{world}",
+                       "l2": "flushed between steps (256 MiB write, outside the timed events)"},
+            "p50_ms": float(np.percentile(e2e_ms, 50)), "p99_ms": float(np.percentile(e2e_ms, 99)),
+            "e2e": {"value": e2e_fps, "unit": "frames/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                    "p50_ms": float(np.percentile(e2e_ms, 50)), "p99_ms": float(np.percentile(e2e_ms, 99))},
+            "gpu_launches": int(launches),
+            "stage_ms": stages, "stage_gbs": stage_gbs,
+            "roofline": roofline,
+            "cpu_baseline": cpu,
+            "clocks": clocks,
+            "detections_kept": [k["num"] for k in kept],
+        }
+        print(json.dumps(line), flush=True)
+    for m in models:
+        m.close()
+    ctx.close()
+    if pg:
+        pg.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="geye", choices=["geye", "reference"])
+    ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS))
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    wl = WORKLOADS[args.workload]
+    if args.impl == "reference":
+        return run_reference(args, wl)
+    return run_gpu(args, wl)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

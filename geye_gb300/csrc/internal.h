@@ -1,0 +1,159 @@
+// internal.h -- shared declarations of libgeye_dpm (host runtime + kernels).
+//
+// Device layouts (all spatial maps column-major like the reference, so a
+// level's stage output is a plain copy):
+//   image level l:   3 float planes [c][w][h]                (x*h + y)
+//   feature level l: [pos][32] float, pos = x*fs0 + y, channel 31 = 0
+//   conv/DT/score maps: [x][y] float (int for argmax), per (level, filter)
+// Every per-frame buffer lives in one arena sized when a plan is built.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "geye_dpm.h"
+
+namespace geye {
+
+constexpr int kFeat = 31;       // HOG channels
+constexpr int kFeatPad = 32;    // channel stride in device feature buffers
+constexpr int kMaxParts = 32;   // parts per component supported by the kernels
+
+// ----------------------------------------------------------------------------
+// job descriptors (device-readable, plain structs)
+// ----------------------------------------------------------------------------
+struct ResizeJob {         // one 1-D resize pass of one level
+  int src_off;             // float offset of the source planes
+  int dst_off;             // float offset of the destination planes
+  int src_h, src_w;        // source dims (rows, cols)
+  int dst_h, dst_w;        // destination dims of this pass
+  int tap_start_off;       // int offset of tap_start[dst_len + 1] in the tap-index table
+  int tap_off;             // offset of the tap (si, alpha) arrays
+};
+
+struct HogJob {
+  int img_off;             // image planes [3][w][h]
+  int h, w;                // image dims
+  int sbin;
+  int b0, b1;              // histogram blocks (rows, cols)
+  int hist_off;            // [18][b1*b0] then norm [b1*b0] at hist_off + 18*b1*b0
+  int fs0, fs1;            // output cells
+  int feat_off;            // [pos][32] float
+  int feat16_off;          // [pos][32] bf16 (element offset), -1 = not written
+};
+
+struct ConvJob {           // a block of outputs of one (level, filter group)
+  int feat_off, a0, a1;    // feature level [pos][32], dims
+  int filt_base;           // first filter index in the model's filter table
+  int n_filt;              // filters in the group (same size)
+  int b0, b1;              // filter dims
+  int c0, c1;              // output dims
+  int out_off;             // output of filter g at out_off + g*c0*c1
+  int tiles_y, tiles_x;    // output tiles of this job
+};
+
+struct DtJob {             // one part map: DT of the negated map
+  int in_off;              // part conv map (negated on load)
+  int d0, d1;
+  int tmpM_off, tmpI_off;  // pass-1 outputs
+  int M_off, Ix_off, Iy_off;
+  float ax, bx, ay, by;
+  int negate;              // 1: run on -map (inverse_Q of the pipeline); 0: plain dt()
+};
+
+struct ScoreJob {          // one (level, component) score map
+  int root_off;            // root conv map
+  int r0, r1;
+  float off;               // offw[ridx[c]]
+  int score_off;           // output score map
+  int np;
+  int comp;
+  float scale;             // sbin / scales[level]
+  int rsize0, rsize1;      // component root size (boxes, A_SCORE)
+  int RY, RX;              // A_SCORE shifts
+  int box_base;            // cumulative count base filled by the scan (device)
+  int part_M[kMaxParts];   // DT outputs per part (M); Ix/Iy at M + ix_delta/iy_delta
+  int part_Ix[kMaxParts];
+  int part_Iy[kMaxParts];
+  int part_d0[kMaxParts];
+  int part_d1[kMaxParts];
+  int ax[kMaxParts];       // anchor+1
+  int ay[kMaxParts];
+  int psize0[kMaxParts];   // part box size (component file)
+  int psize1[kMaxParts];
+};
+
+// ----------------------------------------------------------------------------
+// host model
+// ----------------------------------------------------------------------------
+struct HostModel {
+  int numcomponent = 0, sbin = 0, interval = 0, max_X = 0, max_Y = 0, padx = 0, pady = 0;
+  float ratio = 1.0f;
+  std::vector<int> ridx, oidx, rsize, numpart;
+  std::vector<float> offw;
+  std::vector<std::vector<int>> pidx, didx, psize;
+  int DefL = 0;
+  std::vector<float> def;
+  std::vector<int> anchor;
+  std::vector<std::vector<float>> x1, y1, x2, y2;
+  int NoR = 0, NoP = 0;
+  std::vector<int> root_size, part_size, part_partner;   // n x 3
+  std::vector<std::vector<float>> rootfilter, partfilter; // [31][w][h]
+};
+
+}  // namespace geye
+
+struct geye_model {
+  geye_ctx *ctx = nullptr;
+  geye::HostModel h;
+  bool ini = true;         // ini_scales latch (featurepyramid.cpp:178-236)
+  int max_scale = -1;
+  int id = 0;
+  // device filter tables, fp32 [31][w][h] per filter, roots then parts
+  float *d_filters = nullptr;
+  int *d_filt_off = nullptr;   // float offsets, NoR + NoP entries
+  float *d_coef = nullptr;     // box regression [comp][x1, y1, x2, y2][ML]
+  std::vector<int> filt_off;
+  // bf16 filter banks for the tensor-core convolution (built on first use)
+  void *d_bank16 = nullptr;
+  size_t bank16_bytes = 0;
+  int gl() const { return (h.numpart[0] + 1) * 4 + 3; }
+};
+
+namespace geye {
+
+// ----------------------------------------------------------------------------
+// kernel launchers (defined in the .cu files)
+// ----------------------------------------------------------------------------
+void launch_fill(float *p, size_t n, float v, cudaStream_t s);
+void launch_ingest(const uint8_t *bgr, int width, int height, int width_step, float *planes, cudaStream_t s);
+void launch_resize_pass(const ResizeJob *d_jobs, int n_jobs, int max_items, int vertical, const int *d_tap_start,
+                        const int *d_tap_si, const float *d_tap_alpha, float *arena, cudaStream_t s);
+void launch_hog(const HogJob *d_jobs, int n_jobs, int max_b, int max_cells, float *arena, void *arena16,
+                cudaStream_t s);
+void launch_to_ref_layout(const float *feat, int fs0, int fs1, float *out, cudaStream_t s);
+void launch_from_ref_layout(const float *ref, int fs0, int fs1, float *feat, cudaStream_t s);
+void launch_conv_fp32(const ConvJob *d_jobs, int n_jobs, int max_tiles_y, int max_tiles_x, const float *filters,
+                      const int *filt_off, const float *arena_in, float *arena_out, int max_b0, int max_b1,
+                      int max_group, cudaStream_t s);
+void launch_dt(const DtJob *d_jobs, int n_jobs, int max_d0, int max_d1, float *arena, int *arena_i,
+               int *fallback_count, cudaStream_t s);
+void launch_score(const ScoreJob *d_jobs, int n_jobs, int max_r, float thresh, float *arena, int *block_counts,
+                  int blocks_per_job_stride, cudaStream_t s);
+void launch_boxes(const ScoreJob *d_jobs, int n_jobs, int max_r, float thresh, const float *arena,
+                  const int *arena_i, const int *block_offsets, int blocks_per_job_stride, int GL, float *boxes,
+                  cudaStream_t s);
+void launch_scan_counts(int *counts, int n, int *total, cudaStream_t s);
+void launch_ascore(const ScoreJob *d_jobs, int n_jobs, const float *arena, float *a_score, int im_w, int im_h,
+                   float thresh, unsigned *max_bits, cudaStream_t s);
+void launch_ascore_normalize(float *a_score, int n, const unsigned *max_bits, cudaStream_t s);
+// one block per model; model m uses boxes/out at m*cap*GL, scratch at m*cap*6 floats and m*cap*5 ints
+void launch_nms(const float *boxes, const int *d_num, int n_models, int GL, float overlap, int cap,
+                float *scratch_f, int *scratch_i, float *out, int *d_kept, int *err, cudaStream_t s);
+void launch_new_rects(const float *kept, const int *d_kept, int GL, int np, const float *coef, int img_w,
+                      int img_h, float ratio, int *point, int *or_point, int *type, float *scale, float *score,
+                      cudaStream_t s);
+
+}  // namespace geye

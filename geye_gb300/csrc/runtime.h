@@ -1,0 +1,114 @@
+// runtime.h -- host-side runtime of libgeye_dpm: context, plans, pipeline.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <map>
+#include <set>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "internal.h"
+
+namespace geye {
+
+// thread-local error text, set by every failing entry point
+void set_error(const std::string &msg);
+
+// Device buffer owned by a plan or context.
+struct DevBuf {
+  void *p = nullptr;
+  size_t bytes = 0;
+  ~DevBuf();
+  geye_status alloc(geye_ctx *ctx, size_t n);
+  void release();
+  template <class T> T *as() const { return reinterpret_cast<T *>(p); }
+};
+
+struct LevelInfo {
+  int img_h = 0, img_w = 0;   // image of this level (aliases for [interval, 2*interval))
+  int img_level = 0;          // level whose image planes are used
+  int img_off = -1;           // word offset of the planes (own image only)
+  int fs0 = 0, fs1 = 0;       // features
+  int sbin = 0;
+  float scale = 0.f;          // scales[] entry
+  int feat_off = -1;          // [pos][32]
+  int feat16_off = -1;        // bf16 elements
+  int hist_off = -1;
+};
+
+struct ModelPlan {
+  geye_model *model = nullptr;
+  int LEN = 0;                          // levels this model uses
+  std::vector<ConvJob> root_jobs, part_jobs;
+  int root_max_b0 = 0, root_max_b1 = 0, root_max_g = 1, root_tiles_y = 0, root_tiles_x = 0;
+  int part_max_b0 = 0, part_max_b1 = 0, part_max_g = 1, part_tiles_y = 0, part_tiles_x = 0;
+  std::vector<DtJob> dt_jobs;
+  int dt_max_d0 = 0, dt_max_d1 = 0;
+  std::vector<ScoreJob> score_jobs;
+  int score_max_r = 0, score_stride = 0;
+  int cap = 0;                          // max detections (sum of root map sizes)
+  // device copies
+  DevBuf d_root_jobs, d_part_jobs, d_dt_jobs, d_score_jobs, d_counts;
+  // per-(level, comp) and per-(L, part) map offsets for stage readback
+  std::vector<int> root_map_off, root_r0, root_r1;     // [level*NoC + c], -1 if none
+  std::vector<int> part_map_off, part_d0, part_d1;     // [L*NoP + p]
+  std::vector<int> skipped;                            // per level
+  double conv_flops = 0, conv_bytes = 0, dt_bytes = 0, score_bytes = 0;
+};
+
+struct Plan {
+  int width = 0, height = 0;           // frame size (0 when built from features)
+  int interval = 0, sbin = 0, LEN = 0;
+  bool from_features = false;
+  std::vector<LevelInfo> lv;
+  // resize phases: each phase is two passes (vertical then horizontal)
+  std::vector<std::vector<ResizeJob>> vjobs, hjobs;
+  std::vector<int> v_max_items, h_max_items;
+  std::vector<DevBuf> d_vjobs, d_hjobs;
+  DevBuf d_tap_start, d_tap_si, d_tap_alpha;
+  std::vector<HogJob> hog_jobs;
+  DevBuf d_hog_jobs;
+  int hog_max_b0 = 0, hog_max_b1 = 0;
+  std::vector<std::unique_ptr<ModelPlan>> models;
+  // memory
+  size_t arena_words = 0, arena16_elems = 0;
+  DevBuf arena, arena16;
+  DevBuf d_bgr;                          // frame upload buffer
+  DevBuf d_boxes, d_kept_boxes, d_nms_f, d_nms_i, d_small, d_ascore, d_result;
+  int gl = 0, max_cap = 0;
+  // algorithmic bytes per stage (for roofline reporting)
+  double bytes_resize = 0, bytes_hog = 0;
+  // last-run results (host)
+  std::vector<int> last_D, last_K;
+};
+
+}  // namespace geye
+
+struct geye_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  geye_conv_mode conv_mode = GEYE_CONV_FP32;
+  std::map<std::string, std::unique_ptr<geye::Plan>> plans;
+  int next_model_id = 1;
+  // timing
+  bool timing = false;
+  cudaEvent_t ev[GEYE_N_STAGES + 1] = {};
+  float stage_ms[GEYE_N_STAGES] = {};
+  double stage_bytes[GEYE_N_STAGES] = {};
+  double conv_flops = 0;
+  int launches = 0;
+  // fault injection (host side)
+  std::string inject_op;
+  int inject_countdown = 0;
+  // fallback counters etc. (device)
+  geye::DevBuf d_diag;
+  // pinned staging for results
+  void *h_pinned = nullptr;
+  size_t h_pinned_bytes = 0;
+  // last device-resident run
+  geye::Plan *last_plan = nullptr;
+  // live models (detached when the context goes away first)
+  std::set<geye_model *> models;
+};

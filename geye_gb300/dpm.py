@@ -1,0 +1,364 @@
+"""Python front end of libgeye_dpm.so (the C ABI in include/geye_dpm.h).
+
+Function names and argument meanings follow the reference's C++ entry points
+so callers (and the parity tests) read like the reference:
+
+    load_model(comp, root, part, ratio)            load_model.cpp:541
+    car_detection(frame, model, thresh, A_SCORE, overlap)   detect.cpp:232
+    calc_f_pyramid(frame, model)                   featurepyramid.cpp:952
+    get_boxes(features, scales, FSIZE, model, A_SCORE, thresh)  get_boxes.cpp:583
+    nms(boxes, overlap, numpart0)                  nms.cpp:94
+    get_new_rects(frame_size, model, boxes)        tracking.cpp:90
+    dt(vals, ax, bx, ay, by)                       dt.cpp:101
+    fconvsMT(feat, filters)                        get_boxes_func.h:28
+    resize(img, scale), calc_feature(img, sbin)    resize.cc:135, featurepyramid.cpp:263
+
+Array layouts are the reference's column-major ones (see oracle/oracle.py for
+the numpy shapes).  Every call runs on the GPU through the C ABI; there is no
+CPU fallback: without the built library or a CUDA device, calls raise.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build as _build
+
+__all__ = ["GeyeError", "Context", "Model", "lib", "symbols"]
+
+_lib = None
+
+
+class GeyeError(RuntimeError):
+    pass
+
+
+def lib(build_if_missing: bool = True):
+    """Loads libgeye_dpm.so (building it with nvcc first if it is missing)."""
+    global _lib
+    if _lib is None:
+        path = _build.LIB
+        if not os.path.exists(path):
+            if not build_if_missing:
+                raise GeyeError(f"{path} is missing; run geye_gb300.build.build()")
+            _build.build()
+        L = C.CDLL(path)
+        vp, ip, fp, i32 = C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_float), C.c_int
+        sig = {
+            "geye_ctx_create": [i32, vp, C.POINTER(vp)],
+            "geye_ctx_destroy": [vp],
+            "geye_ctx_set_conv_mode": [vp, i32],
+            "geye_ctx_synchronize": [vp],
+            "geye_model_load_csv": [vp, C.c_char_p, C.c_char_p, C.c_char_p, C.c_float, C.POINTER(vp)],
+            "geye_model_free": [vp],
+            "geye_model_info": [vp, vp],
+            "geye_model_reset_scales": [vp],
+            "geye_car_detection": [vp, vp, vp, i32, i32, i32, C.c_float, C.c_float, vp, vp],
+            "geye_detect_multi": [vp, vp, i32, vp, i32, i32, i32, C.c_float, C.c_float, vp, vp],
+            "geye_result_free": [vp],
+            "geye_calc_f_pyramid": [vp, vp, vp, i32, i32, i32, ip, C.POINTER(fp), C.POINTER(ip), C.POINTER(fp)],
+            "geye_get_boxes": [vp, vp, vp, vp, vp, i32, i32, i32, C.c_float, vp, C.POINTER(fp), ip],
+            "geye_nms": [vp, vp, C.c_float, ip, i32, C.POINTER(fp)],
+            "geye_get_new_rects": [vp, vp, vp, i32, i32, i32, vp],
+            "geye_dt": [vp, vp, C.c_float, C.c_float, C.c_float, C.c_float, vp, vp, vp, vp],
+            "geye_fconv": [vp, vp, vp, vp, vp, i32, vp],
+            "geye_resize": [vp, vp, vp, vp, C.c_float, vp],
+            "geye_calc_feature": [vp, vp, vp, i32, vp, vp],
+            "geye_free": [vp],
+            "geye_detect_device": [vp, vp, i32, vp, i32, i32, C.c_float, C.c_float],
+            "geye_fetch_result": [vp, i32, vp, ip],
+            "geye_ctx_enable_timing": [vp, i32],
+            "geye_ctx_stage_times": [vp, vp, vp, C.POINTER(C.c_double), ip],
+            "geye_debug_inject_fault": [vp, C.c_char_p, i32],
+        }
+        for name, args in sig.items():
+            f = getattr(L, name)
+            f.argtypes = args
+            f.restype = C.c_int
+        L.geye_last_error.restype = C.c_char_p
+        L.geye_last_error.argtypes = []
+        L.geye_version.restype = C.c_char_p
+        L.geye_version.argtypes = []
+        _lib = L
+    return _lib
+
+
+def symbols() -> list[str]:
+    """Entry points declared in include/geye_dpm.h."""
+    import re
+    hdr = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include", "geye_dpm.h")
+    pat = r"^\s*(?:geye_status|const char \*|void)\s*\**\s*(geye_[a-z0-9_]+)\s*\("
+    return sorted(set(re.findall(pat, open(hdr).read(), flags=re.M)))
+
+
+class _Result(C.Structure):
+    _fields_ = [("num", C.c_int), ("point", C.POINTER(C.c_int)), ("or_point", C.POINTER(C.c_int)),
+                ("type", C.POINTER(C.c_int)), ("scale", C.POINTER(C.c_float)), ("score", C.POINTER(C.c_float))]
+
+
+def _check(status: int, what: str):
+    if status != 0:
+        msg = lib().geye_last_error()
+        raise GeyeError(f"{what} failed (status {status}): {msg.decode() if msg else ''}")
+
+
+def _p(a: np.ndarray):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+def _result_to_dict(r: _Result) -> dict:
+    n = r.num
+
+    def arr(ptr, k, dt):
+        if n <= 0:
+            return np.zeros((0,) if k == 1 else (0, k), dt)
+        a = np.ctypeslib.as_array(ptr, shape=(n * k,)).astype(dt, copy=True)
+        return a if k == 1 else a.reshape(n, k)
+
+    out = dict(num=n, point=arr(r.point, 4, np.int32), or_point=arr(r.or_point, 4, np.int32),
+               type=arr(r.type, 1, np.int32), scale=arr(r.scale, 1, np.float32), score=arr(r.score, 1, np.float32))
+    lib().geye_result_free(C.byref(r))
+    return out
+
+
+CONV_FP32, CONV_BF16 = 0, 1
+
+
+class Context:
+    """One device and one stream (replaces init_cuda / clean_cuda, GPU_init.cpp:50-356)."""
+
+    def __init__(self, device: int = 0, stream: int | None = None, conv: int = CONV_FP32):
+        h = C.c_void_p()
+        _check(lib().geye_ctx_create(device, C.c_void_p(stream) if stream else None, C.byref(h)), "geye_ctx_create")
+        self.h = h
+        if conv != CONV_FP32:
+            self.set_conv_mode(conv)
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().geye_ctx_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_conv_mode(self, mode: int):
+        _check(lib().geye_ctx_set_conv_mode(self.h, mode), "set_conv_mode")
+
+    def synchronize(self):
+        _check(lib().geye_ctx_synchronize(self.h), "synchronize")
+
+    # ---- whole path -------------------------------------------------------
+    def car_detection(self, frame: np.ndarray, model: "Model", thresh: float = -0.5, A_SCORE: np.ndarray | None = None,
+                      overlap: float = 0.5) -> dict:
+        """frame (h, w, 3) uint8 BGR; A_SCORE (w, h) float32 updated in place if given."""
+        fr = np.ascontiguousarray(frame, dtype=np.uint8)
+        h, w, _ = fr.shape
+        r = _Result()
+        a = _p(A_SCORE) if A_SCORE is not None else None
+        if A_SCORE is not None:
+            assert A_SCORE.dtype == np.float32 and A_SCORE.flags.c_contiguous and A_SCORE.size == w * h
+        _check(lib().geye_car_detection(self.h, model.h, _p(fr), w, h, 3 * w, thresh, overlap, a, C.byref(r)),
+               "car_detection")
+        return _result_to_dict(r)
+
+    def detect_multi(self, frame: np.ndarray, models: list, thresh: float = -0.5, overlap: float = 0.5,
+                     A_SCOREs: list | None = None) -> list:
+        fr = np.ascontiguousarray(frame, dtype=np.uint8)
+        h, w, _ = fr.shape
+        n = len(models)
+        arr = (C.c_void_p * n)(*[m.h for m in models])
+        res = (_Result * n)()
+        ap = None
+        if A_SCOREs is not None:
+            ap = (C.c_void_p * n)(*[_p(a) for a in A_SCOREs])
+        _check(lib().geye_detect_multi(self.h, arr, n, _p(fr), w, h, 3 * w, thresh, overlap, ap, res), "detect_multi")
+        return [_result_to_dict(res[i]) for i in range(n)]
+
+    # ---- stages -----------------------------------------------------------
+    def calc_f_pyramid(self, frame: np.ndarray, model: "Model"):
+        """-> (list of (31, fs1, fs0) features, FTSIZE (LEN, 2), scales (LEN,))."""
+        fr = np.ascontiguousarray(frame, dtype=np.uint8)
+        h, w, _ = fr.shape
+        n = C.c_int()
+        fp, ip, sp = C.POINTER(C.c_float)(), C.POINTER(C.c_int)(), C.POINTER(C.c_float)()
+        _check(lib().geye_calc_f_pyramid(self.h, model.h, _p(fr), w, h, 3 * w, C.byref(n), C.byref(fp), C.byref(ip),
+                                         C.byref(sp)), "calc_f_pyramid")
+        L = n.value
+        fs = np.ctypeslib.as_array(ip, shape=(2 * L,)).reshape(L, 2).copy()
+        sc = np.ctypeslib.as_array(sp, shape=(L,)).copy()
+        total = int(sum(31 * a * b for a, b in fs))
+        flat = np.ctypeslib.as_array(fp, shape=(max(total, 1),))[:total].copy()
+        for q in (fp, ip, sp):
+            lib().geye_free(C.cast(q, C.c_void_p))
+        feats, o = [], 0
+        for a, b in fs:
+            k = 31 * a * b
+            feats.append(flat[o:o + k].reshape(31, b, a))
+            o += k
+        return feats, fs, sc
+
+    def get_boxes(self, feats, scales, ftsize, model: "Model", thresh: float = -0.5, A_SCORE=None,
+                  img_size: tuple | None = None) -> np.ndarray:
+        """feats: list of (31, fs1, fs0); returns boxes [D][GL]."""
+        flat = np.ascontiguousarray(np.concatenate([np.asarray(f, np.float32).ravel() for f in feats]))
+        sc = np.ascontiguousarray(scales, np.float32)
+        fs = np.ascontiguousarray(ftsize, np.int32).ravel()
+        w, h = img_size if img_size else (0, 0)
+        bp = C.POINTER(C.c_float)()
+        d = C.c_int()
+        _check(lib().geye_get_boxes(self.h, model.h, _p(flat), _p(sc), _p(fs), len(feats), w, h, thresh,
+                                    _p(A_SCORE) if A_SCORE is not None else None, C.byref(bp), C.byref(d)),
+               "get_boxes")
+        GL = model.gl
+        D = d.value
+        out = np.ctypeslib.as_array(bp, shape=(max(D, 1) * GL,))[:D * GL].reshape(D, GL).copy()
+        lib().geye_free(C.cast(bp, C.c_void_p))
+        return out
+
+    def nms(self, boxes: np.ndarray, overlap: float, numpart0: int) -> np.ndarray:
+        b = np.ascontiguousarray(boxes, np.float32)
+        num = C.c_int(b.shape[0] if b.ndim == 2 else 0)
+        GL = (numpart0 + 1) * 4 + 3
+        op = C.POINTER(C.c_float)()
+        _check(lib().geye_nms(self.h, _p(b) if b.size else None, overlap, C.byref(num), numpart0, C.byref(op)), "nms")
+        K = num.value
+        if not op:
+            return np.zeros((0, GL), np.float32)
+        out = np.ctypeslib.as_array(op, shape=(max(K, 1) * GL,))[:K * GL].reshape(K, GL).copy()
+        lib().geye_free(C.cast(op, C.c_void_p))
+        return out
+
+    def get_new_rects(self, img_size: tuple, model: "Model", boxes: np.ndarray) -> dict:
+        b = np.ascontiguousarray(boxes, np.float32)
+        r = _Result()
+        w, h = img_size
+        _check(lib().geye_get_new_rects(self.h, model.h, _p(b) if b.size else None, b.shape[0], w, h, C.byref(r)),
+               "get_new_rects")
+        return _result_to_dict(r)
+
+    def dt(self, vals: np.ndarray, ax, bx, ay, by):
+        v = np.ascontiguousarray(vals, np.float32)
+        d1, d0 = v.shape
+        M = np.zeros_like(v)
+        Ix = np.zeros(v.shape, np.int32)
+        Iy = np.zeros(v.shape, np.int32)
+        dims = np.array([d0, d1], np.int32)
+        _check(lib().geye_dt(self.h, _p(v), ax, bx, ay, by, _p(dims), _p(M), _p(Ix), _p(Iy)), "dt")
+        return M, Ix, Iy
+
+    def fconvsMT(self, feat: np.ndarray, filters: list) -> list:
+        f = np.ascontiguousarray(feat, np.float32)
+        _, a1, a0 = f.shape
+        fl = [np.ascontiguousarray(x, np.float32) for x in filters]
+        ptrs = (C.c_void_p * len(fl))(*[x.ctypes.data for x in fl])
+        bd = np.array([[x.shape[2], x.shape[1]] for x in fl], np.int32).ravel()
+        sizes = [(a1 - x.shape[1] + 1, a0 - x.shape[2] + 1) for x in fl]
+        out = np.zeros(sum(p * q for p, q in sizes), np.float32)
+        _check(lib().geye_fconv(self.h, _p(f), _p(np.array([a0, a1], np.int32)), ptrs, _p(bd), len(fl), _p(out)),
+               "fconv")
+        res, o = [], 0
+        for p, q in sizes:
+            res.append(out[o:o + p * q].reshape(p, q))
+            o += p * q
+        return res
+
+    def resize(self, img: np.ndarray, scale: float) -> np.ndarray:
+        a = np.ascontiguousarray(img, np.float32)
+        c, w, h = a.shape
+        sd = np.array([h, w, c], np.int32)
+        od = np.zeros(3, np.int32)
+        if scale == 1.0:
+            return a.copy()
+        oh, ow = int(np.float32(h) * np.float32(scale) + 0.5), int(np.float32(w) * np.float32(scale) + 0.5)
+        out = np.zeros((c, ow, oh), np.float32)
+        _check(lib().geye_resize(self.h, _p(a), _p(sd), _p(od), scale, _p(out)), "resize")
+        assert (od[0], od[1]) == (oh, ow)
+        return out
+
+    def calc_feature(self, img: np.ndarray, sbin: int) -> np.ndarray:
+        a = np.ascontiguousarray(img, np.float32)
+        _, w, h = a.shape
+        b0, b1 = int(np.floor(h / sbin + 0.5)), int(np.floor(w / sbin + 0.5))
+        f0, f1 = max(b0 - 2, 0), max(b1 - 2, 0)
+        out = np.zeros((31, f1, f0), np.float32)
+        fs = np.zeros(2, np.int32)
+        _check(lib().geye_calc_feature(self.h, _p(a), _p(np.array([h, w, 3], np.int32)), sbin, _p(fs), _p(out)),
+               "calc_feature")
+        return out
+
+    # ---- device-resident path ---------------------------------------------
+    def detect_device(self, d_bgr_ptr: int, width: int, height: int, models: list, thresh: float = -0.5,
+                      overlap: float = 0.5):
+        arr = (C.c_void_p * len(models))(*[m.h for m in models])
+        _check(lib().geye_detect_device(self.h, arr, len(models), C.c_void_p(d_bgr_ptr), width, height, thresh,
+                                        overlap), "detect_device")
+
+    def fetch_result(self, model_index: int = 0):
+        r = _Result()
+        D = C.c_int()
+        _check(lib().geye_fetch_result(self.h, model_index, C.byref(r), C.byref(D)), "fetch_result")
+        out = _result_to_dict(r)
+        out["D"] = D.value
+        return out
+
+    def enable_timing(self, on: bool = True):
+        _check(lib().geye_ctx_enable_timing(self.h, 1 if on else 0), "enable_timing")
+
+    def stage_times(self) -> dict:
+        ms = (C.c_float * 7)()
+        by = (C.c_double * 7)()
+        fl = C.c_double()
+        nl = C.c_int()
+        _check(lib().geye_ctx_stage_times(self.h, ms, by, C.byref(fl), C.byref(nl)), "stage_times")
+        names = ["pyramid", "hog", "conv", "dt", "score", "nms", "total"]
+        return dict(ms={n: ms[i] for i, n in enumerate(names)}, bytes={n: by[i] for i, n in enumerate(names)},
+                    conv_flops=fl.value, launches=nl.value)
+
+    def inject_fault(self, op: str | None, nth: int):
+        _check(lib().geye_debug_inject_fault(self.h, op.encode() if op else None, nth), "inject_fault")
+
+
+class Model:
+    """A DPM model on the device (replaces load_model / free_model)."""
+
+    def __init__(self, ctx: Context, comp: str, root: str, part: str, ratio: float = 1.0):
+        h = C.c_void_p()
+        _check(lib().geye_model_load_csv(ctx.h, comp.encode(), root.encode(), part.encode(), ratio, C.byref(h)),
+               "model_load_csv")
+        self.h = h
+        self.ctx = ctx
+        info = np.zeros(8, np.int32)
+        _check(lib().geye_model_info(h, _p(info)), "model_info")
+        self.numcomponent, self.sbin, self.interval, self.numpart0, self.gl, self.NoR, self.NoP, _ = [int(v) for v in info]
+
+    def info(self) -> dict:
+        info = np.zeros(8, np.int32)
+        _check(lib().geye_model_info(self.h, _p(info)), "model_info")
+        keys = ["numcomponent", "sbin", "interval", "numpart0", "GL", "NoR", "NoP", "max_scale"]
+        return dict(zip(keys, [int(v) for v in info]))
+
+    def reset_scales(self):
+        _check(lib().geye_model_reset_scales(self.h), "reset_scales")
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().geye_model_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,167 @@
+/*
+ * geye_dpm.h -- C ABI of libgeye_dpm.so, the GB300 (sm_103a) implementation
+ * of CPFL/geye's DPM detection path:
+ *   image resize pyramid -> 31-channel HOG pyramid -> root/part filter
+ *   convolution -> generalized distance transform with argmax -> score
+ *   assembly and box records -> greedy NMS -> box regression.
+ *
+ * Every entry point returns a geye_status (0 = success).  Plain pointers and
+ * sizes only.  Array layouts are the reference's: a map of d0 rows (y) by d1
+ * columns (x) is column-major (element (x, y) at x*d0 + y); a feature level
+ * is [31][d1][d0]; a box record is GL = (numpart+1)*4+3 floats
+ * [root y1,x1,y2,x2, part boxes..., component, score, scale].
+ *
+ * Reference interfaces replaced (paths relative to the reference project):
+ *   init_cuda / clean_cuda        CAR_TRACKING/for_use_GPU.h:128-130
+ *   load_model / free_model       CAR_TRACKING/car_det_func.h:22-23
+ *   car_detection                 CAR_TRACKING/car_det_func.h:30
+ *   calc_f_pyramid                CAR_TRACKING/detect_func.h:27
+ *   get_boxes                     CAR_TRACKING/detect_func.h:36
+ *   nms                           CAR_TRACKING/detect_func.h:45
+ *   get_new_rects                 CAR_TRACKING/detect_func.h:54 (tracking.cpp:90)
+ *   dt                            CAR_TRACKING/get_boxes_func.h:34
+ *   fconvsMT / fconvsMT_GPU       CAR_TRACKING/get_boxes_func.h:28, for_use_GPU.h:136-160
+ *   resize                        CAR_TRACKING/resize.cc:135
+ *   calc_feature                  CAR_TRACKING/featurepyramid.cpp:263
+ */
+#ifndef GEYE_DPM_H
+#define GEYE_DPM_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int geye_status;
+#define GEYE_OK               0
+#define GEYE_ERR_ARG          1   /* bad argument (null pointer, bad size)          */
+#define GEYE_ERR_CUDA         2   /* a CUDA call failed; see geye_last_error()      */
+#define GEYE_ERR_MODEL        3   /* model file missing or malformed                */
+#define GEYE_ERR_NOMEM        4   /* device or host allocation failed               */
+#define GEYE_ERR_UNSUPPORTED  5   /* model shape outside what the kernels cover     */
+#define GEYE_ERR_INJECTED     6   /* fault injected by geye_debug_inject_fault      */
+#define GEYE_ERR_TIMEOUT      7   /* a bounded device-side wait gave up             */
+
+typedef struct geye_ctx geye_ctx;       /* one device + one stream + work buffers */
+typedef struct geye_model geye_model;   /* a DPM model resident on the device     */
+
+/* Convolution arithmetic. */
+typedef enum {
+    GEYE_CONV_FP32 = 0,   /* CUDA-core FP32 in the reference's summation order (bit-exact) */
+    GEYE_CONV_BF16 = 1,   /* tcgen05 implicit GEMM, BF16 operands, FP32 accumulation        */
+} geye_conv_mode;
+
+/* Detection result; mirrors RESULT (CAR_TRACKING/MODEL_info.h:158-166)
+ * without the per-box IplImage crops. */
+typedef struct {
+    int num;
+    int *point;      /* num x 4: x1, y1, x2, y2 clamped to the image            */
+    int *or_point;   /* num x 4: point / model ratio                            */
+    int *type;       /* component index                                         */
+    float *scale;
+    float *score;
+} geye_result;
+
+/* ---- runtime: replaces init_cuda / clean_cuda ------------------------- */
+/* stream may be NULL (the context creates its own non-blocking stream). */
+geye_status geye_ctx_create(int device, void *cuda_stream, geye_ctx **out);
+geye_status geye_ctx_destroy(geye_ctx *ctx);
+geye_status geye_ctx_set_conv_mode(geye_ctx *ctx, geye_conv_mode mode);
+geye_status geye_ctx_synchronize(geye_ctx *ctx);
+const char *geye_last_error(void);
+const char *geye_version(void);
+
+/* ---- models: replaces load_model / free_model ------------------------- */
+geye_status geye_model_load_csv(geye_ctx *ctx, const char *comp_csv, const char *root_csv,
+                                const char *part_csv, float ratio, geye_model **out);
+geye_status geye_model_free(geye_model *model);
+/* numcomponent, sbin, interval, numpart[0], GL, NoR, NoP, latched max_scale (-1 if none) */
+geye_status geye_model_info(const geye_model *model, int info[8]);
+/* Clears the ini_scales latch so the next frame fixes max_scale again. */
+geye_status geye_model_reset_scales(geye_model *model);
+
+/* ---- whole path: replaces car_detection -------------------------------- */
+/* bgr: height rows of width*3 bytes (B,G,R) at width_step bytes apart, host memory.
+ * a_score: height*width floats, column-major, host, updated in place (the caller
+ * fills it with -100 first, as ini_ac_score does); may be NULL.
+ * out: filled with callee-allocated arrays; release with geye_result_free. */
+geye_status geye_car_detection(geye_ctx *ctx, geye_model *model, const uint8_t *bgr, int width, int height,
+                               int width_step, float thresh, float overlap, float *a_score, geye_result *out);
+geye_status geye_result_free(geye_result *res);
+
+/* Several models on one frame; the feature pyramid is computed once and shared.
+ * out[m] receives model m's result. */
+geye_status geye_detect_multi(geye_ctx *ctx, geye_model *const *models, int n_models, const uint8_t *bgr,
+                              int width, int height, int width_step, float thresh, float overlap,
+                              float *const *a_scores, geye_result *out);
+
+/* ---- stage entry points (reference layouts, host buffers) --------------- */
+/* calc_f_pyramid: *n_levels gets LEN; *features (callee-allocated, geye_free)
+ * holds the levels back to back, level l at offset sum_{k<l} 31*fs0*fs1;
+ * ftsize (2*LEN ints) and scales (LEN floats) are callee-allocated too. */
+geye_status geye_calc_f_pyramid(geye_ctx *ctx, geye_model *model, const uint8_t *bgr, int width, int height,
+                                int width_step, int *n_levels, float **features, int **ftsize, float **scales);
+
+/* get_boxes: features as produced by geye_calc_f_pyramid.  *boxes is [D][GL]
+ * (callee-allocated, geye_free), *dnum = D.  a_score as in geye_car_detection. */
+geye_status geye_get_boxes(geye_ctx *ctx, geye_model *model, const float *features, const float *scales,
+                           const int *ftsize, int n_levels, int img_width, int img_height, float thresh,
+                           float *a_score, float **boxes, int *dnum);
+
+/* nms: boxes [num][GL] -> *out [kept][GL] in input order (callee-allocated); *num updated. */
+geye_status geye_nms(geye_ctx *ctx, const float *boxes, float overlap, int *num, int numpart0, float **out);
+
+/* get_new_rects: kept boxes -> result (callee-allocated arrays, geye_result_free). */
+geye_status geye_get_new_rects(geye_ctx *ctx, const geye_model *model, const float *boxes, int num,
+                               int img_width, int img_height, geye_result *out);
+
+/* dt: vals/M column-major dims[0] x dims[1]; M, Ix, Iy caller-allocated. */
+geye_status geye_dt(geye_ctx *ctx, const float *vals, float ax, float bx, float ay, float by, const int *dims,
+                    float *M, int *Ix, int *Iy);
+
+/* fconvsMT for one feature level and n filters: feat [31][a1][a0] (a_dims = {a0, a1});
+ * filters[i] [31][b1][b0] (b_dims 2*i, 2*i+1); out receives the n maps back to back,
+ * each (a0-b0+1) x (a1-b1+1) column-major.  Uses the context's convolution mode. */
+geye_status geye_fconv(geye_ctx *ctx, const float *feat, const int *a_dims, const float *const *filters,
+                       const int *b_dims, int n_filters, float *out);
+
+/* resize: src [c][w][h] with sdims = {h, w, c}; odims receives the output size;
+ * dst must hold the output (size from the same rounding as the reference). */
+geye_status geye_resize(geye_ctx *ctx, const float *src, const int *sdims, int *odims, float scale, float *dst);
+
+/* calc_feature: src [3][w][h] (isize = {h, w, 3}) -> feat [31][fs1][fs0]; ftsize receives {fs0, fs1}. */
+geye_status geye_calc_feature(geye_ctx *ctx, const float *src, const int *isize, int sbin, int *ftsize,
+                              float *feat);
+
+void geye_free(void *p);
+
+/* ---- device-resident path (benchmarks, batching) ------------------------ */
+/* Runs the whole path on a frame already in device memory (d_bgr, tightly packed
+ * width*3 bytes per row), leaving boxes and the kept set on the device.  Results
+ * can be read with geye_fetch_result.  Nothing is copied between host and device
+ * except a 4-byte count per model needed to size NMS. */
+geye_status geye_detect_device(geye_ctx *ctx, geye_model *const *models, int n_models, const uint8_t *d_bgr,
+                               int width, int height, float thresh, float overlap);
+geye_status geye_fetch_result(geye_ctx *ctx, int model_index, geye_result *out, int *n_boxes_before_nms);
+
+/* ---- measurement ---------------------------------------------------------- */
+/* When enabled, the context records CUDA events around each stage on its stream.
+ * ms receives per-stage milliseconds of the last run, in this order:
+ * ingest+resize, hog, conv, dt, score, nms, total; bytes receives the
+ * algorithmic bytes of each stage and flops the conv FLOPs. */
+#define GEYE_N_STAGES 7
+geye_status geye_ctx_enable_timing(geye_ctx *ctx, int enable);
+geye_status geye_ctx_stage_times(geye_ctx *ctx, float ms[GEYE_N_STAGES], double bytes[GEYE_N_STAGES],
+                                 double *conv_flops, int *kernel_launches);
+
+/* ---- fault injection (host side only) ------------------------------------ */
+/* The n-th subsequent call of the named operation ("alloc", "h2d", "launch")
+ * fails with GEYE_ERR_INJECTED; n = 0 clears.  No device fault is ever raised. */
+geye_status geye_debug_inject_fault(geye_ctx *ctx, const char *op, int nth);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

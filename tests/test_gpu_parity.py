@@ -1,0 +1,164 @@
+"""GPU parity: every stage of the CUDA path against the CPU oracle on the
+same inputs, through the C ABI.  Integer, index and float results of the
+FP32 path are compared bit for bit (the kernels repeat the reference's
+arithmetic and summation order with no FMA contraction)."""
+import numpy as np
+import pytest
+
+from geye_gb300 import synth
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+def bits(a):
+    return np.ascontiguousarray(a, np.float32).view(np.int32)
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    import geye_gb300 as g
+    c = g.Context(0)
+    yield c
+    c.close()
+
+
+@pytest.fixture(scope="module")
+def car(ctx, car_paths):
+    import geye_gb300 as g
+    return g.Model(ctx, *car_paths), O.Model(*car_paths)
+
+
+@pytest.fixture(scope="module")
+def person(ctx, person_paths):
+    import geye_gb300 as g
+    return g.Model(ctx, *person_paths), O.Model(*person_paths)
+
+
+def _img(w, h, seed):
+    rng = np.random.default_rng(seed)
+    img = rng.integers(0, 256, size=(3, w, h)).astype(np.float32)
+    img[:, : w // 3, : h // 3] = 91.0
+    return img
+
+
+@pytest.mark.parametrize("w,h", [(64, 48), (157, 93), (640, 480)])
+def test_resize(ctx, w, h):
+    img = _img(w, h, w)
+    sc = np.float32(2.0 ** 0.1)
+    for ii in (1, 3, 7, 9):
+        st = float(np.float32(1.0 / (float(sc) ** ii)))
+        assert np.array_equal(bits(ctx.resize(img, st)), bits(O.resize(img, st)))
+    assert np.array_equal(bits(ctx.resize(img, 0.5)), bits(O.resize(img, 0.5)))
+
+
+@pytest.mark.parametrize("sbin", [4, 8])
+@pytest.mark.parametrize("w,h", [(64, 48), (131, 99), (640, 480)])
+def test_calc_feature(ctx, sbin, w, h):
+    img = O.resize(_img(w, h, 3 * w + sbin), 0.91)
+    assert np.array_equal(bits(ctx.calc_feature(img, sbin)), bits(O.calc_feature(img, sbin)))
+
+
+def test_pyramid(ctx, car):
+    gm, om = car
+    fr = synth.make_frame(640, 480, seed=0)
+    gm.reset_scales()
+    feats, fs, sc = ctx.calc_f_pyramid(fr, gm)
+    P = O.Pyramid(om, fr)
+    assert len(feats) == P.LEN == 35
+    assert np.array_equal(bits(sc), bits(P.scales))
+    for l in range(P.LEN):
+        assert tuple(fs[l]) == P.ftsize[l]
+        assert np.array_equal(bits(feats[l]), bits(P.feat(l))), f"level {l}"
+
+
+@pytest.mark.parametrize("shape", [(6, 6), (6, 16), (8, 13), (11, 5)])
+def test_fconv(ctx, shape):
+    rng = np.random.default_rng(shape[0] * 100 + shape[1])
+    feat = rng.random((31, 47, 38)).astype(np.float32) * 0.2
+    filt = rng.normal(0, 0.01, size=(31, shape[1], shape[0])).astype(np.float32)
+    got = ctx.fconvsMT(feat, [filt, filt * 0.5])
+    assert np.array_equal(bits(got[0]), bits(O.fconv(feat, filt)))
+    assert np.array_equal(bits(got[1]), bits(O.fconv(feat, filt * 0.5)))
+
+
+@pytest.mark.parametrize("seed", range(8))
+def test_dt(ctx, seed):
+    rng = np.random.default_rng(seed)
+    d0, d1 = (int(v) for v in rng.integers(1, 200, size=2))
+    vals = rng.normal(0, 0.3, size=(d1, d0)).astype(np.float32)
+    if seed % 2:
+        vals = (np.round(vals * 4) / 4).astype(np.float32)
+    lo = 0.001 if seed < 6 else -0.05
+    a = rng.uniform(lo, 0.1, size=4).astype(np.float32)
+    M, Ix, Iy = ctx.dt(vals, *[float(x) for x in a])
+    rM, rIx, rIy = O.dt(vals, *[float(x) for x in a])
+    assert np.array_equal(Ix, rIx) and np.array_equal(Iy, rIy)
+    assert np.array_equal(bits(M), bits(rM))
+
+
+@pytest.mark.parametrize("seed", range(4))
+def test_nms_ties(ctx, seed):
+    rng = np.random.default_rng(seed)
+    n = [1, 2, 700, 5000][seed]
+    GL = 39
+    boxes = np.zeros((n, GL), np.float32)
+    xy = rng.uniform(0, 600, size=(n, 2)); wh = rng.uniform(10, 150, size=(n, 2))
+    boxes[:, 0], boxes[:, 1] = xy[:, 1], xy[:, 0]
+    boxes[:, 2], boxes[:, 3] = xy[:, 1] + wh[:, 1], xy[:, 0] + wh[:, 0]
+    boxes[:, GL - 2] = np.round(rng.normal(size=n) * 3) / 4
+    boxes[:, GL - 1] = np.arange(n)
+    keep, _, k = O.nms_keep(boxes, 0.5)
+    got = ctx.nms(boxes, 0.5, 8)
+    assert got.shape[0] == k
+    assert np.array_equal(bits(got), bits(boxes[keep]))
+
+
+def test_get_boxes_from_oracle_features(ctx, car):
+    gm, om = car
+    fr = synth.make_frame(320, 240, seed=4)
+    P = O.Pyramid(om, fr)
+    feats = [P.feat(l) for l in range(P.LEN)]
+    S = O.Scores(om, P)
+    a_ref = np.full((320, 240), -100, np.float32)
+    om.m.im_w, om.m.im_h = 320, 240
+    ref, oob = S.boxes(-0.5, a_ref)
+    assert oob == 0
+    a_gpu = np.full((320, 240), -100, np.float32)
+    got = ctx.get_boxes(feats, P.scales, np.array(P.ftsize), gm, -0.5, a_gpu, (320, 240))
+    assert got.shape == ref.shape
+    assert np.array_equal(bits(got), bits(ref))
+    assert np.array_equal(bits(a_gpu), bits(a_ref))
+
+
+@pytest.mark.parametrize("w,h,seed", [(640, 480, 0), (320, 240, 7)])
+def test_car_detection_end_to_end(ctx, car, w, h, seed):
+    gm, om = car
+    gm.reset_scales()
+    om.m.ini = 1
+    fr = synth.make_frame(w, h, seed=seed)
+    a_gpu = np.full((w, h), -100, np.float32)
+    a_ref = np.full((w, h), -100, np.float32)
+    got = ctx.car_detection(fr, gm, -0.5, a_gpu, 0.5)
+    ref = O.car_detection(om, fr, -0.5, 0.5, a_score=a_ref)
+    assert got["num"] == ref["K"] > 0
+    assert np.array_equal(got["point"], ref["point"])
+    assert np.array_equal(got["or_point"], ref["or_point"])
+    assert np.array_equal(got["type"], ref["type"])
+    assert np.array_equal(bits(got["score"]), bits(ref["score"]))
+    assert np.array_equal(bits(got["scale"]), bits(ref["scale"]))
+    assert np.array_equal(bits(a_gpu), bits(a_ref))
+
+
+def test_car_and_person_1280x720(ctx, car, person):
+    (gc, oc), (gp, op) = car, person
+    for gm, om in ((gc, oc), (gp, op)):
+        gm.reset_scales()
+        om.m.ini = 1
+    fr = synth.make_frame(1280, 720, seed=1)
+    got = ctx.detect_multi(fr, [gc, gp], -0.5, 0.5)
+    for res, om in zip(got, (oc, op)):
+        ref = O.car_detection(om, fr, -0.5, 0.5)
+        assert res["num"] == ref["K"]
+        assert np.array_equal(res["point"], ref["point"])
+        assert np.array_equal(bits(res["score"]), bits(ref["score"]))
