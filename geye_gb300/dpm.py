@@ -72,6 +72,7 @@ def lib(build_if_missing: bool = True):
             "geye_ctx_enable_timing": [vp, i32],
             "geye_ctx_stage_times": [vp, vp, vp, C.POINTER(C.c_double), ip],
             "geye_debug_inject_fault": [vp, C.c_char_p, i32],
+            "geye_nms_noalloc": [vp, i32, i32, C.c_float, vp, vp, vp],
         }
         for name, args in sig.items():
             f = getattr(L, name)

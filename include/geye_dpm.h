@@ -146,6 +146,26 @@ geye_status geye_detect_device(geye_ctx *ctx, geye_model *const *models, int n_m
                                int width, int height, float thresh, float overlap);
 geye_status geye_fetch_result(geye_ctx *ctx, int model_index, geye_result *out, int *n_boxes_before_nms);
 
+/* ---- allocation-free NMS --------------------------------------------------- */
+/* No counterpart in the reference: an addition for callers that cannot call
+ * cudaMalloc (their device memory belongs to another allocator, such as a
+ * framework's caching pool or a fixed per-process budget, or they run a
+ * real-time loop that cannot take cudaMalloc's latency and synchronisation).
+ * Same computation as geye_nms (reference tie order and kept set) on
+ * caller-owned DEVICE buffers: d_boxes [num][GL], d_out with room for
+ * num*GL floats (kept records in input order), *d_kept (device int) = kept
+ * count, or -1 on an internal error.  Asynchronous on cuda_stream (NULL = the
+ * legacy default stream).  Allocates nothing: working memory is a fixed
+ * __device__ array sized for GEYE_NMS_NOALLOC_MAX_BOXES boxes (~2.8 MB, held by
+ * every GPU that loads the library until exit); num above that returns
+ * GEYE_ERR_ARG.  All calls share that array and it keeps the last call's
+ * contents, so calls that overlap on the GPU race.  The first call on each
+ * device looks up the array's device address (cudaGetSymbolAddress); make that
+ * first call before any stream capture. */
+#define GEYE_NMS_NOALLOC_MAX_BOXES 65536
+geye_status geye_nms_noalloc(const float *d_boxes, int num, int numpart0, float overlap, float *d_out,
+                             int *d_kept, void *cuda_stream);
+
 /* ---- measurement ---------------------------------------------------------- */
 /* When enabled, the context records CUDA events around each stage on its stream.
  * ms receives per-stage milliseconds of the last run, in this order:
