@@ -169,6 +169,19 @@ geye_status geye_debug_inject_fault(geye_ctx *ctx, const char *op, int nth) {
 
 const char *geye_last_error(void);
 
+geye_status geye_ctx_debug_counters(geye_ctx *ctx, long long *out, int n) {
+  ARG_CHECK(ctx && out && n > 0 && n <= 64, "bad argument");
+  ARG_CHECK(ctx->last_plan, "no run yet");
+  CUDA_TRY(cudaMemcpyAsync(out, ctx->last_plan->d_small.as<int>() + 512, sizeof(long long) * n, cudaMemcpyDeviceToHost,
+                           ctx->stream));
+  int errw = 0;
+  CUDA_TRY(cudaMemcpyAsync(&errw, ctx->last_plan->d_small.as<int>() + 128, sizeof(int), cudaMemcpyDeviceToHost,
+                           ctx->stream));
+  CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  if (n > 15) out[15] = errw;
+  return GEYE_OK;
+}
+
 void geye_free(void *p) { free(p); }
 
 // ---------------------------------------------------------------------------

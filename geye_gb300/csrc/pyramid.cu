@@ -141,8 +141,10 @@ __device__ __forceinline__ void hog_interp(int p, int sbin, int &ip, float &w0, 
 }
 
 // Histogram + block energy for a tile of kTB0 x kTB1 blocks.  Pixels of the
-// tile region get their (bin, magnitude) once into shared memory; then each
-// thread sums its block's votes in the reference's pixel order.
+// tile region get their (bin, magnitude) once into shared memory, and each
+// pixel row/column its interpolation cell and weights (the reference's double
+// expression, evaluated once per tile row/column instead of per vote); then
+// each thread sums its block's votes in the reference's pixel order.
 __global__ void __launch_bounds__(kTB0 *kTB1) k_hog_hist(const HogJob *__restrict__ jobs, float *__restrict__ arena) {
   extern __shared__ unsigned char smem_raw[];
   const HogJob J = jobs[blockIdx.z];
@@ -155,6 +157,12 @@ __global__ void __launch_bounds__(kTB0 *kTB1) k_hog_hist(const HogJob *__restric
   float *mag_s = reinterpret_cast<float *>(smem_raw);
   unsigned char *bin_s = smem_raw + sizeof(float) * PW * PH;
   float *hist_s = reinterpret_cast<float *>(smem_raw + ((sizeof(float) + 1) * PW * PH + 15) / 16 * 16);
+  float *wx0_s = hist_s + 18 * kTB0 * kTB1;   // per region column: vx0, vx1, ixp
+  float *wx1_s = wx0_s + PW;
+  int *ix_s = reinterpret_cast<int *>(wx1_s + PW);
+  float *wy0_s = reinterpret_cast<float *>(ix_s + PW);   // per region row
+  float *wy1_s = wy0_s + PH;
+  int *iy_s = reinterpret_cast<int *>(wy1_s + PH);
   const float *img = arena + J.img_off;
   const int visible0 = J.b0 * sbin, visible1 = J.b1 * sbin;
   const int nthreads = blockDim.x;
@@ -167,6 +175,16 @@ __global__ void __launch_bounds__(kTB0 *kTB1) k_hog_hist(const HogJob *__restric
     mag_s[i] = mag;
     bin_s[i] = (unsigned char)bin;
   }
+  for (int i = threadIdx.x; i < PW + PH; i += nthreads) {
+    int ip; float w0, w1;
+    if (i < PW) {
+      hog_interp(px0 + i, sbin, ip, w0, w1);
+      wx0_s[i] = w0; wx1_s[i] = w1; ix_s[i] = ip;
+    } else {
+      hog_interp(py0 + i - PW, sbin, ip, w0, w1);
+      wy0_s[i - PW] = w0; wy1_s[i - PW] = w1; iy_s[i - PW] = ip;
+    }
+  }
   for (int i = threadIdx.x; i < 18 * nthreads; i += nthreads) hist_s[i] = 0.f;
   __syncthreads();
 
@@ -176,20 +194,19 @@ __global__ void __launch_bounds__(kTB0 *kTB1) k_hog_hist(const HogJob *__restric
   float *myh = hist_s + threadIdx.x;   // bin o at myh[o * nthreads]
   if (active) {
     // candidate pixel range: any pixel whose interpolation cell is bx-1 or bx
-    const int xlo = max(1, bx * sbin - sbin), xhi = min(visible1 - 2, bx * sbin + 2 * sbin);
-    const int ylo = max(1, by * sbin - sbin), yhi = min(visible0 - 2, by * sbin + 2 * sbin);
+    const int xlo = max(1, bx * sbin - sbin), xhi = min(visible1 - 2, bx * sbin + 2 * sbin - 1);
+    const int ylo = max(1, by * sbin - sbin), yhi = min(visible0 - 2, by * sbin + 2 * sbin - 1);
     for (int x = xlo; x <= xhi; x++) {
-      int ixp; float vx0, vx1;
-      hog_interp(x, sbin, ixp, vx0, vx1);
-      float wx;
-      if (ixp == bx) wx = vx1; else if (ixp + 1 == bx) wx = vx0; else continue;
       const int lx = x - px0;
+      const int ixp = ix_s[lx];
+      float wx;
+      if (ixp == bx) wx = wx1_s[lx]; else if (ixp + 1 == bx) wx = wx0_s[lx]; else continue;
       for (int y = ylo; y <= yhi; y++) {
-        int iyp; float vy0, vy1;
-        hog_interp(y, sbin, iyp, vy0, vy1);
+        const int ly = y - py0;
+        const int iyp = iy_s[ly];
         float wy;
-        if (iyp == by) wy = vy1; else if (iyp + 1 == by) wy = vy0; else continue;
-        const int li = lx * PH + (y - py0);
+        if (iyp == by) wy = wy1_s[ly]; else if (iyp + 1 == by) wy = wy0_s[ly]; else continue;
+        const int li = lx * PH + ly;
         const int o = bin_s[li];
         myh[o * nthreads] += wx * wy * mag_s[li];
       }
@@ -278,7 +295,8 @@ void launch_hog(const HogJob *d_jobs, int n_jobs, int max_b0, int max_b1, float 
   // dynamic shared memory of the widest sbin in the plan (8): 18 bins x 128 threads + pixel tile
   const int sbin_max = 8;
   const int PW = (kTB1 + 2) * sbin_max, PH = (kTB0 + 2) * sbin_max;
-  size_t smem = ((sizeof(float) + 1) * PW * PH + 15) / 16 * 16 + sizeof(float) * 18 * kTB0 * kTB1;
+  size_t smem = ((sizeof(float) + 1) * PW * PH + 15) / 16 * 16 + sizeof(float) * 18 * kTB0 * kTB1 +
+                sizeof(float) * 3 * (PW + PH);
   static bool attr_set = false;
   if (!attr_set) {
     cudaFuncSetAttribute(k_hog_hist, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);

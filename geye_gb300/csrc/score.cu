@@ -102,7 +102,7 @@ void launch_scan_counts(int *counts, int n, int *total, cudaStream_t s) {
 
 __global__ void k_boxes(const ScoreJob *__restrict__ jobs, float thresh, const float *__restrict__ arena,
                         const int *__restrict__ arena_i, const int *__restrict__ block_offsets, int stride, int GL,
-                        float *__restrict__ boxes) {
+                        float *__restrict__ boxes, int *__restrict__ pos2box, int *__restrict__ box2pos) {
   __shared__ int warp_cnt[kScoreThreads / 32];
   const ScoreJob &J = jobs[blockIdx.y];
   const int n = J.r0 * J.r1;
@@ -119,17 +119,14 @@ __global__ void k_boxes(const ScoreJob *__restrict__ jobs, float thresh, const f
   __syncthreads();
   int rank = __popc(bal & ((1u << lane) - 1));
   for (int w = 0; w < warp; w++) rank += warp_cnt[w];
+  const int idx = block_offsets[blockIdx.y * stride + blockIdx.x] + rank;
+  if (pos2box && i < n) pos2box[J.pos_off + i] = flag ? idx : -1;
   if (!flag) return;
+  if (box2pos) box2pos[idx] = J.pos_off + i;
   const int y = i % J.r0, x = i / J.r0;
-  float *P = boxes + (size_t)(block_offsets[blockIdx.y * stride + blockIdx.x] + rank) * GL;
+  float *P = boxes + (size_t)idx * GL;
   const float scale = J.scale;
-  // rootbox (pad = 0)
-  float o0 = ((float)y - (float)0 + 1) * scale;
-  float o1 = ((float)x - (float)0 + 1) * scale;
-  P[0] = o0;
-  P[1] = o1;
-  P[2] = o0 + (float)J.rsize0 * scale - 1.0;
-  P[3] = o1 + (float)J.rsize1 * scale - 1.0;
+  root_box(x, y, scale, J.rsize0, J.rsize1, P);
   float *Q = P + 4;
   for (int k = 0; k < J.np; k++) {
     const int probex = (x - 1) * 2 + J.ax[k];
@@ -153,10 +150,12 @@ __global__ void k_boxes(const ScoreJob *__restrict__ jobs, float thresh, const f
 }
 
 void launch_boxes(const ScoreJob *d_jobs, int n_jobs, int max_r, float thresh, const float *arena,
-                  const int *arena_i, const int *block_offsets, int stride, int GL, float *boxes, cudaStream_t s) {
+                  const int *arena_i, const int *block_offsets, int stride, int GL, float *boxes, int *pos2box,
+                  int *box2pos, cudaStream_t s) {
   if (n_jobs <= 0) return;
   dim3 grid((max_r + kScoreThreads - 1) / kScoreThreads, n_jobs);
-  k_boxes<<<grid, kScoreThreads, 0, s>>>(d_jobs, thresh, arena, arena_i, block_offsets, stride, GL, boxes);
+  k_boxes<<<grid, kScoreThreads, 0, s>>>(d_jobs, thresh, arena, arena_i, block_offsets, stride, GL, boxes, pos2box,
+                                         box2pos);
 }
 
 // A_SCORE in gather form: target pixel (X, Y) takes the max over every

@@ -73,6 +73,7 @@ def lib(build_if_missing: bool = True):
             "geye_ctx_stage_times": [vp, vp, vp, C.POINTER(C.c_double), ip],
             "geye_debug_inject_fault": [vp, C.c_char_p, i32],
             "geye_nms_noalloc": [vp, i32, i32, C.c_float, vp, vp, vp],
+            "geye_ctx_debug_counters": [vp, vp, i32],
         }
         for name, args in sig.items():
             f = getattr(L, name)
@@ -326,6 +327,11 @@ class Context:
         names = ["pyramid", "hog", "conv", "dt", "score", "nms", "total"]
         return dict(ms={n: ms[i] for i, n in enumerate(names)}, bytes={n: by[i] for i, n in enumerate(names)},
                     conv_flops=fl.value, launches=nl.value)
+
+    def debug_counters(self, n: int = 16) -> list:
+        out = (C.c_longlong * n)()
+        _check(lib().geye_ctx_debug_counters(self.h, out, n), "debug_counters")
+        return list(out)
 
     def inject_fault(self, op: str | None, nth: int):
         _check(lib().geye_debug_inject_fault(self.h, op.encode() if op else None, nth), "inject_fault")

@@ -176,6 +176,10 @@ geye_status geye_ctx_enable_timing(geye_ctx *ctx, int enable);
 geye_status geye_ctx_stage_times(geye_ctx *ctx, float ms[GEYE_N_STAGES], double bytes[GEYE_N_STAGES],
                                  double *conv_flops, int *kernel_launches);
 
+/* Diagnostic counters of the last whole-path run (per model, 8 values each:
+ * NMS sort cycles, NMS greedy cycles, greedy batches, picks, ...). */
+geye_status geye_ctx_debug_counters(geye_ctx *ctx, long long *out, int n);
+
 /* ---- fault injection (host side only) ------------------------------------ */
 /* The n-th subsequent call of the named operation ("alloc", "h2d", "launch")
  * fails with GEYE_ERR_INJECTED; n = 0 clears.  No device fault is ever raised. */
