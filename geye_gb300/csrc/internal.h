@@ -73,7 +73,6 @@ struct ScoreJob {          // one (level, component) score map
   float scale;             // sbin / scales[level]
   int rsize0, rsize1;      // component root size (boxes, A_SCORE)
   int RY, RX;              // A_SCORE shifts
-  int pos_off;             // first position of this map in the model's position space
   int part_M[kMaxParts];   // DT outputs per part (M); Ix/Iy at M + ix_delta/iy_delta
   int part_Ix[kMaxParts];
   int part_Iy[kMaxParts];
@@ -85,8 +84,7 @@ struct ScoreJob {          // one (level, component) score map
   int psize1[kMaxParts];
 };
 
-// Root box of position (x, y) of a score map (get_boxes.cpp:227-235, pad = 0);
-// shared by the record writer and the pipeline NMS so both see identical floats.
+// Root box of position (x, y) of a score map (get_boxes.cpp:227-235, pad = 0).
 __host__ __device__ __forceinline__ void root_box(int x, int y, float scale, int rs0, int rs1, float *o) {
   o[0] = ((float)y - (float)0 + 1) * scale;
   o[1] = ((float)x - (float)0 + 1) * scale;
@@ -151,10 +149,9 @@ void launch_dt(const DtJob *d_jobs, int n_jobs, int max_d0, int max_d1, float *a
                int *fallback_count, cudaStream_t s);
 void launch_score(const ScoreJob *d_jobs, int n_jobs, int max_r, float thresh, float *arena, int *block_counts,
                   int blocks_per_job_stride, cudaStream_t s);
-// pos2box/box2pos may be null (stage entry points); otherwise every position gets its box or -1
 void launch_boxes(const ScoreJob *d_jobs, int n_jobs, int max_r, float thresh, const float *arena,
                   const int *arena_i, const int *block_offsets, int blocks_per_job_stride, int GL, float *boxes,
-                  int *pos2box, int *box2pos, cudaStream_t s);
+                  cudaStream_t s);
 void launch_scan_counts(int *counts, int n, int *total, cudaStream_t s);
 void launch_ascore(const ScoreJob *d_jobs, int n_jobs, const float *arena, float *a_score, int im_w, int im_h,
                    float thresh, unsigned *max_bits, cudaStream_t s);
@@ -162,16 +159,13 @@ void launch_ascore_normalize(float *a_score, int n, const unsigned *max_bits, cu
 // one block per model; model m uses boxes/out at m*cap*GL, scratch at m*cap*6 floats and m*cap*5 ints
 void launch_nms(const float *boxes, const int *d_num, int n_models, int GL, float overlap, int cap,
                 float *scratch_f, int *scratch_i, float *out, int *d_kept, int *err, cudaStream_t s);
-// pipeline NMS over the models' score maps (jobs_all, job_start[n+1]); scratch
-// holds nms_model_words(cap) ints per model, pos2box / box2pos filled by launch_boxes
-constexpr int kNmsMapsScratchWords = 8;
-__host__ __device__ inline size_t nms_model_words(int cap) { return (size_t)kNmsMapsScratchWords * cap; }
-__host__ __device__ inline int *nms_pos2box(int *scratch, int m, int cap) { return scratch + (size_t)m * nms_model_words(cap) + 5 * (size_t)cap; }
-__host__ __device__ inline int *nms_box2pos(int *scratch, int m, int cap) { return scratch + (size_t)m * nms_model_words(cap) + 6 * (size_t)cap; }
-// diag (optional): per model m, diag[8m..8m+3] = sort cycles, greedy cycles, batches, picks
-void launch_nms_maps(const float *boxes, const int *d_num, int n_models, const ScoreJob *jobs, const int *job_start,
-                     int GL, float overlap, int cap, int max_positions, int *scratch, float *out, int *d_kept, int *err,
-                     long long *diag, cudaStream_t s);
+// pipeline NMS (nms_batch.cu): per model nms_model_words(cap) ints of scratch
+// and 5 * cap floats (the boxes in sorted order)
+constexpr int kNmsBatch = 256;
+__host__ __device__ inline size_t nms_model_words(int cap) { return 8 * (size_t)cap + 64 + 5 * kNmsBatch; }
+// diag (optional): per model m, diag[8m..8m+4] = sort cycles, -, batches, picks, fallback rounds used
+void launch_nms_batch(const float *boxes, const int *d_num, int n_models, int GL, float overlap, int cap, int *si,
+                      float *sf, float *out, int *d_kept, int *err, long long *diag, cudaStream_t s);
 void launch_new_rects(const float *kept, const int *d_kept, int GL, int np, const float *coef, int img_w,
                       int img_h, float ratio, int *point, int *or_point, int *type, float *scale, float *score,
                       cudaStream_t s);

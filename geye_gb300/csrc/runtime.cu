@@ -359,7 +359,6 @@ static geye_status build_model_plan(geye_ctx *ctx, Plan &P, geye_model *mdl, int
       S.np = m.numpart[c];
       S.comp = c;
       S.scale = (float)m.sbin / P.lv[level].scale;
-      S.pos_off = mp->cap;
       S.rsize0 = m.rsize[2 * c];
       S.rsize1 = m.rsize[2 * c + 1];
       int block_pad = (int)(S.scale / 2.0);
@@ -553,21 +552,6 @@ static geye_status finish_plan(geye_ctx *ctx, Plan &P, ArenaAlloc &A) {
   GEYE_TRY(P.d_kept_boxes.alloc(ctx, sizeof(float) * nm * P.max_cap * std::max(gl, 1)));
   GEYE_TRY(P.d_nms_f.alloc(ctx, sizeof(float) * nm * P.max_cap * 6));
   GEYE_TRY(P.d_nms_i.alloc(ctx, sizeof(int) * nm * nms_model_words(P.max_cap)));
-  {
-    std::vector<ScoreJob> all;
-    std::vector<int> start;
-    int maxpos = 0;
-    for (auto &mp : P.models) {
-      start.push_back((int)all.size());
-      mp->job_start = (int)all.size();
-      all.insert(all.end(), mp->score_jobs.begin(), mp->score_jobs.end());
-      maxpos = std::max(maxpos, mp->cap);
-    }
-    start.push_back((int)all.size());
-    P.max_positions = maxpos;
-    GEYE_TRY(upload(ctx, P.d_all_score_jobs, all));
-    GEYE_TRY(upload(ctx, P.d_job_start, start));
-  }
   GEYE_TRY(P.d_small.alloc(ctx, 4096));
   if (P.width > 0) GEYE_TRY(P.d_ascore.alloc(ctx, sizeof(float) * nm * P.width * P.height));
   // result arrays: point, or_point (4 ints each), type, scale, score per kept box
@@ -713,8 +697,7 @@ geye_status run_score(geye_ctx *ctx, Plan &P, ModelPlan &mp, int mi, float thres
   GEYE_TRY(check_launch(ctx, "scan"));
   float *boxes = P.d_boxes.as<float>() + (size_t)mi * P.max_cap * P.gl;
   launch_boxes(mp.d_score_jobs.as<ScoreJob>(), nj, mp.score_max_r, thresh, P.arena.as<float>(), P.arena.as<int>(),
-               counts, mp.score_stride, mp.model->gl(), boxes, nms_pos2box(P.d_nms_i.as<int>(), mi, P.max_cap),
-               nms_box2pos(P.d_nms_i.as<int>(), mi, P.max_cap), ctx->stream);
+               counts, mp.score_stride, mp.model->gl(), boxes, ctx->stream);
   return check_launch(ctx, "boxes");
 }
 
@@ -741,9 +724,9 @@ geye_status run_nms(geye_ctx *ctx, Plan &P, int n_models, float overlap) {
   int *d_num = P.d_small.as<int>();
   int *d_kept = d_num + 32;
   int *err = d_num + 128;
-  launch_nms_maps(P.d_boxes.as<float>(), d_num, n_models, P.d_all_score_jobs.as<ScoreJob>(), P.d_job_start.as<int>(),
-                  P.gl, overlap, P.max_cap, P.max_positions, P.d_nms_i.as<int>(), P.d_kept_boxes.as<float>(), d_kept,
-                  err, reinterpret_cast<long long *>(d_num + 512), ctx->stream);
+  launch_nms_batch(P.d_boxes.as<float>(), d_num, n_models, P.gl, overlap, P.max_cap, P.d_nms_i.as<int>(),
+                   P.d_nms_f.as<float>(), P.d_kept_boxes.as<float>(), d_kept, err,
+                   reinterpret_cast<long long *>(d_num + 512), ctx->stream);
   GEYE_TRY(check_launch(ctx, "nms"));
   for (int mi = 0; mi < n_models; mi++) {
     ModelPlan &mp = *P.models[mi];

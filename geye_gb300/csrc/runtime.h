@@ -48,7 +48,6 @@ struct ModelPlan {
   std::vector<ScoreJob> score_jobs;
   int score_max_r = 0, score_stride = 0;
   int cap = 0;                          // max detections (sum of root map sizes)
-  int job_start = 0;                    // first score job in the plan's concatenated table
   // device copies
   DevBuf d_root_jobs, d_part_jobs, d_dt_jobs, d_score_jobs, d_counts;
   // per-(level, comp) and per-(L, part) map offsets for stage readback
@@ -77,8 +76,6 @@ struct Plan {
   DevBuf arena, arena16;
   DevBuf d_bgr;                          // frame upload buffer
   DevBuf d_boxes, d_kept_boxes, d_nms_f, d_nms_i, d_small, d_ascore, d_result;
-  DevBuf d_all_score_jobs, d_job_start;   // every model's score jobs back to back, for the NMS
-  int max_positions = 0;
   int gl = 0, max_cap = 0;
   // algorithmic bytes per stage (for roofline reporting)
   double bytes_resize = 0, bytes_hog = 0;

@@ -102,7 +102,7 @@ void launch_scan_counts(int *counts, int n, int *total, cudaStream_t s) {
 
 __global__ void k_boxes(const ScoreJob *__restrict__ jobs, float thresh, const float *__restrict__ arena,
                         const int *__restrict__ arena_i, const int *__restrict__ block_offsets, int stride, int GL,
-                        float *__restrict__ boxes, int *__restrict__ pos2box, int *__restrict__ box2pos) {
+                        float *__restrict__ boxes) {
   __shared__ int warp_cnt[kScoreThreads / 32];
   const ScoreJob &J = jobs[blockIdx.y];
   const int n = J.r0 * J.r1;
@@ -120,9 +120,7 @@ __global__ void k_boxes(const ScoreJob *__restrict__ jobs, float thresh, const f
   int rank = __popc(bal & ((1u << lane) - 1));
   for (int w = 0; w < warp; w++) rank += warp_cnt[w];
   const int idx = block_offsets[blockIdx.y * stride + blockIdx.x] + rank;
-  if (pos2box && i < n) pos2box[J.pos_off + i] = flag ? idx : -1;
   if (!flag) return;
-  if (box2pos) box2pos[idx] = J.pos_off + i;
   const int y = i % J.r0, x = i / J.r0;
   float *P = boxes + (size_t)idx * GL;
   const float scale = J.scale;
@@ -150,12 +148,10 @@ __global__ void k_boxes(const ScoreJob *__restrict__ jobs, float thresh, const f
 }
 
 void launch_boxes(const ScoreJob *d_jobs, int n_jobs, int max_r, float thresh, const float *arena,
-                  const int *arena_i, const int *block_offsets, int stride, int GL, float *boxes, int *pos2box,
-                  int *box2pos, cudaStream_t s) {
+                  const int *arena_i, const int *block_offsets, int stride, int GL, float *boxes, cudaStream_t s) {
   if (n_jobs <= 0) return;
   dim3 grid((max_r + kScoreThreads - 1) / kScoreThreads, n_jobs);
-  k_boxes<<<grid, kScoreThreads, 0, s>>>(d_jobs, thresh, arena, arena_i, block_offsets, stride, GL, boxes, pos2box,
-                                         box2pos);
+  k_boxes<<<grid, kScoreThreads, 0, s>>>(d_jobs, thresh, arena, arena_i, block_offsets, stride, GL, boxes);
 }
 
 // A_SCORE in gather form: target pixel (X, Y) takes the max over every
