@@ -77,6 +77,7 @@ geye_status geye_ctx_create(int device, void *cuda_stream, geye_ctx **out) {
   }
   geye_ctx *ctx = new geye_ctx();
   ctx->device = device;
+  if (const char *e = getenv("GEYE_NO_GRAPHS")) ctx->use_graphs = !(e[0] == '1');
   if (cuda_stream) {
     ctx->stream = reinterpret_cast<cudaStream_t>(cuda_stream);
   } else {

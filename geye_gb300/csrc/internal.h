@@ -159,11 +159,19 @@ void launch_ascore_normalize(float *a_score, int n, const unsigned *max_bits, cu
 // one block per model; model m uses boxes/out at m*cap*GL, scratch at m*cap*6 floats and m*cap*5 ints
 void launch_nms(const float *boxes, const int *d_num, int n_models, int GL, float overlap, int cap,
                 float *scratch_f, int *scratch_i, float *out, int *d_kept, int *err, cudaStream_t s);
-// pipeline NMS (nms_batch.cu): per model nms_model_words(cap) ints of scratch
-// and 5 * cap floats (the boxes in sorted order)
-constexpr int kNmsBatch = 256;
-__host__ __device__ inline size_t nms_model_words(int cap) { return 8 * (size_t)cap + 64 + 5 * kNmsBatch; }
-// diag (optional): per model m, diag[8m..8m+4] = sort cycles, -, batches, picks, fallback rounds used
+// pipeline NMS (nms_sort.cu, nms_batch.cu): per model nms_model_words(cap) ints
+// of scratch and 5 * cap floats (the boxes in sorted order)
+constexpr int kNmsBatch = 256;     // boxes resolved per round
+constexpr int kNmsSegS = 16384;    // sort segments finished in shared memory
+constexpr int kNmsTile = 4096;     // elements per block in the sort's grid-wide partitions
+__host__ __device__ inline int nms_big_cap(int cap) { return cap / kNmsSegS + 2; }
+__host__ __device__ inline int nms_tile_cap(int cap) { return cap / kNmsTile + nms_big_cap(cap) + 1; }
+__host__ __device__ inline size_t nms_model_words(int cap) {
+  const size_t w = 8 * (size_t)cap + 64 + 5 * kNmsBatch + 4 * (size_t)nms_big_cap(cap) + 2 * (size_t)nms_tile_cap(cap);
+  return (w + 31) & ~(size_t)31;
+}
+// diag (optional): per model m, diag[8m+1..8m+4] = sort segments left to the fallback, batches, picks,
+// whether the finish kernel ran rounds itself
 void launch_nms_batch(const float *boxes, const int *d_num, int n_models, int GL, float overlap, int cap, int *si,
                       float *sf, float *out, int *d_kept, int *err, long long *diag, cudaStream_t s);
 void launch_new_rects(const float *kept, const int *d_kept, int GL, int np, const float *coef, int img_w,

@@ -613,7 +613,10 @@ struct StageTimer {
   geye_ctx *ctx;
   explicit StageTimer(geye_ctx *c) : ctx(c) {}
   void mark(int i) {
-    if (ctx->timing) cudaEventRecord(ctx->ev[i], ctx->stream);
+    if (!ctx->timing) return;
+    // inside a capture the record becomes an event-record node of the graph
+    if (ctx->capturing) cudaEventRecordWithFlags(ctx->ev[i], ctx->stream, cudaEventRecordExternal);
+    else cudaEventRecord(ctx->ev[i], ctx->stream);
   }
 };
 
@@ -627,12 +630,15 @@ static geye_status check_launch(geye_ctx *ctx, const char *what) {
   return GEYE_OK;
 }
 
-geye_status run_pyramid(geye_ctx *ctx, Plan &P, const uint8_t *d_bgr, int width_step) {
+geye_status run_ingest(geye_ctx *ctx, Plan &P, const uint8_t *d_bgr, int width_step) {
+  if (injected(ctx, "launch")) { set_error("injected launch failure"); return GEYE_ERR_INJECTED; }
+  launch_ingest(d_bgr, P.width, P.height, width_step, P.arena.as<float>() + P.lv[0].img_off, ctx->stream);
+  return check_launch(ctx, "ingest");
+}
+
+geye_status run_resize(geye_ctx *ctx, Plan &P) {
   cudaStream_t s = ctx->stream;
   float *arena = P.arena.as<float>();
-  if (injected(ctx, "launch")) { set_error("injected launch failure"); return GEYE_ERR_INJECTED; }
-  launch_ingest(d_bgr, P.width, P.height, width_step, arena + P.lv[0].img_off, s);
-  GEYE_TRY(check_launch(ctx, "ingest"));
   for (size_t ph = 0; ph < P.vjobs.size(); ph++) {
     if (P.vjobs[ph].empty()) continue;
     launch_resize_pass(P.d_vjobs[ph].as<ResizeJob>(), (int)P.vjobs[ph].size(), P.v_max_items[ph], 1,
@@ -643,6 +649,11 @@ geye_status run_pyramid(geye_ctx *ctx, Plan &P, const uint8_t *d_bgr, int width_
     GEYE_TRY(check_launch(ctx, "resize (horizontal)"));
   }
   return GEYE_OK;
+}
+
+geye_status run_pyramid(geye_ctx *ctx, Plan &P, const uint8_t *d_bgr, int width_step) {
+  GEYE_TRY(run_ingest(ctx, P, d_bgr, width_step));
+  return run_resize(ctx, P);
 }
 
 geye_status run_hog(geye_ctx *ctx, Plan &P) {
@@ -701,16 +712,22 @@ geye_status run_score(geye_ctx *ctx, Plan &P, ModelPlan &mp, int mi, float thres
   return check_launch(ctx, "boxes");
 }
 
-geye_status run_ascore(geye_ctx *ctx, Plan &P, ModelPlan &mp, int mi, float thresh, const float *h_init) {
+// A_SCORE starts from the caller's map or from ini_ac_score's -100 (detect.cpp:136-145)
+static geye_status ascore_init(geye_ctx *ctx, Plan &P, int mi, const float *h_init) {
   float *a = P.d_ascore.as<float>() + (size_t)mi * P.width * P.height;
   const size_t n = (size_t)P.width * P.height;
   if (h_init) {
     if (injected(ctx, "h2d")) { set_error("injected host-to-device copy failure"); return GEYE_ERR_INJECTED; }
     CUDA_TRY(cudaMemcpyAsync(a, h_init, n * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
-  } else {
-    launch_fill(a, n, -100.0f, ctx->stream);   // ini_ac_score (detect.cpp:136-145)
-    GEYE_TRY(check_launch(ctx, "fill"));
+    return GEYE_OK;
   }
+  launch_fill(a, n, -100.0f, ctx->stream);
+  return check_launch(ctx, "fill");
+}
+
+static geye_status ascore_compute(geye_ctx *ctx, Plan &P, ModelPlan &mp, int mi, float thresh) {
+  float *a = P.d_ascore.as<float>() + (size_t)mi * P.width * P.height;
+  const size_t n = (size_t)P.width * P.height;
   unsigned *maxb = reinterpret_cast<unsigned *>(P.d_small.as<int>() + 64 + mi);
   CUDA_TRY(cudaMemsetAsync(maxb, 0, sizeof(unsigned), ctx->stream));
   launch_ascore(mp.d_score_jobs.as<ScoreJob>(), (int)mp.score_jobs.size(), P.arena.as<float>(), a, P.width,
@@ -718,6 +735,11 @@ geye_status run_ascore(geye_ctx *ctx, Plan &P, ModelPlan &mp, int mi, float thre
   GEYE_TRY(check_launch(ctx, "a_score"));
   launch_ascore_normalize(a, (int)n, maxb, ctx->stream);
   return check_launch(ctx, "a_score normalise");
+}
+
+geye_status run_ascore(geye_ctx *ctx, Plan &P, ModelPlan &mp, int mi, float thresh, const float *h_init) {
+  GEYE_TRY(ascore_init(ctx, P, mi, h_init));
+  return ascore_compute(ctx, P, mp, mi, thresh);
 }
 
 geye_status run_nms(geye_ctx *ctx, Plan &P, int n_models, float overlap) {
@@ -742,14 +764,11 @@ geye_status run_nms(geye_ctx *ctx, Plan &P, int n_models, float overlap) {
   return GEYE_OK;
 }
 
-// Whole path for n models on a frame already on the device.
-geye_status run_frame(geye_ctx *ctx, Plan &P, const uint8_t *d_bgr, int width_step, float thresh, float overlap,
-                      const float *const *h_ascore_init) {
+// Everything after the ingest and the A_SCORE initialisation: plan-static, so
+// it is captured once per (plan, threshold, overlap, timing) as a CUDA graph.
+static geye_status run_body(geye_ctx *ctx, Plan &P, float thresh, float overlap) {
   StageTimer T(ctx);
-  ctx->launches = 0;
-  CUDA_TRY(cudaMemsetAsync(P.d_small.p, 0, 4096, ctx->stream));
-  T.mark(0);
-  GEYE_TRY(run_pyramid(ctx, P, d_bgr, width_step));
+  GEYE_TRY(run_resize(ctx, P));
   T.mark(1);
   GEYE_TRY(run_hog(ctx, P));
   T.mark(2);
@@ -759,11 +778,76 @@ geye_status run_frame(geye_ctx *ctx, Plan &P, const uint8_t *d_bgr, int width_st
   T.mark(4);
   for (size_t mi = 0; mi < P.models.size(); mi++) {
     GEYE_TRY(run_score(ctx, P, *P.models[mi], (int)mi, thresh));
-    GEYE_TRY(run_ascore(ctx, P, *P.models[mi], (int)mi, thresh, h_ascore_init ? h_ascore_init[mi] : nullptr));
+    GEYE_TRY(ascore_compute(ctx, P, *P.models[mi], (int)mi, thresh));
   }
   T.mark(5);
   GEYE_TRY(run_nms(ctx, P, (int)P.models.size(), overlap));
   T.mark(6);
+  return GEYE_OK;
+}
+
+static geye_status run_body_graph(geye_ctx *ctx, Plan &P, float thresh, float overlap) {
+  char key[64];
+  unsigned tb, ob;
+  memcpy(&tb, &thresh, 4);
+  memcpy(&ob, &overlap, 4);
+  snprintf(key, sizeof key, "%08x:%08x:%d", tb, ob, ctx->timing ? 1 : 0);
+  Plan::FrameGraph &g = P.graphs[key];
+  if (!g.exec) {
+    const int before = ctx->launches;
+    cudaGraph_t graph = nullptr;
+    ctx->capturing = true;
+    CUDA_TRY(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeRelaxed));
+    const geye_status st = run_body(ctx, P, thresh, overlap);
+    const cudaError_t e = cudaStreamEndCapture(ctx->stream, &graph);
+    ctx->capturing = false;
+    ctx->launches = before;
+    if (st != GEYE_OK) {
+      if (graph) cudaGraphDestroy(graph);
+      P.graphs.erase(key);
+      return st;
+    }
+    if (e != cudaSuccess) {
+      P.graphs.erase(key);
+      set_error(std::string("frame graph capture: ") + cudaGetErrorString(e));
+      return GEYE_ERR_CUDA;
+    }
+    size_t n = 0;
+    cudaGraphGetNodes(graph, nullptr, &n);
+    std::vector<cudaGraphNode_t> nodes(n);
+    if (n) cudaGraphGetNodes(graph, nodes.data(), &n);
+    int kernels = 0;
+    for (auto nd : nodes) {
+      cudaGraphNodeType t;
+      if (cudaGraphNodeGetType(nd, &t) == cudaSuccess && t == cudaGraphNodeTypeKernel) kernels++;
+    }
+    const cudaError_t ie = cudaGraphInstantiate(&g.exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (ie != cudaSuccess) {
+      g.exec = nullptr;
+      P.graphs.erase(key);
+      set_error(std::string("frame graph instantiate: ") + cudaGetErrorString(ie));
+      return GEYE_ERR_CUDA;
+    }
+    g.kernels = kernels;
+  }
+  CUDA_TRY(cudaGraphLaunch(g.exec, ctx->stream));
+  ctx->launches += g.kernels;
+  return GEYE_OK;
+}
+
+// Whole path for n models on a frame already on the device.
+geye_status run_frame(geye_ctx *ctx, Plan &P, const uint8_t *d_bgr, int width_step, float thresh, float overlap,
+                      const float *const *h_ascore_init) {
+  StageTimer T(ctx);
+  ctx->launches = 0;
+  CUDA_TRY(cudaMemsetAsync(P.d_small.p, 0, 4096, ctx->stream));
+  T.mark(0);
+  GEYE_TRY(run_ingest(ctx, P, d_bgr, width_step));
+  for (size_t mi = 0; mi < P.models.size(); mi++)
+    GEYE_TRY(ascore_init(ctx, P, (int)mi, h_ascore_init ? h_ascore_init[mi] : nullptr));
+  if (ctx->use_graphs) GEYE_TRY(run_body_graph(ctx, P, thresh, overlap));
+  else GEYE_TRY(run_body(ctx, P, thresh, overlap));
   if (ctx->timing) {
     // stage bytes / flops for the roofline report
     double conv_b = 0, conv_f = 0, dt_b = 0, sc_b = 0;

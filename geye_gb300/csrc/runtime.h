@@ -81,6 +81,16 @@ struct Plan {
   double bytes_resize = 0, bytes_hog = 0;
   // last-run results (host)
   std::vector<int> last_D, last_K;
+  // the frame after its ingest, captured as CUDA graphs keyed by threshold, overlap and timing
+  struct FrameGraph {
+    cudaGraphExec_t exec = nullptr;
+    int kernels = 0;
+  };
+  std::map<std::string, FrameGraph> graphs;
+  ~Plan() {
+    for (auto &g : graphs)
+      if (g.second.exec) cudaGraphExecDestroy(g.second.exec);
+  }
 };
 
 }  // namespace geye
@@ -99,6 +109,8 @@ struct geye_ctx {
   double stage_bytes[GEYE_N_STAGES] = {};
   double conv_flops = 0;
   int launches = 0;
+  bool use_graphs = true;   // replay the frame as a CUDA graph (GEYE_NO_GRAPHS=1 at creation: plain launches)
+  bool capturing = false;
   // fault injection (host side)
   std::string inject_op;
   int inject_countdown = 0;
