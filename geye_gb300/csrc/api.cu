@@ -34,26 +34,6 @@ void launch_nms(const float *boxes, const int *d_num, int n_models, int GL, floa
 
 using namespace geye;
 
-#define CUDA_TRY(call)                                                               \
-  do {                                                                               \
-    cudaError_t e_ = (call);                                                         \
-    if (e_ != cudaSuccess) {                                                         \
-      set_error(std::string(#call) + ": " + cudaGetErrorString(e_));                 \
-      return GEYE_ERR_CUDA;                                                          \
-    }                                                                                \
-  } while (0)
-#define GEYE_TRY(call)            \
-  do {                            \
-    geye_status s_ = (call);      \
-    if (s_ != GEYE_OK) return s_; \
-  } while (0)
-#define ARG_CHECK(cond, msg)        \
-  do {                              \
-    if (!(cond)) {                  \
-      set_error(msg);               \
-      return GEYE_ERR_ARG;          \
-    }                               \
-  } while (0)
 
 static thread_local std::string *g_err_ptr = nullptr;
 

@@ -1,12 +1,486 @@
-// conv_bf16.cu -- tensor-core (tcgen05) convolution; see the kernel file header.
+// conv_bf16.cu -- root/part filter convolution on the tcgen05 tensor cores
+// (BF16 operands, FP32 accumulation in tensor memory).
+//
+// Same contraction as conv_fp32.cu (CAR_TRACKING/GPU_function.cu:302-358 and
+// :630-685): C[x][y] = sum_{c, xp, yp} A[c][x+xp][y+yp] * B[c][xp][yp], here
+// as an implicit GEMM without an im2col copy.  A level's features are kept as
+// four channel planes [q][pos][8] bf16 (pos = x*fs0 + y, channels 8q..8q+7),
+// so the 8-channel chunks of consecutive positions lie 16 bytes apart: exactly
+// the row stride of the canonical K-major, no-swizzle operand layout.  For
+// filter tap (xp, yp) the A operand of 128 consecutive output positions p is
+// then the slab rows p + xp*fs0 + yp of the staged planes: one shared-memory
+// descriptor per tap, LBO = the plane stride (next 8 channels), SBO = 128 B
+// (next 8 rows).  Positions whose window crosses a column edge are computed
+// and discarded (about (b0-1)/fs0 of the work).
+//
+// B (the filters) is precomputed per model as [tap][q][n][8] bf16, N padded to
+// a multiple of 16, so one descriptor per (tap, channel pair) as well.
+//
+// A CTA (4 warps) owns a run of 128-position tiles of one (level, filter
+// group): one thread bulk-copies the group's filter bank and the feature slab
+// the run touches (cp.async.bulk, completion on an mbarrier), issues 2 MMAs
+// (M=128, K=16, N=n_pad) per tap into a TMEM accumulator and commits them to
+// a second mbarrier; the four warps read the accumulator back with
+// tcgen05.ld (warp w owns TMEM lanes 32w..32w+31) and write the maps in the
+// reference layout.  Every mbarrier wait is bounded; a timeout sets an error
+// bit and the CTA still waits (bounded) for its own copies and MMAs before it
+// frees TMEM and leaves.
+#include <stdint.h>
+#include <string.h>
+
+#include <cuda_bf16.h>
+
+#include <algorithm>
+
 #include "runtime.h"
 
 namespace geye {
 
+constexpr int kTcThreads = 128;
+constexpr int kTcM = 128;                        // positions per tile (TMEM lanes)
+constexpr int kTcMaxTiles = 16;                  // tiles per CTA
+constexpr size_t kTcSmemBudget = 220 * 1024;     // dynamic shared memory per CTA
+constexpr int kTcHead = 128;                     // barriers + TMEM address at the front
+constexpr unsigned long long kWaitNs = 1000000000ull;   // a wait gives up after 1 s (then 4 s for the drain)
+
+struct TcJob {
+  int plane_off;     // bf16 element offset of plane 0 in arena16
+  int plane_cells;   // cells per plane
+  int fs0, fs1;      // feature rows, columns
+  int b0, b1;        // filter rows, columns
+  int c0, c1;        // output rows, columns
+  int n, n_pad;      // filters; padded to 16 or 32
+  int bank_off;      // byte offset of the group's bank in the model's bank buffer
+  int out_tab;       // first entry of the job's map offsets
+  int ntiles;        // 128-position tiles up to the last valid output
+};
+
+// ---------------------------------------------------------------------------
+// PTX wrappers
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_fence_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+  return t;
+}
+// bounded wait on a phase: false once limit_ns have passed
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, unsigned long long limit_ns) {
+  const unsigned long long t0 = global_ns();
+  while (!mbar_try_wait(bar, parity))
+    if (global_ns() - t0 > limit_ns) return false;
+  return true;
+}
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_u32(dst)),
+               "l"(src), "r"(bytes), "r"(smem_u32(bar))
+               : "memory");
+}
+__device__ __forceinline__ void tmem_alloc(uint32_t *slot, uint32_t ncols) {
+  asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(slot)), "r"(ncols)
+               : "memory");
+  asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
+  asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
+}
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_mma(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                       uint32_t accumulate) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+__device__ __forceinline__ void tc_commit(uint64_t *bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+               : "memory");
+}
+__device__ __forceinline__ void tc_ld16(uint32_t taddr, uint32_t (&r)[16]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+}
+__device__ __forceinline__ void tc_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
+// shared-memory operand descriptor: K-major, no swizzle; lbo = byte distance
+// between the two 8-element K chunks, sbo = between 8-row groups
+__device__ __forceinline__ uint64_t sdesc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+  uint64_t d = (uint64_t)((saddr & 0x3FFFFu) >> 4);
+  d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
+  d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+  d |= (uint64_t)1 << 46;   // descriptor version of tcgen05
+  return d;                 // base offset 0, relative LBO, no swizzle
+}
+
+// instruction descriptor of kind::f16: D = F32, A = B = BF16, both K-major
+__host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+// ---------------------------------------------------------------------------
+// kernel
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kTcThreads, 1) k_conv_tc(const TcJob *__restrict__ jobs, const int4 *__restrict__ chunks,
+                                                           const int *__restrict__ outs,
+                                                           const __nv_bfloat16 *__restrict__ arena16,
+                                                           const uint8_t *__restrict__ bank, float *__restrict__ arena,
+                                                           int *err) {
+  extern __shared__ __align__(128) uint8_t sm[];
+  uint64_t *bar_load = reinterpret_cast<uint64_t *>(sm);
+  uint64_t *bar_mma = reinterpret_cast<uint64_t *>(sm + 8);
+  uint32_t *tslot = reinterpret_cast<uint32_t *>(sm + 16);
+  const int4 ch = chunks[blockIdx.x];
+  const TcJob J = jobs[ch.x];
+  const int tile0 = ch.y, ntile = ch.z, S = ch.w;   // S = slab cells per plane
+  const int taps = J.b0 * J.b1;
+  const uint32_t bank_bytes = (uint32_t)taps * 4u * (uint32_t)J.n_pad * 16u;
+  uint8_t *sB = sm + kTcHead;
+  uint8_t *sA = sB + ((bank_bytes + 127u) & ~127u);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int p_begin = tile0 * kTcM;
+  const uint32_t ncols = J.n_pad <= 16 ? 32u : 64u;   // accumulator columns (power of two >= 32)
+
+  if (threadIdx.x == 0) {
+    mbar_init(bar_load, 1);
+    mbar_init(bar_mma, 1);
+    mbar_fence_init();
+  }
+  if (warp == 0) tmem_alloc(tslot, ncols);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tslot;
+
+  bool ok = true;   // uniform across the CTA (every wait outcome is combined with __syncthreads_and)
+  if (threadIdx.x == 0) {
+    const uint32_t slab_plane = (uint32_t)S * 16u;
+    mbar_expect_tx(bar_load, bank_bytes + 4u * slab_plane);
+    bulk_g2s(sB, bank + J.bank_off, bank_bytes, bar_load);
+    for (int q = 0; q < 4; q++)
+      bulk_g2s(sA + (size_t)q * slab_plane,
+               arena16 + J.plane_off + ((size_t)q * J.plane_cells + (size_t)p_begin) * 8, slab_plane, bar_load);
+  }
+  if (!mbar_wait(bar_load, 0, kWaitNs)) {
+    ok = false;
+    atomicOr(err, 1);
+    mbar_wait(bar_load, 0, 4 * kWaitNs);   // the copies must land before the CTA leaves
+  }
+  ok = __syncthreads_and(ok);
+
+  const uint32_t idesc = idesc_bf16(kTcM, J.n_pad);
+  const uint32_t sA_addr = smem_u32(sA), sB_addr = smem_u32(sB);
+  const uint32_t plane_bytes = (uint32_t)S * 16u, bq = (uint32_t)J.n_pad * 16u;
+  for (int i = 0; i < ntile && ok; i++) {
+    if (threadIdx.x == 0) {
+      tc_fence_after();
+      uint32_t acc = 0;
+      for (int xp = 0; xp < J.b1; xp++)
+        for (int yp = 0; yp < J.b0; yp++) {
+          const uint32_t cell = (uint32_t)(i * kTcM + xp * J.fs0 + yp);
+          const int t = xp * J.b0 + yp;
+          for (int qp = 0; qp < 2; qp++) {
+            const uint64_t ad = sdesc(sA_addr + 2u * qp * plane_bytes + cell * 16u, plane_bytes, 128u);
+            const uint64_t bd = sdesc(sB_addr + (uint32_t)(t * 4 + 2 * qp) * bq, bq, 128u);
+            tc_mma(tmem, ad, bd, idesc, acc);
+            acc = 1;
+          }
+        }
+      tc_commit(bar_mma);
+    }
+    bool done = mbar_wait(bar_mma, (uint32_t)(i & 1), kWaitNs);
+    if (!done) {
+      atomicOr(err, 2);
+      mbar_wait(bar_mma, (uint32_t)(i & 1), 4 * kWaitNs);   // the MMAs must finish before TMEM is freed
+    }
+    ok = __syncthreads_and(done);
+    tc_fence_after();
+    // epilogue: row r of the tile is TMEM lane r; this thread owns row 32*warp + lane
+    const int p = p_begin + i * kTcM + warp * 32 + lane;
+    const int x = p / J.fs0, y = p - x * J.fs0;
+    const bool valid = ok && x < J.c1 && y < J.c0;
+    for (int c0 = 0; c0 < J.n_pad; c0 += 16) {
+      uint32_t r[16];
+      tc_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, r);
+      tc_wait_ld();
+      if (valid) {
+        for (int k = 0; k < 16 && c0 + k < J.n; k++) {
+          float v;
+          memcpy(&v, &r[k], 4);
+          arena[(size_t)outs[J.out_tab + c0 + k] + (size_t)x * J.c0 + y] = v;
+        }
+      }
+    }
+    tc_fence_before();
+    __syncthreads();   // every accumulator read is done before the next tile's MMAs
+  }
+  __syncthreads();
+  if (warp == 0) tmem_dealloc(tmem, ncols);
+}
+
+// feature planes for a standalone call: [pos][32] float -> [4][ncell + pad][8] bf16
+__global__ void k_feat_planes(const float *__restrict__ feat, int ncell, __nv_bfloat16 *__restrict__ planes) {
+  const size_t plane = ((size_t)ncell + kTcPlanePad) * 8;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < ncell + kTcPlanePad; i += gridDim.x * blockDim.x)
+    for (int q = 0; q < 4; q++) {
+      __nv_bfloat162 v[4];
+      for (int k = 0; k < 4; k++) {
+        const float a = i < ncell ? feat[(size_t)i * kFeatPad + 8 * q + 2 * k] : 0.f;
+        const float b = i < ncell ? feat[(size_t)i * kFeatPad + 8 * q + 2 * k + 1] : 0.f;
+        v[k] = __floats2bfloat162_rn(a, b);
+      }
+      *reinterpret_cast<uint4 *>(planes + q * plane + (size_t)i * 8) = *reinterpret_cast<uint4 *>(v);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// host: filter banks and job tables
+// ---------------------------------------------------------------------------
+static uint16_t to_bf16(float f) {   // round to nearest even
+  uint32_t u;
+  memcpy(&u, &f, 4);
+  if ((u & 0x7f800000u) == 0x7f800000u) return (uint16_t)(u >> 16);   // inf / nan
+  const uint32_t lsb = (u >> 16) & 1u;
+  u += 0x7fffu + lsb;
+  return (uint16_t)(u >> 16);
+}
+
+// filters of one size, one bank [tap][q][n_pad][8] bf16 each
+struct BankGroup {
+  int b0, b1, n, n_pad, bank_off, kind;
+  std::vector<int> filt;   // indices into the caller's filter list
+};
+
+// groups filters by (kind, size), at most 32 per group, and lays out their banks
+// (filter f is [31][b1][b0] as conv_fp32 reads it: element (c, xp, yp) at c*b0*b1 + xp*b0 + yp)
+static void build_banks(const std::vector<const float *> &filt, const std::vector<int> &b0s,
+                        const std::vector<int> &b1s, const std::vector<int> &kinds, std::vector<BankGroup> &groups,
+                        std::vector<uint16_t> &bank) {
+  groups.clear();
+  for (size_t f = 0; f < filt.size(); f++) {
+    bool placed = false;
+    for (auto &g : groups)
+      if (g.kind == kinds[f] && g.b0 == b0s[f] && g.b1 == b1s[f] && g.n < 32) {
+        g.filt.push_back((int)f);
+        g.n++;
+        placed = true;
+        break;
+      }
+    if (!placed) groups.push_back(BankGroup{b0s[f], b1s[f], 1, 0, 0, kinds[f], {(int)f}});
+  }
+  size_t total = 0;
+  for (auto &g : groups) {
+    g.n_pad = g.n <= 16 ? 16 : 32;
+    g.bank_off = (int)total;
+    total += (size_t)g.b0 * g.b1 * 4 * g.n_pad * 16;
+  }
+  bank.assign(total / 2, 0);
+  for (auto &g : groups) {
+    uint16_t *dst = bank.data() + g.bank_off / 2;
+    const int taps = g.b0 * g.b1;
+    for (int n = 0; n < g.n; n++) {
+      const float *F = filt[g.filt[n]];
+      for (int xp = 0; xp < g.b1; xp++)
+        for (int yp = 0; yp < g.b0; yp++) {
+          const int t = xp * g.b0 + yp;
+          for (int c = 0; c < kFeat; c++)
+            dst[(((size_t)t * 4 + (c >> 3)) * g.n_pad + n) * 8 + (c & 7)] = to_bf16(F[(size_t)c * taps + t]);
+        }
+    }
+  }
+}
+
+struct TcTables {
+  std::vector<TcJob> jobs;
+  std::vector<int4> chunks;
+  std::vector<int> outs;
+  size_t max_smem = 0;
+};
+
+// one job: group g on a level whose planes start at plane_off; map_off[k] is
+// the float offset of filter k's output map.  False if it cannot fit in shared memory.
+static bool add_tc_job(TcTables &T, int plane_off, int fs0, int fs1, const BankGroup &g,
+                       const std::vector<int> &map_off) {
+  TcJob J{};
+  J.plane_off = plane_off;
+  J.plane_cells = fs0 * fs1 + kTcPlanePad;
+  J.fs0 = fs0; J.fs1 = fs1;
+  J.b0 = g.b0; J.b1 = g.b1;
+  J.c0 = fs0 - g.b0 + 1; J.c1 = fs1 - g.b1 + 1;
+  if (J.c0 < 1 || J.c1 < 1) return false;
+  J.n = g.n; J.n_pad = g.n_pad;
+  J.bank_off = g.bank_off;
+  J.out_tab = (int)T.outs.size();
+  for (int k = 0; k < g.n; k++) T.outs.push_back(map_off[k]);
+  const int P_valid = (J.c1 - 1) * J.fs0 + J.c0;
+  J.ntiles = (P_valid + kTcM - 1) / kTcM;
+  const size_t bank_bytes = ((size_t)g.b0 * g.b1 * 4 * g.n_pad * 16 + 127) & ~(size_t)127;
+  const long long reach = (long long)(g.b1 - 1) * J.fs0 + (g.b0 - 1);
+  // tiles per CTA: as many as the shared-memory budget allows (each tile adds 128 cells x 64 B)
+  const long long room = ((long long)kTcSmemBudget - kTcHead - (long long)bank_bytes - reach * 64) / (kTcM * 64);
+  if (room < 1) return false;
+  const int T_cta = (int)std::min<long long>(room, kTcMaxTiles);
+  const int jid = (int)T.jobs.size();
+  T.jobs.push_back(J);
+  for (int t0 = 0; t0 < J.ntiles; t0 += T_cta) {
+    const int nt = std::min(T_cta, J.ntiles - t0);
+    const int S = nt * kTcM + (int)reach;
+    if ((long long)t0 * kTcM + S > J.plane_cells) return false;   // the slab stays inside its planes
+    T.chunks.push_back(make_int4(jid, t0, nt, S));
+    T.max_smem = std::max(T.max_smem, (size_t)kTcHead + bank_bytes + (size_t)S * 64);
+  }
+  return true;
+}
+
+static void launch_conv_tc(const TcJob *jobs, const int4 *chunks, int n_chunks, const int *outs,
+                           const __nv_bfloat16 *arena16, const uint8_t *bank, float *out, int *err, size_t smem,
+                           cudaStream_t s) {
+  cudaFuncSetAttribute(k_conv_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  k_conv_tc<<<n_chunks, kTcThreads, smem, s>>>(jobs, chunks, outs, arena16, bank, out, err);
+}
+
+// the model's banks (built once per model, roots and parts in separate groups)
+static geye_status ensure_bank(geye_model *m, std::vector<BankGroup> &groups) {
+  const HostModel &h = m->h;
+  std::vector<const float *> filt;
+  std::vector<int> b0s, b1s, kinds;
+  for (int r = 0; r < h.NoR; r++) {
+    filt.push_back(h.rootfilter[r].data());
+    b0s.push_back(h.root_size[3 * r]); b1s.push_back(h.root_size[3 * r + 1]); kinds.push_back(0);
+  }
+  for (int p = 0; p < h.NoP; p++) {
+    filt.push_back(h.partfilter[p].data());
+    b0s.push_back(h.part_size[3 * p]); b1s.push_back(h.part_size[3 * p + 1]); kinds.push_back(1);
+  }
+  std::vector<uint16_t> bank;
+  build_banks(filt, b0s, b1s, kinds, groups, bank);
+  if (m->d_bank16) return GEYE_OK;
+  cudaError_t e = cudaMalloc(&m->d_bank16, std::max<size_t>(bank.size() * 2, 16));
+  if (e == cudaSuccess) e = cudaMemcpy(m->d_bank16, bank.data(), bank.size() * 2, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    set_error(std::string("bf16 filter bank: ") + cudaGetErrorString(e));
+    return GEYE_ERR_CUDA;
+  }
+  m->bank16_bytes = bank.size() * 2;
+  return GEYE_OK;
+}
+
+geye_status build_tc_jobs(geye_ctx *ctx, Plan &P, ModelPlan &mp) {
+  geye_model *m = mp.model;
+  const HostModel &h = m->h;
+  std::vector<BankGroup> groups;
+  GEYE_TRY(ensure_bank(m, groups));
+  TcTables T;
+  const int NoC = h.numcomponent, NoP = h.NoP, interval = h.interval;
+  for (int level = interval; level < mp.LEN; level++) {
+    if (mp.skipped[level]) continue;
+    const int Lv = level - interval;
+    for (auto &g : groups) {
+      std::vector<int> map_off;
+      const bool root = g.kind == 0;
+      for (int f : g.filt) map_off.push_back(root ? mp.root_map_off[level * NoC + f] : mp.part_map_off[Lv * NoP + (f - h.NoR)]);
+      for (int v : map_off)
+        if (v < 0) { set_error("bf16 conv: filter map missing from the plan"); return GEYE_ERR_UNSUPPORTED; }
+      const LevelInfo &L = root ? P.lv[level] : P.lv[Lv];
+      if (!add_tc_job(T, L.feat16_off, L.fs0, L.fs1, g, map_off)) {
+        set_error("bf16 conv: a filter bank and its feature reach exceed shared memory");
+        return GEYE_ERR_UNSUPPORTED;
+      }
+    }
+  }
+  mp.tc_smem = T.max_smem;
+  mp.tc_chunks = (int)T.chunks.size();
+  GEYE_TRY(upload_bytes(ctx, mp.d_tc_jobs, T.jobs.data(), sizeof(TcJob) * T.jobs.size()));
+  GEYE_TRY(upload_bytes(ctx, mp.d_tc_chunks, T.chunks.data(), sizeof(int4) * T.chunks.size()));
+  GEYE_TRY(upload_bytes(ctx, mp.d_tc_outs, T.outs.data(), sizeof(int) * T.outs.size()));
+  return GEYE_OK;
+}
+
 geye_status run_conv_bf16(geye_ctx *ctx, Plan &P, ModelPlan &mp) {
-  (void)ctx; (void)P; (void)mp;
-  set_error("BF16 convolution is not built yet");
-  return GEYE_ERR_UNSUPPORTED;
+  if (mp.tc_chunks == 0) return GEYE_OK;
+  if (!P.arena16.p) {
+    set_error("bf16 conv: the plan has no bf16 feature planes");
+    return GEYE_ERR_UNSUPPORTED;
+  }
+  launch_conv_tc(mp.d_tc_jobs.as<TcJob>(), mp.d_tc_chunks.as<int4>(), mp.tc_chunks, mp.d_tc_outs.as<int>(),
+                 P.arena16.as<__nv_bfloat16>(), reinterpret_cast<const uint8_t *>(mp.model->d_bank16),
+                 P.arena.as<float>(), P.d_small.as<int>() + 130, mp.tc_smem, ctx->stream);
+  ctx->launches++;
+  const cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    set_error(std::string("bf16 conv: ") + cudaGetErrorString(e));
+    return GEYE_ERR_CUDA;
+  }
+  return GEYE_OK;
+}
+
+// fconvsMT on the tensor cores for the stage entry point: d_feat is [pos][32]
+// float on the device (a0 x a1 cells), filters on the host; maps go to
+// d_out + out_off[i].  Temporary device buffers live in tmp.
+geye_status conv_bf16_maps(geye_ctx *ctx, const float *d_feat, int a0, int a1, const float *const *filters,
+                           const int *b_dims, int n_filters, float *d_out, const std::vector<int> &out_off,
+                           std::vector<std::unique_ptr<DevBuf>> &tmp) {
+  std::vector<const float *> filt(filters, filters + n_filters);
+  std::vector<int> b0s, b1s, kinds(n_filters, 0);
+  for (int i = 0; i < n_filters; i++) { b0s.push_back(b_dims[2 * i]); b1s.push_back(b_dims[2 * i + 1]); }
+  std::vector<BankGroup> groups;
+  std::vector<uint16_t> bank;
+  build_banks(filt, b0s, b1s, kinds, groups, bank);
+  TcTables T;
+  for (auto &g : groups) {
+    std::vector<int> map_off;
+    for (int f : g.filt) map_off.push_back(out_off[f]);
+    if (!add_tc_job(T, 0, a0, a1, g, map_off)) {
+      set_error("bf16 conv: a filter bank and its feature reach exceed shared memory");
+      return GEYE_ERR_UNSUPPORTED;
+    }
+  }
+  auto buf = [&]() { tmp.push_back(std::make_unique<DevBuf>()); return tmp.back().get(); };
+  DevBuf *planes = buf(), *d_bank = buf(), *d_jobs = buf(), *d_chunks = buf(), *d_outs = buf(), *d_err = buf();
+  const int ncell = a0 * a1;
+  GEYE_TRY(planes->alloc(ctx, (size_t)4 * (ncell + kTcPlanePad) * 8 * 2));
+  GEYE_TRY(upload_bytes(ctx, *d_bank, bank.data(), bank.size() * 2));
+  GEYE_TRY(upload_bytes(ctx, *d_jobs, T.jobs.data(), sizeof(TcJob) * T.jobs.size()));
+  GEYE_TRY(upload_bytes(ctx, *d_chunks, T.chunks.data(), sizeof(int4) * T.chunks.size()));
+  GEYE_TRY(upload_bytes(ctx, *d_outs, T.outs.data(), sizeof(int) * T.outs.size()));
+  GEYE_TRY(d_err->alloc(ctx, 16));
+  CUDA_TRY(cudaMemsetAsync(d_err->p, 0, 16, ctx->stream));
+  k_feat_planes<<<std::max(1, std::min((ncell + kTcPlanePad + 255) / 256, 1024)), 256, 0, ctx->stream>>>(
+      d_feat, ncell, planes->as<__nv_bfloat16>());
+  launch_conv_tc(d_jobs->as<TcJob>(), d_chunks->as<int4>(), (int)T.chunks.size(), d_outs->as<int>(),
+                 planes->as<__nv_bfloat16>(), d_bank->as<uint8_t>(), d_out, d_err->as<int>(), T.max_smem,
+                 ctx->stream);
+  CUDA_TRY(cudaGetLastError());
+  int errw = 0;
+  CUDA_TRY(cudaMemcpyAsync(&errw, d_err->p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  if (errw) {
+    set_error("bf16 conv: a tensor-core wait ran out (error bits " + std::to_string(errw) + ")");
+    return GEYE_ERR_TIMEOUT;
+  }
+  return GEYE_OK;
 }
 
 }  // namespace geye

@@ -20,6 +20,7 @@ namespace geye {
 constexpr int kFeat = 31;       // HOG channels
 constexpr int kFeatPad = 32;    // channel stride in device feature buffers
 constexpr int kMaxParts = 32;   // parts per component supported by the kernels
+constexpr int kTcPlanePad = 128;   // cells after each bf16 feature plane (reach of a 128-position tile)
 
 // ----------------------------------------------------------------------------
 // job descriptors (device-readable, plain structs)
@@ -41,7 +42,7 @@ struct HogJob {
   int hist_off;            // [18][b1*b0] then norm [b1*b0] at hist_off + 18*b1*b0
   int fs0, fs1;            // output cells
   int feat_off;            // [pos][32] float
-  int feat16_off;          // [pos][32] bf16 (element offset), -1 = not written
+  int feat16_off;          // bf16 planes [4][fs0*fs1 + kTcPlanePad][8] (element offset), -1 = not written
 };
 
 struct ConvJob {           // a block of outputs of one (level, filter group)

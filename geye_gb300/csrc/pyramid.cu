@@ -227,7 +227,8 @@ __global__ void __launch_bounds__(kTB0 *kTB1) k_hog_hist(const HogJob *__restric
 }
 
 // 31 features per output cell (featurepyramid.cpp:421-487), written as 32
-// floats [pos][32] (channel 31 = 0), plus an optional bf16 copy.
+// floats [pos][32] (channel 31 = 0), plus an optional bf16 copy as four
+// channel planes [q][pos][8].
 __global__ void k_hog_feat(const HogJob *__restrict__ jobs, float *__restrict__ arena,
                            __nv_bfloat16 *__restrict__ arena16) {
   const HogJob J = jobs[blockIdx.y];
@@ -281,10 +282,15 @@ __global__ void k_hog_feat(const HogJob *__restrict__ jobs, float *__restrict__ 
     float4 *dst = reinterpret_cast<float4 *>(feat + (size_t)i * kFeatPad);
 #pragma unroll
     for (int q = 0; q < 8; q++) dst[q] = make_float4(out[4 * q], out[4 * q + 1], out[4 * q + 2], out[4 * q + 3]);
-    if (J.feat16_off >= 0 && arena16) {
-      __nv_bfloat162 *d16 = reinterpret_cast<__nv_bfloat162 *>(arena16 + J.feat16_off + (size_t)i * kFeatPad);
+    if (J.feat16_off >= 0 && arena16) {   // planes [q][pos][8] for the tensor-core convolution
+      const size_t plane = ((size_t)ncell + kTcPlanePad) * 8;
 #pragma unroll
-      for (int q = 0; q < 16; q++) d16[q] = __floats2bfloat162_rn(out[2 * q], out[2 * q + 1]);
+      for (int q = 0; q < 4; q++) {
+        __nv_bfloat162 v[4];
+#pragma unroll
+        for (int k = 0; k < 4; k++) v[k] = __floats2bfloat162_rn(out[8 * q + 2 * k], out[8 * q + 2 * k + 1]);
+        *reinterpret_cast<uint4 *>(arena16 + J.feat16_off + q * plane + (size_t)i * 8) = *reinterpret_cast<uint4 *>(v);
+      }
     }
   }
 }

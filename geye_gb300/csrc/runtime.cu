@@ -25,20 +25,7 @@ namespace geye {
 static thread_local std::string g_err;
 void set_error(const std::string &msg) { g_err = msg; }
 
-#define CUDA_TRY(call)                                                                   \
-  do {                                                                                   \
-    cudaError_t e_ = (call);                                                             \
-    if (e_ != cudaSuccess) {                                                             \
-      set_error(std::string(#call) + ": " + cudaGetErrorString(e_));                     \
-      return GEYE_ERR_CUDA;                                                              \
-    }                                                                                    \
-  } while (0)
 
-#define GEYE_TRY(call)                 \
-  do {                                 \
-    geye_status s_ = (call);           \
-    if (s_ != GEYE_OK) return s_;      \
-  } while (0)
 
 static bool injected(geye_ctx *ctx, const char *op) {
   if (!ctx || ctx->inject_countdown <= 0 || ctx->inject_op != op) return false;
@@ -70,6 +57,12 @@ geye_status DevBuf::alloc(geye_ctx *ctx, size_t n) {
     return GEYE_ERR_NOMEM;
   }
   bytes = n;
+  return GEYE_OK;
+}
+
+geye_status upload_bytes(geye_ctx *ctx, DevBuf &buf, const void *src, size_t n) {
+  GEYE_TRY(buf.alloc(ctx, std::max<size_t>(n, 16)));
+  if (n) CUDA_TRY(cudaMemcpyAsync(buf.p, src, n, cudaMemcpyHostToDevice, ctx->stream));
   return GEYE_OK;
 }
 
@@ -407,6 +400,7 @@ static geye_status build_model_plan(geye_ctx *ctx, Plan &P, geye_model *mdl, int
   GEYE_TRY(upload(ctx, mp->d_dt_jobs, mp->dt_jobs));
   GEYE_TRY(upload(ctx, mp->d_score_jobs, mp->score_jobs));
   GEYE_TRY(mp->d_counts.alloc(ctx, sizeof(int) * ((size_t)std::max<size_t>(mp->score_jobs.size(), 1) * std::max(mp->score_stride, 1) + 8)));
+  if (ctx->conv_mode == GEYE_CONV_BF16) GEYE_TRY(build_tc_jobs(ctx, P, *mp));
   P.models.push_back(std::move(mp));
   return GEYE_OK;
 }
@@ -506,10 +500,10 @@ static geye_status build_pyramid_plan(geye_ctx *ctx, Plan &P, int width, int hei
     int b0, b1;
     feature_dims(L.img_h, L.img_w, L.sbin, b0, b1, L.fs0, L.fs1);
     L.feat_off = A.take((size_t)std::max(L.fs0 * L.fs1, 1) * kFeatPad);
-    if (want_bf16) {
+    if (want_bf16) {   // 4 planes [fs0*fs1 + kTcPlanePad][8]
       size_t o = (P.arena16_elems + 63) & ~size_t(63);
       L.feat16_off = (int)o;
-      P.arena16_elems = o + (size_t)std::max(L.fs0 * L.fs1, 1) * kFeatPad + 4096;
+      P.arena16_elems = o + (size_t)4 * ((size_t)L.fs0 * L.fs1 + kTcPlanePad) * 8;
     }
     L.hist_off = A.take((size_t)19 * std::max(b0 * b1, 1));
     if (b0 > 0 && b1 > 0) {
@@ -538,7 +532,11 @@ static geye_status build_pyramid_plan(geye_ctx *ctx, Plan &P, int width, int hei
 static geye_status finish_plan(geye_ctx *ctx, Plan &P, ArenaAlloc &A) {
   P.arena_words = A.words + 64;
   GEYE_TRY(P.arena.alloc(ctx, P.arena_words * 4));
-  if (P.arena16_elems) GEYE_TRY(P.arena16.alloc(ctx, P.arena16_elems * 2));
+  if (P.arena16_elems) {
+    GEYE_TRY(P.arena16.alloc(ctx, P.arena16_elems * 2));
+    // plane tails are read (and their outputs discarded) but never written: keep them zero
+    CUDA_TRY(cudaMemsetAsync(P.arena16.p, 0, P.arena16_elems * 2, ctx->stream));
+  }
   int gl = 0, cap = 0;
   for (auto &mp : P.models) {
     gl = std::max(gl, mp->model->gl());

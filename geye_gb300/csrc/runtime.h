@@ -10,10 +10,44 @@
 
 #include "internal.h"
 
+// status plumbing shared by the host translation units
+#define CUDA_TRY(call)                                                   \
+  do {                                                                   \
+    cudaError_t e_ = (call);                                             \
+    if (e_ != cudaSuccess) {                                             \
+      geye::set_error(std::string(#call) + ": " + cudaGetErrorString(e_)); \
+      return GEYE_ERR_CUDA;                                              \
+    }                                                                    \
+  } while (0)
+#define GEYE_TRY(call)            \
+  do {                            \
+    geye_status s_ = (call);      \
+    if (s_ != GEYE_OK) return s_; \
+  } while (0)
+#define ARG_CHECK(cond, msg)   \
+  do {                         \
+    if (!(cond)) {             \
+      geye::set_error(msg);    \
+      return GEYE_ERR_ARG;     \
+    }                          \
+  } while (0)
+
 namespace geye {
 
 // thread-local error text, set by every failing entry point
 void set_error(const std::string &msg);
+
+struct DevBuf;
+struct Plan;
+struct ModelPlan;
+// copies n bytes from the host into buf (allocated to fit)
+geye_status upload_bytes(geye_ctx *ctx, DevBuf &buf, const void *src, size_t n);
+// tensor-core convolution job tables of one model of a plan (conv_bf16.cu)
+geye_status build_tc_jobs(geye_ctx *ctx, Plan &P, ModelPlan &mp);
+// tensor-core fconvsMT of one feature map ([pos][32] float on the device) for the stage entry point
+geye_status conv_bf16_maps(geye_ctx *ctx, const float *d_feat, int a0, int a1, const float *const *filters,
+                           const int *b_dims, int n_filters, float *d_out, const std::vector<int> &out_off,
+                           std::vector<std::unique_ptr<DevBuf>> &tmp);
 
 // Device buffer owned by a plan or context.
 struct DevBuf {
@@ -55,6 +89,10 @@ struct ModelPlan {
   std::vector<int> part_map_off, part_d0, part_d1;     // [L*NoP + p]
   std::vector<int> skipped;                            // per level
   double conv_flops = 0, conv_bytes = 0, dt_bytes = 0, score_bytes = 0;
+  // tensor-core convolution (conv_bf16.cu): jobs, CTA chunks, map offsets
+  DevBuf d_tc_jobs, d_tc_chunks, d_tc_outs;
+  int tc_chunks = 0;
+  size_t tc_smem = 0;
 };
 
 struct Plan {

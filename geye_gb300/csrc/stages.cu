@@ -26,26 +26,6 @@ const char *last_error_cstr();
 
 using namespace geye;
 
-#define CUDA_TRY(call)                                                               \
-  do {                                                                               \
-    cudaError_t e_ = (call);                                                         \
-    if (e_ != cudaSuccess) {                                                         \
-      set_error(std::string(#call) + ": " + cudaGetErrorString(e_));                 \
-      return GEYE_ERR_CUDA;                                                          \
-    }                                                                                \
-  } while (0)
-#define GEYE_TRY(call)            \
-  do {                            \
-    geye_status s_ = (call);      \
-    if (s_ != GEYE_OK) return s_; \
-  } while (0)
-#define ARG_CHECK(cond, msg) \
-  do {                       \
-    if (!(cond)) {           \
-      set_error(msg);        \
-      return GEYE_ERR_ARG;   \
-    }                        \
-  } while (0)
 
 // scoped temporary device buffers for one stage call
 struct Scratch {
@@ -404,7 +384,14 @@ geye_status geye_fconv(geye_ctx *ctx, const float *feat, const int *a_dims, cons
   ConvJob *d_jobs;
   GEYE_TRY(S.put(jobs.data(), jobs.size(), &d_jobs));
   launch_from_ref_layout(d_ref, a0, a1, arena, ctx->stream);
-  launch_conv_fp32(d_jobs, (int)jobs.size(), mty, mtx, d_filt, d_off, arena, arena, mb0, mb1, 1, ctx->stream);
+  if (ctx->conv_mode == GEYE_CONV_BF16) {
+    std::vector<int> out_off;
+    for (auto &J : jobs) out_off.push_back(J.out_off);
+    std::vector<std::unique_ptr<DevBuf>> tmp;
+    GEYE_TRY(conv_bf16_maps(ctx, arena, a0, a1, filters, b_dims, n_filters, arena, out_off, tmp));
+  } else {
+    launch_conv_fp32(d_jobs, (int)jobs.size(), mty, mtx, d_filt, d_off, arena, arena, mb0, mb1, 1, ctx->stream);
+  }
   CUDA_TRY(cudaGetLastError());
   CUDA_TRY(cudaMemcpyAsync(out, arena + cells * kFeatPad, sizeof(float) * out_words, cudaMemcpyDeviceToHost,
                            ctx->stream));
