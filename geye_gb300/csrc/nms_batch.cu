@@ -33,6 +33,7 @@ constexpr int kBatch = kNmsBatch;
 constexpr int kBW = kBatch / 32;   // words of a suppression row
 constexpr int kPassNT = 256;
 constexpr int kRounds = 8;         // resolve/pass rounds launched before the finish kernel
+constexpr int kRankSortMax = 4096; // kept boxes ordered by ranking in shared memory up to this many
 
 // ---------------------------------------------------------------------------
 // 2. sorted boxes and the alive bitmap
@@ -279,31 +280,48 @@ __global__ void __launch_bounds__(kSortNT) k_nms_finish(const float *__restrict_
   }
   const int npk = st.npicks;
   const int K = npk - ((npk > 0 && S.flag[npk - 1] == 0) ? 1 : 0);
-  int *keep = S.Rpos;
-  for (int i = threadIdx.x; i < D; i += kSortNT) keep[i] = 0;
-  __syncthreads();
-  for (int k = threadIdx.x; k < K; k += kSortNT) keep[S.ord[S.picks[k]]] = 1;
-  __syncthreads();
   int written = 0;
-  for (int base = 0; base < D; base += kSortNT) {
-    const int i = base + threadIdx.x;
-    const int f = i < D && keep[i];
-    const unsigned bal = __ballot_sync(0xffffffffu, f);
-    if (lane == 0) wcnt[warp] = __popc(bal);
+  if (K <= kRankSortMax) {
+    // few kept boxes: their input indices ranked in shared memory (all distinct)
+    static_assert(sizeof(ResolveSmem) >= sizeof(int) * kRankSortMax, "rank buffer");
+    int *idx = reinterpret_cast<int *>(&R);   // the round's buffers are free now
+    for (int k = threadIdx.x; k < K; k += kSortNT) idx[k] = S.ord[S.picks[k]];
     __syncthreads();
-    int before = 0, tot = 0;
-    for (int w = 0; w < kSortNT / 32; w++) {
-      const int c = wcnt[w];
-      if (w < warp) before += c;
-      tot += c;
-    }
-    if (f) {
-      const float *P = boxes + (size_t)i * GL;
-      float *Q = out + (size_t)(written + before + __popc(bal & ((1u << lane) - 1))) * GL;
+    for (int k = threadIdx.x; k < K; k += kSortNT) {
+      const int v = idx[k];
+      int rank = 0;
+      for (int j = 0; j < K; j++) rank += idx[j] < v;
+      const float *P = boxes + (size_t)v * GL;
+      float *Q = out + (size_t)rank * GL;
       for (int t = 0; t < GL; t++) Q[t] = P[t];
     }
-    written += tot;
+    written = K;
+  } else {
+    int *keep = S.Rpos;
+    for (int i = threadIdx.x; i < D; i += kSortNT) keep[i] = 0;
     __syncthreads();
+    for (int k = threadIdx.x; k < K; k += kSortNT) keep[S.ord[S.picks[k]]] = 1;
+    __syncthreads();
+    for (int base = 0; base < D; base += kSortNT) {
+      const int i = base + threadIdx.x;
+      const int f = i < D && keep[i];
+      const unsigned bal = __ballot_sync(0xffffffffu, f);
+      if (lane == 0) wcnt[warp] = __popc(bal);
+      __syncthreads();
+      int before = 0, tot = 0;
+      for (int w = 0; w < kSortNT / 32; w++) {
+        const int c = wcnt[w];
+        if (w < warp) before += c;
+        tot += c;
+      }
+      if (f) {
+        const float *P = boxes + (size_t)i * GL;
+        float *Q = out + (size_t)(written + before + __popc(bal & ((1u << lane) - 1))) * GL;
+        for (int t = 0; t < GL; t++) Q[t] = P[t];
+      }
+      written += tot;
+      __syncthreads();
+    }
   }
   if (threadIdx.x == 0) {
     d_kept[m] = written;

@@ -125,9 +125,16 @@ struct Plan {
     int kernels = 0;
   };
   std::map<std::string, FrameGraph> graphs;
+  // asynchronous submission (serve.cu): pinned frame staging, pinned result
+  // block (counts, then per model kHostRes records) and the completion event
+  void *h_bgr = nullptr, *h_res = nullptr;
+  cudaEvent_t ev_done = nullptr;
   ~Plan() {
     for (auto &g : graphs)
       if (g.second.exec) cudaGraphExecDestroy(g.second.exec);
+    if (h_bgr) cudaFreeHost(h_bgr);
+    if (h_res) cudaFreeHost(h_res);
+    if (ev_done) cudaEventDestroy(ev_done);
   }
 };
 
@@ -159,6 +166,8 @@ struct geye_ctx {
   size_t h_pinned_bytes = 0;
   // last device-resident run
   geye::Plan *last_plan = nullptr;
+  // frame submitted with geye_detect_submit and not collected yet
+  geye::Plan *pending = nullptr;
   // live models (detached when the context goes away first)
   std::set<geye_model *> models;
 };

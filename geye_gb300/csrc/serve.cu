@@ -1,0 +1,446 @@
+// serve.cu -- asynchronous frame submission and the multi-stream detection
+// server (no counterpart in the reference, whose car_detection handles one
+// frame at a time from main.cpp's loop).
+//
+// A context is a slot: geye_detect_submit stages a frame through pinned
+// memory, replays the frame graph on the context's stream and queues the
+// result copies; a completion event tells when it is done.  The server keeps a
+// pool of slots and a FIFO of submitted frames.  A frame goes to a free slot
+// that already holds a plan for its size, else to a free slot that gets one,
+// else to a new slot while the device memory held by slots stays within the
+// budget.  Frames in different slots overlap on the GPU; a stream's frames are
+// dispatched in submission order and its tracker updates are chained with
+// events so they run in that order too.
+#include <stdlib.h>
+#include <string.h>
+
+#include <algorithm>
+#include <chrono>
+#include <deque>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "runtime.h"
+#include "tracker.h"
+
+namespace geye {
+geye_status run_frame(geye_ctx *ctx, Plan &P, const uint8_t *d_bgr, int width_step, float thresh, float overlap,
+                      const float *const *h_ascore_init);
+geye_status frame_plan(geye_ctx *ctx, geye_model *const *models, int n, int w, int h, Plan **out);
+size_t plan_device_bytes(const Plan &P);
+
+constexpr int kHostRes = 4096;   // records per model returned through pinned memory
+
+// pinned result block: ints [0, 32) boxes before NMS per model, [32, 64) kept
+// per model, then per model point[4R], or_point[4R], type[R], scale[R], score[R]
+static size_t res_block_ints(int n_models) { return 64 + (size_t)n_models * 11 * kHostRes; }
+
+static long long now_ns() {
+  return std::chrono::duration_cast<std::chrono::nanoseconds>(std::chrono::steady_clock::now().time_since_epoch())
+      .count();
+}
+
+// queue everything of one frame on the context's stream (the frame already in P.h_bgr)
+static geye_status enqueue_frame(geye_ctx *ctx, Plan &P, float thresh, float overlap, TrackerSet *trk, int stream,
+                                 cudaEvent_t after, cudaEvent_t tracked) {
+  const int n_models = (int)P.models.size();
+  CUDA_TRY(cudaMemcpyAsync(P.d_bgr.p, P.h_bgr, (size_t)3 * P.width * P.height, cudaMemcpyHostToDevice, ctx->stream));
+  GEYE_TRY(run_frame(ctx, P, P.d_bgr.as<uint8_t>(), 3 * P.width, thresh, overlap, nullptr));
+  if (trk) {
+    if (after) CUDA_TRY(cudaStreamWaitEvent(ctx->stream, after, 0));
+    GEYE_TRY(tracker_update(*trk, stream, P.d_result.as<int>(), P.max_cap, P.d_small.as<int>() + 32, n_models,
+                            ctx->stream));
+    CUDA_TRY(cudaEventRecord(tracked, ctx->stream));
+  }
+  int *h = static_cast<int *>(P.h_res);
+  CUDA_TRY(cudaMemcpyAsync(h, P.d_small.p, sizeof(int) * 64, cudaMemcpyDeviceToHost, ctx->stream));
+  const size_t R = (size_t)std::min(P.max_cap, kHostRes);
+  for (int mi = 0; mi < n_models; mi++) {
+    const int *res = P.d_result.as<int>() + (size_t)mi * P.max_cap * 11;
+    int *dst = h + 64 + (size_t)mi * 11 * kHostRes;
+    CUDA_TRY(cudaMemcpyAsync(dst, res, sizeof(int) * 4 * R, cudaMemcpyDeviceToHost, ctx->stream));
+    CUDA_TRY(cudaMemcpyAsync(dst + 4 * kHostRes, res + 4 * (size_t)P.max_cap, sizeof(int) * 4 * R,
+                             cudaMemcpyDeviceToHost, ctx->stream));
+    for (int f = 8; f < 11; f++)   // type, scale, score (max_cap apart on the device, kHostRes apart here)
+      CUDA_TRY(cudaMemcpyAsync(dst + f * kHostRes, res + f * (size_t)P.max_cap, sizeof(int) * R,
+                               cudaMemcpyDeviceToHost, ctx->stream));
+  }
+  CUDA_TRY(cudaEventRecord(P.ev_done, ctx->stream));
+  ctx->pending = &P;
+  return GEYE_OK;
+}
+
+static geye_status ensure_staging(Plan &P) {
+  const int n_models = (int)P.models.size();
+  if (!P.h_bgr) CUDA_TRY(cudaMallocHost(&P.h_bgr, (size_t)3 * P.width * P.height));
+  if (!P.h_res) CUDA_TRY(cudaMallocHost(&P.h_res, sizeof(int) * res_block_ints(n_models)));
+  if (!P.ev_done) CUDA_TRY(cudaEventCreateWithFlags(&P.ev_done, cudaEventDisableTiming));
+  return GEYE_OK;
+}
+
+static geye_status collect_frame(geye_ctx *ctx, geye_result *out) {
+  Plan &P = *ctx->pending;
+  CUDA_TRY(cudaEventSynchronize(P.ev_done));
+  const int n_models = (int)P.models.size();
+  const int *h = static_cast<const int *>(P.h_res);
+  geye_status st = GEYE_OK;
+  for (int mi = 0; mi < n_models && out; mi++) {
+    const int K = h[32 + mi];
+    geye_result &r = out[mi];
+    memset(&r, 0, sizeof(r));
+    r.num = K;
+    const size_t k = std::max(K, 1);
+    r.point = (int *)malloc(sizeof(int) * 4 * k);
+    r.or_point = (int *)malloc(sizeof(int) * 4 * k);
+    r.type = (int *)malloc(sizeof(int) * k);
+    r.scale = (float *)malloc(sizeof(float) * k);
+    r.score = (float *)malloc(sizeof(float) * k);
+    if (!r.point || !r.or_point || !r.type || !r.scale || !r.score) {
+      set_error("host allocation failed");
+      st = GEYE_ERR_NOMEM;
+      continue;
+    }
+    const int *src = h + 64 + (size_t)mi * 11 * kHostRes;
+    const int n = std::min(K, kHostRes);
+    memcpy(r.point, src, sizeof(int) * 4 * n);
+    memcpy(r.or_point, src + 4 * kHostRes, sizeof(int) * 4 * n);
+    memcpy(r.type, src + 8 * kHostRes, sizeof(int) * n);
+    memcpy(r.scale, src + 9 * kHostRes, sizeof(float) * n);
+    memcpy(r.score, src + 10 * kHostRes, sizeof(float) * n);
+    if (K > n) {   // more kept boxes than the pinned block holds: the rest straight from the device
+      const int *res = P.d_result.as<int>() + (size_t)mi * P.max_cap * 11;
+      const size_t rest = (size_t)(K - n);
+      CUDA_TRY(cudaMemcpy(r.point + 4 * n, res + 4 * n, sizeof(int) * 4 * rest, cudaMemcpyDeviceToHost));
+      CUDA_TRY(cudaMemcpy(r.or_point + 4 * n, res + 4 * (size_t)P.max_cap + 4 * n, sizeof(int) * 4 * rest,
+                          cudaMemcpyDeviceToHost));
+      CUDA_TRY(cudaMemcpy(r.type + n, res + 8 * (size_t)P.max_cap + n, sizeof(int) * rest, cudaMemcpyDeviceToHost));
+      CUDA_TRY(cudaMemcpy(r.scale + n, res + 9 * (size_t)P.max_cap + n, sizeof(float) * rest,
+                          cudaMemcpyDeviceToHost));
+      CUDA_TRY(cudaMemcpy(r.score + n, res + 10 * (size_t)P.max_cap + n, sizeof(float) * rest,
+                          cudaMemcpyDeviceToHost));
+    }
+  }
+  P.last_D.assign(h, h + n_models);
+  P.last_K.assign(h + 32, h + 32 + n_models);
+  ctx->last_plan = &P;
+  ctx->pending = nullptr;
+  return st;
+}
+
+}  // namespace geye
+
+using namespace geye;
+
+extern "C" {
+
+geye_status geye_detect_submit(geye_ctx *ctx, geye_model *const *models, int n_models, const uint8_t *bgr, int width,
+                               int height, int width_step, float thresh, float overlap) {
+  ARG_CHECK(ctx && models && bgr && n_models > 0, "null argument");
+  ARG_CHECK(width >= 16 && height >= 16 && width_step >= 3 * width, "bad frame size");
+  ARG_CHECK(!ctx->pending, "a submitted frame has not been collected");
+  for (int i = 0; i < n_models; i++) ARG_CHECK(models[i], "null model");
+  CUDA_TRY(cudaSetDevice(ctx->device));
+  Plan *P = nullptr;
+  GEYE_TRY(frame_plan(ctx, models, n_models, width, height, &P));
+  GEYE_TRY(ensure_staging(*P));
+  uint8_t *dst = static_cast<uint8_t *>(P->h_bgr);
+  for (int y = 0; y < height; y++) memcpy(dst + (size_t)y * 3 * width, bgr + (size_t)y * width_step, (size_t)3 * width);
+  return enqueue_frame(ctx, *P, thresh, overlap, nullptr, 0, nullptr, nullptr);
+}
+
+geye_status geye_detect_query(geye_ctx *ctx) {
+  ARG_CHECK(ctx && ctx->pending, "no submitted frame");
+  const cudaError_t e = cudaEventQuery(ctx->pending->ev_done);
+  if (e == cudaSuccess) return GEYE_OK;
+  if (e == cudaErrorNotReady) return GEYE_BUSY;
+  set_error(std::string("detect_query: ") + cudaGetErrorString(e));
+  return GEYE_ERR_CUDA;
+}
+
+geye_status geye_detect_collect(geye_ctx *ctx, geye_result *out) {
+  ARG_CHECK(ctx && ctx->pending && out, "no submitted frame or null output");
+  return collect_frame(ctx, out);
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// server
+// ---------------------------------------------------------------------------
+struct geye_server {
+  int device = 0;
+  std::vector<geye_model *> models;
+  geye_conv_mode mode = GEYE_CONV_BF16;
+  size_t budget = 0, held = 0;
+  int max_slots = 1;
+  float thresh = -0.5f, overlap = 0.5f;
+  bool track = false;
+  struct Slot {
+    geye_ctx *ctx = nullptr;
+    bool busy = false;
+    int w = 0, h = 0;               // size of the plan the slot holds
+    size_t bytes = 0;
+    long long ticket = 0, t_submit = 0, t_dispatch = 0;
+    int stream = 0;
+    cudaEvent_t tracked = nullptr;  // this frame's tracker update
+  };
+  std::vector<Slot> slots;
+  struct Req {
+    long long ticket, t_submit;
+    int stream, w, h;
+    std::vector<uint8_t> bgr;
+  };
+  std::deque<Req> queue;
+  struct Done {
+    geye_served info;
+    std::vector<geye_result> res;
+  };
+  std::deque<Done> done;
+  long long next_ticket = 1, completed = 0;
+  geye::TrackerSet trk;
+  std::map<int, cudaEvent_t> last_tracked;   // per stream: the event of its latest dispatched tracker update
+  std::map<int, long long> stream_busy;      // per stream: frames dispatched and not finished
+};
+
+namespace {
+
+geye_status new_slot(geye_server *s, int *idx) {
+  geye_ctx *c = nullptr;
+  GEYE_TRY(geye_ctx_create(s->device, nullptr, &c));
+  geye_status st = geye_ctx_set_conv_mode(c, s->mode);
+  if (st != GEYE_OK) { geye_ctx_destroy(c); return st; }
+  geye_server::Slot sl;
+  sl.ctx = c;
+  if (cudaEventCreateWithFlags(&sl.tracked, cudaEventDisableTiming) != cudaSuccess) {
+    geye_ctx_destroy(c);
+    set_error("server: event creation failed");
+    return GEYE_ERR_CUDA;
+  }
+  s->slots.push_back(sl);
+  *idx = (int)s->slots.size() - 1;
+  return GEYE_OK;
+}
+
+// dispatch the queue head into a slot; false when nothing fits right now
+geye_status dispatch_one(geye_server *s, bool *dispatched) {
+  *dispatched = false;
+  if (s->queue.empty()) return GEYE_OK;
+  geye_server::Req &r = s->queue.front();
+  int pick = -1;
+  for (size_t i = 0; i < s->slots.size() && pick < 0; i++)
+    if (!s->slots[i].busy && s->slots[i].w == r.w && s->slots[i].h == r.h) pick = (int)i;
+  if (pick < 0)   // a free slot whose plan (if any) is dropped for this size
+    for (size_t i = 0; i < s->slots.size() && pick < 0; i++)
+      if (!s->slots[i].busy && s->held < s->budget) pick = (int)i;
+  if (pick < 0 && (int)s->slots.size() < s->max_slots && s->held < s->budget) GEYE_TRY(new_slot(s, &pick));
+  if (pick < 0) return GEYE_OK;
+  geye_server::Slot &sl = s->slots[pick];
+  if (sl.w != r.w || sl.h != r.h) {   // rebuild for the new size: the old plan's memory goes back
+    sl.ctx->plans.clear();
+    sl.ctx->last_plan = nullptr;
+    s->held -= sl.bytes;
+    sl.bytes = 0;
+  }
+  Plan *P = nullptr;
+  GEYE_TRY(frame_plan(sl.ctx, s->models.data(), (int)s->models.size(), r.w, r.h, &P));
+  GEYE_TRY(ensure_staging(*P));
+  if (sl.w != r.w || sl.h != r.h) {
+    sl.w = r.w;
+    sl.h = r.h;
+    sl.bytes = plan_device_bytes(*P);
+    s->held += sl.bytes;
+  }
+  memcpy(P->h_bgr, r.bgr.data(), r.bgr.size());
+  cudaEvent_t after = nullptr;
+  auto it = s->last_tracked.find(r.stream);
+  if (it != s->last_tracked.end() && s->stream_busy[r.stream] > 0) after = it->second;
+  GEYE_TRY(enqueue_frame(sl.ctx, *P, s->thresh, s->overlap, s->track ? &s->trk : nullptr, r.stream, after,
+                         sl.tracked));
+  s->last_tracked[r.stream] = sl.tracked;
+  s->stream_busy[r.stream]++;
+  sl.busy = true;
+  sl.ticket = r.ticket;
+  sl.stream = r.stream;
+  sl.t_submit = r.t_submit;
+  sl.t_dispatch = now_ns();
+  s->queue.pop_front();
+  *dispatched = true;
+  return GEYE_OK;
+}
+
+geye_status pump(geye_server *s) {
+  for (;;) {
+    bool d = false;
+    GEYE_TRY(dispatch_one(s, &d));
+    if (!d) return GEYE_OK;
+  }
+}
+
+geye_status complete(geye_server *s, geye_server::Slot &sl) {
+  geye_server::Done d;
+  d.res.resize(s->models.size());
+  GEYE_TRY(collect_frame(sl.ctx, d.res.data()));
+  const long long t = now_ns();
+  d.info.ticket = sl.ticket;
+  d.info.stream = sl.stream;
+  d.info.queued_ns = sl.t_dispatch - sl.t_submit;
+  d.info.latency_ns = t - sl.t_submit;
+  d.info.n_tracks = s->track ? tracker_count(s->trk, sl.stream) : 0;
+  s->done.push_back(std::move(d));
+  s->stream_busy[sl.stream]--;
+  sl.busy = false;
+  s->completed++;
+  return GEYE_OK;
+}
+
+geye_status reap(geye_server *s, bool block) {
+  for (auto &sl : s->slots) {
+    if (!sl.busy) continue;
+    const cudaError_t e = block ? cudaEventSynchronize(sl.ctx->pending->ev_done) : cudaEventQuery(sl.ctx->pending->ev_done);
+    if (e == cudaErrorNotReady) continue;
+    if (e != cudaSuccess) {
+      set_error(std::string("server: ") + cudaGetErrorString(e));
+      return GEYE_ERR_CUDA;
+    }
+    GEYE_TRY(complete(s, sl));
+  }
+  return GEYE_OK;
+}
+
+}  // namespace
+
+namespace geye {
+size_t plan_device_bytes(const Plan &P) {
+  size_t b = P.arena.bytes + P.arena16.bytes + P.d_bgr.bytes + P.d_boxes.bytes + P.d_kept_boxes.bytes +
+             P.d_nms_f.bytes + P.d_nms_i.bytes + P.d_small.bytes + P.d_ascore.bytes + P.d_result.bytes;
+  for (auto &mp : P.models)
+    b += mp->d_root_jobs.bytes + mp->d_part_jobs.bytes + mp->d_dt_jobs.bytes + mp->d_score_jobs.bytes +
+         mp->d_counts.bytes + mp->d_tc_jobs.bytes + mp->d_tc_chunks.bytes + mp->d_tc_outs.bytes;
+  return b;
+}
+}  // namespace geye
+
+extern "C" {
+
+geye_status geye_server_create(int device, geye_model *const *models, int n_models, geye_conv_mode mode,
+                               size_t hbm_budget, int max_slots, float thresh, float overlap, int track,
+                               geye_server **out) {
+  ARG_CHECK(out && models && n_models > 0 && max_slots > 0, "bad argument");
+  for (int i = 0; i < n_models; i++) ARG_CHECK(models[i], "null model");
+  CUDA_TRY(cudaSetDevice(device));
+  geye_server *s = new geye_server();
+  s->device = device;
+  s->models.assign(models, models + n_models);
+  s->mode = mode;
+  s->budget = hbm_budget;
+  s->max_slots = max_slots;
+  s->thresh = thresh;
+  s->overlap = overlap;
+  s->track = track != 0;
+  if (s->track) {
+    const geye_status st = tracker_init(s->trk, 0x5eed5eedull);
+    if (st != GEYE_OK) { delete s; return st; }
+  }
+  *out = s;
+  return GEYE_OK;
+}
+
+geye_status geye_server_destroy(geye_server *s) {
+  if (!s) return GEYE_OK;
+  cudaSetDevice(s->device);
+  for (auto &sl : s->slots) {
+    if (sl.ctx) cudaStreamSynchronize(sl.ctx->stream);
+  }
+  for (auto &d : s->done)
+    for (auto &r : d.res) geye_result_free(&r);
+  for (auto &sl : s->slots) {
+    if (sl.tracked) cudaEventDestroy(sl.tracked);
+    geye_ctx_destroy(sl.ctx);
+  }
+  tracker_free(s->trk);
+  delete s;
+  return GEYE_OK;
+}
+
+geye_status geye_server_submit(geye_server *s, int stream, const uint8_t *bgr, int width, int height, int width_step,
+                               long long *ticket) {
+  ARG_CHECK(s && bgr && ticket, "null argument");
+  ARG_CHECK(width >= 16 && height >= 16 && width_step >= 3 * width, "bad frame size");
+  ARG_CHECK(stream >= 0 && stream < kTrackerStreams, "stream id out of range");
+  CUDA_TRY(cudaSetDevice(s->device));
+  geye_server::Req r;
+  r.ticket = s->next_ticket++;
+  r.t_submit = now_ns();
+  r.stream = stream;
+  r.w = width;
+  r.h = height;
+  r.bgr.resize((size_t)3 * width * height);
+  for (int y = 0; y < height; y++)
+    memcpy(r.bgr.data() + (size_t)y * 3 * width, bgr + (size_t)y * width_step, (size_t)3 * width);
+  *ticket = r.ticket;
+  s->queue.push_back(std::move(r));
+  GEYE_TRY(reap(s, false));
+  return pump(s);
+}
+
+geye_status geye_server_poll(geye_server *s, int max, geye_served *info, geye_result *results, int *n) {
+  ARG_CHECK(s && n && (max == 0 || info), "null argument");
+  CUDA_TRY(cudaSetDevice(s->device));
+  GEYE_TRY(reap(s, false));
+  GEYE_TRY(pump(s));
+  int k = 0;
+  while (k < max && !s->done.empty()) {
+    geye_server::Done &d = s->done.front();
+    info[k] = d.info;
+    for (size_t m = 0; m < d.res.size(); m++) {
+      if (results) results[(size_t)k * s->models.size() + m] = d.res[m];
+      else geye_result_free(&d.res[m]);
+    }
+    s->done.pop_front();
+    k++;
+  }
+  *n = k;
+  return GEYE_OK;
+}
+
+geye_status geye_server_drain(geye_server *s) {
+  ARG_CHECK(s, "null server");
+  CUDA_TRY(cudaSetDevice(s->device));
+  for (int guard = 0; guard < 1 << 30; guard++) {
+    GEYE_TRY(pump(s));
+    bool busy = false;
+    for (auto &sl : s->slots) busy |= sl.busy;
+    if (!busy && s->queue.empty()) return GEYE_OK;
+    GEYE_TRY(reap(s, true));
+  }
+  set_error("server drain did not finish");
+  return GEYE_ERR_TIMEOUT;
+}
+
+geye_status geye_server_stats(geye_server *s, long long out[8]) {
+  ARG_CHECK(s && out, "null argument");
+  long long busy = 0;
+  for (auto &sl : s->slots) busy += sl.busy;
+  out[0] = (long long)s->slots.size();
+  out[1] = busy;
+  out[2] = (long long)s->queue.size();
+  out[3] = (long long)s->done.size();
+  out[4] = (long long)s->held;
+  out[5] = s->completed;
+  out[6] = s->track ? tracker_streams(s->trk) : 0;
+  out[7] = 0;
+  return GEYE_OK;
+}
+
+geye_status geye_server_tracks(geye_server *s, int stream, int max, float *boxes, int *n) {
+  ARG_CHECK(s && n && (max == 0 || boxes), "null argument");
+  ARG_CHECK(s->track, "the server was created without trackers");
+  ARG_CHECK(stream >= 0 && stream < kTrackerStreams, "stream id out of range");
+  CUDA_TRY(cudaSetDevice(s->device));
+  for (auto &sl : s->slots)
+    if (sl.ctx) CUDA_TRY(cudaStreamSynchronize(sl.ctx->stream));
+  return tracker_read(s->trk, stream, max, boxes, n);
+}
+
+}  // extern "C"

@@ -26,7 +26,7 @@ import numpy as np
 
 from . import build as _build
 
-__all__ = ["GeyeError", "Context", "Model", "lib", "symbols"]
+__all__ = ["GeyeError", "Context", "Model", "Server", "lib", "symbols"]
 
 _lib = None
 
@@ -74,6 +74,16 @@ def lib(build_if_missing: bool = True):
             "geye_debug_inject_fault": [vp, C.c_char_p, i32],
             "geye_nms_noalloc": [vp, i32, i32, C.c_float, vp, vp, vp],
             "geye_ctx_debug_counters": [vp, vp, i32],
+            "geye_detect_submit": [vp, vp, i32, vp, i32, i32, i32, C.c_float, C.c_float],
+            "geye_detect_query": [vp],
+            "geye_detect_collect": [vp, vp],
+            "geye_server_create": [i32, vp, i32, i32, C.c_size_t, i32, C.c_float, C.c_float, i32, C.POINTER(vp)],
+            "geye_server_destroy": [vp],
+            "geye_server_submit": [vp, i32, vp, i32, i32, i32, C.POINTER(C.c_longlong)],
+            "geye_server_poll": [vp, i32, vp, vp, ip],
+            "geye_server_drain": [vp],
+            "geye_server_stats": [vp, vp],
+            "geye_server_tracks": [vp, i32, i32, vp, ip],
         }
         for name, args in sig.items():
             f = getattr(L, name)
@@ -186,6 +196,28 @@ class Context:
         if A_SCOREs is not None:
             ap = (C.c_void_p * n)(*[_p(a) for a in A_SCOREs])
         _check(lib().geye_detect_multi(self.h, arr, n, _p(fr), w, h, 3 * w, thresh, overlap, ap, res), "detect_multi")
+        return [_result_to_dict(res[i]) for i in range(n)]
+
+    # ---- asynchronous submission ------------------------------------------
+    def detect_submit(self, frame: np.ndarray, models: list, thresh: float = -0.5, overlap: float = 0.5):
+        fr = np.ascontiguousarray(frame, dtype=np.uint8)
+        h, w, _ = fr.shape
+        arr = (C.c_void_p * len(models))(*[m.h for m in models])
+        _check(lib().geye_detect_submit(self.h, arr, len(models), _p(fr), w, h, 3 * w, thresh, overlap),
+               "detect_submit")
+        self._submitted = len(models)
+
+    def detect_done(self) -> bool:
+        st = lib().geye_detect_query(self.h)
+        if st == 8:   # GEYE_BUSY
+            return False
+        _check(st, "detect_query")
+        return True
+
+    def detect_collect(self) -> list:
+        n = getattr(self, "_submitted", 0)
+        res = (_Result * max(n, 1))()
+        _check(lib().geye_detect_collect(self.h, res), "detect_collect")
         return [_result_to_dict(res[i]) for i in range(n)]
 
     # ---- stages -----------------------------------------------------------
@@ -335,6 +367,72 @@ class Context:
 
     def inject_fault(self, op: str | None, nth: int):
         _check(lib().geye_debug_inject_fault(self.h, op.encode() if op else None, nth), "inject_fault")
+
+
+class _Served(C.Structure):
+    _fields_ = [("ticket", C.c_longlong), ("stream", C.c_int), ("n_tracks", C.c_int), ("queued_ns", C.c_longlong),
+                ("latency_ns", C.c_longlong)]
+
+
+class Server:
+    """Multi-stream detection server (geye_server_*): frames are admitted into
+    slots as they arrive and overlap on the GPU; optional per-stream trackers."""
+
+    def __init__(self, models: list, conv: int = CONV_BF16, hbm_budget: int = 40 << 30, max_slots: int = 16,
+                 thresh: float = -0.5, overlap: float = 0.5, track: bool = False, device: int = 0):
+        h = C.c_void_p()
+        arr = (C.c_void_p * len(models))(*[m.h for m in models])
+        _check(lib().geye_server_create(device, arr, len(models), conv, hbm_budget, max_slots, thresh, overlap,
+                                        1 if track else 0, C.byref(h)), "server_create")
+        self.h = h
+        self.n_models = len(models)
+
+    def submit(self, stream: int, frame: np.ndarray) -> int:
+        fr = np.ascontiguousarray(frame, dtype=np.uint8)
+        hh, w, _ = fr.shape
+        t = C.c_longlong()
+        _check(lib().geye_server_submit(self.h, stream, _p(fr), w, hh, 3 * w, C.byref(t)), "server_submit")
+        return t.value
+
+    def poll(self, max_results: int = 256, with_results: bool = True) -> list:
+        info = (_Served * max_results)()
+        res = (_Result * (max_results * self.n_models))() if with_results else None
+        n = C.c_int()
+        _check(lib().geye_server_poll(self.h, max_results, info, res, C.byref(n)), "server_poll")
+        out = []
+        for i in range(n.value):
+            d = dict(ticket=info[i].ticket, stream=info[i].stream, n_tracks=info[i].n_tracks,
+                     queued_ns=info[i].queued_ns, latency_ns=info[i].latency_ns)
+            if with_results:
+                d["results"] = [_result_to_dict(res[i * self.n_models + m]) for m in range(self.n_models)]
+            out.append(d)
+        return out
+
+    def drain(self):
+        _check(lib().geye_server_drain(self.h), "server_drain")
+
+    def stats(self) -> dict:
+        o = np.zeros(8, np.int64)
+        _check(lib().geye_server_stats(self.h, _p(o)), "server_stats")
+        keys = ["slots", "busy", "queued", "finished", "bytes_held", "completed", "tracked_streams"]
+        return dict(zip(keys, [int(v) for v in o[:7]]))
+
+    def tracks(self, stream: int, max_tracks: int = 64) -> np.ndarray:
+        b = np.zeros((max_tracks, 4), np.float32)
+        n = C.c_int()
+        _check(lib().geye_server_tracks(self.h, stream, max_tracks, _p(b), C.byref(n)), "server_tracks")
+        return b[:min(n.value, max_tracks)].copy()
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().geye_server_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
 
 
 class Model:

@@ -43,6 +43,7 @@ typedef int geye_status;
 #define GEYE_ERR_UNSUPPORTED  5   /* model shape outside what the kernels cover     */
 #define GEYE_ERR_INJECTED     6   /* fault injected by geye_debug_inject_fault      */
 #define GEYE_ERR_TIMEOUT      7   /* a bounded device-side wait gave up             */
+#define GEYE_BUSY             8   /* the submitted frame is still on the GPU        */
 
 typedef struct geye_ctx geye_ctx;       /* one device + one stream + work buffers */
 typedef struct geye_model geye_model;   /* a DPM model resident on the device     */
@@ -140,8 +141,8 @@ void geye_free(void *p);
 /* ---- device-resident path (benchmarks, batching) ------------------------ */
 /* Runs the whole path on a frame already in device memory (d_bgr, tightly packed
  * width*3 bytes per row), leaving boxes and the kept set on the device.  Results
- * can be read with geye_fetch_result.  Nothing is copied between host and device
- * except a 4-byte count per model needed to size NMS. */
+ * can be read with geye_fetch_result.  Asynchronous on the context's stream:
+ * nothing is copied between host and device. */
 geye_status geye_detect_device(geye_ctx *ctx, geye_model *const *models, int n_models, const uint8_t *d_bgr,
                                int width, int height, float thresh, float overlap);
 geye_status geye_fetch_result(geye_ctx *ctx, int model_index, geye_result *out, int *n_boxes_before_nms);
@@ -165,6 +166,54 @@ geye_status geye_fetch_result(geye_ctx *ctx, int model_index, geye_result *out, 
 #define GEYE_NMS_NOALLOC_MAX_BOXES 65536
 geye_status geye_nms_noalloc(const float *d_boxes, int num, int numpart0, float overlap, float *d_out,
                              int *d_kept, void *cuda_stream);
+
+/* ---- asynchronous submission (no counterpart in the reference) ------------ */
+/* The work of geye_detect_multi without waiting: the frame is copied (the
+ * caller's buffer is free on return), staged through pinned memory, run on the
+ * context's stream and its results copied back into pinned memory.  One frame
+ * per context may be outstanding; geye_detect_query returns GEYE_OK when it is
+ * done and GEYE_BUSY while it runs; geye_detect_collect waits for it and fills
+ * out[0..n_models) (free each with geye_result_free).  Several contexts on one
+ * device run their frames concurrently. */
+geye_status geye_detect_submit(geye_ctx *ctx, geye_model *const *models, int n_models, const uint8_t *bgr, int width,
+                               int height, int width_step, float thresh, float overlap);
+geye_status geye_detect_query(geye_ctx *ctx);
+geye_status geye_detect_collect(geye_ctx *ctx, geye_result *out);
+
+/* ---- multi-stream server (no counterpart in the reference) --------------- */
+/* Frames from many camera streams are admitted as they arrive into slots (one
+ * context and stream each, created on demand while the device memory held by
+ * slots stays within hbm_budget bytes and at most max_slots exist); frames of
+ * different resolutions and streams overlap on the GPU.  Each stream's frames
+ * are dispatched in submission order.  When track is nonzero every stream
+ * keeps a device-resident particle-filter tracker fed with its detections. */
+typedef struct geye_server geye_server;
+typedef struct {
+    long long ticket;        /* from geye_server_submit                         */
+    int stream;              /* camera stream id                                */
+    int n_tracks;            /* live tracks of the stream after this frame      */
+    long long queued_ns;     /* submit -> dispatch to a slot                     */
+    long long latency_ns;    /* submit -> results on the host                    */
+} geye_served;
+geye_status geye_server_create(int device, geye_model *const *models, int n_models, geye_conv_mode mode,
+                               size_t hbm_budget, int max_slots, float thresh, float overlap, int track,
+                               geye_server **out);
+geye_status geye_server_destroy(geye_server *s);
+/* Copies the frame and queues it; dispatches whatever fits.  *ticket identifies it. */
+geye_status geye_server_submit(geye_server *s, int stream, const uint8_t *bgr, int width, int height,
+                               int width_step, long long *ticket);
+/* Completes finished frames and dispatches queued ones without blocking; up to
+ * max finished frames are returned (info[i], and n_models results per frame in
+ * results[i*n_models ...] when results is not NULL).  *n = how many. */
+geye_status geye_server_poll(geye_server *s, int max, geye_served *info, geye_result *results, int *n);
+/* Blocks until every submitted frame has finished (collect them with poll). */
+geye_status geye_server_drain(geye_server *s);
+/* out[0..7]: slots, busy slots, queued frames, finished not yet polled,
+ * device bytes held by slots, frames completed, streams with trackers, 0. */
+geye_status geye_server_stats(geye_server *s, long long out[8]);
+/* Copies stream `stream`'s live tracks (up to max) as x1, y1, x2, y2 floats into
+ * boxes[4*i]; *n = count. */
+geye_status geye_server_tracks(geye_server *s, int stream, int max, float *boxes, int *n);
 
 /* ---- measurement ---------------------------------------------------------- */
 /* When enabled, the context records CUDA events around each stage on its stream.

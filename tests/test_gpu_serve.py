@@ -1,0 +1,102 @@
+"""Asynchronous submission, the multi-stream server and its trackers.
+
+The server's contract: frames admitted into slots as they arrive overlap on
+the GPU, and each frame's result is the same in the mix as alone (the
+kernels are deterministic, so bit for bit).  The tracker is checked against
+its CPU restatement (oracle/tracker.py) on the frames where it is a smooth
+function of its inputs (start and first update; later frames resample).
+"""
+import numpy as np
+import pytest
+
+from oracle import tracker as TR
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def setup(tmp_path_factory):
+    import geye_gb300 as g
+    from geye_gb300 import synth
+    d = str(tmp_path_factory.mktemp("models"))
+    ctx = g.Context(0, conv=g.CONV_BF16)
+    models = [g.Model(ctx, *synth.write_model_csv(s, d)) for s in (synth.CAR_SPEC, synth.PERSON_SPEC)]
+    yield g, synth, ctx, models
+    for m in models:
+        m.close()
+    ctx.close()
+
+
+def same(a, b):
+    return all(x["num"] == y["num"] and all(np.array_equal(x[k], y[k]) for k in ("point", "or_point", "type", "scale", "score"))
+               for x, y in zip(a, b))
+
+
+def test_submit_collect_matches_detect_multi(setup):
+    g, synth, ctx, models = setup
+    frame = synth.make_frame(640, 480, seed=4)
+    ref = ctx.detect_multi(frame, models, -0.5, 0.5, None)
+    ctx.detect_submit(frame, models, -0.5, 0.5)
+    while not ctx.detect_done():
+        pass
+    assert same(ctx.detect_collect(), ref)
+
+
+def test_server_results_same_in_the_mix_as_alone(setup):
+    g, synth, ctx, models = setup
+    sizes = [(320, 240), (640, 480), (320, 240), (640, 480), (640, 480), (320, 240)]
+    frames = {(s, k): synth.make_frame(*sizes[s], seed=10 * s + k) for s in range(len(sizes)) for k in range(2)}
+    alone = {key: ctx.detect_multi(f, models, -0.5, 0.5, None) for key, f in frames.items()}
+    with g.Server(models, conv=g.CONV_BF16, max_slots=4) as srv:
+        tickets = {}
+        for k in range(2):
+            for s in range(len(sizes)):
+                tickets[srv.submit(s, frames[(s, k)])] = (s, k)
+        srv.drain()
+        done = srv.poll(64)
+        assert len(done) == len(frames)
+        for d in done:
+            assert same(d["results"], alone[tickets[d["ticket"]]])
+            assert d["latency_ns"] >= d["queued_ns"] >= 0
+        st = srv.stats()
+        assert 1 <= st["slots"] <= 4 and st["completed"] == len(frames) and st["queued"] == 0
+
+
+def test_server_admission_respects_the_memory_budget(setup):
+    g, synth, ctx, models = setup
+    with g.Server(models, conv=g.CONV_BF16, hbm_budget=1, max_slots=8) as srv:
+        for k in range(5):
+            srv.submit(k, synth.make_frame(320, 240, seed=k))
+        srv.drain()
+        assert len(srv.poll(16)) == 5
+        assert srv.stats()["slots"] == 1   # the first slot's plan already exceeds the budget
+
+
+def _dets(results):
+    return np.concatenate([r["point"].astype(np.float64).reshape(-1, 4) for r in results])
+
+
+def test_tracker_matches_its_restatement_and_isolates_streams(setup):
+    g, synth, ctx, models = setup
+    seq0 = [synth.make_frame(320, 240, seed=100 + k) for k in range(3)]
+    seq1 = [synth.make_frame(320, 240, seed=200 + k) for k in range(2)]
+    with g.Server(models, conv=g.CONV_BF16, max_slots=3, track=True) as mix:
+        order = [(0, seq0[0]), (1, seq1[0]), (0, seq0[1]), (1, seq1[1]), (0, seq0[2])]
+        tk = {mix.submit(s, f): s for s, f in order}
+        mix.drain()
+        done = sorted(mix.poll(16), key=lambda d: d["ticket"])
+        tracks_mix = mix.tracks(0)
+    with g.Server(models, conv=g.CONV_BF16, max_slots=1, track=True) as solo:
+        ref = TR.StreamTracker(0)
+        for k, f in enumerate(seq0):
+            solo.submit(0, f)
+            solo.drain()
+            d = solo.poll(4)[0]
+            ref.step(_dets(d["results"])[:TR.MAX_DET])
+            got = solo.tracks(0)
+            assert d["n_tracks"] == len(got) == len(ref.boxes())
+            if k < 2:   # start and first update: no resampling has happened yet
+                assert np.allclose(got, ref.boxes(), rtol=0, atol=0.05), np.abs(got - ref.boxes()).max()
+        tracks_solo = solo.tracks(0)
+    assert [tk[d["ticket"]] for d in done] == [0, 1, 0, 1, 0]
+    assert np.array_equal(tracks_mix, tracks_solo)   # stream 1 did not disturb stream 0
