@@ -1,25 +1,32 @@
 """Benchmark of the DPM detection path (one JSON line on rank 0).
 
-Workload (default): DPM car + person models together on one synthetic
-1280x720 frame, FP32 GPU drop-in (the plain path whose results match the
-reference CPU path bit for bit).  A step is one frame through the whole path:
-resize pyramid, HOG pyramid, root/part convolution, distance transforms,
-score assembly and boxes, accumulated score map, NMS and box regression, for
-both models.
+Default workload (served_bf16_car+person_640x480): DPM car + person models on
+synthetic 640x480 frames from 16 camera streams, BF16 tensor-core convolution,
+frames of all streams in flight at once.  A step is one frame per stream
+(16 frames) through the whole path: resize pyramid, HOG pyramid, root/part
+convolution, distance transforms, score assembly and boxes, accumulated score
+map, NMS and box regression, for both models.
 
-  value  frames/s with the frame already in device memory (geye_detect_device),
-         CUDA events on the library's stream around each step, L2 flushed
-         between steps (a 256 MiB write outside the timed events).
-  e2e    frames/s through the C ABI a caller uses (geye_detect_multi) with host
-         buffers: frame + A_SCORE maps copied in, results + A_SCORE maps copied
-         out inside the timed region; p50/p99 per-frame latency from the same calls.
-  roofline  the dominant kernel (the convolution) from live CUDA events.
+  value  frames/s with the frames already in device memory: 16 slot contexts
+         (one stream each) replay their frame graphs concurrently; CUDA events
+         on a master stream bracket each step; L2 flushed between steps.
+  e2e    frames/s through the server API a caller uses (geye_server_submit /
+         geye_server_poll): host frames in, host results out, 16 streams kept
+         busy; p50/p99 = per-frame submit-to-results latency.
+  plain_fp32  the plain FP32 drop-in (geye_detect_multi, one frame at a time)
+         on the same frame and GPU; served_vs_plain_fp32 = e2e / plain.
+  roofline  the BF16 convolution from live CUDA events (per-stage times of one frame).
   cpu_baseline  the CPU oracle (this project's restatement of the reference's
-         CPU path) timed on this host's cores on one frame of the same workload.
+         CPU path) timed on this host's cores on one frame.
+
+Other workloads: the single-frame FP32 drop-in at 1280x720 (car+person_1280x720_fp32,
+value = device-resident frames/s, e2e = geye_detect_multi with host buffers),
+BF16 single-frame forms, and serve64_mixed_bf16 (64 cameras, Poisson arrivals
+at 30 fps each, 640x480/1280x720/1920x1080, trackers, 40 GB budget).
 
 --impl reference times the CPU oracle alone (all host threads) on the same
-workload and prints the reference arm's line.  Synthetic data: seeded frames
-and random-init models in the reference's CSV format (no dataset is needed).
+frame size and models.  Synthetic data: seeded frames and random-init models in
+the reference's CSV format (no dataset is needed).
 """
 from __future__ import annotations
 
@@ -39,11 +46,19 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 WORKLOADS = {
+    # served: frames from many streams in flight at once through geye_server_* (BF16 tensor-core conv)
+    "served_bf16_car+person_640x480": dict(w=640, h=480, models=("car", "person"), conv="bf16", served=True, slots=16),
+    # 64 simulated cameras, Poisson arrivals at 30 fps each, mixed resolutions, trackers on, 40 GB budget
+    "serve64_mixed_bf16": dict(w=640, h=480, models=("car", "person"), conv="bf16", sim=True, streams=64, fps=30.0,
+                               sizes=((640, 480), (1280, 720), (1920, 1080)), seconds=6.0),
+    # one frame at a time
     "car+person_1280x720_fp32": dict(w=1280, h=720, models=("car", "person"), conv="fp32"),
+    "car+person_1280x720_bf16": dict(w=1280, h=720, models=("car", "person"), conv="bf16"),
     "car+person_640x480_fp32": dict(w=640, h=480, models=("car", "person"), conv="fp32"),
+    "car+person_640x480_bf16": dict(w=640, h=480, models=("car", "person"), conv="bf16"),
     "car_640x480_fp32": dict(w=640, h=480, models=("car",), conv="fp32"),
 }
-DEFAULT_WORKLOAD = "car+person_1280x720_fp32"
+DEFAULT_WORKLOAD = "served_bf16_car+person_640x480"
 
 
 def _peaks():
@@ -304,7 +319,8 @@ def run_gpu(args, wl):
         line = {
             "metric": "frames_per_sec", "value": value, "unit": "frames/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1000.0 * t_total / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "scaling": "weak", "vs_baseline": None, "dtype": "bf16" if wl["conv"] == "bf16" else "f32",
+            "data": "synthetic",
             "config": {"workload": args.workload, "frame": f"{W}x{H}", "models": list(wl["models"]),
                        "conv": wl["conv"], "thresh": -0.5, "overlap": 0.5, "parallelism": f"replicas{world}",
                        "l2": "flushed between steps (256 MiB write, outside the timed events)"},
@@ -327,6 +343,275 @@ def run_gpu(args, wl):
     return 0
 
 
+def _plain_fp32(paths_models, frame, n):
+    """The plain FP32 drop-in (geye_detect_multi, one frame at a time) on the same frame."""
+    import geye_gb300 as g
+    ctx = g.Context(0, conv=g.CONV_FP32)
+    models = [g.Model(ctx, *p) for p in paths_models]
+    for _ in range(3):
+        ctx.detect_multi(frame, models, -0.5, 0.5, None)
+    t = []
+    for _ in range(n):
+        t0 = time.perf_counter()
+        ctx.detect_multi(frame, models, -0.5, 0.5, None)
+        t.append(time.perf_counter() - t0)
+    for m in models:
+        m.close()
+    ctx.close()
+    return {"value": n / sum(t), "unit": "frames/s", "p50_ms": 1000 * float(np.percentile(t, 50)),
+            "p99_ms": 1000 * float(np.percentile(t, 99)), "api": "geye_detect_multi, FP32 CUDA-core conv, one frame at a time"}
+
+
+def _stage_breakdown(paths_models, frame, conv_mode, reps=5):
+    """Per-stage times of one frame (CUDA events inside the frame graph) and the conv roofline inputs."""
+    import geye_gb300 as g
+    import torch
+    ctx = g.Context(0, conv=conv_mode)
+    models = [g.Model(ctx, *p) for p in paths_models]
+    H, W, _ = frame.shape
+    d = torch.from_numpy(frame).cuda()
+    acc = {}
+    ctx.enable_timing(True)
+    for r in range(reps + 2):
+        ctx.detect_device(d.data_ptr(), W, H, models)
+        ctx.synchronize()
+        st = ctx.stage_times()
+        if r >= 2:
+            for k, v in st["ms"].items():
+                acc.setdefault(k, []).append(v)
+    last = ctx.stage_times()
+    for m in models:
+        m.close()
+    ctx.close()
+    return {k: statistics.median(v) for k, v in acc.items()}, last
+
+
+def run_served(args, wl):
+    """Headline: served BF16 frames/s at 640x480 car+person (frames from `slots` streams in flight at once)."""
+    import torch
+    import geye_gb300 as g
+    from geye_gb300 import synth
+    rank, world, local = dist_info()
+    dev = local if world > 1 else 0
+    torch.cuda.set_device(dev)
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+        pg = dist
+    S, W, H = wl["slots"], wl["w"], wl["h"]
+    tmp = tempfile.TemporaryDirectory()
+    paths = _write_models(wl["models"], tmp.name)
+    frames = [synth.make_frame(W, H, seed=100 * rank + k) for k in range(S)]
+    owner = g.Context(dev, conv=g.CONV_BF16)
+    models = [g.Model(owner, *p) for p in paths]
+
+    # ---- value: S slots, frames resident in HBM, all S in flight per step
+    master = torch.cuda.Stream(device=dev)
+    streams = [torch.cuda.Stream(device=dev) for _ in range(S)]
+    slots = [g.Context(dev, stream=st.cuda_stream, conv=g.CONV_BF16) for st in streams]
+    d_frames = [torch.from_numpy(f).to(f"cuda:{dev}") for f in frames]
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{dev}")
+    launches_per_frame = 0
+
+    def step():
+        for c, df in zip(slots, d_frames):
+            c.detect_device(df.data_ptr(), W, H, models)
+
+    for _ in range(max(args.warmup, 3)):
+        step()
+        torch.cuda.synchronize()
+    launches_per_frame = slots[0].stage_times()["launches"]
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    ends = [torch.cuda.Event() for _ in range(S)]
+    if pg:
+        pg.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(dev) as clk:
+        for i in range(args.steps):
+            with torch.cuda.stream(master):
+                flush.fill_(float(i))
+                ev[i][0].record(master)
+            for st in streams:
+                st.wait_event(ev[i][0])
+            step()
+            for st, e in zip(streams, ends):
+                e.record(st)
+                master.wait_event(e)
+            ev[i][1].record(master)
+        torch.cuda.synchronize()
+    if pg:
+        pg.barrier()
+    t_total = sum(a.elapsed_time(b) for a, b in ev) / 1000.0
+    if pg:
+        t = torch.tensor([t_total], dtype=torch.float64)
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        t_total = float(t.item())
+    value = world * args.steps * S / t_total
+    for c in slots:
+        c.close()
+
+    # ---- e2e: the server API with host frames, S streams kept busy (closed loop)
+    n_frames = args.steps * S
+    srv = g.Server(models, conv=g.CONV_BF16, max_slots=S)
+    for k in range(S):   # warm the slots' plans and graphs
+        srv.submit(k, frames[k])
+    srv.drain()
+    srv.poll(4 * S)
+    lat = []
+    submitted = done = 0
+    t0 = time.perf_counter()
+    while submitted < min(S, n_frames):
+        srv.submit(submitted % S, frames[submitted % S])
+        submitted += 1
+    while done < n_frames:
+        out = srv.poll(4 * S)
+        for d in out:
+            lat.append(d["latency_ns"] / 1e6)
+            done += 1
+            if submitted < n_frames:
+                srv.submit(d["stream"], frames[d["stream"]])
+                submitted += 1
+        if not out:
+            time.sleep(0.0001)
+    e2e_t = time.perf_counter() - t0
+    srv_stats = srv.stats()
+    srv.close()
+    if pg:
+        t = torch.tensor([e2e_t], dtype=torch.float64)
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        e2e_t = float(t.item())
+    e2e_fps = world * n_frames / e2e_t
+    res_bytes = 4 * (64 + len(models) * 11 * 4096)
+
+    # ---- the plain FP32 drop-in on the same frame, stage breakdown and roofline of the conv
+    plain = _plain_fp32(paths, frames[0], 30)
+    stages, last = _stage_breakdown(paths, frames[0], g.CONV_BF16)
+    hbm, bf16, bf16s, peak_src = _peaks()
+    conv_flops = last["conv_flops"]
+    achieved = conv_flops / (stages["conv"] / 1000.0) / 1e12
+    roofline = {"kernel": "conv (tcgen05 BF16 implicit GEMM, k_conv_tc)", "bound": "tensor", "achieved": achieved,
+                "peak": bf16, "unit": "TFLOP/s", "frac": achieved / bf16, "traffic": _traffic("conv_bf16"),
+                "note": f"peak = dense bf16 tensor ({peak_src}); conv timed alone on one frame with CUDA events",
+                "flops_per_launch": conv_flops, "ms_per_launch": stages["conv"]}
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        from oracle import oracle as O
+        O.build()
+        nthreads = os.cpu_count() or 1
+        fps_cpu, dt = cpu_oracle_frames_per_sec(wl, paths, frames[0], nthreads, n_frames=1)
+        cpu = {"value": fps_cpu, "unit": "frames/s", "cores": nthreads, "kind": "port",
+               "sample": f"1 frame of the workload ({dt:.2f} s wall, both models, oracle with {nthreads} threads)"}
+    clocks = clk.summary()
+    if rank == 0:
+        line = {
+            "metric": "frames_per_sec", "value": value, "unit": "frames/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1000.0 * t_total / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "bf16", "data": "synthetic",
+            "config": {"workload": args.workload, "frame": f"{W}x{H}", "models": list(wl["models"]),
+                       "conv": "bf16 (tcgen05, FP32 accumulation)", "thresh": -0.5, "overlap": 0.5,
+                       "frames_in_flight": S, "step": f"{S} frames from {S} streams, one per slot",
+                       "parallelism": f"replicas{world}",
+                       "l2": "flushed between steps (256 MiB write, outside the timed events)"},
+            "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+            "e2e": {"value": e2e_fps, "unit": "frames/s", "api": "geye_server_submit/poll (host frames in, host results out)",
+                    "h2d_bytes_per_step": int(S * W * H * 3), "d2h_bytes_per_step": int(S * res_bytes),
+                    "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+                    "slots": srv_stats["slots"]},
+            "plain_fp32": plain,
+            "served_vs_plain_fp32": e2e_fps / plain["value"],
+            "gpu_launches": int(launches_per_frame * S * args.steps),
+            "stage_ms": stages,
+            "roofline": roofline,
+            "cpu_baseline": cpu,
+            "clocks": clocks,
+        }
+        print(json.dumps(line), flush=True)
+    for m in models:
+        m.close()
+    owner.close()
+    if pg:
+        pg.destroy_process_group()
+    return 0
+
+
+def run_serve_sim(args, wl):
+    """64 simulated cameras: Poisson arrivals, mixed resolutions, trackers, HBM budget; open loop."""
+    import geye_gb300 as g
+    from geye_gb300 import synth
+    rank, world, local = dist_info()
+    if world > 1 and rank != 0:
+        return 0
+    rng = np.random.default_rng(7)
+    tmp = tempfile.TemporaryDirectory()
+    paths = _write_models(wl["models"], tmp.name)
+    owner = g.Context(0, conv=g.CONV_BF16)
+    models = [g.Model(owner, *p) for p in paths]
+    n = wl["streams"]
+    sizes = [wl["sizes"][i] for i in rng.integers(0, len(wl["sizes"]), size=n)]
+    frames = {}
+    for s in range(n):
+        for k in range(2):
+            frames[(s, k)] = synth.make_frame(*sizes[s], seed=1000 * s + k)
+    srv = g.Server(models, conv=g.CONV_BF16, hbm_budget=40 << 30, max_slots=64, track=True)
+    for sz in set(sizes):   # plans and graphs for every resolution before the clock starts
+        s0 = sizes.index(sz)
+        srv.submit(s0, frames[(s0, 0)])
+    srv.drain()
+    srv.poll(1024)
+    T = wl["seconds"]
+    arrivals = []
+    for s in range(n):
+        t = rng.exponential(1.0 / wl["fps"])
+        while t < T:
+            arrivals.append((t, s))
+            t += rng.exponential(1.0 / wl["fps"])
+    arrivals.sort()
+    lat, sub_at, k_of = [], {}, {}
+    i = done = 0
+    t0 = time.perf_counter()
+    with ClockSampler(0) as clk:
+        while done < len(arrivals):
+            now = time.perf_counter() - t0
+            while i < len(arrivals) and arrivals[i][0] <= now:
+                ta, s = arrivals[i]
+                k_of[s] = k_of.get(s, -1) + 1
+                tk = srv.submit(s, frames[(s, k_of[s] % 2)])
+                sub_at[tk] = (ta, time.perf_counter() - t0)
+                i += 1
+            out = srv.poll(256, with_results=False)
+            for d in out:
+                ta, ts = sub_at.pop(d["ticket"])
+                lat.append(1000.0 * (ts - ta) + d["latency_ns"] / 1e6)
+                done += 1
+            if not out:
+                time.sleep(0.0002)
+    wall = time.perf_counter() - t0
+    st = srv.stats()
+    tracks = sum(len(srv.tracks(s)) for s in range(n))
+    srv.close()
+    for m in models:
+        m.close()
+    owner.close()
+    line = {
+        "metric": "frames_per_sec", "value": len(arrivals) / wall, "unit": "frames/s", "n_gpus": 1,
+        "steps": len(arrivals), "warmup": len(set(sizes)), "ms_per_step": 1000.0 * wall / len(arrivals),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "bf16", "data": "synthetic",
+        "config": {"workload": args.workload, "streams": n, "arrivals": f"Poisson {wl['fps']} fps per stream",
+                   "offered_fps": len(arrivals) / T, "sizes": {f"{a}x{b}": sizes.count((a, b)) for a, b in set(sizes)},
+                   "seconds": T, "tracker": "500 particles/track, Philox, sigma 4 px", "hbm_budget_gb": 40,
+                   "models": list(wl["models"]), "conv": "bf16"},
+        "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+        "e2e": {"value": len(arrivals) / wall, "unit": "frames/s", "api": "geye_server_submit/poll",
+                "h2d_bytes_per_step": int(np.mean([a * b * 3 for a, b in sizes])), "d2h_bytes_per_step": 4 * (64 + 2 * 11 * 4096),
+                "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99))},
+        "server": {"slots": st["slots"], "bytes_held": st["bytes_held"], "live_tracks_end": tracks},
+        "clocks": clk.summary(),
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -339,6 +624,10 @@ def main():
     wl = WORKLOADS[args.workload]
     if args.impl == "reference":
         return run_reference(args, wl)
+    if wl.get("served"):
+        return run_served(args, wl)
+    if wl.get("sim"):
+        return run_serve_sim(args, wl)
     return run_gpu(args, wl)
 
 

@@ -154,14 +154,17 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_conv_tc(const TcJob *__restri
   uint32_t *tslot = reinterpret_cast<uint32_t *>(sm + 16);
   const int4 ch = chunks[blockIdx.x];
   const TcJob J = jobs[ch.x];
-  const int tile0 = ch.y, ntile = ch.z, S = ch.w;   // S = slab cells per plane
-  const int taps = J.b0 * J.b1;
-  const uint32_t bank_bytes = (uint32_t)taps * 4u * (uint32_t)J.n_pad * 16u;
-  uint8_t *sB = sm + kTcHead;
-  uint8_t *sA = sB + ((bank_bytes + 127u) & ~127u);
+  const int tile0 = ch.y, ntile = ch.z, cs = ch.w;   // cs = filter columns per phase
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int p_begin = tile0 * kTcM;
-  const uint32_t ncols = J.n_pad <= 16 ? 32u : 64u;   // accumulator columns (power of two >= 32)
+  const uint32_t bq = (uint32_t)J.n_pad * 16u;                 // one (tap, q) slice of the bank
+  const uint32_t col_bytes = (uint32_t)J.b0 * 4u * bq;         // one filter column of the bank
+  const uint32_t bank_room = ((uint32_t)cs * col_bytes + 127u) & ~127u;
+  uint8_t *sB = sm + kTcHead;
+  uint8_t *sA = sB + bank_room;
+  // accumulators: tile i at TMEM columns i*n_pad .. i*n_pad + n_pad - 1
+  uint32_t ncols = 32;
+  while (ncols < (uint32_t)(ntile * J.n_pad)) ncols <<= 1;
 
   if (threadIdx.x == 0) {
     mbar_init(bar_load, 1);
@@ -174,56 +177,60 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_conv_tc(const TcJob *__restri
   tc_fence_after();
   const uint32_t tmem = *tslot;
 
-  bool ok = true;   // uniform across the CTA (every wait outcome is combined with __syncthreads_and)
-  if (threadIdx.x == 0) {
-    const uint32_t slab_plane = (uint32_t)S * 16u;
-    mbar_expect_tx(bar_load, bank_bytes + 4u * slab_plane);
-    bulk_g2s(sB, bank + J.bank_off, bank_bytes, bar_load);
-    for (int q = 0; q < 4; q++)
-      bulk_g2s(sA + (size_t)q * slab_plane,
-               arena16 + J.plane_off + ((size_t)q * J.plane_cells + (size_t)p_begin) * 8, slab_plane, bar_load);
-  }
-  if (!mbar_wait(bar_load, 0, kWaitNs)) {
-    ok = false;
-    atomicOr(err, 1);
-    mbar_wait(bar_load, 0, 4 * kWaitNs);   // the copies must land before the CTA leaves
-  }
-  ok = __syncthreads_and(ok);
-
   const uint32_t idesc = idesc_bf16(kTcM, J.n_pad);
   const uint32_t sA_addr = smem_u32(sA), sB_addr = smem_u32(sB);
-  const uint32_t plane_bytes = (uint32_t)S * 16u, bq = (uint32_t)J.n_pad * 16u;
-  for (int i = 0; i < ntile && ok; i++) {
+  const int phases = (J.b1 + cs - 1) / cs;
+  bool ok = true;   // uniform across the CTA (every wait outcome is combined with __syncthreads_and)
+  for (int ph = 0; ph < phases && ok; ph++) {
+    const int xp0 = ph * cs, ncol = min(cs, J.b1 - xp0);
+    const int S = ntile * kTcM + (ncol - 1) * J.fs0 + (J.b0 - 1);   // slab cells per plane this phase
+    const uint32_t plane_bytes = (uint32_t)S * 16u;
+    if (threadIdx.x == 0) {
+      mbar_expect_tx(bar_load, (uint32_t)ncol * col_bytes + 4u * plane_bytes);
+      bulk_g2s(sB, bank + J.bank_off + (size_t)xp0 * col_bytes, (uint32_t)ncol * col_bytes, bar_load);
+      for (int q = 0; q < 4; q++)
+        bulk_g2s(sA + (size_t)q * plane_bytes,
+                 arena16 + J.plane_off + ((size_t)q * J.plane_cells + (size_t)p_begin + (size_t)xp0 * J.fs0) * 8,
+                 plane_bytes, bar_load);
+    }
+    bool landed = mbar_wait(bar_load, (uint32_t)(ph & 1), kWaitNs);
+    if (!landed) {
+      atomicOr(err, 1);
+      mbar_wait(bar_load, (uint32_t)(ph & 1), 4 * kWaitNs);   // the copies must land before the CTA leaves
+    }
+    ok = __syncthreads_and(landed);
+    if (!ok) break;
     if (threadIdx.x == 0) {
       tc_fence_after();
-      uint32_t acc = 0;
-      for (int xp = 0; xp < J.b1; xp++)
-        for (int yp = 0; yp < J.b0; yp++) {
-          const uint32_t cell = (uint32_t)(i * kTcM + xp * J.fs0 + yp);
-          const int t = xp * J.b0 + yp;
-          for (int qp = 0; qp < 2; qp++) {
-            const uint64_t ad = sdesc(sA_addr + 2u * qp * plane_bytes + cell * 16u, plane_bytes, 128u);
-            const uint64_t bd = sdesc(sB_addr + (uint32_t)(t * 4 + 2 * qp) * bq, bq, 128u);
-            tc_mma(tmem, ad, bd, idesc, acc);
-            acc = 1;
+      for (int i = 0; i < ntile; i++)
+        for (int xp = 0; xp < ncol; xp++)
+          for (int yp = 0; yp < J.b0; yp++) {
+            const uint32_t cell = (uint32_t)(i * kTcM + xp * J.fs0 + yp);
+            const int t = xp * J.b0 + yp;   // tap within this phase's bank columns
+            for (int qp = 0; qp < 2; qp++) {
+              const uint64_t ad = sdesc(sA_addr + 2u * qp * plane_bytes + cell * 16u, plane_bytes, 128u);
+              const uint64_t bd = sdesc(sB_addr + (uint32_t)(t * 4 + 2 * qp) * bq, bq, 128u);
+              tc_mma(tmem + (uint32_t)(i * J.n_pad), ad, bd, idesc, (ph | xp | yp | qp) ? 1u : 0u);
+            }
           }
-        }
       tc_commit(bar_mma);
     }
-    bool done = mbar_wait(bar_mma, (uint32_t)(i & 1), kWaitNs);
+    bool done = mbar_wait(bar_mma, (uint32_t)(ph & 1), kWaitNs);
     if (!done) {
       atomicOr(err, 2);
-      mbar_wait(bar_mma, (uint32_t)(i & 1), 4 * kWaitNs);   // the MMAs must finish before TMEM is freed
+      mbar_wait(bar_mma, (uint32_t)(ph & 1), 4 * kWaitNs);   // the MMAs must finish before smem or TMEM is reused
     }
     ok = __syncthreads_and(done);
-    tc_fence_after();
-    // epilogue: row r of the tile is TMEM lane r; this thread owns row 32*warp + lane
+  }
+  tc_fence_after();
+  // epilogue: row r of a tile is TMEM lane r; this thread owns row 32*warp + lane of every tile
+  for (int i = 0; i < ntile; i++) {
     const int p = p_begin + i * kTcM + warp * 32 + lane;
     const int x = p / J.fs0, y = p - x * J.fs0;
     const bool valid = ok && x < J.c1 && y < J.c0;
     for (int c0 = 0; c0 < J.n_pad; c0 += 16) {
       uint32_t r[16];
-      tc_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, r);
+      tc_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(i * J.n_pad + c0), r);
       tc_wait_ld();
       if (valid) {
         for (int k = 0; k < 16 && c0 + k < J.n; k++) {
@@ -233,9 +240,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_conv_tc(const TcJob *__restri
         }
       }
     }
-    tc_fence_before();
-    __syncthreads();   // every accumulator read is done before the next tile's MMAs
   }
+  tc_fence_before();
   __syncthreads();
   if (warp == 0) tmem_dealloc(tmem, ncols);
 }
@@ -336,20 +342,32 @@ static bool add_tc_job(TcTables &T, int plane_off, int fs0, int fs1, const BankG
   for (int k = 0; k < g.n; k++) T.outs.push_back(map_off[k]);
   const int P_valid = (J.c1 - 1) * J.fs0 + J.c0;
   J.ntiles = (P_valid + kTcM - 1) / kTcM;
-  const size_t bank_bytes = ((size_t)g.b0 * g.b1 * 4 * g.n_pad * 16 + 127) & ~(size_t)127;
-  const long long reach = (long long)(g.b1 - 1) * J.fs0 + (g.b0 - 1);
-  // tiles per CTA: as many as the shared-memory budget allows (each tile adds 128 cells x 64 B)
-  const long long room = ((long long)kTcSmemBudget - kTcHead - (long long)bank_bytes - reach * 64) / (kTcM * 64);
-  if (room < 1) return false;
-  const int T_cta = (int)std::min<long long>(room, kTcMaxTiles);
+  // tiles per CTA (T) and filter columns per phase (cs): one phase when the whole
+  // bank and slab fit, else fewer columns per phase; every phase needs
+  // head + bank columns + (T*128 + (cs-1)*fs0 + b0-1) cells x 64 B
+  const size_t col_bytes = (size_t)g.b0 * 4 * g.n_pad * 16;
+  auto need = [&](int Tc, int cs) {
+    return (size_t)kTcHead + ((cs * col_bytes + 127) & ~(size_t)127) +
+           ((size_t)Tc * kTcM + (size_t)(cs - 1) * fs0 + (g.b0 - 1)) * 64;
+  };
+  int T_cta = 0, cs = 0;
+  for (int Tc : {kTcMaxTiles, 8, 4}) {
+    if (need(Tc, g.b1) <= kTcSmemBudget) { T_cta = Tc; cs = g.b1; break; }
+  }
+  for (int Tc : {8, 4, 2, 1}) {
+    if (T_cta) break;
+    for (int c = g.b1; c >= 1; c--)
+      if (need(Tc, c) <= kTcSmemBudget) { T_cta = Tc; cs = c; break; }
+  }
+  if (!T_cta) return false;
   const int jid = (int)T.jobs.size();
   T.jobs.push_back(J);
+  const long long reach = (long long)(g.b1 - 1) * fs0 + (g.b0 - 1);
   for (int t0 = 0; t0 < J.ntiles; t0 += T_cta) {
     const int nt = std::min(T_cta, J.ntiles - t0);
-    const int S = nt * kTcM + (int)reach;
-    if ((long long)t0 * kTcM + S > J.plane_cells) return false;   // the slab stays inside its planes
-    T.chunks.push_back(make_int4(jid, t0, nt, S));
-    T.max_smem = std::max(T.max_smem, (size_t)kTcHead + bank_bytes + (size_t)S * 64);
+    if ((long long)t0 * kTcM + nt * kTcM + reach > J.plane_cells) return false;   // slabs stay inside the planes
+    T.chunks.push_back(make_int4(jid, t0, nt, cs));
+    T.max_smem = std::max(T.max_smem, need(nt, cs));
   }
   return true;
 }

@@ -94,3 +94,14 @@ def test_bf16_pipeline_detection_agreement(tmp_path):
     for r32, r16 in zip(res[g.CONV_FP32], res[g.CONV_BF16]):
         assert r32["num"] > 0
         assert agreement(r32, r16) >= 0.9
+
+
+def test_bf16_filter_columns_in_phases(ctx16):
+    # 16 filter columns over 320-row levels: bank and slab of the whole filter do not fit in shared
+    # memory at once, so the kernel walks the filter columns in phases, accumulating in TMEM
+    rng = np.random.default_rng(11)
+    feat = (rng.integers(0, 5, size=(31, 60, 320)) * 0.25).astype(np.float32)
+    filters = [rng.integers(-2, 3, size=(31, 16, 6)).astype(np.float32) for _ in range(3)]
+    got = ctx16.fconvsMT(feat, filters)
+    for m, f in zip(got, filters):
+        assert np.array_equal(m, O.fconv(feat, f))
