@@ -70,7 +70,7 @@ def _peaks():
 
 
 def _traffic(kernel_key: str):
-    """Per-launch DRAM bytes of a kernel from a committed ncu summary, if any."""
+    """DRAM bytes of one frame's conv stage from the committed ncu summary (profiles/), if any."""
     p = os.path.join(ROOT, "profiles", "traffic_per_launch.txt")
     if not os.path.exists(p):
         return None
@@ -292,7 +292,7 @@ def run_gpu(args, wl):
     conv_med_ms = statistics.median(stage_acc["conv"])
     conv_flops = st_last["conv_flops"]
     achieved_tflops = conv_flops / (conv_med_ms / 1000.0) / 1e12
-    traffic = _traffic("conv_fp32" if wl["conv"] == "fp32" else "conv_bf16")
+    traffic = _traffic(f"conv_{wl['conv']}_{W}x{H}")
     roofline = {"kernel": "conv (root + part filters, k_conv_fp32)" if wl["conv"] == "fp32" else "conv (tcgen05)",
                 "bound": "tensor", "achieved": achieved_tflops, "peak": bf16, "unit": "TFLOP/s",
                 "frac": achieved_tflops / bf16, "traffic": traffic,
@@ -491,7 +491,7 @@ def run_served(args, wl):
     conv_flops = last["conv_flops"]
     achieved = conv_flops / (stages["conv"] / 1000.0) / 1e12
     roofline = {"kernel": "conv (tcgen05 BF16 implicit GEMM, k_conv_tc)", "bound": "tensor", "achieved": achieved,
-                "peak": bf16, "unit": "TFLOP/s", "frac": achieved / bf16, "traffic": _traffic("conv_bf16"),
+                "peak": bf16, "unit": "TFLOP/s", "frac": achieved / bf16, "traffic": _traffic(f"conv_bf16_{W}x{H}"),
                 "note": f"peak = dense bf16 tensor ({peak_src}); conv timed alone on one frame with CUDA events",
                 "flops_per_launch": conv_flops, "ms_per_launch": stages["conv"]}
     cpu = None
