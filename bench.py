@@ -158,6 +158,16 @@ def cpu_oracle_frames_per_sec(wl, paths, frame, nthreads, n_frames=1):
     return n_frames / dt, dt
 
 
+def max_over_ranks(pg, seconds: float) -> float:
+    """The slowest rank's time (replicas: whole-job throughput = all ranks' units / this)."""
+    if pg is None:
+        return seconds
+    import torch
+    t = torch.tensor([seconds], dtype=torch.float64)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
 def dist_info():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -256,10 +266,7 @@ def run_gpu(args, wl):
         pg.barrier()
     step_ms = [a.elapsed_time(b) for a, b in ev]
     t_total = sum(step_ms) / 1000.0
-    if pg:
-        t = torch.tensor([t_total], dtype=torch.float64)
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        t_total = float(t.item())
+    t_total = max_over_ranks(pg, t_total)
     value = world * args.steps / t_total
     st_last = ctx.stage_times()
     ctx.enable_timing(False)
@@ -279,10 +286,7 @@ def run_gpu(args, wl):
         kept = ctx.detect_multi(frame, models, -0.5, 0.5, a_scores)
         e2e_ms.append(1000.0 * (time.perf_counter() - t0))
     e2e_t = sum(e2e_ms) / 1000.0
-    if pg:
-        t = torch.tensor([e2e_t], dtype=torch.float64)
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        e2e_t = float(t.item())
+    e2e_t = max_over_ranks(pg, e2e_t)
     e2e_fps = world * args.steps / e2e_t
     h2d = frame.nbytes + sum(a.nbytes for a in a_scores)
     d2h = sum(a.nbytes for a in a_scores) + sum(k["num"] * (4 * 4 + 4 * 4 + 4 + 4 + 4) + 8 for k in kept)
@@ -399,7 +403,7 @@ def run_served(args, wl):
         import torch.distributed as dist
         dist.init_process_group("gloo")
         pg = dist
-    S, W, H = wl["slots"], wl["w"], wl["h"]
+    S, W, H = (args.slots or wl["slots"]), wl["w"], wl["h"]
     tmp = tempfile.TemporaryDirectory()
     paths = _write_models(wl["models"], tmp.name)
     frames = [synth.make_frame(W, H, seed=100 * rank + k) for k in range(S)]
@@ -443,10 +447,7 @@ def run_served(args, wl):
     if pg:
         pg.barrier()
     t_total = sum(a.elapsed_time(b) for a, b in ev) / 1000.0
-    if pg:
-        t = torch.tensor([t_total], dtype=torch.float64)
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        t_total = float(t.item())
+    t_total = max_over_ranks(pg, t_total)
     value = world * args.steps * S / t_total
     for c in slots:
         c.close()
@@ -477,10 +478,7 @@ def run_served(args, wl):
     e2e_t = time.perf_counter() - t0
     srv_stats = srv.stats()
     srv.close()
-    if pg:
-        t = torch.tensor([e2e_t], dtype=torch.float64)
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        e2e_t = float(t.item())
+    e2e_t = max_over_ranks(pg, e2e_t)
     e2e_fps = world * n_frames / e2e_t
     res_bytes = 4 * (64 + len(models) * 11 * 4096)
 
@@ -620,6 +618,7 @@ def main():
     ap.add_argument("--impl", default="geye", choices=["geye", "reference"])
     ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--slots", type=int, default=0, help="frames in flight for the served workload (0: workload default)")
     args = ap.parse_args()
     wl = WORKLOADS[args.workload]
     if args.impl == "reference":

@@ -40,7 +40,7 @@ constexpr int kTcThreads = 128;
 constexpr int kTcM = 128;                        // positions per tile (TMEM lanes)
 constexpr int kTcMaxTiles = 16;                  // tiles per CTA
 constexpr size_t kTcSmemBudget = 220 * 1024;     // dynamic shared memory per CTA
-constexpr int kTcHead = 128;                     // barriers + TMEM address at the front
+constexpr int kTcHead = 256;                     // barriers, TMEM address and map offsets at the front
 constexpr unsigned long long kWaitNs = 1000000000ull;   // a wait gives up after 1 s (then 4 s for the drain)
 
 struct TcJob {
@@ -152,9 +152,11 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_conv_tc(const TcJob *__restri
   uint64_t *bar_load = reinterpret_cast<uint64_t *>(sm);
   uint64_t *bar_mma = reinterpret_cast<uint64_t *>(sm + 8);
   uint32_t *tslot = reinterpret_cast<uint32_t *>(sm + 16);
+  int *out_s = reinterpret_cast<int *>(sm + 32);   // the job's map offsets (n <= 32)
   const int4 ch = chunks[blockIdx.x];
   const TcJob J = jobs[ch.x];
   const int tile0 = ch.y, ntile = ch.z, cs = ch.w;   // cs = filter columns per phase
+  if (threadIdx.x < J.n) out_s[threadIdx.x] = outs[J.out_tab + threadIdx.x];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int p_begin = tile0 * kTcM;
   const uint32_t bq = (uint32_t)J.n_pad * 16u;                 // one (tap, q) slice of the bank
@@ -202,17 +204,29 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_conv_tc(const TcJob *__restri
     if (!ok) break;
     if (threadIdx.x == 0) {
       tc_fence_after();
-      for (int i = 0; i < ntile; i++)
-        for (int xp = 0; xp < ncol; xp++)
+      // The start-address field of a descriptor is (address >> 4) in its low 14 bits and
+      // every operand lies below 2^18 bytes, so moving an operand by a 16-byte multiple off
+      // is adding off >> 4 to the descriptor: A moves by cells (16 B), B by (tap, q) slices.
+      const uint64_t a_base = sdesc(sA_addr, plane_bytes, 128u);
+      const uint64_t b_base = sdesc(sB_addr, bq, 128u);
+      const uint32_t a_hi = 2u * (uint32_t)S;           // planes 2, 3: 2 * plane_bytes >> 4
+      const uint32_t b_tap = 4u * (uint32_t)J.n_pad;    // one tap of the bank: 4 * bq >> 4
+      const uint32_t b_hi = 2u * (uint32_t)J.n_pad;     // channels 16..31 of a tap
+      for (int i = 0; i < ntile; i++) {
+        const uint32_t d = tmem + (uint32_t)(i * J.n_pad);
+        uint32_t acc = ph ? 1u : 0u;
+        for (int xp = 0; xp < ncol; xp++) {
+          const uint32_t cell0 = (uint32_t)(i * kTcM + xp * J.fs0);
+          const uint32_t tap0 = (uint32_t)(xp * J.b0) * b_tap;
           for (int yp = 0; yp < J.b0; yp++) {
-            const uint32_t cell = (uint32_t)(i * kTcM + xp * J.fs0 + yp);
-            const int t = xp * J.b0 + yp;   // tap within this phase's bank columns
-            for (int qp = 0; qp < 2; qp++) {
-              const uint64_t ad = sdesc(sA_addr + 2u * qp * plane_bytes + cell * 16u, plane_bytes, 128u);
-              const uint64_t bd = sdesc(sB_addr + (uint32_t)(t * 4 + 2 * qp) * bq, bq, 128u);
-              tc_mma(tmem + (uint32_t)(i * J.n_pad), ad, bd, idesc, (ph | xp | yp | qp) ? 1u : 0u);
-            }
+            const uint64_t ad = a_base + (cell0 + (uint32_t)yp);
+            const uint64_t bd = b_base + (tap0 + (uint32_t)yp * b_tap);
+            tc_mma(d, ad, bd, idesc, acc);
+            tc_mma(d, ad + a_hi, bd + b_hi, idesc, 1u);
+            acc = 1u;
           }
+        }
+      }
       tc_commit(bar_mma);
     }
     bool done = mbar_wait(bar_mma, (uint32_t)(ph & 1), kWaitNs);
@@ -236,7 +250,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_conv_tc(const TcJob *__restri
         for (int k = 0; k < 16 && c0 + k < J.n; k++) {
           float v;
           memcpy(&v, &r[k], 4);
-          arena[(size_t)outs[J.out_tab + c0 + k] + (size_t)x * J.c0 + y] = v;
+          arena[(size_t)out_s[c0 + k] + (size_t)x * J.c0 + y] = v;
         }
       }
     }

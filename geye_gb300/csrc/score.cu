@@ -100,12 +100,20 @@ void launch_scan_counts(int *counts, int n, int *total, cudaStream_t s) {
   k_scan<<<1, 1024, 0, s>>>(counts, n, total);
 }
 
-__global__ void k_boxes(const ScoreJob *__restrict__ jobs, float thresh, const float *__restrict__ arena,
-                        const int *__restrict__ arena_i, const int *__restrict__ block_offsets, int stride, int GL,
-                        float *__restrict__ boxes) {
+// Records of a block are contiguous in the output (its offset from the scan,
+// then rank order), so they are built in shared memory and written out with
+// coalesced stores.
+
+__global__ void __launch_bounds__(kScoreThreads) k_boxes(const ScoreJob *__restrict__ jobs, float thresh,
+                                                         const float *__restrict__ arena,
+                                                         const int *__restrict__ arena_i,
+                                                         const int *__restrict__ block_offsets, int stride, int GL,
+                                                         float *__restrict__ boxes) {
+  extern __shared__ float rec_s[];   // [count][GL]
   __shared__ int warp_cnt[kScoreThreads / 32];
   const ScoreJob &J = jobs[blockIdx.y];
   const int n = J.r0 * J.r1;
+  if ((int)blockIdx.x * kScoreThreads >= n) return;
   const int i = blockIdx.x * kScoreThreads + threadIdx.x;
   float s = 0.f;
   int flag = 0;
@@ -117,41 +125,54 @@ __global__ void k_boxes(const ScoreJob *__restrict__ jobs, float thresh, const f
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   if (lane == 0) warp_cnt[warp] = __popc(bal);
   __syncthreads();
-  int rank = __popc(bal & ((1u << lane) - 1));
-  for (int w = 0; w < warp; w++) rank += warp_cnt[w];
-  const int idx = block_offsets[blockIdx.y * stride + blockIdx.x] + rank;
-  if (!flag) return;
-  const int y = i % J.r0, x = i / J.r0;
-  float *P = boxes + (size_t)idx * GL;
-  const float scale = J.scale;
-  root_box(x, y, scale, J.rsize0, J.rsize1, P);
-  float *Q = P + 4;
-  for (int k = 0; k < J.np; k++) {
-    const int probex = (x - 1) * 2 + J.ax[k];
-    const int probey = (y - 1) * 2 + J.ay[k];
-    long Pi = probey + (long)probex * J.part_d0[k];
-    // the reference reads outside the map here (undefined); use entry 0 instead
-    if (Pi < 0 || Pi >= (long)J.part_d0[k] * J.part_d1[k]) Pi = 0;
-    const float px = (float)arena_i[J.part_Ix[k] + Pi] + 1.0;
-    const float py = (float)arena_i[J.part_Iy[k] + Pi] + 1.0;
-    float q0 = ((py - 2.0) / 2.0 + 1.0 - (float)0) * scale;
-    float q1 = ((px - 2.0) / 2.0 + 1.0 - (float)0) * scale;
-    Q[0] = q0;
-    Q[1] = q1;
-    Q[2] = q0 + (float)J.psize0[k] * scale / 2.0 - 1.0;
-    Q[3] = q1 + (float)J.psize1[k] * scale / 2.0 - 1.0;
-    Q += 4;
+  int rank = __popc(bal & ((1u << lane) - 1)), count = 0;
+  for (int w = 0; w < kScoreThreads / 32; w++) {
+    if (w < warp) rank += warp_cnt[w];
+    count += warp_cnt[w];
   }
-  Q[0] = (float)J.comp;
-  Q[1] = s;
-  Q[2] = scale;
+  if (count == 0) return;
+  if (flag) {
+    const int y = i % J.r0, x = i / J.r0;
+    float *P = rec_s + rank * GL;
+    const float scale = J.scale;
+    root_box(x, y, scale, J.rsize0, J.rsize1, P);
+    float *Q = P + 4;
+    for (int k = 0; k < J.np; k++) {
+      const int probex = (x - 1) * 2 + J.ax[k];
+      const int probey = (y - 1) * 2 + J.ay[k];
+      long Pi = probey + (long)probex * J.part_d0[k];
+      // the reference reads outside the map here (undefined); use entry 0 instead
+      if (Pi < 0 || Pi >= (long)J.part_d0[k] * J.part_d1[k]) Pi = 0;
+      const float px = (float)arena_i[J.part_Ix[k] + Pi] + 1.0;
+      const float py = (float)arena_i[J.part_Iy[k] + Pi] + 1.0;
+      float q0 = ((py - 2.0) / 2.0 + 1.0 - (float)0) * scale;
+      float q1 = ((px - 2.0) / 2.0 + 1.0 - (float)0) * scale;
+      Q[0] = q0;
+      Q[1] = q1;
+      Q[2] = q0 + (float)J.psize0[k] * scale / 2.0 - 1.0;
+      Q[3] = q1 + (float)J.psize1[k] * scale / 2.0 - 1.0;
+      Q += 4;
+    }
+    Q[0] = (float)J.comp;
+    Q[1] = s;
+    Q[2] = scale;
+  }
+  __syncthreads();
+  float *out = boxes + (size_t)block_offsets[blockIdx.y * stride + blockIdx.x] * GL;
+  for (int t = threadIdx.x; t < count * GL; t += kScoreThreads) out[t] = rec_s[t];
 }
 
 void launch_boxes(const ScoreJob *d_jobs, int n_jobs, int max_r, float thresh, const float *arena,
                   const int *arena_i, const int *block_offsets, int stride, int GL, float *boxes, cudaStream_t s) {
   if (n_jobs <= 0) return;
   dim3 grid((max_r + kScoreThreads - 1) / kScoreThreads, n_jobs);
-  k_boxes<<<grid, kScoreThreads, 0, s>>>(d_jobs, thresh, arena, arena_i, block_offsets, stride, GL, boxes);
+  const size_t smem = sizeof(float) * kScoreThreads * GL;
+  static size_t set = 0;
+  if (smem > set && smem > 48 * 1024) {
+    cudaFuncSetAttribute(k_boxes, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    set = smem;
+  }
+  k_boxes<<<grid, kScoreThreads, smem, s>>>(d_jobs, thresh, arena, arena_i, block_offsets, stride, GL, boxes);
 }
 
 // A_SCORE in gather form: target pixel (X, Y) takes the max over every
