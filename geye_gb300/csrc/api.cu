@@ -86,7 +86,8 @@ geye_status geye_ctx_destroy(geye_ctx *ctx) {
     if (m->d_filt_off) cudaFree(m->d_filt_off);
     if (m->d_coef) cudaFree(m->d_coef);
     if (m->d_bank16) cudaFree(m->d_bank16);
-    m->d_filters = nullptr; m->d_filt_off = nullptr; m->d_coef = nullptr; m->d_bank16 = nullptr;
+    if (m->d_bank8) cudaFree(m->d_bank8);
+    m->d_filters = nullptr; m->d_filt_off = nullptr; m->d_coef = nullptr; m->d_bank16 = nullptr; m->d_bank8 = nullptr;
     m->ctx = nullptr;
   }
   ctx->models.clear();
@@ -101,7 +102,7 @@ geye_status geye_ctx_destroy(geye_ctx *ctx) {
 
 geye_status geye_ctx_set_conv_mode(geye_ctx *ctx, geye_conv_mode mode) {
   ARG_CHECK(ctx, "ctx is null");
-  ARG_CHECK(mode == GEYE_CONV_FP32 || mode == GEYE_CONV_BF16, "unknown conv mode");
+  ARG_CHECK(mode == GEYE_CONV_FP32 || mode == GEYE_CONV_BF16 || mode == GEYE_CONV_FP8, "unknown conv mode");
   ctx->conv_mode = mode;
   return GEYE_OK;
 }
@@ -161,6 +162,30 @@ geye_status geye_ctx_debug_counters(geye_ctx *ctx, long long *out, int n) {
   CUDA_TRY(cudaStreamSynchronize(ctx->stream));
   if (n > 15) out[15] = errw;
   return GEYE_OK;
+}
+
+geye_status geye_score_map(geye_ctx *ctx, const geye_model *m, int level, int comp, float *out, int cap,
+                           int dims[2]) {
+  ARG_CHECK(ctx && m && dims, "null argument");
+  ARG_CHECK(ctx->last_plan, "no run yet");
+  const geye::Plan &P = *ctx->last_plan;
+  for (auto &mp : P.models) {
+    if (mp->model != m) continue;
+    for (auto &S : mp->score_jobs) {
+      if (S.level != level || S.comp != comp) continue;
+      dims[0] = S.r0;
+      dims[1] = S.r1;
+      const size_t n = (size_t)S.r0 * S.r1;
+      if (!out) return GEYE_OK;
+      ARG_CHECK((size_t)cap >= n, "output buffer too small");
+      CUDA_TRY(cudaMemcpyAsync(out, P.arena.as<float>() + S.score_off, sizeof(float) * n, cudaMemcpyDeviceToHost,
+                               ctx->stream));
+      CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+      return GEYE_OK;
+    }
+  }
+  ARG_CHECK(false, "the last run has no score map for this model, level and component");
+  return GEYE_ERR_ARG;
 }
 
 void geye_free(void *p) { free(p); }
@@ -233,6 +258,7 @@ geye_status geye_model_free(geye_model *m) {
   if (m->d_filt_off) cudaFree(m->d_filt_off);
   if (m->d_coef) cudaFree(m->d_coef);
   if (m->d_bank16) cudaFree(m->d_bank16);
+  if (m->d_bank8) cudaFree(m->d_bank8);
   delete m;
   return GEYE_OK;
 }

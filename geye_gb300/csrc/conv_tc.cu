@@ -1,38 +1,46 @@
-// conv_bf16.cu -- root/part filter convolution on the tcgen05 tensor cores
-// (BF16 operands, FP32 accumulation in tensor memory).
+// conv_tc.cu -- root/part filter convolution on the tcgen05 tensor cores:
+// BF16 operands (kind::f16) or FP8-e4m3 operands with per-filter scaling
+// (kind::f8f6f4), FP32 accumulation in tensor memory.
 //
 // Same contraction as conv_fp32.cu (CAR_TRACKING/GPU_function.cu:302-358 and
 // :630-685): C[x][y] = sum_{c, xp, yp} A[c][x+xp][y+yp] * B[c][xp][yp], here
 // as an implicit GEMM without an im2col copy.  A level's features are kept as
-// four channel planes [q][pos][8] bf16 (pos = x*fs0 + y, channels 8q..8q+7),
-// so the 8-channel chunks of consecutive positions lie 16 bytes apart: exactly
-// the row stride of the canonical K-major, no-swizzle operand layout.  For
-// filter tap (xp, yp) the A operand of 128 consecutive output positions p is
-// then the slab rows p + xp*fs0 + yp of the staged planes: one shared-memory
-// descriptor per tap, LBO = the plane stride (next 8 channels), SBO = 128 B
-// (next 8 rows).  Positions whose window crosses a column edge are computed
-// and discarded (about (b0-1)/fs0 of the work).
+// NQ channel planes of 16 bytes per position ([q][pos][16 B], pos = x*fs0 + y):
+// four planes of 8 bf16 channels, or two planes of 16 e4m3 channels (features
+// scaled by kFp8FeatScale).  The chunks of consecutive positions lie 16 bytes
+// apart, exactly the row stride of the canonical K-major, no-swizzle operand
+// layout, so for filter tap (xp, yp) the A operand of 128 consecutive output
+// positions p is the slab rows p + xp*fs0 + yp of the staged planes: one
+// shared-memory descriptor per tap, LBO = the plane stride (next chunk of
+// channels), SBO = 128 B (next 8 rows).  An MMA takes two planes (K = 16 bf16
+// or 32 e4m3), so a tap is 2 MMAs in BF16 and 1 in FP8.  Positions whose
+// window crosses a column edge are computed and discarded ((b0-1)/fs0 of the work).
 //
-// B (the filters) is precomputed per model as [tap][q][n][8] bf16, N padded to
-// a multiple of 16, so one descriptor per (tap, channel pair) as well.
+// B (the filters) is precomputed per model as [tap][q][n][16 B] (N padded to 16
+// or 32), one descriptor per (tap, plane pair) as well.  FP8 filters are scaled
+// per filter by the power of two that brings their absolute maximum under 448;
+// the epilogue multiplies by the exact inverse of both scales.
 //
-// A CTA (4 warps) owns a run of 128-position tiles of one (level, filter
-// group): one thread bulk-copies the group's filter bank and the feature slab
-// the run touches (cp.async.bulk, completion on an mbarrier), issues 2 MMAs
-// (M=128, K=16, N=n_pad) per tap into a TMEM accumulator and commits them to
-// a second mbarrier; the four warps read the accumulator back with
-// tcgen05.ld (warp w owns TMEM lanes 32w..32w+31) and write the maps in the
-// reference layout.  Every mbarrier wait is bounded; a timeout sets an error
-// bit and the CTA still waits (bounded) for its own copies and MMAs before it
-// frees TMEM and leaves.
+// A CTA (4 warps) owns a run of up to 16 tiles of 128 positions of one (level,
+// filter group), each tile with its own TMEM accumulator.  The filter is walked
+// in column phases whose bank columns and feature slab fit in shared memory:
+// one thread bulk-copies them (cp.async.bulk, completion on an mbarrier) and
+// issues every tile's MMAs, committed to a second mbarrier; after the last
+// phase the four warps read the accumulators with tcgen05.ld (warp w owns TMEM
+// lanes 32w..32w+31) and write the maps in the reference layout.  Every
+// mbarrier wait is bounded; a timeout sets an error bit and the CTA still
+// waits (bounded) for its own copies and MMAs before it frees TMEM and leaves.
 #include <stdint.h>
 #include <string.h>
 
 #include <cuda_bf16.h>
+#include <cuda_fp8.h>
 
 #include <algorithm>
+#include <cmath>
 
 #include "runtime.h"
+#include "tc_planes.h"
 
 namespace geye {
 
@@ -40,11 +48,11 @@ constexpr int kTcThreads = 128;
 constexpr int kTcM = 128;                        // positions per tile (TMEM lanes)
 constexpr int kTcMaxTiles = 16;                  // tiles per CTA
 constexpr size_t kTcSmemBudget = 220 * 1024;     // dynamic shared memory per CTA
-constexpr int kTcHead = 256;                     // barriers, TMEM address and map offsets at the front
+constexpr int kTcHead = 384;                    // barriers, TMEM address, map offsets and scales at the front
 constexpr unsigned long long kWaitNs = 1000000000ull;   // a wait gives up after 1 s (then 4 s for the drain)
 
 struct TcJob {
-  int plane_off;     // bf16 element offset of plane 0 in arena16
+  int plane_off;     // offset of plane 0 in arena16, in 2-byte units
   int plane_cells;   // cells per plane
   int fs0, fs1;      // feature rows, columns
   int b0, b1;        // filter rows, columns
@@ -104,13 +112,21 @@ __device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
 }
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+template <int NQ>
 __device__ __forceinline__ void tc_mma(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
                                        uint32_t accumulate) {
-  asm volatile(
-      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
-      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
-      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
-      : "memory");
+  if constexpr (NQ == 4)
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+        : "memory");
+  else
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+        : "memory");
 }
 __device__ __forceinline__ void tc_commit(uint64_t *bar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
@@ -135,32 +151,42 @@ __device__ __forceinline__ uint64_t sdesc(uint32_t saddr, uint32_t lbo, uint32_t
   return d;                 // base offset 0, relative LBO, no swizzle
 }
 
-// instruction descriptor of kind::f16: D = F32, A = B = BF16, both K-major
+// instruction descriptors, D = F32, both operands K-major, dense:
+// kind::f16 with A = B = BF16 (format 1); kind::f8f6f4 with A = B = E4M3 (format 0)
 __host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
   return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+__host__ __device__ constexpr uint32_t idesc_e4m3(int M, int N) {
+  return (1u << 4) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
 }
 
 // ---------------------------------------------------------------------------
 // kernel
 // ---------------------------------------------------------------------------
+template <int NQ>
 __global__ void __launch_bounds__(kTcThreads, 1) k_conv_tc(const TcJob *__restrict__ jobs, const int4 *__restrict__ chunks,
                                                            const int *__restrict__ outs,
-                                                           const __nv_bfloat16 *__restrict__ arena16,
+                                                           const float *__restrict__ inv_scale,
+                                                           const uint8_t *__restrict__ arena16,
                                                            const uint8_t *__restrict__ bank, float *__restrict__ arena,
                                                            int *err) {
   extern __shared__ __align__(128) uint8_t sm[];
   uint64_t *bar_load = reinterpret_cast<uint64_t *>(sm);
   uint64_t *bar_mma = reinterpret_cast<uint64_t *>(sm + 8);
   uint32_t *tslot = reinterpret_cast<uint32_t *>(sm + 16);
-  int *out_s = reinterpret_cast<int *>(sm + 32);   // the job's map offsets (n <= 32)
+  int *out_s = reinterpret_cast<int *>(sm + 32);       // the job's map offsets (n <= 32)
+  float *scl_s = reinterpret_cast<float *>(sm + 160);   // and output scales
   const int4 ch = chunks[blockIdx.x];
   const TcJob J = jobs[ch.x];
   const int tile0 = ch.y, ntile = ch.z, cs = ch.w;   // cs = filter columns per phase
-  if (threadIdx.x < J.n) out_s[threadIdx.x] = outs[J.out_tab + threadIdx.x];
+  if (threadIdx.x < J.n) {
+    out_s[threadIdx.x] = outs[J.out_tab + threadIdx.x];
+    scl_s[threadIdx.x] = inv_scale[J.out_tab + threadIdx.x];
+  }
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int p_begin = tile0 * kTcM;
   const uint32_t bq = (uint32_t)J.n_pad * 16u;                 // one (tap, q) slice of the bank
-  const uint32_t col_bytes = (uint32_t)J.b0 * 4u * bq;         // one filter column of the bank
+  const uint32_t col_bytes = (uint32_t)J.b0 * NQ * bq;         // one filter column of the bank
   const uint32_t bank_room = ((uint32_t)cs * col_bytes + 127u) & ~127u;
   uint8_t *sB = sm + kTcHead;
   uint8_t *sA = sB + bank_room;
@@ -179,7 +205,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_conv_tc(const TcJob *__restri
   tc_fence_after();
   const uint32_t tmem = *tslot;
 
-  const uint32_t idesc = idesc_bf16(kTcM, J.n_pad);
+  const uint32_t idesc = NQ == 4 ? idesc_bf16(kTcM, J.n_pad) : idesc_e4m3(kTcM, J.n_pad);
   const uint32_t sA_addr = smem_u32(sA), sB_addr = smem_u32(sB);
   const int phases = (J.b1 + cs - 1) / cs;
   bool ok = true;   // uniform across the CTA (every wait outcome is combined with __syncthreads_and)
@@ -188,11 +214,12 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_conv_tc(const TcJob *__restri
     const int S = ntile * kTcM + (ncol - 1) * J.fs0 + (J.b0 - 1);   // slab cells per plane this phase
     const uint32_t plane_bytes = (uint32_t)S * 16u;
     if (threadIdx.x == 0) {
-      mbar_expect_tx(bar_load, (uint32_t)ncol * col_bytes + 4u * plane_bytes);
+      mbar_expect_tx(bar_load, (uint32_t)ncol * col_bytes + NQ * plane_bytes);
       bulk_g2s(sB, bank + J.bank_off + (size_t)xp0 * col_bytes, (uint32_t)ncol * col_bytes, bar_load);
-      for (int q = 0; q < 4; q++)
+      for (int q = 0; q < NQ; q++)
         bulk_g2s(sA + (size_t)q * plane_bytes,
-                 arena16 + J.plane_off + ((size_t)q * J.plane_cells + (size_t)p_begin + (size_t)xp0 * J.fs0) * 8,
+                 arena16 + 2 * (size_t)J.plane_off +
+                     ((size_t)q * J.plane_cells + (size_t)p_begin + (size_t)xp0 * J.fs0) * 16,
                  plane_bytes, bar_load);
     }
     bool landed = mbar_wait(bar_load, (uint32_t)(ph & 1), kWaitNs);
@@ -210,8 +237,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_conv_tc(const TcJob *__restri
       const uint64_t a_base = sdesc(sA_addr, plane_bytes, 128u);
       const uint64_t b_base = sdesc(sB_addr, bq, 128u);
       const uint32_t a_hi = 2u * (uint32_t)S;           // planes 2, 3: 2 * plane_bytes >> 4
-      const uint32_t b_tap = 4u * (uint32_t)J.n_pad;    // one tap of the bank: 4 * bq >> 4
-      const uint32_t b_hi = 2u * (uint32_t)J.n_pad;     // channels 16..31 of a tap
+      const uint32_t b_tap = NQ * (uint32_t)J.n_pad;    // one tap of the bank: NQ * bq >> 4
+      const uint32_t b_hi = 2u * (uint32_t)J.n_pad;     // planes 2, 3 of a tap
       for (int i = 0; i < ntile; i++) {
         const uint32_t d = tmem + (uint32_t)(i * J.n_pad);
         uint32_t acc = ph ? 1u : 0u;
@@ -221,8 +248,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_conv_tc(const TcJob *__restri
           for (int yp = 0; yp < J.b0; yp++) {
             const uint64_t ad = a_base + (cell0 + (uint32_t)yp);
             const uint64_t bd = b_base + (tap0 + (uint32_t)yp * b_tap);
-            tc_mma(d, ad, bd, idesc, acc);
-            tc_mma(d, ad + a_hi, bd + b_hi, idesc, 1u);
+            tc_mma<NQ>(d, ad, bd, idesc, acc);
+            if constexpr (NQ == 4) tc_mma<NQ>(d, ad + a_hi, bd + b_hi, idesc, 1u);
             acc = 1u;
           }
         }
@@ -250,7 +277,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_conv_tc(const TcJob *__restri
         for (int k = 0; k < 16 && c0 + k < J.n; k++) {
           float v;
           memcpy(&v, &r[k], 4);
-          arena[(size_t)out_s[c0 + k] + (size_t)x * J.c0 + y] = v;
+          arena[(size_t)out_s[c0 + k] + (size_t)x * J.c0 + y] = v * scl_s[c0 + k];
         }
       }
     }
@@ -260,19 +287,15 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_conv_tc(const TcJob *__restri
   if (warp == 0) tmem_dealloc(tmem, ncols);
 }
 
-// feature planes for a standalone call: [pos][32] float -> [4][ncell + pad][8] bf16
-__global__ void k_feat_planes(const float *__restrict__ feat, int ncell, __nv_bfloat16 *__restrict__ planes) {
-  const size_t plane = ((size_t)ncell + kTcPlanePad) * 8;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < ncell + kTcPlanePad; i += gridDim.x * blockDim.x)
-    for (int q = 0; q < 4; q++) {
-      __nv_bfloat162 v[4];
-      for (int k = 0; k < 4; k++) {
-        const float a = i < ncell ? feat[(size_t)i * kFeatPad + 8 * q + 2 * k] : 0.f;
-        const float b = i < ncell ? feat[(size_t)i * kFeatPad + 8 * q + 2 * k + 1] : 0.f;
-        v[k] = __floats2bfloat162_rn(a, b);
-      }
-      *reinterpret_cast<uint4 *>(planes + q * plane + (size_t)i * 8) = *reinterpret_cast<uint4 *>(v);
-    }
+// feature planes for a standalone call: [pos][32] float -> NQ planes [ncell + pad][16 B]
+template <int NQ>
+__global__ void k_feat_planes(const float *__restrict__ feat, int ncell, uint8_t *__restrict__ planes) {
+  const size_t plane = ((size_t)ncell + kTcPlanePad) * 16;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < ncell + kTcPlanePad; i += gridDim.x * blockDim.x) {
+    float f[32];
+    for (int c = 0; c < 32; c++) f[c] = i < ncell ? feat[(size_t)i * kFeatPad + c] : 0.f;
+    tc_store_planes<NQ>(f, planes, plane, i);
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -287,17 +310,47 @@ static uint16_t to_bf16(float f) {   // round to nearest even
   return (uint16_t)(u >> 16);
 }
 
-// filters of one size, one bank [tap][q][n_pad][8] bf16 each
+// e4m3 bank from FP32 filters on the device (CUDA's own conversion, as for the
+// features): element (tap t, plane q, filter n, lane k) = channel 16q + k of
+// filter n at tap t times scale[n]
+__global__ void k_bank_e4m3(const float *const *__restrict__ filt, const float *__restrict__ scale, int n, int n_pad,
+                            int taps, uint8_t *__restrict__ out) {
+  const int total = taps * 2 * n_pad * 16;
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x) {
+    const int k = e % 16, f = (e / 16) % n_pad, q = (e / (16 * n_pad)) % 2, t = e / (32 * n_pad);
+    const int c = 16 * q + k;
+    float v = 0.f;
+    if (f < n && c < kFeat) v = filt[f][(size_t)c * taps + t] * scale[f];
+    out[e] = (uint8_t)__nv_cvt_float_to_fp8(v, __NV_SATFINITE, __NV_E4M3);
+  }
+}
+
+// filters of one size, one bank [tap][q][n_pad][16 B] each
 struct BankGroup {
   int b0, b1, n, n_pad, bank_off, kind;
-  std::vector<int> filt;   // indices into the caller's filter list
+  std::vector<int> filt;      // indices into the caller's filter list
+  std::vector<float> inv;     // per filter: factor that undoes the operand scaling
 };
 
-// groups filters by (kind, size), at most 32 per group, and lays out their banks
-// (filter f is [31][b1][b0] as conv_fp32 reads it: element (c, xp, yp) at c*b0*b1 + xp*b0 + yp)
+static int tc_planes_of(geye_conv_mode mode) { return mode == GEYE_CONV_FP8 ? 2 : 4; }
+
+// power of two that brings a filter's absolute maximum under e4m3's 448
+static float e4m3_filter_scale(const float *F, size_t n) {
+  float m = 0.f;
+  for (size_t i = 0; i < n; i++) m = std::max(m, std::fabs(F[i]));
+  if (!(m > 0.f)) return 1.f;
+  return std::ldexp(1.0f, (int)std::floor(std::log2(448.0 / m)));
+}
+
+// groups filters by (kind, size), at most 32 per group; lays out their banks
+// (filter f is [31][b1][b0] as conv_fp32 reads it: element (c, xp, yp) at
+// c*b0*b1 + xp*b0 + yp).  BF16 banks are built here into bank16; for FP8
+// scale[f] is filled and the caller converts on the device.
 static void build_banks(const std::vector<const float *> &filt, const std::vector<int> &b0s,
-                        const std::vector<int> &b1s, const std::vector<int> &kinds, std::vector<BankGroup> &groups,
-                        std::vector<uint16_t> &bank) {
+                        const std::vector<int> &b1s, const std::vector<int> &kinds, geye_conv_mode mode,
+                        std::vector<BankGroup> &groups, std::vector<uint16_t> &bank16, std::vector<float> &scale,
+                        size_t &total) {
+  const int NQ = tc_planes_of(mode);
   groups.clear();
   for (size_t f = 0; f < filt.size(); f++) {
     bool placed = false;
@@ -308,40 +361,81 @@ static void build_banks(const std::vector<const float *> &filt, const std::vecto
         placed = true;
         break;
       }
-    if (!placed) groups.push_back(BankGroup{b0s[f], b1s[f], 1, 0, 0, kinds[f], {(int)f}});
+    if (!placed) groups.push_back(BankGroup{b0s[f], b1s[f], 1, 0, 0, kinds[f], {(int)f}, {}});
   }
-  size_t total = 0;
+  total = 0;
   for (auto &g : groups) {
     g.n_pad = g.n <= 16 ? 16 : 32;
     g.bank_off = (int)total;
-    total += (size_t)g.b0 * g.b1 * 4 * g.n_pad * 16;
+    total += (size_t)g.b0 * g.b1 * NQ * g.n_pad * 16;
   }
-  bank.assign(total / 2, 0);
+  scale.assign(filt.size(), 1.f);
   for (auto &g : groups) {
-    uint16_t *dst = bank.data() + g.bank_off / 2;
+    const int taps = g.b0 * g.b1;
+    for (int f : g.filt) {
+      if (mode == GEYE_CONV_FP8) scale[f] = e4m3_filter_scale(filt[f], (size_t)taps * kFeat);
+      g.inv.push_back(mode == GEYE_CONV_FP8 ? 1.0f / (scale[f] * kFp8FeatScale) : 1.0f);
+    }
+  }
+  if (mode == GEYE_CONV_FP8) return;
+  bank16.assign(total / 2, 0);
+  for (auto &g : groups) {
+    uint16_t *dst = bank16.data() + g.bank_off / 2;
     const int taps = g.b0 * g.b1;
     for (int n = 0; n < g.n; n++) {
       const float *F = filt[g.filt[n]];
-      for (int xp = 0; xp < g.b1; xp++)
-        for (int yp = 0; yp < g.b0; yp++) {
-          const int t = xp * g.b0 + yp;
-          for (int c = 0; c < kFeat; c++)
-            dst[(((size_t)t * 4 + (c >> 3)) * g.n_pad + n) * 8 + (c & 7)] = to_bf16(F[(size_t)c * taps + t]);
-        }
+      for (int t = 0; t < taps; t++)
+        for (int c = 0; c < kFeat; c++)
+          dst[(((size_t)t * 4 + (c >> 3)) * g.n_pad + n) * 8 + (c & 7)] = to_bf16(F[(size_t)c * taps + t]);
     }
   }
+}
+
+// device bank of the groups (d_bank sized total); d_filt: the filters on the device
+static geye_status upload_bank(const std::vector<BankGroup> &groups, geye_conv_mode mode,
+                               const std::vector<uint16_t> &bank16, const std::vector<const float *> &d_filt,
+                               const std::vector<float> &scale, size_t total, void *d_bank, cudaStream_t s) {
+  if (mode != GEYE_CONV_FP8) {
+    CUDA_TRY(cudaMemcpyAsync(d_bank, bank16.data(), total, cudaMemcpyHostToDevice, s));
+    return GEYE_OK;
+  }
+  for (auto &g : groups) {
+    std::vector<const float *> ptrs;
+    std::vector<float> sc;
+    for (int f : g.filt) { ptrs.push_back(d_filt[f]); sc.push_back(scale[f]); }
+    const float **d_ptrs = nullptr;
+    float *d_sc = nullptr;
+    CUDA_TRY(cudaMalloc(&d_ptrs, sizeof(float *) * ptrs.size()));
+    cudaError_t e = cudaMalloc(&d_sc, sizeof(float) * sc.size());
+    if (e == cudaSuccess) e = cudaMemcpy(d_ptrs, ptrs.data(), sizeof(float *) * ptrs.size(), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(d_sc, sc.data(), sizeof(float) * sc.size(), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) {
+      const int taps = g.b0 * g.b1, elems = taps * 2 * g.n_pad * 16;
+      k_bank_e4m3<<<std::max(1, std::min((elems + 255) / 256, 1024)), 256, 0, s>>>(
+          d_ptrs, d_sc, g.n, g.n_pad, taps, static_cast<uint8_t *>(d_bank) + g.bank_off);
+      e = cudaStreamSynchronize(s);
+    }
+    cudaFree(d_ptrs);
+    cudaFree(d_sc);
+    if (e != cudaSuccess) {
+      set_error(std::string("e4m3 filter bank: ") + cudaGetErrorString(e));
+      return GEYE_ERR_CUDA;
+    }
+  }
+  return GEYE_OK;
 }
 
 struct TcTables {
   std::vector<TcJob> jobs;
   std::vector<int4> chunks;
   std::vector<int> outs;
+  std::vector<float> inv;
   size_t max_smem = 0;
 };
 
 // one job: group g on a level whose planes start at plane_off; map_off[k] is
 // the float offset of filter k's output map.  False if it cannot fit in shared memory.
-static bool add_tc_job(TcTables &T, int plane_off, int fs0, int fs1, const BankGroup &g,
+static bool add_tc_job(TcTables &T, int NQ, int plane_off, int fs0, int fs1, const BankGroup &g,
                        const std::vector<int> &map_off) {
   TcJob J{};
   J.plane_off = plane_off;
@@ -353,16 +447,19 @@ static bool add_tc_job(TcTables &T, int plane_off, int fs0, int fs1, const BankG
   J.n = g.n; J.n_pad = g.n_pad;
   J.bank_off = g.bank_off;
   J.out_tab = (int)T.outs.size();
-  for (int k = 0; k < g.n; k++) T.outs.push_back(map_off[k]);
+  for (int k = 0; k < g.n; k++) {
+    T.outs.push_back(map_off[k]);
+    T.inv.push_back(g.inv[k]);
+  }
   const int P_valid = (J.c1 - 1) * J.fs0 + J.c0;
   J.ntiles = (P_valid + kTcM - 1) / kTcM;
   // tiles per CTA (T) and filter columns per phase (cs): one phase when the whole
   // bank and slab fit, else fewer columns per phase; every phase needs
-  // head + bank columns + (T*128 + (cs-1)*fs0 + b0-1) cells x 64 B
-  const size_t col_bytes = (size_t)g.b0 * 4 * g.n_pad * 16;
+  // head + bank columns + NQ planes of (T*128 + (cs-1)*fs0 + b0-1) cells x 16 B
+  const size_t col_bytes = (size_t)g.b0 * NQ * g.n_pad * 16;
   auto need = [&](int Tc, int cs) {
     return (size_t)kTcHead + ((cs * col_bytes + 127) & ~(size_t)127) +
-           ((size_t)Tc * kTcM + (size_t)(cs - 1) * fs0 + (g.b0 - 1)) * 64;
+           ((size_t)Tc * kTcM + (size_t)(cs - 1) * fs0 + (g.b0 - 1)) * 16 * NQ;
   };
   int T_cta = 0, cs = 0;
   for (int Tc : {kTcMaxTiles, 8, 4}) {
@@ -386,46 +483,54 @@ static bool add_tc_job(TcTables &T, int plane_off, int fs0, int fs1, const BankG
   return true;
 }
 
-static void launch_conv_tc(const TcJob *jobs, const int4 *chunks, int n_chunks, const int *outs,
-                           const __nv_bfloat16 *arena16, const uint8_t *bank, float *out, int *err, size_t smem,
-                           cudaStream_t s) {
-  cudaFuncSetAttribute(k_conv_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  k_conv_tc<<<n_chunks, kTcThreads, smem, s>>>(jobs, chunks, outs, arena16, bank, out, err);
+static void launch_conv_tc(int NQ, const TcJob *jobs, const int4 *chunks, int n_chunks, const int *outs,
+                           const float *inv, const uint8_t *planes, const uint8_t *bank, float *out, int *err,
+                           size_t smem, cudaStream_t s) {
+  if (NQ == 4) {
+    cudaFuncSetAttribute(k_conv_tc<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k_conv_tc<4><<<n_chunks, kTcThreads, smem, s>>>(jobs, chunks, outs, inv, planes, bank, out, err);
+  } else {
+    cudaFuncSetAttribute(k_conv_tc<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k_conv_tc<2><<<n_chunks, kTcThreads, smem, s>>>(jobs, chunks, outs, inv, planes, bank, out, err);
+  }
 }
 
-// the model's banks (built once per model, roots and parts in separate groups)
-static geye_status ensure_bank(geye_model *m, std::vector<BankGroup> &groups) {
+// the model's banks for a precision (built once per model and mode; roots and
+// parts in separate groups)
+static geye_status ensure_bank(geye_ctx *ctx, geye_model *m, geye_conv_mode mode, std::vector<BankGroup> &groups) {
   const HostModel &h = m->h;
-  std::vector<const float *> filt;
+  std::vector<const float *> filt, d_filt;
   std::vector<int> b0s, b1s, kinds;
   for (int r = 0; r < h.NoR; r++) {
     filt.push_back(h.rootfilter[r].data());
+    d_filt.push_back(m->d_filters + m->filt_off[r]);
     b0s.push_back(h.root_size[3 * r]); b1s.push_back(h.root_size[3 * r + 1]); kinds.push_back(0);
   }
   for (int p = 0; p < h.NoP; p++) {
     filt.push_back(h.partfilter[p].data());
+    d_filt.push_back(m->d_filters + m->filt_off[h.NoR + p]);
     b0s.push_back(h.part_size[3 * p]); b1s.push_back(h.part_size[3 * p + 1]); kinds.push_back(1);
   }
-  std::vector<uint16_t> bank;
-  build_banks(filt, b0s, b1s, kinds, groups, bank);
-  if (m->d_bank16) return GEYE_OK;
-  cudaError_t e = cudaMalloc(&m->d_bank16, std::max<size_t>(bank.size() * 2, 16));
-  if (e == cudaSuccess) e = cudaMemcpy(m->d_bank16, bank.data(), bank.size() * 2, cudaMemcpyHostToDevice);
-  if (e != cudaSuccess) {
-    set_error(std::string("bf16 filter bank: ") + cudaGetErrorString(e));
-    return GEYE_ERR_CUDA;
-  }
-  m->bank16_bytes = bank.size() * 2;
-  return GEYE_OK;
+  std::vector<uint16_t> bank16;
+  std::vector<float> scale;
+  size_t total = 0;
+  build_banks(filt, b0s, b1s, kinds, mode, groups, bank16, scale, total);
+  void *&d_bank = mode == GEYE_CONV_FP8 ? m->d_bank8 : m->d_bank16;
+  if (d_bank) return GEYE_OK;
+  CUDA_TRY(cudaMalloc(&d_bank, std::max<size_t>(total, 16)));
+  const geye_status st = upload_bank(groups, mode, bank16, d_filt, scale, total, d_bank, ctx->stream);
+  CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  return st;
 }
 
 geye_status build_tc_jobs(geye_ctx *ctx, Plan &P, ModelPlan &mp) {
   geye_model *m = mp.model;
   const HostModel &h = m->h;
+  const geye_conv_mode mode = ctx->conv_mode;
   std::vector<BankGroup> groups;
-  GEYE_TRY(ensure_bank(m, groups));
+  GEYE_TRY(ensure_bank(ctx, m, mode, groups));
   TcTables T;
-  const int NoC = h.numcomponent, NoP = h.NoP, interval = h.interval;
+  const int NoC = h.numcomponent, NoP = h.NoP, interval = h.interval, NQ = tc_planes_of(mode);
   for (int level = interval; level < mp.LEN; level++) {
     if (mp.skipped[level]) continue;
     const int Lv = level - interval;
@@ -434,82 +539,100 @@ geye_status build_tc_jobs(geye_ctx *ctx, Plan &P, ModelPlan &mp) {
       const bool root = g.kind == 0;
       for (int f : g.filt) map_off.push_back(root ? mp.root_map_off[level * NoC + f] : mp.part_map_off[Lv * NoP + (f - h.NoR)]);
       for (int v : map_off)
-        if (v < 0) { set_error("bf16 conv: filter map missing from the plan"); return GEYE_ERR_UNSUPPORTED; }
+        if (v < 0) { set_error("tensor-core conv: filter map missing from the plan"); return GEYE_ERR_UNSUPPORTED; }
       const LevelInfo &L = root ? P.lv[level] : P.lv[Lv];
-      if (!add_tc_job(T, L.feat16_off, L.fs0, L.fs1, g, map_off)) {
-        set_error("bf16 conv: a filter bank and its feature reach exceed shared memory");
+      if (!add_tc_job(T, NQ, L.feat16_off, L.fs0, L.fs1, g, map_off)) {
+        set_error("tensor-core conv: a filter bank and its feature reach exceed shared memory");
         return GEYE_ERR_UNSUPPORTED;
       }
     }
   }
   mp.tc_smem = T.max_smem;
   mp.tc_chunks = (int)T.chunks.size();
+  mp.tc_planes = NQ;
   GEYE_TRY(upload_bytes(ctx, mp.d_tc_jobs, T.jobs.data(), sizeof(TcJob) * T.jobs.size()));
   GEYE_TRY(upload_bytes(ctx, mp.d_tc_chunks, T.chunks.data(), sizeof(int4) * T.chunks.size()));
   GEYE_TRY(upload_bytes(ctx, mp.d_tc_outs, T.outs.data(), sizeof(int) * T.outs.size()));
+  GEYE_TRY(upload_bytes(ctx, mp.d_tc_inv, T.inv.data(), sizeof(float) * T.inv.size()));
   return GEYE_OK;
 }
 
-geye_status run_conv_bf16(geye_ctx *ctx, Plan &P, ModelPlan &mp) {
+geye_status run_conv_tc(geye_ctx *ctx, Plan &P, ModelPlan &mp) {
   if (mp.tc_chunks == 0) return GEYE_OK;
   if (!P.arena16.p) {
-    set_error("bf16 conv: the plan has no bf16 feature planes");
+    set_error("tensor-core conv: the plan has no feature planes");
     return GEYE_ERR_UNSUPPORTED;
   }
-  launch_conv_tc(mp.d_tc_jobs.as<TcJob>(), mp.d_tc_chunks.as<int4>(), mp.tc_chunks, mp.d_tc_outs.as<int>(),
-                 P.arena16.as<__nv_bfloat16>(), reinterpret_cast<const uint8_t *>(mp.model->d_bank16),
-                 P.arena.as<float>(), P.d_small.as<int>() + 130, mp.tc_smem, ctx->stream);
+  const void *bank = mp.tc_planes == 2 ? mp.model->d_bank8 : mp.model->d_bank16;
+  launch_conv_tc(mp.tc_planes, mp.d_tc_jobs.as<TcJob>(), mp.d_tc_chunks.as<int4>(), mp.tc_chunks,
+                 mp.d_tc_outs.as<int>(), mp.d_tc_inv.as<float>(), P.arena16.as<uint8_t>(),
+                 static_cast<const uint8_t *>(bank), P.arena.as<float>(), P.d_small.as<int>() + 130, mp.tc_smem,
+                 ctx->stream);
   ctx->launches++;
   const cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) {
-    set_error(std::string("bf16 conv: ") + cudaGetErrorString(e));
+    set_error(std::string("tensor-core conv: ") + cudaGetErrorString(e));
     return GEYE_ERR_CUDA;
   }
   return GEYE_OK;
 }
 
-// fconvsMT on the tensor cores for the stage entry point: d_feat is [pos][32]
-// float on the device (a0 x a1 cells), filters on the host; maps go to
-// d_out + out_off[i].  Temporary device buffers live in tmp.
-geye_status conv_bf16_maps(geye_ctx *ctx, const float *d_feat, int a0, int a1, const float *const *filters,
-                           const int *b_dims, int n_filters, float *d_out, const std::vector<int> &out_off,
-                           std::vector<std::unique_ptr<DevBuf>> &tmp) {
-  std::vector<const float *> filt(filters, filters + n_filters);
+// fconvsMT on the tensor cores for the stage entry point (the context's conv
+// mode): d_feat is [pos][32] float on the device (a0 x a1 cells), filters on
+// the host; maps go to d_out + out_off[i].  Temporary device buffers live in tmp.
+geye_status conv_tc_maps(geye_ctx *ctx, const float *d_feat, int a0, int a1, const float *const *filters,
+                         const int *b_dims, int n_filters, float *d_out, const std::vector<int> &out_off,
+                         std::vector<std::unique_ptr<DevBuf>> &tmp) {
+  const geye_conv_mode mode = ctx->conv_mode;
+  const int NQ = tc_planes_of(mode);
+  auto buf = [&]() { tmp.push_back(std::make_unique<DevBuf>()); return tmp.back().get(); };
+  std::vector<const float *> filt(filters, filters + n_filters), d_filt;
   std::vector<int> b0s, b1s, kinds(n_filters, 0);
   for (int i = 0; i < n_filters; i++) { b0s.push_back(b_dims[2 * i]); b1s.push_back(b_dims[2 * i + 1]); }
   std::vector<BankGroup> groups;
-  std::vector<uint16_t> bank;
-  build_banks(filt, b0s, b1s, kinds, groups, bank);
+  std::vector<uint16_t> bank16;
+  std::vector<float> scale;
+  size_t total = 0;
+  build_banks(filt, b0s, b1s, kinds, mode, groups, bank16, scale, total);
+  for (int i = 0; i < n_filters; i++) {   // the FP8 bank is converted on the device from FP32 copies
+    DevBuf *f = buf();
+    const size_t n = (size_t)b0s[i] * b1s[i] * kFeat;
+    GEYE_TRY(upload_bytes(ctx, *f, filters[i], sizeof(float) * n));
+    d_filt.push_back(f->as<float>());
+  }
   TcTables T;
   for (auto &g : groups) {
     std::vector<int> map_off;
     for (int f : g.filt) map_off.push_back(out_off[f]);
-    if (!add_tc_job(T, 0, a0, a1, g, map_off)) {
-      set_error("bf16 conv: a filter bank and its feature reach exceed shared memory");
+    if (!add_tc_job(T, NQ, 0, a0, a1, g, map_off)) {
+      set_error("tensor-core conv: a filter bank and its feature reach exceed shared memory");
       return GEYE_ERR_UNSUPPORTED;
     }
   }
-  auto buf = [&]() { tmp.push_back(std::make_unique<DevBuf>()); return tmp.back().get(); };
-  DevBuf *planes = buf(), *d_bank = buf(), *d_jobs = buf(), *d_chunks = buf(), *d_outs = buf(), *d_err = buf();
+  DevBuf *planes = buf(), *d_bank = buf(), *d_jobs = buf(), *d_chunks = buf(), *d_outs = buf(), *d_inv = buf(),
+         *d_err = buf();
   const int ncell = a0 * a1;
-  GEYE_TRY(planes->alloc(ctx, (size_t)4 * (ncell + kTcPlanePad) * 8 * 2));
-  GEYE_TRY(upload_bytes(ctx, *d_bank, bank.data(), bank.size() * 2));
+  GEYE_TRY(planes->alloc(ctx, (size_t)NQ * (ncell + kTcPlanePad) * 16));
+  GEYE_TRY(d_bank->alloc(ctx, std::max<size_t>(total, 16)));
+  GEYE_TRY(upload_bank(groups, mode, bank16, d_filt, scale, total, d_bank->p, ctx->stream));
   GEYE_TRY(upload_bytes(ctx, *d_jobs, T.jobs.data(), sizeof(TcJob) * T.jobs.size()));
   GEYE_TRY(upload_bytes(ctx, *d_chunks, T.chunks.data(), sizeof(int4) * T.chunks.size()));
   GEYE_TRY(upload_bytes(ctx, *d_outs, T.outs.data(), sizeof(int) * T.outs.size()));
+  GEYE_TRY(upload_bytes(ctx, *d_inv, T.inv.data(), sizeof(float) * T.inv.size()));
   GEYE_TRY(d_err->alloc(ctx, 16));
   CUDA_TRY(cudaMemsetAsync(d_err->p, 0, 16, ctx->stream));
-  k_feat_planes<<<std::max(1, std::min((ncell + kTcPlanePad + 255) / 256, 1024)), 256, 0, ctx->stream>>>(
-      d_feat, ncell, planes->as<__nv_bfloat16>());
-  launch_conv_tc(d_jobs->as<TcJob>(), d_chunks->as<int4>(), (int)T.chunks.size(), d_outs->as<int>(),
-                 planes->as<__nv_bfloat16>(), d_bank->as<uint8_t>(), d_out, d_err->as<int>(), T.max_smem,
-                 ctx->stream);
+  const int grid = std::max(1, std::min((ncell + kTcPlanePad + 255) / 256, 1024));
+  if (NQ == 4) k_feat_planes<4><<<grid, 256, 0, ctx->stream>>>(d_feat, ncell, planes->as<uint8_t>());
+  else k_feat_planes<2><<<grid, 256, 0, ctx->stream>>>(d_feat, ncell, planes->as<uint8_t>());
+  launch_conv_tc(NQ, d_jobs->as<TcJob>(), d_chunks->as<int4>(), (int)T.chunks.size(), d_outs->as<int>(),
+                 d_inv->as<float>(), planes->as<uint8_t>(), d_bank->as<uint8_t>(), d_out, d_err->as<int>(),
+                 T.max_smem, ctx->stream);
   CUDA_TRY(cudaGetLastError());
   int errw = 0;
   CUDA_TRY(cudaMemcpyAsync(&errw, d_err->p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
   CUDA_TRY(cudaStreamSynchronize(ctx->stream));
   if (errw) {
-    set_error("bf16 conv: a tensor-core wait ran out (error bits " + std::to_string(errw) + ")");
+    set_error("tensor-core conv: a tensor-core wait ran out (error bits " + std::to_string(errw) + ")");
     return GEYE_ERR_TIMEOUT;
   }
   return GEYE_OK;

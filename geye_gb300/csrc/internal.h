@@ -42,7 +42,8 @@ struct HogJob {
   int hist_off;            // [18][b1*b0] then norm [b1*b0] at hist_off + 18*b1*b0
   int fs0, fs1;            // output cells
   int feat_off;            // [pos][32] float
-  int feat16_off;          // bf16 planes [4][fs0*fs1 + kTcPlanePad][8] (element offset), -1 = not written
+  int feat16_off;          // tensor-core planes (offset in 2-byte units), -1 = not written
+  int tc_planes;           // 4: bf16 planes [4][fs0*fs1 + kTcPlanePad][16 B]; 2: e4m3 planes; 0: none
 };
 
 struct ConvJob {           // a block of outputs of one (level, filter group)
@@ -71,6 +72,7 @@ struct ScoreJob {          // one (level, component) score map
   int score_off;           // output score map
   int np;
   int comp;
+  int level;               // pyramid level of the root map
   float scale;             // sbin / scales[level]
   int rsize0, rsize1;      // component root size (boxes, A_SCORE)
   int RY, RX;              // A_SCORE shifts
@@ -124,9 +126,9 @@ struct geye_model {
   int *d_filt_off = nullptr;   // float offsets, NoR + NoP entries
   float *d_coef = nullptr;     // box regression [comp][x1, y1, x2, y2][ML]
   std::vector<int> filt_off;
-  // bf16 filter banks for the tensor-core convolution (built on first use)
+  // filter banks for the tensor-core convolution (built on first use): bf16, e4m3
   void *d_bank16 = nullptr;
-  size_t bank16_bytes = 0;
+  void *d_bank8 = nullptr;
   int gl() const { return (h.numpart[0] + 1) * 4 + 3; }
 };
 
@@ -140,7 +142,7 @@ void launch_ingest(const uint8_t *bgr, int width, int height, int width_step, fl
 void launch_resize_pass(const ResizeJob *d_jobs, int n_jobs, int max_items, int vertical, const int *d_tap_start,
                         const int *d_tap_si, const float *d_tap_alpha, float *arena, cudaStream_t s);
 void launch_hog(const HogJob *d_jobs, int n_jobs, int max_b, int max_cells, float *arena, void *arena16,
-                cudaStream_t s);
+                cudaStream_t s);   // arena16: base of the tensor-core planes (bytes)
 void launch_to_ref_layout(const float *feat, int fs0, int fs1, float *out, cudaStream_t s);
 void launch_from_ref_layout(const float *ref, int fs0, int fs1, float *feat, cudaStream_t s);
 void launch_conv_fp32(const ConvJob *d_jobs, int n_jobs, int max_tiles_y, int max_tiles_x, const float *filters,

@@ -13,6 +13,7 @@
 #include <cuda_bf16.h>
 
 #include "internal.h"
+#include "tc_planes.h"
 
 namespace geye {
 
@@ -227,10 +228,9 @@ __global__ void __launch_bounds__(kTB0 *kTB1) k_hog_hist(const HogJob *__restric
 }
 
 // 31 features per output cell (featurepyramid.cpp:421-487), written as 32
-// floats [pos][32] (channel 31 = 0), plus an optional bf16 copy as four
-// channel planes [q][pos][8].
-__global__ void k_hog_feat(const HogJob *__restrict__ jobs, float *__restrict__ arena,
-                           __nv_bfloat16 *__restrict__ arena16) {
+// floats [pos][32] (channel 31 = 0), plus an optional copy as the tensor-core
+// convolution's channel planes (tc_planes.h).
+__global__ void k_hog_feat(const HogJob *__restrict__ jobs, float *__restrict__ arena, uint8_t *__restrict__ arena16) {
   const HogJob J = jobs[blockIdx.y];
   const int ncell = J.fs0 * J.fs1;
   const int b0 = J.b0, nb = J.b0 * J.b1;
@@ -282,15 +282,11 @@ __global__ void k_hog_feat(const HogJob *__restrict__ jobs, float *__restrict__ 
     float4 *dst = reinterpret_cast<float4 *>(feat + (size_t)i * kFeatPad);
 #pragma unroll
     for (int q = 0; q < 8; q++) dst[q] = make_float4(out[4 * q], out[4 * q + 1], out[4 * q + 2], out[4 * q + 3]);
-    if (J.feat16_off >= 0 && arena16) {   // planes [q][pos][8] for the tensor-core convolution
-      const size_t plane = ((size_t)ncell + kTcPlanePad) * 8;
-#pragma unroll
-      for (int q = 0; q < 4; q++) {
-        __nv_bfloat162 v[4];
-#pragma unroll
-        for (int k = 0; k < 4; k++) v[k] = __floats2bfloat162_rn(out[8 * q + 2 * k], out[8 * q + 2 * k + 1]);
-        *reinterpret_cast<uint4 *>(arena16 + J.feat16_off + q * plane + (size_t)i * 8) = *reinterpret_cast<uint4 *>(v);
-      }
+    if (J.feat16_off >= 0 && arena16) {   // planes for the tensor-core convolution
+      uint8_t *planes = arena16 + 2 * (size_t)J.feat16_off;
+      const size_t plane = ((size_t)ncell + kTcPlanePad) * 16;
+      if (J.tc_planes == 4) tc_store_planes<4>(out, planes, plane, i);
+      else if (J.tc_planes == 2) tc_store_planes<2>(out, planes, plane, i);
     }
   }
 }
@@ -314,7 +310,7 @@ void launch_hog(const HogJob *d_jobs, int n_jobs, int max_b0, int max_b1, float 
   int bx = (max_cells + 255) / 256;
   if (bx > 512) bx = 512;
   dim3 g2(bx, n_jobs);
-  k_hog_feat<<<g2, 256, 0, s>>>(d_jobs, arena, reinterpret_cast<__nv_bfloat16 *>(arena16));
+  k_hog_feat<<<g2, 256, 0, s>>>(d_jobs, arena, reinterpret_cast<uint8_t *>(arena16));
 }
 
 // ----------------------------------------------------------------------------

@@ -351,6 +351,7 @@ static geye_status build_model_plan(geye_ctx *ctx, Plan &P, geye_model *mdl, int
       S.score_off = A.take((size_t)r0 * r1);
       S.np = m.numpart[c];
       S.comp = c;
+      S.level = level;
       S.scale = (float)m.sbin / P.lv[level].scale;
       S.rsize0 = m.rsize[2 * c];
       S.rsize1 = m.rsize[2 * c + 1];
@@ -400,14 +401,14 @@ static geye_status build_model_plan(geye_ctx *ctx, Plan &P, geye_model *mdl, int
   GEYE_TRY(upload(ctx, mp->d_dt_jobs, mp->dt_jobs));
   GEYE_TRY(upload(ctx, mp->d_score_jobs, mp->score_jobs));
   GEYE_TRY(mp->d_counts.alloc(ctx, sizeof(int) * ((size_t)std::max<size_t>(mp->score_jobs.size(), 1) * std::max(mp->score_stride, 1) + 8)));
-  if (ctx->conv_mode == GEYE_CONV_BF16) GEYE_TRY(build_tc_jobs(ctx, P, *mp));
+  if (ctx->conv_mode != GEYE_CONV_FP32) GEYE_TRY(build_tc_jobs(ctx, P, *mp));
   P.models.push_back(std::move(mp));
   return GEYE_OK;
 }
 
 // Pyramid levels of a frame: sizes (featurepyramid.cpp.org:578-628) and jobs.
 static geye_status build_pyramid_plan(geye_ctx *ctx, Plan &P, int width, int height, int LEN, int interval, int sbin,
-                                      ArenaAlloc &A, bool want_bf16) {
+                                      ArenaAlloc &A, int tc_planes) {
   P.width = width; P.height = height; P.LEN = LEN; P.interval = interval; P.sbin = sbin;
   P.lv.assign(LEN, LevelInfo{});
   const int sbin2 = (int)floor((double)sbin / 2.0);
@@ -500,16 +501,17 @@ static geye_status build_pyramid_plan(geye_ctx *ctx, Plan &P, int width, int hei
     int b0, b1;
     feature_dims(L.img_h, L.img_w, L.sbin, b0, b1, L.fs0, L.fs1);
     L.feat_off = A.take((size_t)std::max(L.fs0 * L.fs1, 1) * kFeatPad);
-    if (want_bf16) {   // 4 planes [fs0*fs1 + kTcPlanePad][8]
+    if (tc_planes) {   // tc_planes planes [fs0*fs1 + kTcPlanePad][16 B]
       size_t o = (P.arena16_elems + 63) & ~size_t(63);
       L.feat16_off = (int)o;
-      P.arena16_elems = o + (size_t)4 * ((size_t)L.fs0 * L.fs1 + kTcPlanePad) * 8;
+      P.arena16_elems = o + (size_t)tc_planes * ((size_t)L.fs0 * L.fs1 + kTcPlanePad) * 8;
     }
     L.hist_off = A.take((size_t)19 * std::max(b0 * b1, 1));
     if (b0 > 0 && b1 > 0) {
       HogJob J{};
       J.img_off = L.img_off; J.h = L.img_h; J.w = L.img_w; J.sbin = L.sbin; J.b0 = b0; J.b1 = b1;
       J.hist_off = L.hist_off; J.fs0 = L.fs0; J.fs1 = L.fs1; J.feat_off = L.feat_off; J.feat16_off = L.feat16_off;
+      J.tc_planes = tc_planes;
       P.hog_jobs.push_back(J);
       P.hog_max_b0 = std::max(P.hog_max_b0, b0);
       P.hog_max_b1 = std::max(P.hog_max_b1, b1);
@@ -559,9 +561,9 @@ static geye_status finish_plan(geye_ctx *ctx, Plan &P, ArenaAlloc &A) {
   return GEYE_OK;
 }
 
-static std::string plan_key(int width, int height, geye_model *const *models, int n, const int *LENs, bool bf16) {
+static std::string plan_key(int width, int height, geye_model *const *models, int n, const int *LENs, int mode) {
   std::ostringstream os;
-  os << width << "x" << height << (bf16 ? "b" : "f");
+  os << width << "x" << height << "m" << mode;
   for (int i = 0; i < n; i++) os << ":" << models[i]->id << "/" << LENs[i];
   return os.str();
 }
@@ -586,13 +588,13 @@ static geye_status get_frame_plan(geye_ctx *ctx, geye_model *const *models, int 
     LENs[i] = m->max_scale + interval;
     LEN = std::max(LEN, LENs[i]);
   }
-  const bool bf16 = ctx->conv_mode == GEYE_CONV_BF16;
-  std::string key = plan_key(width, height, models, n_models, LENs.data(), bf16);
+  const int tc_planes = ctx->conv_mode == GEYE_CONV_BF16 ? 4 : ctx->conv_mode == GEYE_CONV_FP8 ? 2 : 0;
+  std::string key = plan_key(width, height, models, n_models, LENs.data(), (int)ctx->conv_mode);
   auto it = ctx->plans.find(key);
   if (it != ctx->plans.end()) { *out = it->second.get(); return GEYE_OK; }
   auto P = std::make_unique<Plan>();
   ArenaAlloc A;
-  GEYE_TRY(build_pyramid_plan(ctx, *P, width, height, LEN, interval, sbin, A, bf16));
+  GEYE_TRY(build_pyramid_plan(ctx, *P, width, height, LEN, interval, sbin, A, tc_planes));
   for (int i = 0; i < n_models; i++) GEYE_TRY(build_model_plan(ctx, *P, models[i], LENs[i], A));
   GEYE_TRY(finish_plan(ctx, *P, A));
   GEYE_TRY(P->d_bgr.alloc(ctx, (size_t)width * height * 3 + 64));
@@ -661,12 +663,12 @@ geye_status run_hog(geye_ctx *ctx, Plan &P) {
   return check_launch(ctx, "hog");
 }
 
-geye_status run_conv_bf16(geye_ctx *ctx, Plan &P, ModelPlan &mp);
+geye_status run_conv_tc(geye_ctx *ctx, Plan &P, ModelPlan &mp);
 
 geye_status run_conv(geye_ctx *ctx, Plan &P, ModelPlan &mp) {
   geye_model *m = mp.model;
   float *arena = P.arena.as<float>();
-  if (ctx->conv_mode == GEYE_CONV_BF16) return run_conv_bf16(ctx, P, mp);
+  if (ctx->conv_mode != GEYE_CONV_FP32) return run_conv_tc(ctx, P, mp);
   if (!mp.root_jobs.empty()) {
     launch_conv_fp32(mp.d_root_jobs.as<ConvJob>(), (int)mp.root_jobs.size(), mp.root_tiles_y, mp.root_tiles_x,
                      m->d_filters, m->d_filt_off, arena, arena, mp.root_max_b0, mp.root_max_b1, mp.root_max_g,

@@ -42,12 +42,12 @@ struct Plan;
 struct ModelPlan;
 // copies n bytes from the host into buf (allocated to fit)
 geye_status upload_bytes(geye_ctx *ctx, DevBuf &buf, const void *src, size_t n);
-// tensor-core convolution job tables of one model of a plan (conv_bf16.cu)
+// tensor-core convolution job tables of one model of a plan (conv_tc.cu)
 geye_status build_tc_jobs(geye_ctx *ctx, Plan &P, ModelPlan &mp);
 // tensor-core fconvsMT of one feature map ([pos][32] float on the device) for the stage entry point
-geye_status conv_bf16_maps(geye_ctx *ctx, const float *d_feat, int a0, int a1, const float *const *filters,
-                           const int *b_dims, int n_filters, float *d_out, const std::vector<int> &out_off,
-                           std::vector<std::unique_ptr<DevBuf>> &tmp);
+geye_status conv_tc_maps(geye_ctx *ctx, const float *d_feat, int a0, int a1, const float *const *filters,
+                         const int *b_dims, int n_filters, float *d_out, const std::vector<int> &out_off,
+                         std::vector<std::unique_ptr<DevBuf>> &tmp);
 
 // Device buffer owned by a plan or context.
 struct DevBuf {
@@ -67,7 +67,7 @@ struct LevelInfo {
   int sbin = 0;
   float scale = 0.f;          // scales[] entry
   int feat_off = -1;          // [pos][32]
-  int feat16_off = -1;        // bf16 elements
+  int feat16_off = -1;        // tensor-core planes, 2-byte units
   int hist_off = -1;
 };
 
@@ -89,9 +89,10 @@ struct ModelPlan {
   std::vector<int> part_map_off, part_d0, part_d1;     // [L*NoP + p]
   std::vector<int> skipped;                            // per level
   double conv_flops = 0, conv_bytes = 0, dt_bytes = 0, score_bytes = 0;
-  // tensor-core convolution (conv_bf16.cu): jobs, CTA chunks, map offsets
-  DevBuf d_tc_jobs, d_tc_chunks, d_tc_outs;
-  int tc_chunks = 0;
+  // tensor-core convolution (conv_tc.cu): jobs, CTA chunks, map offsets and
+  // per-map factors undoing the operand scaling; planes per position (4 bf16, 2 e4m3)
+  DevBuf d_tc_jobs, d_tc_chunks, d_tc_outs, d_tc_inv;
+  int tc_chunks = 0, tc_planes = 0;
   size_t tc_smem = 0;
 };
 

@@ -316,7 +316,8 @@ size_t plan_device_bytes(const Plan &P) {
              P.d_nms_f.bytes + P.d_nms_i.bytes + P.d_small.bytes + P.d_ascore.bytes + P.d_result.bytes;
   for (auto &mp : P.models)
     b += mp->d_root_jobs.bytes + mp->d_part_jobs.bytes + mp->d_dt_jobs.bytes + mp->d_score_jobs.bytes +
-         mp->d_counts.bytes + mp->d_tc_jobs.bytes + mp->d_tc_chunks.bytes + mp->d_tc_outs.bytes;
+         mp->d_counts.bytes + mp->d_tc_jobs.bytes + mp->d_tc_chunks.bytes + mp->d_tc_outs.bytes +
+         mp->d_tc_inv.bytes;
   return b;
 }
 }  // namespace geye

@@ -384,11 +384,11 @@ geye_status geye_fconv(geye_ctx *ctx, const float *feat, const int *a_dims, cons
   ConvJob *d_jobs;
   GEYE_TRY(S.put(jobs.data(), jobs.size(), &d_jobs));
   launch_from_ref_layout(d_ref, a0, a1, arena, ctx->stream);
-  if (ctx->conv_mode == GEYE_CONV_BF16) {
+  if (ctx->conv_mode != GEYE_CONV_FP32) {
     std::vector<int> out_off;
     for (auto &J : jobs) out_off.push_back(J.out_off);
     std::vector<std::unique_ptr<DevBuf>> tmp;
-    GEYE_TRY(conv_bf16_maps(ctx, arena, a0, a1, filters, b_dims, n_filters, arena, out_off, tmp));
+    GEYE_TRY(conv_tc_maps(ctx, arena, a0, a1, filters, b_dims, n_filters, arena, out_off, tmp));
   } else {
     launch_conv_fp32(d_jobs, (int)jobs.size(), mty, mtx, d_filt, d_off, arena, arena, mb0, mb1, 1, ctx->stream);
   }

@@ -74,6 +74,7 @@ def lib(build_if_missing: bool = True):
             "geye_debug_inject_fault": [vp, C.c_char_p, i32],
             "geye_nms_noalloc": [vp, i32, i32, C.c_float, vp, vp, vp],
             "geye_ctx_debug_counters": [vp, vp, i32],
+            "geye_score_map": [vp, vp, i32, i32, vp, i32, vp],
             "geye_detect_submit": [vp, vp, i32, vp, i32, i32, i32, C.c_float, C.c_float],
             "geye_detect_query": [vp],
             "geye_detect_collect": [vp, vp],
@@ -135,7 +136,7 @@ def _result_to_dict(r: _Result) -> dict:
     return out
 
 
-CONV_FP32, CONV_BF16 = 0, 1
+CONV_FP32, CONV_BF16, CONV_FP8 = 0, 1, 2
 
 
 class Context:
@@ -364,6 +365,15 @@ class Context:
         out = (C.c_longlong * n)()
         _check(lib().geye_ctx_debug_counters(self.h, out, n), "debug_counters")
         return list(out)
+
+    def score_map(self, model: "Model", level: int, comp: int) -> np.ndarray:
+        """Score map of (level, component) from the last whole-path run, shape (r1, r0)
+        (column-major r0 x r1 as the reference stores it)."""
+        dims = np.zeros(2, np.int32)
+        _check(lib().geye_score_map(self.h, model.h, level, comp, None, 0, _p(dims)), "score_map")
+        out = np.zeros((int(dims[1]), int(dims[0])), np.float32)
+        _check(lib().geye_score_map(self.h, model.h, level, comp, _p(out), out.size, _p(dims)), "score_map")
+        return out
 
     def inject_fault(self, op: str | None, nth: int):
         _check(lib().geye_debug_inject_fault(self.h, op.encode() if op else None, nth), "inject_fault")

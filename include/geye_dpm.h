@@ -52,6 +52,9 @@ typedef struct geye_model geye_model;   /* a DPM model resident on the device   
 typedef enum {
     GEYE_CONV_FP32 = 0,   /* CUDA-core FP32 in the reference's summation order (bit-exact) */
     GEYE_CONV_BF16 = 1,   /* tcgen05 implicit GEMM, BF16 operands, FP32 accumulation        */
+    GEYE_CONV_FP8 = 2,    /* tcgen05 implicit GEMM, FP8-e4m3 operands (features x 256, each
+                             filter x a power of two under 448), FP32 accumulation, scales
+                             undone exactly in the epilogue                                  */
 } geye_conv_mode;
 
 /* Detection result; mirrors RESULT (CAR_TRACKING/MODEL_info.h:158-166)
@@ -228,6 +231,14 @@ geye_status geye_ctx_stage_times(geye_ctx *ctx, float ms[GEYE_N_STAGES], double 
 /* Diagnostic counters of the last whole-path run (per model, 8 values each:
  * NMS sort cycles, NMS greedy cycles, greedy batches, picks, ...). */
 geye_status geye_ctx_debug_counters(geye_ctx *ctx, long long *out, int n);
+
+/* Score map (root + offset - parts, before the threshold) of pyramid level
+ * `level` and component `comp` of model m, from the last whole-path run on this
+ * context, column-major r0 x r1 as get_boxes.cpp:1022-1041 builds it.
+ * dims receives {r0, r1}; out (cap floats) may be null to ask the size only.
+ * GEYE_ERR_ARG when the last run has no such map (skipped level, other model). */
+geye_status geye_score_map(geye_ctx *ctx, const geye_model *m, int level, int comp, float *out, int cap,
+                           int dims[2]);
 
 /* ---- fault injection (host side only) ------------------------------------ */
 /* The n-th subsequent call of the named operation ("alloc", "h2d", "launch")

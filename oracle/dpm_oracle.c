@@ -604,6 +604,9 @@ void orc_fconv_f64(const float *A, int a0, int a1, const float *B, int b0, int b
     const int c0 = a0 - b0 + 1, c1 = a1 - b1 + 1;
     if (c0 < 1 || c1 < 1) return;
     const size_t ASQ = (size_t)a0 * a1, BSQ = (size_t)b0 * b1;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static)
+#endif
     for (int x = 0; x < c1; x++)
         for (int y = 0; y < c0; y++) {
             double acc = 0;
@@ -613,6 +616,28 @@ void orc_fconv_f64(const float *A, int a0, int a1, const float *B, int b0, int b
                         acc += (double)A[f * ASQ + (size_t)(x + xp) * a0 + y + yp] * (double)B[f * BSQ + xp * b0 + yp];
             C[(size_t)x * c0 + y] = acc;
         }
+}
+
+/* max over positions of sum |A| |B| (the magnitude that bounds rounding errors) */
+static double fconv_abs_max(const float *A, int a0, int a1, const float *B, int b0, int b1)
+{
+    const int c0 = a0 - b0 + 1, c1 = a1 - b1 + 1;
+    if (c0 < 1 || c1 < 1) return 0;
+    const size_t ASQ = (size_t)a0 * a1, BSQ = (size_t)b0 * b1;
+    double best = 0;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static) reduction(max : best)
+#endif
+    for (int x = 0; x < c1; x++)
+        for (int y = 0; y < c0; y++) {
+            double acc = 0;
+            for (int f = 0; f < 31; f++)
+                for (int xp = 0; xp < b1; xp++)
+                    for (int yp = 0; yp < b0; yp++)
+                        acc += fabs((double)A[f * ASQ + (size_t)(x + xp) * a0 + y + yp]) * fabs((double)B[f * BSQ + xp * b0 + yp]);
+            if (acc > best) best = acc;
+        }
+    return best;
 }
 
 /* ------------------------------------------------------------------------- */
@@ -845,6 +870,63 @@ orc_scores *orc_compute_scores(const orc_model *m, const orc_pyramid *P, int nth
         }
     }
     return S;
+}
+
+/* The same lower-envelope recursion as dt_helper in double: only for measuring
+ * the error of the FP32 and reduced-precision paths. */
+static void dt_helper_f64(const double *src, double *dst, int step, int s1, int s2, int d1, int d2, double a, double b)
+{
+    while (d2 >= d1) {
+        int d = (d1 + d2) >> 1;
+        int s = s1;
+        for (int p = s1 + 1; p <= s2; p++) {
+            double t1 = d - s, t2 = d - p;
+            if (src[s * step] + a * t1 * t1 + b * t1 > src[p * step] + a * t2 * t2 + b * t2) s = p;
+        }
+        double D = d - s;
+        dst[d * step] = src[s * step] + a * D * D + b * D;
+        dt_helper_f64(src, dst, step, s1, s, d1, d - 1, a, b);
+        s1 = s;
+        d1 = d + 1;
+    }
+}
+
+int orc_score_f64(const orc_model *m, const orc_pyramid *P, int level, int c, double *out, int *dims, double *mag)
+{
+    const int interval = m->interval, L = level - interval;
+    const int *FSIZE = P->ftsize;
+    if (level < interval || level >= P->LEN || level_skipped(m, FSIZE, level)) return -1;
+    const int a0 = FSIZE[2 * level], a1 = FSIZE[2 * level + 1];
+    const int *rs = m->root_size + 3 * c;
+    const int r0 = a0 - rs[0] + 1, r1 = a1 - rs[1] + 1;
+    if (r0 < 1 || r1 < 1) return -1;
+    dims[0] = r0; dims[1] = r1;
+    orc_fconv_f64(P->feat[level], a0, a1, m->rootfilter[c], rs[0], rs[1], out);
+    if (mag) *mag = fconv_abs_max(P->feat[level], a0, a1, m->rootfilter[c], rs[0], rs[1]);
+    const double off = m->offw[m->ridx[c]];
+    for (size_t i = 0; i < (size_t)r0 * r1; i++) out[i] += off;
+    const int p0 = FSIZE[2 * L], p1 = FSIZE[2 * L + 1];
+    for (int k = 0; k < m->numpart[c]; k++) {
+        const int pi = m->pidx[c][k], di = m->didx[c][k];
+        const int *ps = m->part_size + 3 * pi;
+        const int d0 = p0 - ps[0] + 1, d1 = p1 - ps[1] + 1;
+        const size_t n = (size_t)d0 * d1;
+        double *v = (double *)malloc(sizeof(double) * n + 8);
+        double *t = (double *)malloc(sizeof(double) * n + 8);
+        double *M = (double *)malloc(sizeof(double) * n + 8);
+        orc_fconv_f64(P->feat[L], p0, p1, m->partfilter[pi], ps[0], ps[1], v);
+        if (mag) *mag += fconv_abs_max(P->feat[L], p0, p1, m->partfilter[pi], ps[0], ps[1]);
+        for (size_t i = 0; i < n; i++) v[i] = -v[i];
+        const double ax = m->def[4 * di], bx = m->def[4 * di + 1], ay = m->def[4 * di + 2], by = m->def[4 * di + 3];
+        for (int x = 0; x < d1; x++) dt_helper_f64(v + (size_t)x * d0, t + (size_t)x * d0, 1, 0, d0 - 1, 0, d0 - 1, ay, by);
+        for (int y = 0; y < d0; y++) dt_helper_f64(t + y, M + y, d0, 0, d1 - 1, 0, d1 - 1, ax, bx);
+        const int pax = m->anchor[di * 2] + 1, pay = m->anchor[di * 2 + 1] + 1;
+        for (int x = 0; x < r1; x++)
+            for (int y = 0; y < r0; y++)
+                out[(size_t)x * r0 + y] -= M[(size_t)(pax - 1 + 2 * x) * d0 + (pay - 1 + 2 * y)];
+        free(v); free(t); free(M);
+    }
+    return 0;
 }
 
 void orc_free_scores(orc_scores *S)

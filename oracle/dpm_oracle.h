@@ -88,6 +88,13 @@ void orc_calc_a_score(float *ac_score, const float *score, const int *ssize, con
                       int im_h, int im_w, int padx, int pady, float scale);
 void orc_normalize_a_score(float *A, int n, float thresh);
 orc_scores *orc_compute_scores(const orc_model *m, const orc_pyramid *P, int nthreads);
+/* Score map of (level, component) in double precision from the same FP32
+ * features: convolutions, distance transforms and the part sum all in double.
+ * out holds r0*r1 doubles (dims = {r0, r1}); returns -1 for a skipped level.
+ * mag (may be null) receives max sum|a||b| of the root plus that of each part:
+ * an operand rounding of relative size u moves no score by more than u * mag,
+ * since the distance transform's minimum moves no more than its input. */
+int orc_score_f64(const orc_model *m, const orc_pyramid *P, int level, int c, double *out, int *dims, double *mag);
 void orc_free_scores(orc_scores *S);
 float *orc_boxes_from_scores(const orc_model *m, const orc_pyramid *P, const orc_scores *S,
                              float thresh, float *a_score, int *Dnum, int *probe_oob);

@@ -104,6 +104,9 @@ def lib():
         L.orc_hog_pixel.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, _fp]
         L.orc_fconv.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_void_p]
         L.orc_fconv_f64.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_void_p]
+        L.orc_score_f64.restype = C.c_int
+        L.orc_score_f64.argtypes = [C.POINTER(_Model), C.POINTER(_Pyramid), C.c_int, C.c_int, C.c_void_p, C.c_void_p,
+                                    C.c_void_p]
         L.orc_dt.argtypes = [C.c_void_p, C.c_float, C.c_float, C.c_float, C.c_float, C.c_void_p, C.c_void_p,
                              C.c_void_p, C.c_void_p]
         L.orc_quicksort.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int]
@@ -336,6 +339,21 @@ class Scores:
         d0, d1 = S.psz[2 * (L * self.NoP + p)], S.psz[2 * (L * self.NoP + p) + 1]
         i = (level * self.NoC + c) * self.maxnp + k
         return (self._map(S.M[i], d0, d1), self._map(S.Ix[i], d0, d1, np.int32), self._map(S.Iy[i], d0, d1, np.int32))
+
+    def score_f64(self, level, c):
+        """(score, mag): the (level, c) score map in double precision from the same features and
+        the magnitude max sum|a||b| of its root and parts, or None if the level is skipped."""
+        S = self._p.contents; i = level * self.NoC + c
+        r0, r1 = S.rsz[2 * i], S.rsz[2 * i + 1]
+        if r0 <= 0 or r1 <= 0:
+            return None
+        out = np.zeros((r1, r0), np.float64)
+        dims = np.zeros(2, np.int32)
+        mag = np.zeros(1, np.float64)
+        if lib().orc_score_f64(self.model._p, self.pyr._p, level, c, _ptr(out), _ptr(dims), _ptr(mag)) != 0:
+            return None
+        assert (dims[0], dims[1]) == (r0, r1)
+        return out, float(mag[0])
 
     def boxes(self, thresh: float, a_score: np.ndarray | None = None):
         D = C.c_int(); oob = C.c_int()

@@ -1,0 +1,120 @@
+"""Score error of each convolution precision against a double-precision oracle,
+level by level, and detection agreement of BF16 and FP8 against FP32.
+
+For every pyramid level and component the whole-path score map (root + offset -
+distance-transformed parts) is read back from the device and compared with the
+oracle's double-precision score from the same features.  Rounding an operand
+by a relative u moves a score by at most u * mag, mag = max sum|a||b| of the
+root plus that of each part (a distance transform's minimum moves no more than
+its input), so: FP32 within 2**-20 * mag (the sums' own rounding), BF16
+within 2**-7 * mag, FP8-e4m3 within 0.13 * mag (2**-4 per operand, plus the
+subnormal range).  Agreement: the share of FP32 detections with a
+same-component detection of IoU >= 0.9 in the other precision.
+
+Set GEYE_PRECISION_REPORT=<file> to write the per-level table as JSON.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+FRAMES = (0, 1, 2)
+W, H = 640, 480
+
+
+def _iou(a, b):
+    x1, y1 = max(a[0], b[0]), max(a[1], b[1])
+    x2, y2 = min(a[2], b[2]), min(a[3], b[3])
+    inter = max(0, x2 - x1 + 1) * max(0, y2 - y1 + 1)
+    ua = (a[2] - a[0] + 1) * (a[3] - a[1] + 1) + (b[2] - b[0] + 1) * (b[3] - b[1] + 1) - inter
+    return inter / ua if ua > 0 else 0.0
+
+
+def _matched(ref, got):
+    hit = 0
+    for i in range(ref["num"]):
+        for j in range(got["num"]):
+            if got["type"][j] == ref["type"][i] and _iou(ref["point"][i], got["point"][j]) >= 0.9:
+                hit += 1
+                break
+    return hit
+
+
+@pytest.fixture(scope="module")
+def report(tmp_path_factory):
+    import geye_gb300 as g
+    from geye_gb300 import synth
+    d = str(tmp_path_factory.mktemp("models"))
+    specs = (synth.CAR_SPEC, synth.PERSON_SPEC)
+    paths = [synth.write_model_csv(s, d) for s in specs]
+    oms = [O.Model(*p) for p in paths]
+    modes = {"fp32": g.CONV_FP32, "bf16": g.CONV_BF16, "fp8": g.CONV_FP8}
+    dets = {k: [] for k in modes}
+    levels = {}   # (mode, level) -> [max err, max err / mag]
+    for seed in FRAMES:
+        frame = synth.make_frame(W, H, seed=seed)
+        f64 = []
+        for om in oms:
+            S = O.Scores(om, O.Pyramid(om, frame))
+            f64.append((S, {(lv, c): S.score_f64(lv, c) for lv in range(S.interval, S.LEN) if not S.skipped[lv]
+                            for c in range(S.NoC)}))
+        for name, mode in modes.items():
+            with g.Context(0, conv=mode) as ctx:
+                ms = [g.Model(ctx, *p) for p in paths]
+                dets[name].append(ctx.detect_multi(frame, ms, -0.5, 0.5, None))
+                for m, (S, ref) in zip(ms, f64):
+                    for (lv, c), (s64, mag) in ref.items():
+                        got = ctx.score_map(m, lv, c).astype(np.float64)
+                        assert got.shape == s64.shape
+                        e = float(np.abs(got - s64).max())
+                        cur = levels.setdefault((name, lv), [0.0, 0.0, 0.0])
+                        cur[0] = max(cur[0], e)
+                        cur[1] = max(cur[1], e / mag)
+                        cur[2] = max(cur[2], mag)
+                for m in ms:
+                    m.close()
+    agree = {}
+    for name in ("bf16", "fp8"):
+        per_model = []
+        for mi, spec in enumerate(specs):
+            n = sum(r[mi]["num"] for r in dets["fp32"])
+            hit = sum(_matched(r32[mi], rx[mi]) for r32, rx in zip(dets["fp32"], dets[name]))
+            per_model.append({"model": spec.name, "fp32_detections": n, "matched": hit, "agreement": hit / max(n, 1)})
+        tot_n = sum(p["fp32_detections"] for p in per_model)
+        tot_h = sum(p["matched"] for p in per_model)
+        agree[name] = {"agreement": tot_h / max(tot_n, 1), "per_model": per_model}
+    rep = {"frames": [f"synthetic {W}x{H} seed {s}" for s in FRAMES], "models": [s.name for s in specs],
+           "levels": {name: [{"level": lv, "max_abs_err": v[0], "max_err_over_mag": v[1], "mag": v[2]}
+                             for (n, lv), v in sorted(levels.items()) if n == name] for name in modes},
+           "agreement_vs_fp32": agree}
+    out = os.environ.get("GEYE_PRECISION_REPORT")
+    if out:
+        with open(out, "w") as f:
+            json.dump(rep, f, indent=1)
+    return rep
+
+
+def test_fp32_scores_within_sum_rounding(report):
+    for row in report["levels"]["fp32"]:
+        assert row["max_err_over_mag"] <= 2.0 ** -20, row
+
+
+def test_bf16_scores_within_operand_rounding(report):
+    for row in report["levels"]["bf16"]:
+        assert row["max_err_over_mag"] <= 2.0 ** -7, row
+
+
+def test_fp8_scores_within_operand_rounding(report):
+    for row in report["levels"]["fp8"]:
+        assert row["max_err_over_mag"] <= 0.13, row
+
+
+def test_detection_agreement(report):
+    a = report["agreement_vs_fp32"]
+    assert a["bf16"]["agreement"] >= 0.9, a["bf16"]
+    assert a["fp8"]["agreement"] >= 0.5, a["fp8"]
