@@ -56,9 +56,15 @@ WORKLOADS = {
     "car+person_1280x720_bf16": dict(w=1280, h=720, models=("car", "person"), conv="bf16"),
     "car+person_640x480_fp32": dict(w=640, h=480, models=("car", "person"), conv="fp32"),
     "car+person_640x480_bf16": dict(w=640, h=480, models=("car", "person"), conv="bf16"),
+    "car+person_640x480_fp8": dict(w=640, h=480, models=("car", "person"), conv="fp8"),
+    "car+person_1280x720_fp8": dict(w=1280, h=720, models=("car", "person"), conv="fp8"),
     "car_640x480_fp32": dict(w=640, h=480, models=("car",), conv="fp32"),
 }
 DEFAULT_WORKLOAD = "served_bf16_car+person_640x480"
+
+
+def _conv_mode(g, name):
+    return {"fp32": g.CONV_FP32, "bf16": g.CONV_BF16, "fp8": g.CONV_FP8}[name]
 
 
 def _peaks():
@@ -223,7 +229,7 @@ def run_gpu(args, wl):
     from geye_gb300 import synth
 
     stream = torch.cuda.Stream(device=dev)
-    ctx = g.Context(dev, stream=stream.cuda_stream, conv=g.CONV_BF16 if wl["conv"] == "bf16" else g.CONV_FP32)
+    ctx = g.Context(dev, stream=stream.cuda_stream, conv=_conv_mode(g, wl["conv"]))
     tmp = tempfile.TemporaryDirectory()
     paths = _write_models(wl["models"], tmp.name)
     models = [g.Model(ctx, *p) for p in paths]
@@ -297,10 +303,14 @@ def run_gpu(args, wl):
     conv_flops = st_last["conv_flops"]
     achieved_tflops = conv_flops / (conv_med_ms / 1000.0) / 1e12
     traffic = _traffic(f"conv_{wl['conv']}_{W}x{H}")
+    # FP8 is rated at twice the bf16 tensor rate; only the bf16 rate is measured
+    peak = 2 * bf16 if wl["conv"] == "fp8" else bf16
     roofline = {"kernel": "conv (root + part filters, k_conv_fp32)" if wl["conv"] == "fp32" else "conv (tcgen05)",
-                "bound": "tensor", "achieved": achieved_tflops, "peak": bf16, "unit": "TFLOP/s",
-                "frac": achieved_tflops / bf16, "traffic": traffic,
-                "note": (f"peak = dense bf16 tensor ({peak_src}); the FP32 drop-in runs this contraction on the "
+                "bound": "tensor", "achieved": achieved_tflops, "peak": peak, "unit": "TFLOP/s",
+                "frac": achieved_tflops / peak, "traffic": traffic,
+                "note": (f"peak = dense bf16 tensor ({peak_src})" +
+                         (" x 2 for e4m3 (the nominal fp8:bf16 ratio)" if wl["conv"] == "fp8" else "") +
+                         "; the FP32 drop-in runs this contraction on the "
                          "FP32 CUDA cores in the reference's summation order"),
                 "flops_per_launch": conv_flops, "ms_per_launch": conv_med_ms}
     stages = {k: statistics.median(v) for k, v in stage_acc.items()}
@@ -319,11 +329,15 @@ def run_gpu(args, wl):
                "sample": f"1 frame of the workload ({dt:.2f} s wall, both models, oracle with {nthreads} threads)"}
 
     clocks = clk.summary()
+    tuning = [ctx.conv_tuning(m) for m in models] if wl["conv"] != "fp32" else None
+    agree = None
+    if rank == 0 and wl["conv"] != "fp32":
+        agree = _agreement(paths, [frame] + [synth.make_frame(W, H, seed=s) for s in (1, 2)], _conv_mode(g, wl["conv"]))
     if rank == 0:
         line = {
             "metric": "frames_per_sec", "value": value, "unit": "frames/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1000.0 * t_total / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "bf16" if wl["conv"] == "bf16" else "f32",
+            "scaling": "weak", "vs_baseline": None, "dtype": {"bf16": "bf16", "fp8": "e4m3"}.get(wl["conv"], "f32"),
             "data": "synthetic",
             "config": {"workload": args.workload, "frame": f"{W}x{H}", "models": list(wl["models"]),
                        "conv": wl["conv"], "thresh": -0.5, "overlap": 0.5, "parallelism": f"replicas{world}",
@@ -337,6 +351,8 @@ def run_gpu(args, wl):
             "cpu_baseline": cpu,
             "clocks": clocks,
             "detections_kept": [k["num"] for k in kept],
+            "agreement_vs_fp32": agree,
+            "conv_tuning": tuning,
         }
         print(json.dumps(line), flush=True)
     for m in models:
@@ -345,6 +361,36 @@ def run_gpu(args, wl):
     if pg:
         pg.destroy_process_group()
     return 0
+
+
+def _iou(a, b):
+    x1, y1 = max(a[0], b[0]), max(a[1], b[1])
+    x2, y2 = min(a[2], b[2]), min(a[3], b[3])
+    inter = max(0, x2 - x1 + 1) * max(0, y2 - y1 + 1)
+    ua = (a[2] - a[0] + 1) * (a[3] - a[1] + 1) + (b[2] - b[0] + 1) * (b[3] - b[1] + 1) - inter
+    return inter / ua if ua > 0 else 0.0
+
+
+def _agreement(paths_models, frames, conv_mode):
+    """Share of the FP32 path's detections matched (same component, IoU >= 0.9) by conv_mode's."""
+    import geye_gb300 as g
+    res = {}
+    for mode in (g.CONV_FP32, conv_mode):
+        with g.Context(0, conv=mode) as ctx:
+            models = [g.Model(ctx, *p) for p in paths_models]
+            res[mode] = [ctx.detect_multi(f, models, -0.5, 0.5, None) for f in frames]
+            for m in models:
+                m.close()
+    n = hit = 0
+    for r32, rx in zip(res[g.CONV_FP32], res[conv_mode]):
+        for a, b in zip(r32, rx):
+            n += a["num"]
+            for i in range(a["num"]):
+                if any(b["type"][j] == a["type"][i] and _iou(a["point"][i], b["point"][j]) >= 0.9
+                       for j in range(b["num"])):
+                    hit += 1
+    return {"value": hit / max(n, 1), "fp32_detections": n, "matched": hit, "frames": len(frames),
+            "rule": "same component, IoU >= 0.9"}
 
 
 def _plain_fp32(paths_models, frame, n):
@@ -484,6 +530,7 @@ def run_served(args, wl):
 
     # ---- the plain FP32 drop-in on the same frame, stage breakdown and roofline of the conv
     plain = _plain_fp32(paths, frames[0], 30)
+    agree = _agreement(paths, frames[:4], g.CONV_BF16)
     stages, last = _stage_breakdown(paths, frames[0], g.CONV_BF16)
     hbm, bf16, bf16s, peak_src = _peaks()
     conv_flops = last["conv_flops"]
@@ -518,6 +565,7 @@ def run_served(args, wl):
                     "slots": srv_stats["slots"]},
             "plain_fp32": plain,
             "served_vs_plain_fp32": e2e_fps / plain["value"],
+            "agreement_vs_fp32": agree,
             "gpu_launches": int(launches_per_frame * S * args.steps),
             "stage_ms": stages,
             "roofline": roofline,

@@ -31,6 +31,7 @@
 // mbarrier wait is bounded; a timeout sets an error bit and the CTA still
 // waits (bounded) for its own copies and MMAs before it frees TMEM and leaves.
 #include <stdint.h>
+#include <stdlib.h>
 #include <string.h>
 
 #include <cuda_bf16.h>
@@ -46,8 +47,8 @@ namespace geye {
 
 constexpr int kTcThreads = 128;
 constexpr int kTcM = 128;                        // positions per tile (TMEM lanes)
-constexpr int kTcMaxTiles = 16;                  // tiles per CTA
-constexpr size_t kTcSmemBudget = 220 * 1024;     // dynamic shared memory per CTA
+constexpr int kTcMaxTiles = 16;                  // tiles per CTA, at most
+constexpr size_t kTcSmemBudget = 220 * 1024;     // dynamic shared memory per CTA, at most
 constexpr int kTcHead = 384;                    // barriers, TMEM address, map offsets and scales at the front
 constexpr unsigned long long kWaitNs = 1000000000ull;   // a wait gives up after 1 s (then 4 s for the drain)
 
@@ -435,8 +436,10 @@ struct TcTables {
 
 // one job: group g on a level whose planes start at plane_off; map_off[k] is
 // the float offset of filter k's output map.  False if it cannot fit in shared memory.
+// t_cap and budget: the largest tile run and shared memory a CTA may take (the
+// tile-shape candidates of the autotuner below).
 static bool add_tc_job(TcTables &T, int NQ, int plane_off, int fs0, int fs1, const BankGroup &g,
-                       const std::vector<int> &map_off) {
+                       const std::vector<int> &map_off, int t_cap = kTcMaxTiles, size_t budget = kTcSmemBudget) {
   TcJob J{};
   J.plane_off = plane_off;
   J.plane_cells = fs0 * fs1 + kTcPlanePad;
@@ -462,14 +465,11 @@ static bool add_tc_job(TcTables &T, int NQ, int plane_off, int fs0, int fs1, con
            ((size_t)Tc * kTcM + (size_t)(cs - 1) * fs0 + (g.b0 - 1)) * 16 * NQ;
   };
   int T_cta = 0, cs = 0;
-  for (int Tc : {kTcMaxTiles, 8, 4}) {
-    if (need(Tc, g.b1) <= kTcSmemBudget) { T_cta = Tc; cs = g.b1; break; }
-  }
-  for (int Tc : {8, 4, 2, 1}) {
-    if (T_cta) break;
+  for (int Tc = t_cap; Tc >= std::min(4, t_cap) && !T_cta; Tc /= 2)
+    if (need(Tc, g.b1) <= budget) { T_cta = Tc; cs = g.b1; }
+  for (int Tc = std::min(8, t_cap); Tc >= 1 && !T_cta; Tc /= 2)
     for (int c = g.b1; c >= 1; c--)
-      if (need(Tc, c) <= kTcSmemBudget) { T_cta = Tc; cs = c; break; }
-  }
+      if (need(Tc, c) <= budget) { T_cta = Tc; cs = c; break; }
   if (!T_cta) return false;
   const int jid = (int)T.jobs.size();
   T.jobs.push_back(J);
@@ -523,14 +523,12 @@ static geye_status ensure_bank(geye_ctx *ctx, geye_model *m, geye_conv_mode mode
   return st;
 }
 
-geye_status build_tc_jobs(geye_ctx *ctx, Plan &P, ModelPlan &mp) {
-  geye_model *m = mp.model;
-  const HostModel &h = m->h;
-  const geye_conv_mode mode = ctx->conv_mode;
-  std::vector<BankGroup> groups;
-  GEYE_TRY(ensure_bank(ctx, m, mode, groups));
-  TcTables T;
-  const int NoC = h.numcomponent, NoP = h.NoP, interval = h.interval, NQ = tc_planes_of(mode);
+// job tables of one model for a tile-shape candidate; chunks ordered by cost,
+// heaviest first, so that the long ones start in the first wave
+static geye_status build_tables(Plan &P, ModelPlan &mp, const std::vector<BankGroup> &groups, int NQ, int t_cap,
+                                size_t budget, TcTables &T) {
+  const HostModel &h = mp.model->h;
+  const int NoC = h.numcomponent, NoP = h.NoP, interval = h.interval;
   for (int level = interval; level < mp.LEN; level++) {
     if (mp.skipped[level]) continue;
     const int Lv = level - interval;
@@ -541,21 +539,139 @@ geye_status build_tc_jobs(geye_ctx *ctx, Plan &P, ModelPlan &mp) {
       for (int v : map_off)
         if (v < 0) { set_error("tensor-core conv: filter map missing from the plan"); return GEYE_ERR_UNSUPPORTED; }
       const LevelInfo &L = root ? P.lv[level] : P.lv[Lv];
-      if (!add_tc_job(T, NQ, L.feat16_off, L.fs0, L.fs1, g, map_off)) {
+      if (!add_tc_job(T, NQ, L.feat16_off, L.fs0, L.fs1, g, map_off, t_cap, budget)) {
         set_error("tensor-core conv: a filter bank and its feature reach exceed shared memory");
         return GEYE_ERR_UNSUPPORTED;
       }
     }
   }
-  mp.tc_smem = T.max_smem;
-  mp.tc_chunks = (int)T.chunks.size();
-  mp.tc_planes = NQ;
-  GEYE_TRY(upload_bytes(ctx, mp.d_tc_jobs, T.jobs.data(), sizeof(TcJob) * T.jobs.size()));
-  GEYE_TRY(upload_bytes(ctx, mp.d_tc_chunks, T.chunks.data(), sizeof(int4) * T.chunks.size()));
-  GEYE_TRY(upload_bytes(ctx, mp.d_tc_outs, T.outs.data(), sizeof(int) * T.outs.size()));
-  GEYE_TRY(upload_bytes(ctx, mp.d_tc_inv, T.inv.data(), sizeof(float) * T.inv.size()));
+  auto cost = [&](const int4 &c) {
+    const TcJob &J = T.jobs[c.x];
+    return (long long)c.z * J.b0 * J.b1 * J.n_pad;
+  };
+  std::stable_sort(T.chunks.begin(), T.chunks.end(), [&](const int4 &x, const int4 &y) { return cost(x) > cost(y); });
   return GEYE_OK;
 }
+
+// Tile-shape autotuner: every candidate (largest tile run per CTA, shared
+// memory per CTA -- fewer tiles and less memory let more CTAs share an SM and
+// overlap one's copies with another's MMAs) is built for this plan's levels,
+// timed on the device (CUDA events, after one untimed launch) and the fastest
+// kept.  Runs once per plan, before the plan's first frame.
+struct TcShape {
+  int t_cap;
+  size_t budget;
+};
+static const TcShape kTcShapes[] = {{16, 220 * 1024}, {8, 220 * 1024}, {4, 220 * 1024},
+                                    {8, 110 * 1024},  {4, 110 * 1024}, {4, 72 * 1024}, {2, 72 * 1024}};
+
+geye_status build_tc_jobs(geye_ctx *ctx, Plan &P, ModelPlan &mp) {
+  geye_model *m = mp.model;
+  const geye_conv_mode mode = ctx->conv_mode;
+  std::vector<BankGroup> groups;
+  GEYE_TRY(ensure_bank(ctx, m, mode, groups));
+  const int NQ = tc_planes_of(mode);
+  const void *bank = NQ == 2 ? m->d_bank8 : m->d_bank16;
+  TcTables best;
+  int best_shape = -1;
+  float best_ms = 0.f;
+  const bool tunable = P.arena16.p && P.arena.p && P.d_small.p;
+  int n_shapes = tunable ? (int)(sizeof(kTcShapes) / sizeof(kTcShapes[0])) : 1;
+  int first = 0;
+  // a geometry this model was tuned at before reuses that choice
+  const std::string key = std::to_string(P.width) + "x" + std::to_string(P.height) + "/" + std::to_string(mp.LEN) +
+                          "/" + std::to_string((int)mode);
+  {
+    std::lock_guard<std::mutex> lk(m->tc_mu);
+    auto it = m->tc_tuned.find(key);
+    if (tunable && it != m->tc_tuned.end()) {
+      first = it->second.first;
+      n_shapes = first + 1;
+      best_ms = 3.0f * it->second.second;
+    }
+  }
+  // GEYE_TC_SHAPE=<i> pins candidate i (reproducible shapes; no timing)
+  if (const char *e = getenv("GEYE_TC_SHAPE")) {
+    const int i = atoi(e);
+    if (i >= 0 && i < (int)(sizeof(kTcShapes) / sizeof(kTcShapes[0]))) { first = i; n_shapes = i + 1; }
+  }
+  const bool timed = tunable && n_shapes - first > 1;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (timed) {
+    CUDA_TRY(cudaEventCreate(&e0));
+    CUDA_TRY(cudaEventCreate(&e1));
+  }
+  for (int si = first; si < n_shapes; si++) {
+    TcTables T;
+    if (build_tables(P, mp, groups, NQ, kTcShapes[si].t_cap, kTcShapes[si].budget, T) != GEYE_OK) continue;
+    if (!timed || T.chunks.empty()) {
+      best = std::move(T);
+      best_shape = si;
+      break;
+    }
+    DevBuf jobs, chunks, outs, inv;
+    GEYE_TRY(upload_bytes(ctx, jobs, T.jobs.data(), sizeof(TcJob) * T.jobs.size()));
+    GEYE_TRY(upload_bytes(ctx, chunks, T.chunks.data(), sizeof(int4) * T.chunks.size()));
+    GEYE_TRY(upload_bytes(ctx, outs, T.outs.data(), sizeof(int) * T.outs.size()));
+    GEYE_TRY(upload_bytes(ctx, inv, T.inv.data(), sizeof(float) * T.inv.size()));
+    auto launch = [&]() {
+      launch_conv_tc(NQ, jobs.as<TcJob>(), chunks.as<int4>(), (int)T.chunks.size(), outs.as<int>(), inv.as<float>(),
+                     P.arena16.as<uint8_t>(), static_cast<const uint8_t *>(bank), P.arena.as<float>(),
+                     P.d_small.as<int>() + 130, T.max_smem, ctx->stream);
+    };
+    launch();
+    CUDA_TRY(cudaEventRecord(e0, ctx->stream));
+    for (int r = 0; r < 3; r++) launch();
+    CUDA_TRY(cudaEventRecord(e1, ctx->stream));
+    CUDA_TRY(cudaEventSynchronize(e1));
+    CUDA_TRY(cudaGetLastError());
+    float ms = 0.f;
+    CUDA_TRY(cudaEventElapsedTime(&ms, e0, e1));
+    if (best_shape < 0 || ms < best_ms) {
+      best = std::move(T);
+      best_shape = si;
+      best_ms = ms;
+    }
+  }
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  if (timed) CUDA_TRY(cudaMemsetAsync(P.d_small.as<int>() + 130, 0, sizeof(int), ctx->stream));
+  if (best_shape < 0) return GEYE_ERR_UNSUPPORTED;   // the error of the last candidate stands
+  if (timed) {
+    std::lock_guard<std::mutex> lk(m->tc_mu);
+    m->tc_tuned[key] = {best_shape, best_ms / 3.0f};
+  }
+  mp.tc_smem = best.max_smem;
+  mp.tc_chunks = (int)best.chunks.size();
+  mp.tc_planes = NQ;
+  mp.tc_shape = best_shape;
+  mp.tc_tuned_ms = best_ms / 3.0f;
+  GEYE_TRY(upload_bytes(ctx, mp.d_tc_jobs, best.jobs.data(), sizeof(TcJob) * best.jobs.size()));
+  GEYE_TRY(upload_bytes(ctx, mp.d_tc_chunks, best.chunks.data(), sizeof(int4) * best.chunks.size()));
+  GEYE_TRY(upload_bytes(ctx, mp.d_tc_outs, best.outs.data(), sizeof(int) * best.outs.size()));
+  GEYE_TRY(upload_bytes(ctx, mp.d_tc_inv, best.inv.data(), sizeof(float) * best.inv.size()));
+  return GEYE_OK;
+}
+
+}  // namespace geye
+
+geye_status geye_conv_tuning(geye_ctx *ctx, const geye_model *m, int shape[3], float *ms) {
+  ARG_CHECK(ctx && m && shape && ms, "null argument");
+  ARG_CHECK(ctx->last_plan, "no run yet");
+  for (auto &mp : ctx->last_plan->models) {
+    if (mp->model != m) continue;
+    ARG_CHECK(mp->tc_shape >= 0, "the last run's plan has no tensor-core convolution");
+    shape[0] = geye::kTcShapes[mp->tc_shape].t_cap;
+    shape[1] = (int)(geye::kTcShapes[mp->tc_shape].budget / 1024);
+    shape[2] = mp->tc_chunks;
+    *ms = mp->tc_tuned_ms;
+    return GEYE_OK;
+  }
+  ARG_CHECK(false, "the last run has no such model");
+  return GEYE_ERR_ARG;
+}
+
+namespace geye {
 
 geye_status run_conv_tc(geye_ctx *ctx, Plan &P, ModelPlan &mp) {
   if (mp.tc_chunks == 0) return GEYE_OK;

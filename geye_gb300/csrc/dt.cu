@@ -9,9 +9,15 @@
 // GPU form.  Let g(d) be the leftmost global argmin of f_d over the whole
 // line.  If g is non-decreasing in d, the recursion returns g(d) for every d
 // (each node's range [s1, s2] then contains g(d), and no smaller index in it
-// reaches the minimum).  So a warp per line computes g(d) for all d in
-// parallel, checks that g is non-decreasing, and only if it is not does one
-// lane replay the recursion exactly (counted in *fallback_count).
+// reaches the minimum).  So every output of a line is computed in parallel,
+// g is checked to be non-decreasing, and only if it is not does one thread
+// replay the recursion exactly (counted in *fallback_count).
+//
+// A block takes a tile of L consecutive lines (about kDtElems outputs) into
+// shared memory, each line padded with +inf, and spreads the tile's outputs
+// over its threads: a thread scans its output's window with no bounds checks
+// (an inf candidate never wins a strict comparison), using per-offset terms
+// (a*t)*t and b*t tabulated once per block -- the same roundings as dt_f.
 //
 // g(d) is searched in a window |d - s| < K.  K is chosen per line so that
 // every s outside the window has f_d(s) > max(v) >= f_d(d): with u = 2^-24,
@@ -20,27 +26,35 @@
 // For a <= 0 the window is the whole line.
 #include <math.h>
 
+#include <algorithm>
+
 #include "internal.h"
 
 namespace geye {
 
-constexpr int kDtMaxLine = 1100;     // longest line the host lets through (shared-memory bound)
-constexpr int kDtWarps = 8;
+constexpr int kDtThreads = 256;
+constexpr int kDtElems = 2048;      // outputs per block (about)
+constexpr int kDtPad = 64;          // largest window half-width served by the fast loop
 
 __device__ __forceinline__ float dt_f(float v, float a, float b, int t) {
   return v + a * t * t + b * t;      // ((v + (a*t)*t) + b*t), each op rounded (no FMA)
 }
 
-// window half-width bound K for one line (a > 0); returns n when unbounded
+// window half-width bound K for one line (a > 0); returns n when unbounded.
+// Float arithmetic (the FP64 pipe is narrow on this GPU): A and B are pushed
+// down and up by 2^-18 and the root up by 2^-16, far more than the few
+// 2^-24 roundings of the expression, so K never falls below the exact bound.
 __device__ __forceinline__ int dt_window(float vmin, float vmax, float vabs, float a, float b, int n) {
   if (!(a > 0.f)) return n;
-  const double u = 8.0 * 5.9604644775390625e-08;   // 8 * 2^-24
-  const double A = (1.0 - u) * (double)a;
-  const double B = (1.0 + u) * fabs((double)b);
-  const double R = ((double)vmax - (double)vmin) + u * (double)vabs + 1e-30;
-  const double root = (B + sqrt(B * B + 4.0 * A * R)) / (2.0 * A);
-  if (!(root < (double)n)) return n;
-  return (int)floor(root) + 2;
+  const float u = 8.0f * 5.9604644775390625e-08f;   // 8 * 2^-24
+  const float lo = 1.0f - 3.814697265625e-06f;      // 1 - 2^-18
+  const float hi = 1.0f + 3.814697265625e-06f;      // 1 + 2^-18
+  const float A = (1.0f - u) * a * lo;
+  const float B = (1.0f + u) * fabsf(b) * hi;
+  const float R = ((vmax - vmin) * hi + u * vabs * hi) * hi + 1e-30f;
+  const float root = (B + sqrtf(B * B * hi + 4.0f * A * R * hi)) / (2.0f * A) * (1.0f + 1.52587890625e-05f);
+  if (!(root < (float)n)) return n;
+  return (int)floorf(root) + 2;
 }
 
 // Exact replay of dt_helper for one line (one thread).
@@ -71,131 +85,243 @@ __device__ void dt_replay(const float *v, int n, float a, float b, float *out, i
   }
 }
 
-// One warp transforms one line held in shared memory v[0..n).
-__device__ void dt_line_warp(const float *v, int n, float a, float b, float *out, int *arg, int *gbuf,
-                             int *fallback_count) {
-  const int lane = threadIdx.x & 31;
-  float vmin = INFINITY, vmax = -INFINITY, vabs = 0.f;
-  for (int i = lane; i < n; i += 32) {
-    float x = v[i];
-    vmin = fminf(vmin, x);
-    vmax = fmaxf(vmax, x);
-    vabs = fmaxf(vabs, fabsf(x));
-  }
+// lines per block: pass 1 (columns, contiguous) any count up to 64; pass 2
+// (rows, strided in memory) a power of two up to 16 so that staging is coalesced
+__host__ __device__ __forceinline__ int dt_lines1(int n) { return max(1, min(64, kDtElems / max(n, 1))); }
+__host__ __device__ __forceinline__ int dt_lg_lines2(int n) {
+  int lg = 0;
+  while (lg < 4 && (2 << lg) * n <= kDtElems) lg++;
+  return lg;
+}
+__host__ __device__ __forceinline__ size_t dt_smem_bytes(int L, int n) {
+  return sizeof(float) * ((size_t)kDtPad + (size_t)L * (n + kDtPad) + 2 * (size_t)L * n + 2 * (2 * kDtPad - 1)) +
+         sizeof(int) * 2 * (size_t)L;
+}
+
+// Every output of lines l0, l0 + G, ... (G groups of n threads) or, for lines
+// longer than the block, outputs d, d + blockDim of every line: window
+// half-width KM (the block's largest K: candidates past a line's own K lose
+// to f_d(d) anyway, so the wider window returns the same leftmost minimum),
+// unrolled with the per-offset terms in registers.
+template <int KM>
+__device__ __forceinline__ void dt_scan_block(const float *__restrict__ v_s, int stride, int n, int nl, float a, float b,
+                                              const int *__restrict__ K_s, float *__restrict__ o_s,
+                                              int *__restrict__ g_s) {
+  float At[2 * KM - 1], Bt[2 * KM - 1];
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    vmin = fminf(vmin, __shfl_xor_sync(0xffffffffu, vmin, o));
-    vmax = fmaxf(vmax, __shfl_xor_sync(0xffffffffu, vmax, o));
-    vabs = fmaxf(vabs, __shfl_xor_sync(0xffffffffu, vabs, o));
+  for (int i = 0; i < 2 * KM - 1; i++) {
+    const float ft = (float)(KM - 1 - i);   // t = KM-1 .. 1-KM
+    At[i] = a * ft * ft;
+    Bt[i] = b * ft;
   }
-  const int K = dt_window(vmin, vmax, vabs, a, b, n);
-  for (int d = lane; d < n; d += 32) {
-    const int lo = max(0, d - K + 1), hi = min(n - 1, d + K - 1);
-    int s = lo;
-    float best = dt_f(v[lo], a, b, d - lo);
-    for (int p = lo + 1; p <= hi; p++) {
-      float fp = dt_f(v[p], a, b, d - p);
-      if (best > fp) { best = fp; s = p; }
+  auto scan = [&](int l, int d) {
+    const float *v = v_s + l * stride + d - (KM - 1);   // v[i] = line[d - t], t = KM-1-i: p ascending
+    float best = INFINITY;
+    int s = -1;
+#pragma unroll
+    for (int i = 0; i < 2 * KM - 1; i++) {
+      const float f = (v[i] + At[i]) + Bt[i];
+      if (f < best) { best = f; s = i; }
     }
-    gbuf[d] = s;
-    out[d] = best;
+    int p = d - (KM - 1) + s;
+    if (s < 0) {   // every candidate was NaN: the reference keeps the window's first index
+      p = max(0, d - K_s[l] + 1);
+      best = dt_f(v_s[l * stride + p], a, b, d - p);
+    }
+    o_s[l * n + d] = best;
+    g_s[l * n + d] = p;
+  };
+  const int tid = threadIdx.x, nth = blockDim.x;
+  if (n <= nth) {
+    const int G = nth / n, l0 = tid / n, d = tid - l0 * n;
+    if (l0 < G)
+      for (int l = l0; l < nl; l += G) scan(l, d);
+  } else {
+    for (int l = 0; l < nl; l++)
+      for (int d = tid; d < n; d += nth) scan(l, d);
   }
-  __syncwarp();
-  bool bad = false;
-  for (int d = lane; d + 1 < n; d += 32) bad |= gbuf[d] > gbuf[d + 1];
-  bad = __any_sync(0xffffffffu, bad);
-  if (bad) {
+}
+
+// PASS 1: along y (dim 0) of each column x of the negated part map -> tmpM, tmpI.
+// PASS 2: along x (dim 1) of each row y of tmpM -> M, Ix, Iy = tmpIy[Ix*d0 + y]
+// (dt.cpp:123-133).
+template <int PASS>
+__global__ void __launch_bounds__(kDtThreads) k_dt(const DtJob *__restrict__ jobs, float *__restrict__ arena,
+                                                    int *__restrict__ arena_i, int *fallback_count) {
+  extern __shared__ float dsm[];
+  __shared__ int kmax_s;
+  const DtJob J = jobs[blockIdx.y];
+  const int d0 = J.d0;
+  const int n = PASS == 1 ? J.d0 : J.d1;           // line length
+  const int nlines = PASS == 1 ? J.d1 : J.d0;
+  const int lgL = PASS == 1 ? 0 : dt_lg_lines2(n);
+  const int L = PASS == 1 ? dt_lines1(n) : (1 << lgL);
+  const int line0 = blockIdx.x * L;
+  if (line0 >= nlines) return;
+  const int nl = min(L, nlines - line0);
+  const int stride = n + kDtPad;
+  float *v_s = dsm + kDtPad;                       // line l at v_s[l * stride], +inf pads between
+  float *o_s = dsm + kDtPad + (size_t)L * stride;  // [L][n]
+  int *g_s = reinterpret_cast<int *>(o_s + (size_t)L * n);
+  float *At = reinterpret_cast<float *>(g_s + (size_t)L * n) + (kDtPad - 1);   // At[t], |t| < kDtPad
+  float *Bt = At + (2 * kDtPad - 1);
+  int *K_s = reinterpret_cast<int *>(Bt + kDtPad);
+  int *bad_s = K_s + L;
+  const float a = PASS == 1 ? J.ay : J.ax, b = PASS == 1 ? J.by : J.bx;
+  const int tid = threadIdx.x, nth = blockDim.x;
+  const int cnt = nl * n;
+  const unsigned magic = 0xFFFFFFFFu / (unsigned)n + 1u;   // e / n for e < 2^32 / n
+
+  // stage the tile, the pads and the per-offset terms
+  if (PASS == 1) {
+    const float *src = arena + J.in_off + (size_t)line0 * n;
+    for (int e = tid; e < cnt; e += nth) {
+      const int l = __umulhi((unsigned)e, magic), d = e - l * n;
+      v_s[l * stride + d] = J.negate ? -src[e] : src[e];   // inverse_Q (GPU_function.cu:695-794)
+    }
+  } else {
+    const float *tm = arena + J.tmpM_off;
+    for (int e = tid; e < (n << lgL); e += nth) {
+      const int l = e & (L - 1), x = e >> lgL;
+      if (l < nl) v_s[l * stride + x] = tm[(size_t)x * d0 + line0 + l];
+    }
+  }
+  for (int i = tid; i < (nl + 1) * kDtPad; i += nth) {
+    const int l = i / kDtPad, k = i - l * kDtPad;
+    v_s[l * stride - kDtPad + k] = INFINITY;   // pad before line l (l = nl: after the last line)
+  }
+  for (int t = tid - (kDtPad - 1); t < kDtPad; t += nth) {
+    const float ft = (float)t;
+    At[t] = a * ft * ft;
+    Bt[t] = b * ft;
+  }
+  if (tid == 0) kmax_s = 0;
+  __syncthreads();
+
+  // per-line window bound
+  const int lane = tid & 31, warp = tid >> 5;
+  for (int l = warp; l < nl; l += nth >> 5) {
+    const float *v = v_s + l * stride;
+    float vmin = INFINITY, vmax = -INFINITY, vabs = 0.f;
+    for (int i = lane; i < n; i += 32) {
+      const float x = v[i];
+      vmin = fminf(vmin, x);
+      vmax = fmaxf(vmax, x);
+      vabs = fmaxf(vabs, fabsf(x));
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      vmin = fminf(vmin, __shfl_xor_sync(0xffffffffu, vmin, o));
+      vmax = fmaxf(vmax, __shfl_xor_sync(0xffffffffu, vmax, o));
+      vabs = fmaxf(vabs, __shfl_xor_sync(0xffffffffu, vabs, o));
+    }
     if (lane == 0) {
-      dt_replay(v, n, a, b, out, gbuf);
+      const int K = dt_window(vmin, vmax, vabs, a, b, n);
+      K_s[l] = K;
+      bad_s[l] = 0;
+      atomicMax(&kmax_s, K);
+    }
+  }
+  __syncthreads();
+
+  // leftmost minimum of every output's window: a fixed window of the block's
+  // largest K when that is small, else each line's own window
+  const int KM = kmax_s;
+  switch (KM <= 2 ? 2 : KM <= 3 ? 3 : KM <= 4 ? 4 : KM <= 5 ? 5 : KM <= 6 ? 6 : KM <= 8 ? 8 : 0) {
+    case 2: dt_scan_block<2>(v_s, stride, n, nl, a, b, K_s, o_s, g_s); break;
+    case 3: dt_scan_block<3>(v_s, stride, n, nl, a, b, K_s, o_s, g_s); break;
+    case 4: dt_scan_block<4>(v_s, stride, n, nl, a, b, K_s, o_s, g_s); break;
+    case 5: dt_scan_block<5>(v_s, stride, n, nl, a, b, K_s, o_s, g_s); break;
+    case 6: dt_scan_block<6>(v_s, stride, n, nl, a, b, K_s, o_s, g_s); break;
+    case 8: dt_scan_block<8>(v_s, stride, n, nl, a, b, K_s, o_s, g_s); break;
+    default:
+      for (int e = tid; e < cnt; e += nth) {
+        const int l = __umulhi((unsigned)e, magic), d = e - l * n;
+        const float *v = v_s + l * stride;
+        const int K = K_s[l];
+        float best;
+        int s;
+        if (K <= kDtPad) {
+          best = INFINITY;
+          s = -1;
+          for (int t = K - 1; t > -K; t--) {   // p = d - t ascending
+            const float f = (v[d - t] + At[t]) + Bt[t];
+            if (f < best) { best = f; s = d - t; }
+          }
+          if (s < 0) {   // every candidate was NaN: the reference keeps the window's first index
+            s = max(0, d - K + 1);
+            best = dt_f(v[s], a, b, d - s);
+          }
+        } else {
+          const int lo = max(0, d - K + 1), hi = min(n - 1, d + K - 1);
+          s = lo;
+          best = dt_f(v[lo], a, b, d - lo);
+          for (int p = lo + 1; p <= hi; p++) {
+            const float fp = dt_f(v[p], a, b, d - p);
+            if (best > fp) { best = fp; s = p; }
+          }
+        }
+        o_s[e] = best;
+        g_s[e] = s;
+      }
+      break;
+  }
+  __syncthreads();
+  for (int e = tid; e < cnt; e += nth) {
+    const int l = __umulhi((unsigned)e, magic), d = e - l * n;
+    if (d + 1 < n && g_s[e] > g_s[e + 1]) bad_s[l] = 1;
+  }
+  __syncthreads();
+  for (int l = tid; l < nl; l += nth)
+    if (bad_s[l]) {
+      dt_replay(v_s + l * stride, n, a, b, o_s + (size_t)l * n, g_s + (size_t)l * n);
       atomicAdd(fallback_count, 1);
     }
-    __syncwarp();
-  }
-  for (int d = lane; d < n; d += 32) arg[d] = gbuf[d];
-  __syncwarp();
-}
-
-// Pass 1: along y (dim 0) for each column x of the negated part map.
-__global__ void __launch_bounds__(kDtWarps * 32) k_dt_pass1(const DtJob *__restrict__ jobs, float *__restrict__ arena,
-                                                            int *__restrict__ arena_i, int *fallback_count,
-                                                            int line_cap) {
-  extern __shared__ float sm1[];
-  const DtJob J = jobs[blockIdx.y];
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  float *v_s = sm1 + (size_t)warp * 3 * line_cap;
-  float *o_s = v_s + line_cap;
-  int *g_s = reinterpret_cast<int *>(o_s + line_cap);
-  const int n = J.d0;
-  for (int x = blockIdx.x * kDtWarps + warp; x < J.d1; x += gridDim.x * kDtWarps) {
-    const float *src = arena + J.in_off + (size_t)x * n;
-    for (int i = lane; i < n; i += 32) v_s[i] = J.negate ? -src[i] : src[i];   // inverse_Q (GPU_function.cu:695-794)
-    __syncwarp();
-    dt_line_warp(v_s, n, J.ay, J.by, o_s, g_s, g_s, fallback_count);
-    float *tm = arena + J.tmpM_off + (size_t)x * n;
-    int *ti = arena_i + J.tmpI_off + (size_t)x * n;
-    for (int i = lane; i < n; i += 32) { tm[i] = o_s[i]; ti[i] = g_s[i]; }
-    __syncwarp();
-  }
-}
-
-// Pass 2: along x (dim 1) for each row y.  A block stages kRows consecutive
-// rows (coalesced along y), each warp transforms rows from shared memory, and
-// the results go back out coalesced; Iy = tmpIy[Ix*d0 + y] (dt.cpp:123-133).
-constexpr int kRows = 16;
-
-__global__ void __launch_bounds__(kDtWarps * 32) k_dt_pass2(const DtJob *__restrict__ jobs, float *__restrict__ arena,
-                                                            int *__restrict__ arena_i, int *fallback_count) {
-  extern __shared__ float sm2[];
-  const DtJob J = jobs[blockIdx.y];
-  const int y0 = blockIdx.x * kRows;
-  if (y0 >= J.d0) return;
-  const int n = J.d1, d0 = J.d0;
-  const int rows = min(kRows, d0 - y0);
-  float *v_s = sm2;                               // [kRows][n]
-  float *o_s = v_s + kRows * n;                   // [kRows][n]
-  int *g_s = reinterpret_cast<int *>(o_s + kRows * n);   // [kRows][n]
-  const float *tm = arena + J.tmpM_off;
-  for (int i = threadIdx.x; i < rows * n; i += blockDim.x) {
-    const int r = i % rows, x = i / rows;
-    v_s[r * n + x] = tm[(size_t)x * d0 + y0 + r];
-  }
   __syncthreads();
-  const int warp = threadIdx.x >> 5;
-  for (int r = warp; r < rows; r += kDtWarps)
-    dt_line_warp(v_s + r * n, n, J.ax, J.bx, o_s + r * n, g_s + r * n, g_s + r * n, fallback_count);
-  __syncthreads();
-  float *M = arena + J.M_off;
-  int *Ix = arena_i + J.Ix_off;
-  int *Iy = arena_i + J.Iy_off;
-  const int *tIy = arena_i + J.tmpI_off;
-  for (int i = threadIdx.x; i < rows * n; i += blockDim.x) {
-    const int r = i % rows, x = i / rows;
-    const size_t o = (size_t)x * d0 + y0 + r;
-    const int ix = g_s[r * n + x];
-    M[o] = o_s[r * n + x];
-    Ix[o] = ix;
-    Iy[o] = tIy[(size_t)ix * d0 + y0 + r];
+
+  if (PASS == 1) {
+    float *tm = arena + J.tmpM_off + (size_t)line0 * n;
+    int *ti = arena_i + J.tmpI_off + (size_t)line0 * n;
+    for (int e = tid; e < cnt; e += nth) {
+      tm[e] = o_s[e];
+      ti[e] = g_s[e];
+    }
+  } else {
+    float *M = arena + J.M_off;
+    int *Ix = arena_i + J.Ix_off;
+    int *Iy = arena_i + J.Iy_off;
+    const int *tIy = arena_i + J.tmpI_off;
+    for (int e = tid; e < (n << lgL); e += nth) {
+      const int l = e & (L - 1), x = e >> lgL;
+      if (l >= nl) continue;
+      const size_t o = (size_t)x * d0 + line0 + l;
+      const int ix = g_s[l * n + x];
+      M[o] = o_s[l * n + x];
+      Ix[o] = ix;
+      Iy[o] = tIy[(size_t)ix * d0 + line0 + l];
+    }
   }
 }
 
 void launch_dt(const DtJob *d_jobs, int n_jobs, int max_d0, int max_d1, float *arena, int *arena_i,
                int *fallback_count, cudaStream_t s) {
   if (n_jobs <= 0) return;
-  int gx1 = (max_d1 + kDtWarps - 1) / kDtWarps;
-  size_t smem1 = (size_t)kDtWarps * 3 * max_d0 * sizeof(float);
-  size_t smem = (size_t)kRows * max_d1 * 3 * sizeof(float);
-  static size_t set1 = 0, set = 0;
+  // the longest lines get the fewest lines per block, so these grids cover every job
+  const int L1 = dt_lines1(max_d0), L2 = 1 << dt_lg_lines2(max_d1);
+  size_t smem1 = 0, smem2 = 0;
+  for (int n = 1; n <= max_d0; n++) smem1 = std::max(smem1, dt_smem_bytes(dt_lines1(n), n));
+  for (int n = 1; n <= max_d1; n++) smem2 = std::max(smem2, dt_smem_bytes(1 << dt_lg_lines2(n), n));
+  static size_t set1 = 0, set2 = 0;
   if (smem1 > set1) {
-    cudaFuncSetAttribute(k_dt_pass1, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem1);
+    cudaFuncSetAttribute(k_dt<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem1);
     set1 = smem1;
   }
-  k_dt_pass1<<<dim3(gx1, n_jobs), kDtWarps * 32, smem1, s>>>(d_jobs, arena, arena_i, fallback_count, max_d0);
-  if (smem > set) {
-    cudaFuncSetAttribute(k_dt_pass2, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    set = smem;
+  if (smem2 > set2) {
+    cudaFuncSetAttribute(k_dt<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem2);
+    set2 = smem2;
   }
-  int gx2 = (max_d0 + kRows - 1) / kRows;
-  k_dt_pass2<<<dim3(gx2, n_jobs), kDtWarps * 32, smem, s>>>(d_jobs, arena, arena_i, fallback_count);
+  k_dt<1><<<dim3((max_d1 + L1 - 1) / L1, n_jobs), kDtThreads, smem1, s>>>(d_jobs, arena, arena_i, fallback_count);
+  k_dt<2><<<dim3((max_d0 + L2 - 1) / L2, n_jobs), kDtThreads, smem2, s>>>(d_jobs, arena, arena_i, fallback_count);
 }
 
 }  // namespace geye

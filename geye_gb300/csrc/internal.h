@@ -10,6 +10,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <map>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -44,6 +46,17 @@ struct HogJob {
   int feat_off;            // [pos][32] float
   int feat16_off;          // tensor-core planes (offset in 2-byte units), -1 = not written
   int tc_planes;           // 4: bf16 planes [4][fs0*fs1 + kTcPlanePad][16 B]; 2: e4m3 planes; 0: none
+  int mag_off, bin_off;    // the image's pixel magnitudes (float) and bins (u8), [x * pix_Y + y]
+  int pix_Y;
+  int corner_off;          // normalisation factors [(fs1 + 1) * (fs0 + 1)]
+};
+
+struct HogPixJob {         // (bin, magnitude) of the pixels of one image
+  int img_off;             // image planes [3][w][h]
+  int h, w;
+  int xe, ye;              // pixels 1 <= x < xe, 1 <= y < ye
+  int Y;                   // row stride of the outputs
+  int mag_off, bin_off;    // float magnitudes; u8 bins at (uint8_t *)(arena + bin_off)
 };
 
 struct ConvJob {           // a block of outputs of one (level, filter group)
@@ -88,11 +101,14 @@ struct ScoreJob {          // one (level, component) score map
 };
 
 // Root box of position (x, y) of a score map (get_boxes.cpp:227-235, pad = 0).
+// (o[0] + rs0*scale) is a float sum; subtracting 1.0 in double and rounding to
+// float equals the float subtraction (the double difference is exact), so the
+// whole box is float arithmetic.
 __host__ __device__ __forceinline__ void root_box(int x, int y, float scale, int rs0, int rs1, float *o) {
   o[0] = ((float)y - (float)0 + 1) * scale;
   o[1] = ((float)x - (float)0 + 1) * scale;
-  o[2] = o[0] + (float)rs0 * scale - 1.0;
-  o[3] = o[1] + (float)rs1 * scale - 1.0;
+  o[2] = (o[0] + (float)rs0 * scale) - 1.0f;
+  o[3] = (o[1] + (float)rs1 * scale) - 1.0f;
 }
 
 // ----------------------------------------------------------------------------
@@ -129,6 +145,10 @@ struct geye_model {
   // filter banks for the tensor-core convolution (built on first use): bf16, e4m3
   void *d_bank16 = nullptr;
   void *d_bank8 = nullptr;
+  // tile shape the autotuner chose per plan geometry (frame size, levels, mode),
+  // shared by every context that plans this model at that geometry
+  std::mutex tc_mu;
+  std::map<std::string, std::pair<int, float>> tc_tuned;   // candidate, ms per launch
   int gl() const { return (h.numpart[0] + 1) * 4 + 3; }
 };
 
@@ -139,10 +159,10 @@ namespace geye {
 // ----------------------------------------------------------------------------
 void launch_fill(float *p, size_t n, float v, cudaStream_t s);
 void launch_ingest(const uint8_t *bgr, int width, int height, int width_step, float *planes, cudaStream_t s);
-void launch_resize_pass(const ResizeJob *d_jobs, int n_jobs, int max_items, int vertical, const int *d_tap_start,
+void launch_resize_pass(const ResizeJob *d_jobs, int n_jobs, int max_cols, int vertical, const int *d_tap_start,
                         const int *d_tap_si, const float *d_tap_alpha, float *arena, cudaStream_t s);
-void launch_hog(const HogJob *d_jobs, int n_jobs, int max_b, int max_cells, float *arena, void *arena16,
-                cudaStream_t s);   // arena16: base of the tensor-core planes (bytes)
+void launch_hog(const HogJob *d_jobs, int n_jobs, int max_b0, int max_b1, const HogPixJob *d_pix, int n_pix,
+                int max_xe, float *arena, void *arena16, cudaStream_t s);   // arena16: base of the tensor-core planes (bytes)
 void launch_to_ref_layout(const float *feat, int fs0, int fs1, float *out, cudaStream_t s);
 void launch_from_ref_layout(const float *ref, int fs0, int fs1, float *feat, cudaStream_t s);
 void launch_conv_fp32(const ConvJob *d_jobs, int n_jobs, int max_tiles_y, int max_tiles_x, const float *filters,
@@ -156,8 +176,8 @@ void launch_boxes(const ScoreJob *d_jobs, int n_jobs, int max_r, float thresh, c
                   const int *arena_i, const int *block_offsets, int blocks_per_job_stride, int GL, float *boxes,
                   cudaStream_t s);
 void launch_scan_counts(int *counts, int n, int *total, cudaStream_t s);
-void launch_ascore(const ScoreJob *d_jobs, int n_jobs, const float *arena, float *a_score, int im_w, int im_h,
-                   float thresh, unsigned *max_bits, cudaStream_t s);
+void launch_ascore(const int *col, const int *row, int n_jobs, const float *arena, float *a_score, int im_w,
+                  int im_h, float thresh, unsigned *max_bits, cudaStream_t s);
 void launch_ascore_normalize(float *a_score, int n, const unsigned *max_bits, cudaStream_t s);
 // one block per model; model m uses boxes/out at m*cap*GL, scratch at m*cap*6 floats and m*cap*5 ints
 void launch_nms(const float *boxes, const int *d_num, int n_models, int GL, float overlap, int cap,

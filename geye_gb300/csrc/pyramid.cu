@@ -57,41 +57,82 @@ void launch_ingest(const uint8_t *bgr, int width, int height, int width_step, fl
 // are tap_si/tap_alpha[tap_start[d] .. tap_start[d+1]) in the reference's order.
 // vertical: out[c][x][d] = sum alpha * src[c][x][si]     (src h -> dst h, same w)
 // horizontal: out[c][d][y] = sum alpha * src[c][si][y]   (src w -> dst w, same h)
+// A warp owns one column x of the output (all three channels), lanes along y:
+// no index division per element, and each tap is loaded once for the three
+// channels (vertical) or once per column (horizontal).
 // ----------------------------------------------------------------------------
-__global__ void k_resize_pass(const ResizeJob *__restrict__ jobs, int vertical, const int *__restrict__ tap_start,
-                              const int *__restrict__ tap_si, const float *__restrict__ tap_alpha,
-                              float *__restrict__ arena) {
+constexpr int kResizeWarps = 8;
+
+__global__ void __launch_bounds__(kResizeWarps * 32) k_resize_pass(const ResizeJob *__restrict__ jobs, int vertical,
+                                                                   const int *__restrict__ tap_start,
+                                                                   const int *__restrict__ tap_si,
+                                                                   const float *__restrict__ tap_alpha,
+                                                                   float *__restrict__ arena) {
   const ResizeJob J = jobs[blockIdx.y];
-  const int n = 3 * J.dst_h * J.dst_w;
   const float *src = arena + J.src_off;
   float *dst = arena + J.dst_off;
   const int *ts = tap_start + J.tap_start_off;
   const int *si = tap_si + J.tap_off;
   const float *al = tap_alpha + J.tap_off;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    const int y = i % J.dst_h;
-    const int rest = i / J.dst_h;
-    const int x = rest % J.dst_w;
-    const int c = rest / J.dst_w;
-    float acc = 0.0f;
+  const int lane = threadIdx.x & 31;
+  const size_t src_plane = (size_t)J.src_w * J.src_h, dst_plane = (size_t)J.dst_w * J.dst_h;
+  for (int x = blockIdx.x * kResizeWarps + (threadIdx.x >> 5); x < J.dst_w; x += gridDim.x * kResizeWarps) {
+    float *out = dst + (size_t)x * J.dst_h;
     if (vertical) {
-      const float *col = src + ((size_t)c * J.src_w + x) * J.src_h;
-      for (int t = ts[y]; t < ts[y + 1]; t++) acc += al[t] * col[si[t]];
+      const float *col = src + (size_t)x * J.src_h;
+      for (int y = lane; y < J.dst_h; y += 32) {
+        float a0 = 0.0f, a1 = 0.0f, a2 = 0.0f;
+        const int t1 = ts[y + 1];
+        for (int t = ts[y]; t < t1; t++) {
+          const float w = al[t];
+          const float *p = col + si[t];
+          a0 += w * p[0];
+          a1 += w * p[src_plane];
+          a2 += w * p[2 * src_plane];
+        }
+        out[y] = a0;
+        out[dst_plane + y] = a1;
+        out[2 * dst_plane + y] = a2;
+      }
     } else {
-      const float *pl = src + (size_t)c * J.src_w * J.src_h;
-      for (int t = ts[x]; t < ts[x + 1]; t++) acc += al[t] * pl[(size_t)si[t] * J.src_h + y];
+      // taps are uniform along the column: two outputs per lane in flight
+      const int t0 = ts[x], t1 = ts[x + 1];
+      for (int y = lane; y < J.dst_h; y += 64) {
+        const bool two = y + 32 < J.dst_h;
+        float a0 = 0.0f, a1 = 0.0f, a2 = 0.0f, b0 = 0.0f, b1 = 0.0f, b2 = 0.0f;
+        for (int t = t0; t < t1; t++) {
+          const float w = al[t];
+          const float *p = src + (size_t)si[t] * J.src_h + y;
+          a0 += w * p[0];
+          a1 += w * p[src_plane];
+          a2 += w * p[2 * src_plane];
+          if (two) {
+            b0 += w * p[32];
+            b1 += w * p[src_plane + 32];
+            b2 += w * p[2 * src_plane + 32];
+          }
+        }
+        out[y] = a0;
+        out[dst_plane + y] = a1;
+        out[2 * dst_plane + y] = a2;
+        if (two) {
+          out[y + 32] = b0;
+          out[dst_plane + y + 32] = b1;
+          out[2 * dst_plane + y + 32] = b2;
+        }
+      }
     }
-    dst[i] = acc;
   }
 }
 
-void launch_resize_pass(const ResizeJob *d_jobs, int n_jobs, int max_items, int vertical, const int *d_tap_start,
+// max_cols: the largest output column count (dst_w) of the phase's jobs
+void launch_resize_pass(const ResizeJob *d_jobs, int n_jobs, int max_cols, int vertical, const int *d_tap_start,
                         const int *d_tap_si, const float *d_tap_alpha, float *arena, cudaStream_t s) {
   if (n_jobs <= 0) return;
-  int bx = (max_items + 255) / 256;
+  int bx = (max_cols + kResizeWarps - 1) / kResizeWarps;
   if (bx > 1024) bx = 1024;
   dim3 grid(bx, n_jobs);
-  k_resize_pass<<<grid, 256, 0, s>>>(d_jobs, vertical, d_tap_start, d_tap_si, d_tap_alpha, arena);
+  k_resize_pass<<<grid, kResizeWarps * 32, 0, s>>>(d_jobs, vertical, d_tap_start, d_tap_si, d_tap_alpha, arena);
 }
 
 // ----------------------------------------------------------------------------
@@ -99,9 +140,6 @@ void launch_resize_pass(const ResizeJob *d_jobs, int n_jobs, int max_items, int 
 // ----------------------------------------------------------------------------
 __constant__ float c_Hcos[9] = {1.0000f, 0.9397f, 0.7660f, 0.5000f, 0.1736f, -0.1736f, -0.5000f, -0.7660f, -0.9397f};
 __constant__ float c_Hsin[9] = {0.0000f, 0.3420f, 0.6428f, 0.8660f, 0.9848f, 0.9848f, 0.8660f, 0.6428f, 0.3420f};
-
-constexpr int kTB0 = 16;   // histogram blocks per tile along y
-constexpr int kTB1 = 8;    // along x
 
 // strongest-channel gradient, orientation snap (featurepyramid.cpp:310-362)
 __device__ __forceinline__ void hog_pixel(const float *__restrict__ img, int h, int w, int x, int y, int &bin,
@@ -141,114 +179,148 @@ __device__ __forceinline__ void hog_interp(int p, int sbin, int &ip, float &w0, 
   w1 = 1.0 - w0;
 }
 
-// Histogram + block energy for a tile of kTB0 x kTB1 blocks.  Pixels of the
-// tile region get their (bin, magnitude) once into shared memory, and each
-// pixel row/column its interpolation cell and weights (the reference's double
-// expression, evaluated once per tile row/column instead of per vote); then
-// each thread sums its block's votes in the reference's pixel order.
-__global__ void __launch_bounds__(kTB0 *kTB1) k_hog_hist(const HogJob *__restrict__ jobs, float *__restrict__ arena) {
-  extern __shared__ unsigned char smem_raw[];
-  const HogJob J = jobs[blockIdx.z];
-  const int by0 = blockIdx.x * kTB0, bx0 = blockIdx.y * kTB1;
-  if (by0 >= J.b0 || bx0 >= J.b1) return;
-  const int sbin = J.sbin;
-  // pixel region covering every vote into blocks [bx0, bx0+kTB1) x [by0, by0+kTB0)
-  const int px0 = bx0 * sbin - sbin, py0 = by0 * sbin - sbin;
-  const int PW = (kTB1 + 2) * sbin, PH = (kTB0 + 2) * sbin;
-  float *mag_s = reinterpret_cast<float *>(smem_raw);
-  unsigned char *bin_s = smem_raw + sizeof(float) * PW * PH;
-  float *hist_s = reinterpret_cast<float *>(smem_raw + ((sizeof(float) + 1) * PW * PH + 15) / 16 * 16);
-  float *wx0_s = hist_s + 18 * kTB0 * kTB1;   // per region column: vx0, vx1, ixp
-  float *wx1_s = wx0_s + PW;
-  int *ix_s = reinterpret_cast<int *>(wx1_s + PW);
-  float *wy0_s = reinterpret_cast<float *>(ix_s + PW);   // per region row
-  float *wy1_s = wy0_s + PH;
-  int *iy_s = reinterpret_cast<int *>(wy1_s + PH);
+// interpolation position for a power-of-two sbin: (p + 0.5) / sbin - 0.5 and
+// everything after it are exact in float, so this equals hog_interp's double form
+__device__ __forceinline__ void hog_interp_pow2(int p, float inv_sbin, int &ip, float &w0, float &w1) {
+  const float pp = ((float)p + 0.5f) * inv_sbin - 0.5f;
+  ip = (int)floorf(pp);
+  w0 = pp - (float)ip;
+  w1 = 1.0f - w0;
+}
+
+// Pass 1: (orientation bin, magnitude) of every pixel that votes, once per
+// image (the levels of the first octave share their images with the levels
+// an octave up, at half the bin size).  A warp owns a pixel column x, lanes
+// run along y; out [x * Y + y] for 1 <= x < xe, 1 <= y < ye.
+constexpr int kPixWarps = 8;
+
+__global__ void __launch_bounds__(kPixWarps * 32) k_hog_pix(const HogPixJob *__restrict__ jobs,
+                                                           float *__restrict__ arena) {
+  const HogPixJob J = jobs[blockIdx.y];
   const float *img = arena + J.img_off;
-  const int visible0 = J.b0 * sbin, visible1 = J.b1 * sbin;
-  const int nthreads = blockDim.x;
-  for (int i = threadIdx.x; i < PW * PH; i += nthreads) {
-    const int ly = i % PH, lx = i / PH;
-    const int x = px0 + lx, y = py0 + ly;
-    int bin = 255;
-    float mag = 0.f;
-    if (x >= 1 && x < visible1 - 1 && y >= 1 && y < visible0 - 1) hog_pixel(img, J.h, J.w, x, y, bin, mag);
-    mag_s[i] = mag;
-    bin_s[i] = (unsigned char)bin;
-  }
-  for (int i = threadIdx.x; i < PW + PH; i += nthreads) {
-    int ip; float w0, w1;
-    if (i < PW) {
-      hog_interp(px0 + i, sbin, ip, w0, w1);
-      wx0_s[i] = w0; wx1_s[i] = w1; ix_s[i] = ip;
-    } else {
-      hog_interp(py0 + i - PW, sbin, ip, w0, w1);
-      wy0_s[i - PW] = w0; wy1_s[i - PW] = w1; iy_s[i - PW] = ip;
+  float *mag = arena + J.mag_off;
+  uint8_t *bin = reinterpret_cast<uint8_t *>(arena + J.bin_off);
+  const int lane = threadIdx.x & 31;
+  for (int x = 1 + blockIdx.x * kPixWarps + (threadIdx.x >> 5); x < J.xe; x += gridDim.x * kPixWarps) {
+    for (int y = 1 + lane; y < J.ye; y += 32) {
+      int b;
+      float m;
+      hog_pixel(img, J.h, J.w, x, y, b, m);
+      mag[(size_t)x * J.Y + y] = m;
+      bin[(size_t)x * J.Y + y] = (uint8_t)b;
     }
   }
-  for (int i = threadIdx.x; i < 18 * nthreads; i += nthreads) hist_s[i] = 0.f;
-  __syncthreads();
+}
 
-  const int ty = threadIdx.x % kTB0, tx = threadIdx.x / kTB0;
-  const int by = by0 + ty, bx = bx0 + tx;
-  const bool active = by < J.b0 && bx < J.b1;
-  float *myh = hist_s + threadIdx.x;   // bin o at myh[o * nthreads]
-  if (active) {
-    // candidate pixel range: any pixel whose interpolation cell is bx-1 or bx
-    const int xlo = max(1, bx * sbin - sbin), xhi = min(visible1 - 2, bx * sbin + 2 * sbin - 1);
-    const int ylo = max(1, by * sbin - sbin), yhi = min(visible0 - 2, by * sbin + 2 * sbin - 1);
-    for (int x = xlo; x <= xhi; x++) {
-      const int lx = x - px0;
-      const int ixp = ix_s[lx];
-      float wx;
-      if (ixp == bx) wx = wx1_s[lx]; else if (ixp + 1 == bx) wx = wx0_s[lx]; else continue;
-      for (int y = ylo; y <= yhi; y++) {
-        const int ly = y - py0;
-        const int iyp = iy_s[ly];
-        float wy;
-        if (iyp == by) wy = wy1_s[ly]; else if (iyp + 1 == by) wy = wy0_s[ly]; else continue;
-        const int li = lx * PH + ly;
-        const int o = bin_s[li];
-        myh[o * nthreads] += wx * wy * mag_s[li];
+// Pass 2: one thread per histogram block sums its votes in the reference's
+// pixel order (x outer, y inner; featurepyramid.cpp:365-416), into 18 bins
+// held in shared memory ([bin][thread], conflict-free), then writes the bins
+// and the block energy.  A block's votes come from pixels whose interpolation
+// cell is (bx-1 or bx, by-1 or by): for a power-of-two sbin these are the
+// column range [bx*sbin - sbin/2, bx*sbin + 3*sbin/2), the first half with
+// weight w0 and the second with w1 (same for rows); otherwise the range is
+// widened by a pixel each side and each pixel's cell is tested.
+constexpr int kVoteThreads = 256;
+
+__global__ void __launch_bounds__(kVoteThreads) k_hog_vote(const HogJob *__restrict__ jobs, float *__restrict__ arena) {
+  __shared__ float hist_s[18 * kVoteThreads];
+  const HogJob J = jobs[blockIdx.y];
+  const int nb = J.b0 * J.b1;
+  const int pos = blockIdx.x * kVoteThreads + threadIdx.x;
+  if ((int)blockIdx.x * kVoteThreads >= nb) return;
+  float *myh = hist_s + threadIdx.x;   // bin o at myh[o * kVoteThreads]
+#pragma unroll
+  for (int o = 0; o < 18; o++) myh[o * kVoteThreads] = 0.f;
+  if (pos >= nb) return;
+  const int bx = pos / J.b0, by = pos - bx * J.b0;
+  const int sbin = J.sbin;
+  const int visible0 = J.b0 * sbin, visible1 = J.b1 * sbin;
+  const float *mag = arena + J.mag_off;
+  const uint8_t *bin = reinterpret_cast<const uint8_t *>(arena + J.bin_off);
+  const size_t Y = J.pix_Y;
+  if ((sbin & (sbin - 1)) == 0) {
+    const float inv = 1.0f / (float)sbin;
+    const int xm = bx * sbin + sbin / 2, ym = by * sbin + sbin / 2;   // first pixel of cell bx / by
+    const int xa = max(1, xm - sbin), xb = min(visible1 - 1, xm + sbin);
+    const int ya = max(1, ym - sbin), yb = min(visible0 - 1, ym + sbin);
+    for (int x = xa; x < xb; x++) {
+      int ixp;
+      float wx0, wx1;
+      hog_interp_pow2(x, inv, ixp, wx0, wx1);
+      const float wx = x < xm ? wx0 : wx1;   // cell bx is ixp + 1 in the first half, ixp in the second
+      const float *mcol = mag + (size_t)x * Y;
+      const uint8_t *bcol = bin + (size_t)x * Y;
+      for (int y = ya; y < yb; y++) {
+        int iyp;
+        float wy0, wy1;
+        hog_interp_pow2(y, inv, iyp, wy0, wy1);
+        const float wy = y < ym ? wy0 : wy1;
+        myh[bcol[y] * kVoteThreads] += wx * wy * mcol[y];
       }
     }
-    const int nb = J.b0 * J.b1;
-    const int pos = bx * J.b0 + by;
-    float *hist = arena + J.hist_off;
-    float norm = 0.f;
-#pragma unroll
-    for (int o = 0; o < 18; o++) hist[(size_t)o * nb + pos] = myh[o * nthreads];
-#pragma unroll
-    for (int o = 0; o < 9; o++) {
-      float s2 = myh[o * nthreads] + myh[(o + 9) * nthreads];
-      norm += s2 * s2;
+  } else {
+    const int xlo = max(1, bx * sbin - sbin / 2 - 2), xhi = min(visible1 - 2, bx * sbin + (3 * sbin) / 2 + 1);
+    const int ylo = max(1, by * sbin - sbin / 2 - 2), yhi = min(visible0 - 2, by * sbin + (3 * sbin) / 2 + 1);
+    for (int x = xlo; x <= xhi; x++) {
+      int ixp;
+      float wx0, wx1, wx;
+      hog_interp(x, sbin, ixp, wx0, wx1);
+      if (ixp == bx) wx = wx1; else if (ixp + 1 == bx) wx = wx0; else continue;
+      for (int y = ylo; y <= yhi; y++) {
+        int iyp;
+        float wy0, wy1, wy;
+        hog_interp(y, sbin, iyp, wy0, wy1);
+        if (iyp == by) wy = wy1; else if (iyp + 1 == by) wy = wy0; else continue;
+        myh[bin[(size_t)x * Y + y] * kVoteThreads] += wx * wy * mag[(size_t)x * Y + y];
+      }
     }
-    hist[(size_t)18 * nb + pos] = norm;
   }
+  float *hist = arena + J.hist_off;
+  float norm = 0.f;
+#pragma unroll
+  for (int o = 0; o < 18; o++) hist[(size_t)o * nb + pos] = myh[o * kVoteThreads];
+#pragma unroll
+  for (int o = 0; o < 9; o++) {
+    float s2 = myh[o * kVoteThreads] + myh[(o + 9) * kVoteThreads];
+    norm += s2 * s2;
+  }
+  hist[(size_t)18 * nb + pos] = norm;
 }
 
 // 31 features per output cell (featurepyramid.cpp:421-487), written as 32
 // floats [pos][32] (channel 31 = 0), plus an optional copy as the tensor-core
 // convolution's channel planes (tc_planes.h).
+// Normalisation factor of every corner of 2x2 histogram blocks,
+// 1 / sqrt(e(x,y) + e(x,y+1) + e(x+1,y) + e(x+1,y+1) + 0.0001) in the reference's
+// expression (float sum, double root and division, rounded to float), once per
+// corner: each is shared by the four output cells around it.
+__global__ void k_hog_norm(const HogJob *__restrict__ jobs, float *__restrict__ arena) {
+  const HogJob J = jobs[blockIdx.y];
+  const int C0 = J.fs0 + 1, nc = C0 * (J.fs1 + 1);
+  const int b0 = J.b0, nb = J.b0 * J.b1;
+  const float *norm = arena + J.hist_off + (size_t)18 * nb;
+  float *N = arena + J.corner_off;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nc; i += gridDim.x * blockDim.x) {
+    const int y = i % C0, x = i / C0;
+    const float *p = norm + x * b0 + y;
+    N[i] = 1.0 / sqrt(p[0] + p[1] + p[b0] + p[b0 + 1] + 0.0001);
+  }
+}
+
 __global__ void k_hog_feat(const HogJob *__restrict__ jobs, float *__restrict__ arena, uint8_t *__restrict__ arena16) {
   const HogJob J = jobs[blockIdx.y];
   const int ncell = J.fs0 * J.fs1;
   const int b0 = J.b0, nb = J.b0 * J.b1;
   const float *hist = arena + J.hist_off;
-  const float *norm = hist + (size_t)18 * nb;
+  const float *N = arena + J.corner_off;
+  const int C0 = J.fs0 + 1;
   float *feat = arena + J.feat_off;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < ncell; i += gridDim.x * blockDim.x) {
     const int y = i % J.fs0, x = i / J.fs0;
-    const float *p;
-    float n1, n2, n3, n4;
-    p = norm + (x + 1) * b0 + y + 1;
-    n1 = 1.0 / sqrt(p[0] + p[1] + p[b0] + p[b0 + 1] + 0.0001);
-    p = norm + (x + 1) * b0 + y;
-    n2 = 1.0 / sqrt(p[0] + p[1] + p[b0] + p[b0 + 1] + 0.0001);
-    p = norm + x * b0 + y + 1;
-    n3 = 1.0 / sqrt(p[0] + p[1] + p[b0] + p[b0 + 1] + 0.0001);
-    p = norm + x * b0 + y;
-    n4 = 1.0 / sqrt(p[0] + p[1] + p[b0] + p[b0 + 1] + 0.0001);
+    const float n1 = N[(x + 1) * C0 + y + 1];
+    const float n2 = N[(x + 1) * C0 + y];
+    const float n3 = N[x * C0 + y + 1];
+    const float n4 = N[x * C0 + y];
     const float *src = hist + (x + 1) * b0 + (y + 1);
     float out[32];
     float t1 = 0, t2 = 0, t3 = 0, t4 = 0;
@@ -291,25 +363,18 @@ __global__ void k_hog_feat(const HogJob *__restrict__ jobs, float *__restrict__ 
   }
 }
 
-void launch_hog(const HogJob *d_jobs, int n_jobs, int max_b0, int max_b1, float *arena, void *arena16,
-                cudaStream_t s) {
+void launch_hog(const HogJob *d_jobs, int n_jobs, int max_b0, int max_b1, const HogPixJob *d_pix, int n_pix,
+                int max_xe, float *arena, void *arena16, cudaStream_t s) {
   if (n_jobs <= 0) return;
-  // dynamic shared memory of the widest sbin in the plan (8): 18 bins x 128 threads + pixel tile
-  const int sbin_max = 8;
-  const int PW = (kTB1 + 2) * sbin_max, PH = (kTB0 + 2) * sbin_max;
-  size_t smem = ((sizeof(float) + 1) * PW * PH + 15) / 16 * 16 + sizeof(float) * 18 * kTB0 * kTB1 +
-                sizeof(float) * 3 * (PW + PH);
-  static bool attr_set = false;
-  if (!attr_set) {
-    cudaFuncSetAttribute(k_hog_hist, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    attr_set = true;
-  }
-  dim3 g1((max_b0 + kTB0 - 1) / kTB0, (max_b1 + kTB1 - 1) / kTB1, n_jobs);
-  k_hog_hist<<<g1, kTB0 * kTB1, smem, s>>>(d_jobs, arena);
-  int max_cells = max_b0 * max_b1;
+  dim3 g0((max_xe + kPixWarps - 1) / kPixWarps, n_pix);
+  k_hog_pix<<<g0, kPixWarps * 32, 0, s>>>(d_pix, arena);
+  const int max_cells = max_b0 * max_b1;
+  dim3 g1((max_cells + kVoteThreads - 1) / kVoteThreads, n_jobs);
+  k_hog_vote<<<g1, kVoteThreads, 0, s>>>(d_jobs, arena);
   int bx = (max_cells + 255) / 256;
   if (bx > 512) bx = 512;
   dim3 g2(bx, n_jobs);
+  k_hog_norm<<<g2, 256, 0, s>>>(d_jobs, arena);
   k_hog_feat<<<g2, 256, 0, s>>>(d_jobs, arena, reinterpret_cast<uint8_t *>(arena16));
 }
 

@@ -15,6 +15,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <map>
 #include <mutex>
 #include <sstream>
 
@@ -401,7 +402,6 @@ static geye_status build_model_plan(geye_ctx *ctx, Plan &P, geye_model *mdl, int
   GEYE_TRY(upload(ctx, mp->d_dt_jobs, mp->dt_jobs));
   GEYE_TRY(upload(ctx, mp->d_score_jobs, mp->score_jobs));
   GEYE_TRY(mp->d_counts.alloc(ctx, sizeof(int) * ((size_t)std::max<size_t>(mp->score_jobs.size(), 1) * std::max(mp->score_stride, 1) + 8)));
-  if (ctx->conv_mode != GEYE_CONV_FP32) GEYE_TRY(build_tc_jobs(ctx, P, *mp));
   P.models.push_back(std::move(mp));
   return GEYE_OK;
 }
@@ -474,8 +474,8 @@ static geye_status build_pyramid_plan(geye_ctx *ctx, Plan &P, int width, int hei
     }
     vj.push_back(v);
     hj.push_back(h);
-    vmax = std::max(vmax, 3 * v.dst_h * v.dst_w);
-    hmax = std::max(hmax, 3 * h.dst_h * h.dst_w);
+    vmax = std::max(vmax, v.dst_w);   // output columns: one warp each
+    hmax = std::max(hmax, h.dst_w);
     P.bytes_resize += 4.0 * 3 * (S.img_h * S.img_w + D.img_h * S.img_w) + 4.0 * 3 * (D.img_h * S.img_w + D.img_h * D.img_w);
   };
   {
@@ -512,10 +512,41 @@ static geye_status build_pyramid_plan(geye_ctx *ctx, Plan &P, int width, int hei
       J.img_off = L.img_off; J.h = L.img_h; J.w = L.img_w; J.sbin = L.sbin; J.b0 = b0; J.b1 = b1;
       J.hist_off = L.hist_off; J.fs0 = L.fs0; J.fs1 = L.fs1; J.feat_off = L.feat_off; J.feat16_off = L.feat16_off;
       J.tc_planes = tc_planes;
+      J.corner_off = A.take((size_t)(L.fs0 + 1) * (L.fs1 + 1));
+      J.mag_off = L.img_level;   // resolved below, once the image's pixel buffer is placed
       P.hog_jobs.push_back(J);
       P.hog_max_b0 = std::max(P.hog_max_b0, b0);
       P.hog_max_b1 = std::max(P.hog_max_b1, b1);
       P.bytes_hog += 12.0 * L.img_h * L.img_w + 124.0 * L.fs0 * L.fs1;
+    }
+  }
+  // one (bin, magnitude) buffer per image, covering the widest visible area of its levels
+  {
+    std::map<int, int> pix_of;   // image level -> pix job
+    for (auto &J : P.hog_jobs) {
+      const int il = J.mag_off;
+      auto it = pix_of.find(il);
+      if (it == pix_of.end()) {
+        HogPixJob X{};
+        X.img_off = J.img_off; X.h = J.h; X.w = J.w;
+        it = pix_of.emplace(il, (int)P.pix_jobs.size()).first;
+        P.pix_jobs.push_back(X);
+      }
+      HogPixJob &X = P.pix_jobs[it->second];
+      X.xe = std::max(X.xe, J.b1 * J.sbin - 1);
+      X.ye = std::max(X.ye, J.b0 * J.sbin - 1);
+    }
+    for (auto &X : P.pix_jobs) {
+      X.Y = X.ye + 1;
+      const size_t n = (size_t)(X.xe + 1) * X.Y;
+      X.mag_off = A.take(n);
+      X.bin_off = A.take((n + 3) / 4);
+      P.pix_max_xe = std::max(P.pix_max_xe, X.xe);
+      P.bytes_hog += 5.0 * n;
+    }
+    for (auto &J : P.hog_jobs) {
+      const HogPixJob &X = P.pix_jobs[pix_of[J.mag_off]];
+      J.mag_off = X.mag_off; J.bin_off = X.bin_off; J.pix_Y = X.Y;
     }
   }
   GEYE_TRY(upload(ctx, P.d_tap_start, tstart));
@@ -528,6 +559,7 @@ static geye_status build_pyramid_plan(geye_ctx *ctx, Plan &P, int width, int hei
     GEYE_TRY(upload(ctx, P.d_hjobs[i], P.hjobs[i]));
   }
   GEYE_TRY(upload(ctx, P.d_hog_jobs, P.hog_jobs));
+  GEYE_TRY(upload(ctx, P.d_pix_jobs, P.pix_jobs));
   return GEYE_OK;
 }
 
@@ -553,7 +585,31 @@ static geye_status finish_plan(geye_ctx *ctx, Plan &P, ArenaAlloc &A) {
   GEYE_TRY(P.d_nms_f.alloc(ctx, sizeof(float) * nm * P.max_cap * 6));
   GEYE_TRY(P.d_nms_i.alloc(ctx, sizeof(int) * nm * nms_model_words(P.max_cap)));
   GEYE_TRY(P.d_small.alloc(ctx, 4096));
-  if (P.width > 0) GEYE_TRY(P.d_ascore.alloc(ctx, sizeof(float) * nm * P.width * P.height));
+  if (P.width > 0) {
+    GEYE_TRY(P.d_ascore.alloc(ctx, sizeof(float) * nm * P.width * P.height));
+    // A_SCORE lookups (get_boxes.cpp:265-300): per score map, the score column of every
+    // image column X and the score row of every image row Y, or -1 where the
+    // reference's loop maps nothing there; the division is the reference's float one.
+    for (auto &mp : P.models) {
+      const int nj = (int)mp->score_jobs.size();
+      std::vector<int> col((size_t)nj * P.width), row((size_t)nj * P.height);
+      for (int j = 0; j < nj; j++) {
+        const ScoreJob &S = mp->score_jobs[j];
+        for (int X = 0; X < P.width; X++) {
+          const int ii = X - S.RX;
+          const int Xn = ii < 0 ? -1 : (int)((float)ii / S.scale + 0);
+          col[(size_t)j * P.width + X] = (Xn >= 0 && Xn < S.r1) ? S.score_off + Xn * S.r0 : -1;
+        }
+        for (int Y = 0; Y < P.height; Y++) {
+          const int jj = Y - S.RY;
+          const int Yn = jj < 0 ? -1 : (int)((float)jj / S.scale + 0);
+          row[(size_t)j * P.height + Y] = (Yn >= 0 && Yn < S.r0) ? Yn : -1;
+        }
+      }
+      GEYE_TRY(upload(ctx, mp->d_as_col, col));
+      GEYE_TRY(upload(ctx, mp->d_as_row, row));
+    }
+  }
   // result arrays: point, or_point (4 ints each), type, scale, score per kept box
   GEYE_TRY(P.d_result.alloc(ctx, nm * (size_t)P.max_cap * 11 * 4));
   P.last_D.assign(nm, 0);
@@ -597,6 +653,8 @@ static geye_status get_frame_plan(geye_ctx *ctx, geye_model *const *models, int 
   GEYE_TRY(build_pyramid_plan(ctx, *P, width, height, LEN, interval, sbin, A, tc_planes));
   for (int i = 0; i < n_models; i++) GEYE_TRY(build_model_plan(ctx, *P, models[i], LENs[i], A));
   GEYE_TRY(finish_plan(ctx, *P, A));
+  if (ctx->conv_mode != GEYE_CONV_FP32)   // after the arena exists: the tile shapes are tuned on it
+    for (auto &mp : P->models) GEYE_TRY(build_tc_jobs(ctx, *P, *mp));
   GEYE_TRY(P->d_bgr.alloc(ctx, (size_t)width * height * 3 + 64));
   if (ctx->plans.size() > 32) ctx->plans.clear();
   *out = P.get();
@@ -657,9 +715,10 @@ geye_status run_pyramid(geye_ctx *ctx, Plan &P, const uint8_t *d_bgr, int width_
 }
 
 geye_status run_hog(geye_ctx *ctx, Plan &P) {
-  launch_hog(P.d_hog_jobs.as<HogJob>(), (int)P.hog_jobs.size(), P.hog_max_b0, P.hog_max_b1, P.arena.as<float>(),
-             P.arena16.p, ctx->stream);
-  ctx->launches++;
+  launch_hog(P.d_hog_jobs.as<HogJob>(), (int)P.hog_jobs.size(), P.hog_max_b0, P.hog_max_b1,
+             P.d_pix_jobs.as<HogPixJob>(), (int)P.pix_jobs.size(), P.pix_max_xe, P.arena.as<float>(), P.arena16.p,
+             ctx->stream);
+  ctx->launches += 3;   // pixels, votes, corner norms, features
   return check_launch(ctx, "hog");
 }
 
@@ -730,8 +789,8 @@ static geye_status ascore_compute(geye_ctx *ctx, Plan &P, ModelPlan &mp, int mi,
   const size_t n = (size_t)P.width * P.height;
   unsigned *maxb = reinterpret_cast<unsigned *>(P.d_small.as<int>() + 64 + mi);
   CUDA_TRY(cudaMemsetAsync(maxb, 0, sizeof(unsigned), ctx->stream));
-  launch_ascore(mp.d_score_jobs.as<ScoreJob>(), (int)mp.score_jobs.size(), P.arena.as<float>(), a, P.width,
-                P.height, thresh, maxb, ctx->stream);
+  launch_ascore(mp.d_as_col.as<int>(), mp.d_as_row.as<int>(), (int)mp.score_jobs.size(), P.arena.as<float>(), a,
+                P.width, P.height, thresh, maxb, ctx->stream);
   GEYE_TRY(check_launch(ctx, "a_score"));
   launch_ascore_normalize(a, (int)n, maxb, ctx->stream);
   return check_launch(ctx, "a_score normalise");
@@ -911,6 +970,8 @@ geye_status features_plan(geye_ctx *ctx, geye_model *model, const int *ftsize, c
   }
   GEYE_TRY(build_model_plan(ctx, *P, model, n_levels, A));
   GEYE_TRY(finish_plan(ctx, *P, A));
+  if (ctx->conv_mode != GEYE_CONV_FP32)
+    for (auto &mp : P->models) GEYE_TRY(build_tc_jobs(ctx, *P, *mp));
   std::string key = "features:" + std::to_string((uintptr_t)P.get());
   *out = P.get();
   ctx->plans[key] = std::move(P);

@@ -92,7 +92,11 @@ struct ModelPlan {
   // tensor-core convolution (conv_tc.cu): jobs, CTA chunks, map offsets and
   // per-map factors undoing the operand scaling; planes per position (4 bf16, 2 e4m3)
   DevBuf d_tc_jobs, d_tc_chunks, d_tc_outs, d_tc_inv;
+  // A_SCORE lookups: [job][image column] score-map column base, [job][image row] score row
+  DevBuf d_as_col, d_as_row;
   int tc_chunks = 0, tc_planes = 0;
+  int tc_shape = -1;          // tile-shape candidate the autotuner chose
+  float tc_tuned_ms = 0.f;    // its measured time per launch
   size_t tc_smem = 0;
 };
 
@@ -103,12 +107,15 @@ struct Plan {
   std::vector<LevelInfo> lv;
   // resize phases: each phase is two passes (vertical then horizontal)
   std::vector<std::vector<ResizeJob>> vjobs, hjobs;
-  std::vector<int> v_max_items, h_max_items;
+  std::vector<int> v_max_items, h_max_items;   // per phase: largest output column count
   std::vector<DevBuf> d_vjobs, d_hjobs;
   DevBuf d_tap_start, d_tap_si, d_tap_alpha;
   std::vector<HogJob> hog_jobs;
   DevBuf d_hog_jobs;
   int hog_max_b0 = 0, hog_max_b1 = 0;
+  std::vector<HogPixJob> pix_jobs;   // one per image
+  DevBuf d_pix_jobs;
+  int pix_max_xe = 0;
   std::vector<std::unique_ptr<ModelPlan>> models;
   // memory
   size_t arena_words = 0, arena16_elems = 0;

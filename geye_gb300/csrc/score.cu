@@ -10,6 +10,8 @@
 //   box regression: CAR_TRACKING/tracking.cpp:90-166 (get_new_rects)
 // Records are written in the reference's order: a per-block count pass, an
 // exclusive scan, and a write pass that recomputes the same flags.
+#include <algorithm>
+
 #include "internal.h"
 
 namespace geye {
@@ -103,6 +105,26 @@ void launch_scan_counts(int *counts, int n, int *total, cudaStream_t s) {
 // Records of a block are contiguous in the output (its offset from the scan,
 // then rank order), so they are built in shared memory and written out with
 // coalesced stores.
+//
+// partbox (get_boxes.cpp:243-258) is written in double; every step of it is
+// exact except the final rounding to float, so it is restated in float and
+// integer arithmetic with that one rounding (the FP64 pipe is narrow here):
+//   q0 = ((py - 2)/2 + 1) * scale  ==  (py * 0.5f) * scale   (exact product, one rounding)
+//   q2 = q0 + psize*scale/2 - 1     ==  one rounding of the exact sum (int64 below)
+
+// float(q + h - 1) with the sum taken exactly.  For |q|, |h| in [0.5, 2^28) the
+// double expression is exact before its rounding to float, and q, h, 1 are
+// multiples of 2^-24 whose scaled sum fits an int64; __ll2float_rn rounds it
+// to nearest even as the double-to-float conversion does.
+__device__ __forceinline__ float sum_minus_one(float q, float h) {
+  const float aq = fabsf(q), ah = fabsf(h);
+  if (aq >= 0.5f && ah >= 0.5f && aq < 268435456.0f && ah < 268435456.0f) {
+    const long long Q = __float2ll_rn(q * 16777216.0f);
+    const long long H = __float2ll_rn(h * 16777216.0f);
+    return __ll2float_rn(Q + H - 16777216LL) * 5.9604644775390625e-08f;
+  }
+  return (float)((double)q + (double)h - 1.0);
+}
 
 __global__ void __launch_bounds__(kScoreThreads) k_boxes(const ScoreJob *__restrict__ jobs, float thresh,
                                                          const float *__restrict__ arena,
@@ -143,14 +165,14 @@ __global__ void __launch_bounds__(kScoreThreads) k_boxes(const ScoreJob *__restr
       long Pi = probey + (long)probex * J.part_d0[k];
       // the reference reads outside the map here (undefined); use entry 0 instead
       if (Pi < 0 || Pi >= (long)J.part_d0[k] * J.part_d1[k]) Pi = 0;
-      const float px = (float)arena_i[J.part_Ix[k] + Pi] + 1.0;
-      const float py = (float)arena_i[J.part_Iy[k] + Pi] + 1.0;
-      float q0 = ((py - 2.0) / 2.0 + 1.0 - (float)0) * scale;
-      float q1 = ((px - 2.0) / 2.0 + 1.0 - (float)0) * scale;
+      const float px = (float)arena_i[J.part_Ix[k] + Pi] + 1.0f;   // an integer: exact
+      const float py = (float)arena_i[J.part_Iy[k] + Pi] + 1.0f;
+      const float q0 = (py * 0.5f) * scale;
+      const float q1 = (px * 0.5f) * scale;
       Q[0] = q0;
       Q[1] = q1;
-      Q[2] = q0 + (float)J.psize0[k] * scale / 2.0 - 1.0;
-      Q[3] = q1 + (float)J.psize1[k] * scale / 2.0 - 1.0;
+      Q[2] = sum_minus_one(q0, ((float)J.psize0[k] * scale) * 0.5f);
+      Q[3] = sum_minus_one(q1, ((float)J.psize1[k] * scale) * 0.5f);
       Q += 4;
     }
     Q[0] = (float)J.comp;
@@ -177,32 +199,47 @@ void launch_boxes(const ScoreJob *d_jobs, int n_jobs, int max_r, float thresh, c
 
 // A_SCORE in gather form: target pixel (X, Y) takes the max over every
 // (level, component) of the score at the cell that the reference's scatter
-// loop maps from source pixel (X - RX, Y - RY); then the threshold/offset of
+// loop maps from source pixel (X - RX, Y - RY) -- looked up in the plan's
+// per-map column and row tables -- then the threshold/offset of
 // get_boxes.cpp:1765-1776 and a running maximum for the normalisation.
-__global__ void k_ascore(const ScoreJob *__restrict__ jobs, int n_jobs, const float *__restrict__ arena,
-                         float *__restrict__ a_score, int im_w, int im_h, float thresh, unsigned *max_bits) {
-  const int n = im_w * im_h;
+// A block owns a 16 x 16 pixel tile and stages the tile's table entries of
+// every map in shared memory, so only the score gathers touch global memory.
+// The maximum is exact in any order.
+constexpr int kAsTile = 16;
+
+__global__ void __launch_bounds__(kAsTile *kAsTile) k_ascore(const int *__restrict__ col, const int *__restrict__ row,
+                                                             int n_jobs, const float *__restrict__ arena,
+                                                             float *__restrict__ a_score, int im_w, int im_h,
+                                                             float thresh, unsigned *max_bits) {
+  extern __shared__ int tab_s[];   // [job][16] column bases, then [job][16] rows
+  const int X0 = blockIdx.y * kAsTile, Y0 = blockIdx.x * kAsTile;
+  for (int i = threadIdx.x; i < n_jobs * kAsTile; i += blockDim.x) {
+    const int j = i / kAsTile, k = i % kAsTile;
+    tab_s[i] = X0 + k < im_w ? col[(size_t)j * im_w + X0 + k] : -1;
+    tab_s[n_jobs * kAsTile + i] = Y0 + k < im_h ? row[(size_t)j * im_h + Y0 + k] : -1;
+  }
+  __syncthreads();
+  const int tx = threadIdx.x / kAsTile, ty = threadIdx.x % kAsTile;
+  const int X = X0 + tx, Y = Y0 + ty;
   unsigned local_max = 0;
-  const float AS_OFF = fabsf(thresh);
-  for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += gridDim.x * blockDim.x) {
-    const int Y = idx % im_h, X = idx / im_h;
+  if (X < im_w && Y < im_h) {
+    const size_t idx = (size_t)X * im_h + Y;
     float a = a_score[idx];
+    const int *tc = tab_s + tx, *tr = tab_s + n_jobs * kAsTile + ty;
+#pragma unroll 2
     for (int j = 0; j < n_jobs; j++) {
-      const ScoreJob &J = jobs[j];
-      const int ii = X - J.RX, jj = Y - J.RY;
-      if (ii < 0 || jj < 0) continue;
-      const int Xn = (int)((float)ii / J.scale + 0);
-      const int Yn = (int)((float)jj / J.scale + 0);
-      if (Yn < J.r0 && Xn < J.r1) {
-        const float sc = arena[J.score_off + Yn + Xn * J.r0];
+      const int c = tc[j * kAsTile], r = tr[j * kAsTile];
+      if ((c | r) >= 0) {
+        const float sc = arena[c + r];
         if (sc > a) a = sc;
       }
     }
+    const float AS_OFF = fabsf(thresh);
     if (a < thresh) a = 0.0;
     else a += AS_OFF;
     a_score[idx] = a;
     const unsigned bits = __float_as_uint(a);
-    if (a > 0.0f && bits > local_max) local_max = bits;
+    if (a > 0.0f) local_max = bits;
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) local_max = max(local_max, __shfl_xor_sync(0xffffffffu, local_max, o));
@@ -216,12 +253,16 @@ __global__ void k_ascore_norm(float *__restrict__ a_score, int n, const unsigned
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) a_score[i] *= ac_ratio;
 }
 
-void launch_ascore(const ScoreJob *d_jobs, int n_jobs, const float *arena, float *a_score, int im_w, int im_h,
-                   float thresh, unsigned *max_bits, cudaStream_t s) {
-  int n = im_w * im_h;
-  int blocks = (n + 255) / 256;
-  if (blocks > 4096) blocks = 4096;
-  k_ascore<<<blocks, 256, 0, s>>>(d_jobs, n_jobs, arena, a_score, im_w, im_h, thresh, max_bits);
+void launch_ascore(const int *col, const int *row, int n_jobs, const float *arena, float *a_score, int im_w,
+                  int im_h, float thresh, unsigned *max_bits, cudaStream_t s) {
+  dim3 grid((im_h + kAsTile - 1) / kAsTile, (im_w + kAsTile - 1) / kAsTile);
+  const size_t smem = sizeof(int) * 2 * kAsTile * (size_t)std::max(n_jobs, 1);
+  static size_t set = 0;
+  if (smem > 48 * 1024 && smem > set) {
+    cudaFuncSetAttribute(k_ascore, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    set = smem;
+  }
+  k_ascore<<<grid, kAsTile * kAsTile, smem, s>>>(col, row, n_jobs, arena, a_score, im_w, im_h, thresh, max_bits);
 }
 
 void launch_ascore_normalize(float *a_score, int n, const unsigned *max_bits, cudaStream_t s) {

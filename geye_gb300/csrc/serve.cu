@@ -317,7 +317,7 @@ size_t plan_device_bytes(const Plan &P) {
   for (auto &mp : P.models)
     b += mp->d_root_jobs.bytes + mp->d_part_jobs.bytes + mp->d_dt_jobs.bytes + mp->d_score_jobs.bytes +
          mp->d_counts.bytes + mp->d_tc_jobs.bytes + mp->d_tc_chunks.bytes + mp->d_tc_outs.bytes +
-         mp->d_tc_inv.bytes;
+         mp->d_tc_inv.bytes + mp->d_as_col.bytes + mp->d_as_row.bytes;
   return b;
 }
 }  // namespace geye

@@ -110,8 +110,8 @@ geye_status geye_resize(geye_ctx *ctx, const float *src, const int *sdims, int *
   ResizeJob *d_jv, *d_jh;
   GEYE_TRY(S.put(&jv, 1, &d_jv));
   GEYE_TRY(S.put(&jh, 1, &d_jh));
-  launch_resize_pass(d_jv, 1, (int)n_tmp, 1, d_st, d_si, d_al, arena, ctx->stream);
-  launch_resize_pass(d_jh, 1, (int)n_dst, 0, d_st, d_si, d_al, arena, ctx->stream);
+  launch_resize_pass(d_jv, 1, w, 1, d_st, d_si, d_al, arena, ctx->stream);
+  launch_resize_pass(d_jh, 1, ow, 0, d_st, d_si, d_al, arena, ctx->stream);
   CUDA_TRY(cudaGetLastError());
   CUDA_TRY(cudaMemcpyAsync(dst, arena + n_src + n_tmp, sizeof(float) * n_dst, cudaMemcpyDeviceToHost, ctx->stream));
   CUDA_TRY(cudaStreamSynchronize(ctx->stream));
@@ -133,16 +133,26 @@ geye_status geye_calc_feature(geye_ctx *ctx, const float *src, const int *isize,
   const size_t n_img = (size_t)3 * h * w;
   const size_t hist = ((n_img + 31) & ~size_t(31));
   const size_t feat_off = ((hist + (size_t)19 * b0 * b1 + 31) & ~size_t(31));
+  HogPixJob X{};
+  X.img_off = 0; X.h = h; X.w = w; X.xe = b1 * sbin - 1; X.ye = b0 * sbin - 1; X.Y = X.ye + 1;
+  const size_t n_pix = (size_t)(X.xe + 1) * X.Y;
+  const size_t mag_off = ((feat_off + (size_t)fs0 * fs1 * kFeatPad + 31) & ~size_t(31));
+  const size_t bin_off = ((mag_off + n_pix + 31) & ~size_t(31));
+  const size_t corner_off = ((bin_off + (n_pix + 3) / 4 + 31) & ~size_t(31));
+  X.mag_off = (int)mag_off; X.bin_off = (int)bin_off;
   float *arena, *out;
-  GEYE_TRY(S.get(feat_off + (size_t)fs0 * fs1 * kFeatPad, &arena));
+  GEYE_TRY(S.get(corner_off + (size_t)(fs0 + 1) * (fs1 + 1), &arena));
   GEYE_TRY(S.get((size_t)fs0 * fs1 * kFeat, &out));
   CUDA_TRY(cudaMemcpyAsync(arena, src, sizeof(float) * n_img, cudaMemcpyHostToDevice, ctx->stream));
   HogJob J{};
   J.img_off = 0; J.h = h; J.w = w; J.sbin = sbin; J.b0 = b0; J.b1 = b1; J.hist_off = (int)hist;
   J.fs0 = fs0; J.fs1 = fs1; J.feat_off = (int)feat_off; J.feat16_off = -1;
+  J.mag_off = X.mag_off; J.bin_off = X.bin_off; J.pix_Y = X.Y; J.corner_off = (int)corner_off;
   HogJob *d_j;
   GEYE_TRY(S.put(&J, 1, &d_j));
-  launch_hog(d_j, 1, b0, b1, arena, nullptr, ctx->stream);
+  HogPixJob *d_x;
+  GEYE_TRY(S.put(&X, 1, &d_x));
+  launch_hog(d_j, 1, b0, b1, d_x, 1, X.xe, arena, nullptr, ctx->stream);
   launch_to_ref_layout(arena + feat_off, fs0, fs1, out, ctx->stream);
   CUDA_TRY(cudaGetLastError());
   CUDA_TRY(cudaMemcpyAsync(feat, out, sizeof(float) * (size_t)fs0 * fs1 * kFeat, cudaMemcpyDeviceToHost, ctx->stream));

@@ -75,6 +75,7 @@ def lib(build_if_missing: bool = True):
             "geye_nms_noalloc": [vp, i32, i32, C.c_float, vp, vp, vp],
             "geye_ctx_debug_counters": [vp, vp, i32],
             "geye_score_map": [vp, vp, i32, i32, vp, i32, vp],
+            "geye_conv_tuning": [vp, vp, vp, vp],
             "geye_detect_submit": [vp, vp, i32, vp, i32, i32, i32, C.c_float, C.c_float],
             "geye_detect_query": [vp],
             "geye_detect_collect": [vp, vp],
@@ -374,6 +375,13 @@ class Context:
         out = np.zeros((int(dims[1]), int(dims[0])), np.float32)
         _check(lib().geye_score_map(self.h, model.h, level, comp, _p(out), out.size, _p(dims)), "score_map")
         return out
+
+    def conv_tuning(self, model: "Model") -> dict:
+        """Tile shape the tensor-core convolution's autotuner chose for the model in the last run's plan."""
+        shape = np.zeros(3, np.int32)
+        ms = np.zeros(1, np.float32)
+        _check(lib().geye_conv_tuning(self.h, model.h, _p(shape), _p(ms)), "conv_tuning")
+        return {"tiles_per_cta": int(shape[0]), "smem_kb": int(shape[1]), "ctas": int(shape[2]), "ms": float(ms[0])}
 
     def inject_fault(self, op: str | None, nth: int):
         _check(lib().geye_debug_inject_fault(self.h, op.encode() if op else None, nth), "inject_fault")

@@ -240,6 +240,12 @@ geye_status geye_ctx_debug_counters(geye_ctx *ctx, long long *out, int n);
 geye_status geye_score_map(geye_ctx *ctx, const geye_model *m, int level, int comp, float *out, int cap,
                            int dims[2]);
 
+/* Tile shape the tensor-core convolution's autotuner chose for model m in the
+ * last run's plan: shape = {largest tile run per CTA (128 positions a tile),
+ * shared-memory budget per CTA in KB, CTAs per launch}; ms = its measured time
+ * per launch.  GEYE_ERR_ARG in FP32 mode or before a run. */
+geye_status geye_conv_tuning(geye_ctx *ctx, const geye_model *m, int shape[3], float *ms);
+
 /* ---- fault injection (host side only) ------------------------------------ */
 /* The n-th subsequent call of the named operation ("alloc", "h2d", "launch")
  * fails with GEYE_ERR_INJECTED; n = 0 clears.  No device fault is ever raised. */

@@ -105,3 +105,18 @@ def test_bf16_filter_columns_in_phases(ctx16):
     got = ctx16.fconvsMT(feat, filters)
     for m, f in zip(got, filters):
         assert np.array_equal(m, O.fconv(feat, f))
+
+
+def test_conv_tile_shape_autotuner(tmp_path):
+    import geye_gb300 as g
+    from geye_gb300 import synth
+    frame = synth.make_frame(640, 480, seed=2)
+    with g.Context(0, conv=g.CONV_BF16) as c:
+        ms = [g.Model(c, *synth.write_model_csv(s, str(tmp_path))) for s in (synth.CAR_SPEC, synth.PERSON_SPEC)]
+        c.detect_multi(frame, ms, -0.5, 0.5, None)
+        tuned = [c.conv_tuning(m) for m in ms]
+        for m in ms:
+            m.close()
+    for t in tuned:
+        assert t["tiles_per_cta"] in (2, 4, 8, 16)
+        assert 64 <= t["smem_kb"] <= 220 and t["ctas"] > 0 and t["ms"] > 0

@@ -9,7 +9,8 @@ root plus that of each part (a distance transform's minimum moves no more than
 its input), so: FP32 within 2**-20 * mag (the sums' own rounding), BF16
 within 2**-7 * mag, FP8-e4m3 within 0.13 * mag (2**-4 per operand, plus the
 subnormal range).  Agreement: the share of FP32 detections with a
-same-component detection of IoU >= 0.9 in the other precision.
+same-component detection of IoU >= 0.9 in the other precision.  The report
+holds the max and the mean absolute error per level.
 
 Set GEYE_PRECISION_REPORT=<file> to write the per-level table as JSON.
 """
@@ -55,7 +56,7 @@ def report(tmp_path_factory):
     oms = [O.Model(*p) for p in paths]
     modes = {"fp32": g.CONV_FP32, "bf16": g.CONV_BF16, "fp8": g.CONV_FP8}
     dets = {k: [] for k in modes}
-    levels = {}   # (mode, level) -> [max err, max err / mag]
+    levels = {}   # (mode, level) -> [max err, max err / mag, max mag, sum of errors, count]
     for seed in FRAMES:
         frame = synth.make_frame(W, H, seed=seed)
         f64 = []
@@ -72,10 +73,12 @@ def report(tmp_path_factory):
                         got = ctx.score_map(m, lv, c).astype(np.float64)
                         assert got.shape == s64.shape
                         e = float(np.abs(got - s64).max())
-                        cur = levels.setdefault((name, lv), [0.0, 0.0, 0.0])
+                        cur = levels.setdefault((name, lv), [0.0, 0.0, 0.0, 0.0, 0])
                         cur[0] = max(cur[0], e)
                         cur[1] = max(cur[1], e / mag)
                         cur[2] = max(cur[2], mag)
+                        cur[3] += float(np.abs(got - s64).sum())
+                        cur[4] += got.size
                 for m in ms:
                     m.close()
     agree = {}
@@ -89,7 +92,8 @@ def report(tmp_path_factory):
         tot_h = sum(p["matched"] for p in per_model)
         agree[name] = {"agreement": tot_h / max(tot_n, 1), "per_model": per_model}
     rep = {"frames": [f"synthetic {W}x{H} seed {s}" for s in FRAMES], "models": [s.name for s in specs],
-           "levels": {name: [{"level": lv, "max_abs_err": v[0], "max_err_over_mag": v[1], "mag": v[2]}
+           "levels": {name: [{"level": lv, "max_abs_err": v[0], "mean_abs_err": v[3] / max(v[4], 1),
+                              "max_err_over_mag": v[1], "mag": v[2]}
                              for (n, lv), v in sorted(levels.items()) if n == name] for name in modes},
            "agreement_vs_fp32": agree}
     out = os.environ.get("GEYE_PRECISION_REPORT")
