@@ -222,7 +222,41 @@ __global__ void __launch_bounds__(kPixWarps * 32) k_hog_pix(const HogPixJob *__r
 // widened by a pixel each side and each pixel's cell is tested.
 constexpr int kVoteThreads = 256;
 
-__global__ void __launch_bounds__(kVoteThreads) k_hog_vote(const HogJob *__restrict__ jobs, float *__restrict__ arena) {
+// the vote loop for a compile-time power-of-two sbin: the 2*SB row weights of
+// the block are formed once and the row loop is unrolled
+template <int SB>
+__device__ __forceinline__ void hog_vote_pow2(float *myh, const float *__restrict__ mag,
+                                              const uint8_t *__restrict__ bin, size_t Y, int bx, int by,
+                                              int visible0, int visible1) {
+  const float inv = 1.0f / (float)SB;
+  const int xm = bx * SB + SB / 2, ym = by * SB + SB / 2;
+  const int xa = max(1, xm - SB), xb = min(visible1 - 1, xm + SB);
+  const int y0 = ym - SB;
+  const int ya = max(1, y0), yb = min(visible0 - 1, ym + SB);
+  float wy[2 * SB];
+#pragma unroll
+  for (int k = 0; k < 2 * SB; k++) {
+    int iyp;
+    float w0, w1;
+    hog_interp_pow2(y0 + k, inv, iyp, w0, w1);
+    wy[k] = k < SB ? w0 : w1;
+  }
+  for (int x = xa; x < xb; x++) {
+    int ixp;
+    float wx0, wx1;
+    hog_interp_pow2(x, inv, ixp, wx0, wx1);
+    const float wx = x < xm ? wx0 : wx1;
+    const float *mcol = mag + (size_t)x * Y + y0;
+    const uint8_t *bcol = bin + (size_t)x * Y + y0;
+#pragma unroll
+    for (int k = 0; k < 2 * SB; k++) {
+      const int y = y0 + k;
+      if (y >= ya && y < yb) myh[bcol[k] * kVoteThreads] += wx * wy[k] * mcol[k];
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kVoteThreads, 4) k_hog_vote(const HogJob *__restrict__ jobs, float *__restrict__ arena) {
   __shared__ float hist_s[18 * kVoteThreads];
   const HogJob J = jobs[blockIdx.y];
   const int nb = J.b0 * J.b1;
@@ -238,7 +272,11 @@ __global__ void __launch_bounds__(kVoteThreads) k_hog_vote(const HogJob *__restr
   const float *mag = arena + J.mag_off;
   const uint8_t *bin = reinterpret_cast<const uint8_t *>(arena + J.bin_off);
   const size_t Y = J.pix_Y;
-  if ((sbin & (sbin - 1)) == 0) {
+  if (sbin == 8) {
+    hog_vote_pow2<8>(myh, mag, bin, Y, bx, by, visible0, visible1);
+  } else if (sbin == 4) {
+    hog_vote_pow2<4>(myh, mag, bin, Y, bx, by, visible0, visible1);
+  } else if ((sbin & (sbin - 1)) == 0) {
     const float inv = 1.0f / (float)sbin;
     const int xm = bx * sbin + sbin / 2, ym = by * sbin + sbin / 2;   // first pixel of cell bx / by
     const int xa = max(1, xm - sbin), xb = min(visible1 - 1, xm + sbin);
