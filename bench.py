@@ -51,6 +51,14 @@ WORKLOADS = {
     # 64 simulated cameras, Poisson arrivals at 30 fps each, mixed resolutions, trackers on, 40 GB budget
     "serve64_mixed_bf16": dict(w=640, h=480, models=("car", "person"), conv="bf16", sim=True, streams=64, fps=30.0,
                                sizes=((640, 480), (1280, 720), (1920, 1080)), seconds=6.0),
+    # 64 cameras at 640x480 only (the served BF16 pipeline's latency target at 64 streams)
+    "serve64_640x480_bf16": dict(w=640, h=480, models=("car", "person"), conv="bf16", sim=True, streams=64, fps=30.0,
+                                 sizes=((640, 480),), seconds=6.0),
+    # a batch of 32 frames of mixed sizes as one CUDA graph (geye_batch_run)
+    "batch32_mixed_fp32": dict(w=640, h=480, models=("car", "person"), conv="fp32", batch=32,
+                               sizes=((320, 240), (640, 480), (1280, 720), (1920, 1080))),
+    "batch32_mixed_bf16": dict(w=640, h=480, models=("car", "person"), conv="bf16", batch=32,
+                               sizes=((320, 240), (640, 480), (1280, 720), (1920, 1080))),
     # one frame at a time
     "car+person_1280x720_fp32": dict(w=1280, h=720, models=("car", "person"), conv="fp32"),
     "car+person_1280x720_bf16": dict(w=1280, h=720, models=("car", "person"), conv="bf16"),
@@ -600,11 +608,12 @@ def run_serve_sim(args, wl):
         for k in range(2):
             frames[(s, k)] = synth.make_frame(*sizes[s], seed=1000 * s + k)
     srv = g.Server(models, conv=g.CONV_BF16, hbm_budget=40 << 30, max_slots=64, track=True)
-    for sz in set(sizes):   # plans and graphs for every resolution before the clock starts
+    for sz in sorted(set(sizes)):   # slots, plans and graphs for every resolution before the clock starts
         s0 = sizes.index(sz)
-        srv.submit(s0, frames[(s0, 0)])
-    srv.drain()
-    srv.poll(1024)
+        for _ in range(64):
+            srv.submit(s0, frames[(s0, 0)])
+        srv.drain()
+        srv.poll(1024)
     T = wl["seconds"]
     arrivals = []
     for s in range(n):
@@ -658,6 +667,74 @@ def run_serve_sim(args, wl):
     return 0
 
 
+def run_batch(args, wl):
+    """A batch of frames of mixed sizes through geye_batch_run: one CUDA graph per batch."""
+    import geye_gb300 as g
+    from geye_gb300 import synth
+    rank, world, local = dist_info()
+    dev = local if world > 1 else 0
+    pg = None
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(dev)
+        dist.init_process_group("gloo")
+        pg = dist
+    rng = np.random.default_rng(3 + rank)
+    B = wl["batch"]
+    sizes = [wl["sizes"][i] for i in rng.integers(0, len(wl["sizes"]), size=B)]
+    frames = [synth.make_frame(w, h, seed=100 * rank + i) for i, (w, h) in enumerate(sizes)]
+    tmp = tempfile.TemporaryDirectory()
+    paths = _write_models(wl["models"], tmp.name)
+    owner = g.Context(dev)
+    models = [g.Model(owner, *p) for p in paths]
+    batch = g.Batch(models, conv=_conv_mode(g, wl["conv"]), max_frames=B, device=dev)
+    for _ in range(max(args.warmup, 3)):
+        batch.run(frames)
+    dev_ms, wall = [], []
+    if pg:
+        pg.barrier()
+    with ClockSampler(dev) as clk:
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            res = batch.run(frames)
+            wall.append(time.perf_counter() - t0)
+            dev_ms.append(batch.stats()["last_ms"])
+    if pg:
+        pg.barrier()
+    st = batch.stats()
+    t_dev = max_over_ranks(pg, sum(dev_ms) / 1000.0)
+    t_wall = max_over_ranks(pg, sum(wall))
+    kept = [[r["num"] for r in fr] for fr in res]
+    batch.close()
+    for m in models:
+        m.close()
+    owner.close()
+    if rank == 0:
+        line = {
+            "metric": "frames_per_sec", "value": world * B * args.steps / t_dev, "unit": "frames/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * t_dev / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": {"bf16": "bf16", "fp8": "e4m3"}.get(wl["conv"], "f32"), "data": "synthetic",
+            "config": {"workload": args.workload, "frames_per_batch": B,
+                       "sizes": {f"{a}x{b}": sizes.count((a, b)) for a, b in sorted(set(sizes))},
+                       "models": list(wl["models"]), "conv": wl["conv"], "thresh": -0.5, "overlap": 0.5,
+                       "step": "one batch: one CUDA graph with a branch per frame (frame upload from pinned "
+                               "memory inside the graph)", "parallelism": f"replicas{world}",
+                       "l2": "working set (frames + per-frame arenas) larger than L2"},
+            "e2e": {"value": world * B * args.steps / t_wall, "unit": "frames/s", "api": "geye_batch_run (host frames in, host results out)",
+                    "h2d_bytes_per_step": int(sum(w * h * 3 for w, h in sizes)),
+                    "d2h_bytes_per_step": int(B * 4 * (64 + len(models) * 11 * 4096))},
+            "gpu_launches": st["kernels"], "graph_launches_per_step": 1,
+            "detections_kept": kept[:4],
+            "clocks": clk.summary(),
+        }
+        print(json.dumps(line), flush=True)
+    if pg:
+        pg.destroy_process_group()
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -675,6 +752,8 @@ def main():
         return run_served(args, wl)
     if wl.get("sim"):
         return run_serve_sim(args, wl)
+    if wl.get("batch"):
+        return run_batch(args, wl)
     return run_gpu(args, wl)
 
 

@@ -43,7 +43,7 @@ static long long now_ns() {
 
 // queue everything of one frame on the context's stream (the frame already in P.h_bgr)
 static geye_status enqueue_frame(geye_ctx *ctx, Plan &P, float thresh, float overlap, TrackerSet *trk, int stream,
-                                 cudaEvent_t after, cudaEvent_t tracked) {
+                                 cudaEvent_t after, cudaEvent_t tracked, bool record_done = true) {
   const int n_models = (int)P.models.size();
   CUDA_TRY(cudaMemcpyAsync(P.d_bgr.p, P.h_bgr, (size_t)3 * P.width * P.height, cudaMemcpyHostToDevice, ctx->stream));
   GEYE_TRY(run_frame(ctx, P, P.d_bgr.as<uint8_t>(), 3 * P.width, thresh, overlap, nullptr));
@@ -66,7 +66,7 @@ static geye_status enqueue_frame(geye_ctx *ctx, Plan &P, float thresh, float ove
       CUDA_TRY(cudaMemcpyAsync(dst + f * kHostRes, res + f * (size_t)P.max_cap, sizeof(int) * R,
                                cudaMemcpyDeviceToHost, ctx->stream));
   }
-  CUDA_TRY(cudaEventRecord(P.ev_done, ctx->stream));
+  if (record_done) CUDA_TRY(cudaEventRecord(P.ev_done, ctx->stream));
   ctx->pending = &P;
   return GEYE_OK;
 }
@@ -79,9 +79,9 @@ static geye_status ensure_staging(Plan &P) {
   return GEYE_OK;
 }
 
-static geye_status collect_frame(geye_ctx *ctx, geye_result *out) {
+static geye_status collect_frame(geye_ctx *ctx, geye_result *out, bool wait = true) {
   Plan &P = *ctx->pending;
-  CUDA_TRY(cudaEventSynchronize(P.ev_done));
+  if (wait) CUDA_TRY(cudaEventSynchronize(P.ev_done));
   const int n_models = (int)P.models.size();
   const int *h = static_cast<const int *>(P.h_res);
   geye_status st = GEYE_OK;
@@ -230,10 +230,12 @@ geye_status dispatch_one(geye_server *s, bool *dispatched) {
   int pick = -1;
   for (size_t i = 0; i < s->slots.size() && pick < 0; i++)
     if (!s->slots[i].busy && s->slots[i].w == r.w && s->slots[i].h == r.h) pick = (int)i;
-  if (pick < 0)   // a free slot whose plan (if any) is dropped for this size
+  // else a new slot while slots and memory last: keeping every slot's plan (and its
+  // frame graph) for the size it holds avoids rebuilding plans when sizes mix
+  if (pick < 0 && (int)s->slots.size() < s->max_slots && s->held < s->budget) GEYE_TRY(new_slot(s, &pick));
+  if (pick < 0)   // else a free slot whose plan is dropped for this size
     for (size_t i = 0; i < s->slots.size() && pick < 0; i++)
       if (!s->slots[i].busy && s->held < s->budget) pick = (int)i;
-  if (pick < 0 && (int)s->slots.size() < s->max_slots && s->held < s->budget) GEYE_TRY(new_slot(s, &pick));
   if (pick < 0) return GEYE_OK;
   geye_server::Slot &sl = s->slots[pick];
   if (sl.w != r.w || sl.h != r.h) {   // rebuild for the new size: the old plan's memory goes back
@@ -442,6 +444,183 @@ geye_status geye_server_tracks(geye_server *s, int stream, int max, float *boxes
   for (auto &sl : s->slots)
     if (sl.ctx) CUDA_TRY(cudaStreamSynchronize(sl.ctx->stream));
   return tracker_read(s->trk, stream, max, boxes, n);
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// batch: several frames (any mix of sizes) as one CUDA graph, one lane
+// (context, stream, plan per size) per frame, the lanes as parallel branches
+// of the graph between a fork and a join on the batch's stream
+// ---------------------------------------------------------------------------
+struct geye_batch {
+  int device = 0;
+  std::vector<geye_model *> models;
+  geye_conv_mode mode = GEYE_CONV_FP32;
+  int max_frames = 0;
+  std::vector<geye_ctx *> lanes;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t fork = nullptr;
+  std::vector<cudaEvent_t> joins;
+  struct Graph {
+    cudaGraphExec_t exec = nullptr;
+    int kernels = 0;
+  };
+  std::map<std::string, Graph> graphs;   // by lane sizes, thresh, overlap
+  int last_kernels = 0;
+  cudaEvent_t t0 = nullptr, t1 = nullptr;   // around the last graph launch
+};
+
+extern "C" {
+
+geye_status geye_batch_create(int device, geye_model *const *models, int n_models, geye_conv_mode mode, int max_frames,
+                              geye_batch **out) {
+  ARG_CHECK(models && n_models > 0 && n_models <= 16 && out, "bad argument");
+  ARG_CHECK(max_frames >= 1 && max_frames <= 256, "max_frames must be in 1..256");
+  ARG_CHECK(mode == GEYE_CONV_FP32 || mode == GEYE_CONV_BF16 || mode == GEYE_CONV_FP8, "unknown conv mode");
+  for (int i = 0; i < n_models; i++) ARG_CHECK(models[i], "null model");
+  CUDA_TRY(cudaSetDevice(device));
+  auto *b = new geye_batch();
+  b->device = device;
+  b->models.assign(models, models + n_models);
+  b->mode = mode;
+  b->max_frames = max_frames;
+  cudaError_t e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreate(&b->t0);
+  if (e == cudaSuccess) e = cudaEventCreate(&b->t1);
+  if (e != cudaSuccess) {
+    if (b->t0) cudaEventDestroy(b->t0);
+    if (b->fork) cudaEventDestroy(b->fork);
+    if (b->stream) cudaStreamDestroy(b->stream);
+    delete b;
+    set_error(std::string("batch: ") + cudaGetErrorString(e));
+    return GEYE_ERR_CUDA;
+  }
+  *out = b;
+  return GEYE_OK;
+}
+
+geye_status geye_batch_destroy(geye_batch *b) {
+  if (!b) return GEYE_OK;
+  cudaSetDevice(b->device);
+  cudaStreamSynchronize(b->stream);
+  for (auto &g : b->graphs)
+    if (g.second.exec) cudaGraphExecDestroy(g.second.exec);
+  for (auto e : b->joins) cudaEventDestroy(e);
+  for (auto *c : b->lanes) geye_ctx_destroy(c);
+  cudaEventDestroy(b->fork);
+  cudaEventDestroy(b->t0);
+  cudaEventDestroy(b->t1);
+  cudaStreamDestroy(b->stream);
+  delete b;
+  return GEYE_OK;
+}
+
+geye_status geye_batch_run(geye_batch *b, int n_frames, const uint8_t *const *bgr, const int *widths,
+                           const int *heights, const int *width_steps, float thresh, float overlap,
+                           geye_result *results) {
+  ARG_CHECK(b && bgr && widths && heights && width_steps && results, "null argument");
+  ARG_CHECK(n_frames >= 1 && n_frames <= b->max_frames, "n_frames out of range");
+  CUDA_TRY(cudaSetDevice(b->device));
+  const int nm = (int)b->models.size();
+  std::string key;
+  std::vector<Plan *> plans(n_frames);
+  for (int i = 0; i < n_frames; i++) {
+    ARG_CHECK(bgr[i] && widths[i] >= 16 && heights[i] >= 16 && width_steps[i] >= 3 * widths[i], "bad frame");
+    while ((int)b->lanes.size() <= i) {
+      geye_ctx *c = nullptr;
+      GEYE_TRY(geye_ctx_create(b->device, nullptr, &c));
+      b->lanes.push_back(c);
+      const geye_status st = geye_ctx_set_conv_mode(c, b->mode);
+      if (st != GEYE_OK) return st;
+      cudaEvent_t j = nullptr;
+      CUDA_TRY(cudaEventCreateWithFlags(&j, cudaEventDisableTiming));
+      b->joins.push_back(j);
+    }
+    GEYE_TRY(frame_plan(b->lanes[i], b->models.data(), nm, widths[i], heights[i], &plans[i]));
+    GEYE_TRY(ensure_staging(*plans[i]));
+    uint8_t *dst = static_cast<uint8_t *>(plans[i]->h_bgr);
+    for (int y = 0; y < heights[i]; y++)
+      memcpy(dst + (size_t)y * 3 * widths[i], bgr[i] + (size_t)y * width_steps[i], (size_t)3 * widths[i]);
+    key += std::to_string(widths[i]) + "x" + std::to_string(heights[i]) + ",";
+  }
+  {
+    unsigned tb, ob;
+    memcpy(&tb, &thresh, 4);
+    memcpy(&ob, &overlap, 4);
+    key += std::to_string(tb) + ":" + std::to_string(ob);
+  }
+  geye_batch::Graph &g = b->graphs[key];
+  if (!g.exec) {
+    cudaGraph_t graph = nullptr;
+    CUDA_TRY(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeRelaxed));
+    geye_status st = GEYE_OK;
+    cudaError_t e = cudaEventRecord(b->fork, b->stream);
+    for (int i = 0; i < n_frames && st == GEYE_OK && e == cudaSuccess; i++) {
+      geye_ctx *c = b->lanes[i];
+      e = cudaStreamWaitEvent(c->stream, b->fork, 0);
+      if (e != cudaSuccess) break;
+      const bool graphs = c->use_graphs;
+      c->use_graphs = false;   // the lane's kernels go straight into the batch graph
+      c->capturing = true;
+      st = enqueue_frame(c, *plans[i], thresh, overlap, nullptr, 0, nullptr, nullptr, false);
+      c->capturing = false;
+      c->use_graphs = graphs;
+      c->pending = nullptr;
+      if (st == GEYE_OK) e = cudaEventRecord(b->joins[i], c->stream);
+      if (e == cudaSuccess && st == GEYE_OK) e = cudaStreamWaitEvent(b->stream, b->joins[i], 0);
+    }
+    const cudaError_t ec = cudaStreamEndCapture(b->stream, &graph);
+    if (st != GEYE_OK || e != cudaSuccess || ec != cudaSuccess) {
+      if (graph) cudaGraphDestroy(graph);
+      b->graphs.erase(key);
+      if (st != GEYE_OK) return st;
+      set_error(std::string("batch graph capture: ") + cudaGetErrorString(e != cudaSuccess ? e : ec));
+      return GEYE_ERR_CUDA;
+    }
+    size_t n = 0;
+    cudaGraphGetNodes(graph, nullptr, &n);
+    std::vector<cudaGraphNode_t> nodes(n);
+    if (n) cudaGraphGetNodes(graph, nodes.data(), &n);
+    int kernels = 0;
+    for (auto nd : nodes) {
+      cudaGraphNodeType t;
+      if (cudaGraphNodeGetType(nd, &t) == cudaSuccess && t == cudaGraphNodeTypeKernel) kernels++;
+    }
+    const cudaError_t ie = cudaGraphInstantiate(&g.exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (ie != cudaSuccess) {
+      g.exec = nullptr;
+      b->graphs.erase(key);
+      set_error(std::string("batch graph instantiate: ") + cudaGetErrorString(ie));
+      return GEYE_ERR_CUDA;
+    }
+    g.kernels = kernels;
+  }
+  CUDA_TRY(cudaEventRecord(b->t0, b->stream));
+  CUDA_TRY(cudaGraphLaunch(g.exec, b->stream));
+  CUDA_TRY(cudaEventRecord(b->t1, b->stream));
+  CUDA_TRY(cudaStreamSynchronize(b->stream));
+  b->last_kernels = g.kernels;
+  geye_status st = GEYE_OK;
+  for (int i = 0; i < n_frames; i++) {
+    b->lanes[i]->pending = plans[i];
+    const geye_status s = collect_frame(b->lanes[i], results + (size_t)i * nm, false);
+    if (st == GEYE_OK) st = s;
+  }
+  return st;
+}
+
+geye_status geye_batch_stats(geye_batch *b, int out[4], float *last_ms) {
+  ARG_CHECK(b && out && last_ms, "null argument");
+  out[0] = (int)b->lanes.size();
+  out[1] = (int)b->graphs.size();
+  out[2] = b->last_kernels;
+  out[3] = 0;
+  *last_ms = 0.f;
+  if (b->last_kernels) CUDA_TRY(cudaEventElapsedTime(last_ms, b->t0, b->t1));
+  return GEYE_OK;
 }
 
 }  // extern "C"

@@ -76,6 +76,10 @@ def lib(build_if_missing: bool = True):
             "geye_ctx_debug_counters": [vp, vp, i32],
             "geye_score_map": [vp, vp, i32, i32, vp, i32, vp],
             "geye_conv_tuning": [vp, vp, vp, vp],
+            "geye_batch_create": [i32, vp, i32, i32, i32, C.POINTER(vp)],
+            "geye_batch_destroy": [vp],
+            "geye_batch_run": [vp, i32, vp, vp, vp, vp, C.c_float, C.c_float, vp],
+            "geye_batch_stats": [vp, vp, vp],
             "geye_detect_submit": [vp, vp, i32, vp, i32, i32, i32, C.c_float, C.c_float],
             "geye_detect_query": [vp],
             "geye_detect_collect": [vp, vp],
@@ -451,6 +455,53 @@ class Server:
 
     def __exit__(self, *a):
         self.close()
+
+
+class Batch:
+    """Several frames of any sizes as one CUDA graph (geye_batch_*): one lane per
+    frame, the lanes parallel branches of one graph; results per frame and model."""
+
+    def __init__(self, models: list, conv: int = CONV_FP32, max_frames: int = 32, device: int = 0):
+        arr = (C.c_void_p * len(models))(*[m.h for m in models])
+        h = C.c_void_p()
+        _check(lib().geye_batch_create(device, arr, len(models), conv, max_frames, C.byref(h)), "batch_create")
+        self.h = h.value
+        self.n_models = len(models)
+        self.models = models
+
+    def run(self, frames: list, thresh: float = -0.5, overlap: float = 0.5) -> list:
+        fr = [np.ascontiguousarray(f, dtype=np.uint8) for f in frames]
+        n = len(fr)
+        ptrs = (C.c_void_p * n)(*[f.ctypes.data for f in fr])
+        w = np.array([f.shape[1] for f in fr], np.int32)
+        h = np.array([f.shape[0] for f in fr], np.int32)
+        st = 3 * w
+        res = (_Result * (n * self.n_models))()
+        _check(lib().geye_batch_run(self.h, n, ptrs, _p(w), _p(h), _p(st), thresh, overlap, res), "batch_run")
+        return [[_result_to_dict(res[i * self.n_models + m]) for m in range(self.n_models)] for i in range(n)]
+
+    def stats(self) -> dict:
+        o = np.zeros(4, np.int32)
+        ms = np.zeros(1, np.float32)
+        _check(lib().geye_batch_stats(self.h, _p(o), _p(ms)), "batch_stats")
+        return {"lanes": int(o[0]), "graphs": int(o[1]), "kernels": int(o[2]), "last_ms": float(ms[0])}
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().geye_batch_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class Model:

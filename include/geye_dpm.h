@@ -218,6 +218,25 @@ geye_status geye_server_stats(geye_server *s, long long out[8]);
  * boxes[4*i]; *n = count. */
 geye_status geye_server_tracks(geye_server *s, int stream, int max, float *boxes, int *n);
 
+/* ---- batches -------------------------------------------------------------- */
+/* Several frames of any sizes as one CUDA graph: each frame gets a lane (its own
+ * context, stream and plan per size, created on first use) and the lanes run as
+ * parallel branches of one graph between a fork and a join, the graph kept per
+ * combination of lane sizes, thresh and overlap.  geye_batch_run copies the
+ * frames into the lanes' pinned buffers, launches the graph, waits, and fills
+ * results[i * n_models + m] (free each with geye_result_free); every result is
+ * the one geye_detect_multi gives for that frame alone. */
+typedef struct geye_batch geye_batch;
+geye_status geye_batch_create(int device, geye_model *const *models, int n_models, geye_conv_mode mode,
+                              int max_frames, geye_batch **out);
+geye_status geye_batch_destroy(geye_batch *b);
+geye_status geye_batch_run(geye_batch *b, int n_frames, const uint8_t *const *bgr, const int *widths,
+                           const int *heights, const int *width_steps, float thresh, float overlap,
+                           geye_result *results);
+/* out = {lanes, graphs built, kernels in the last graph, 0}; last_ms = device
+ * time of the last graph launch (CUDA events on the batch stream). */
+geye_status geye_batch_stats(geye_batch *b, int out[4], float *last_ms);
+
 /* ---- measurement ---------------------------------------------------------- */
 /* When enabled, the context records CUDA events around each stage on its stream.
  * ms receives per-stage milliseconds of the last run, in this order:

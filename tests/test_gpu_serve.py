@@ -100,3 +100,28 @@ def test_tracker_matches_its_restatement_and_isolates_streams(setup):
         tracks_solo = solo.tracks(0)
     assert [tk[d["ticket"]] for d in done] == [0, 1, 0, 1, 0]
     assert np.array_equal(tracks_mix, tracks_solo)   # stream 1 did not disturb stream 0
+
+
+@pytest.mark.parametrize("conv", ["fp32", "bf16"])
+def test_batch_graph_matches_single_frames(tmp_path, conv):
+    """A batch of mixed sizes as one CUDA graph gives each frame's single-frame result."""
+    import geye_gb300 as g
+    from geye_gb300 import synth
+    mode = {"fp32": g.CONV_FP32, "bf16": g.CONV_BF16}[conv]
+    sizes = [(320, 240), (640, 480), (320, 240), (400, 300), (640, 480)]
+    frames = [synth.make_frame(w, h, seed=50 + i) for i, (w, h) in enumerate(sizes)]
+    with g.Context(0, conv=mode) as c:
+        ms = [g.Model(c, *synth.write_model_csv(s, str(tmp_path))) for s in (synth.CAR_SPEC, synth.PERSON_SPEC)]
+        alone = [c.detect_multi(f, ms, -0.5, 0.5, None) for f in frames]
+        with g.Batch(ms, conv=mode, max_frames=8) as b:
+            for rep in range(2):   # the second run replays the same graph
+                got = b.run(frames)
+                for ra, rb in zip(alone, got):
+                    for x, y in zip(ra, rb):
+                        assert x["num"] == y["num"]
+                        for k in ("point", "or_point", "type", "scale", "score"):
+                            assert np.array_equal(x[k], y[k]), k
+            st = b.stats()
+            assert st["lanes"] == len(frames) and st["graphs"] == 1 and st["kernels"] > 0 and st["last_ms"] > 0
+        for m in ms:
+            m.close()
