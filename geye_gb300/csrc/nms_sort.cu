@@ -25,7 +25,7 @@
 
 namespace geye {
 
-constexpr int kLevels = 16;      // grid-wide partition levels launched per frame
+constexpr int kLevels = 10;      // grid-wide partition levels launched per frame
 constexpr int kT = kNmsTile;     // elements per tile (4 per thread)
 constexpr int kWarpSeg = 1024;   // shared-memory kernel: block partitions above this
 constexpr int kWL = 256;         // its queue of warp segments
