@@ -24,8 +24,10 @@
 // A CTA (4 warps) owns a run of up to 16 tiles of 128 positions of one (level,
 // filter group), each tile with its own TMEM accumulator.  The filter is walked
 // in column phases whose bank columns and feature slab fit in shared memory:
-// one thread bulk-copies them (cp.async.bulk, completion on an mbarrier) and
-// issues every tile's MMAs, committed to a second mbarrier; after the last
+// one thread bulk-copies them (cp.async.bulk, completion on an mbarrier); one
+// thread per warp issues the MMAs of every fourth tile (each tile's chain from
+// one thread, in order) and commits them to a second mbarrier that expects the
+// four warps' commits; after the last
 // phase the four warps read the accumulators with tcgen05.ld (warp w owns TMEM
 // lanes 32w..32w+31) and write the maps in the reference layout.  Every
 // mbarrier wait is bounded; a timeout sets an error bit and the CTA still
@@ -197,7 +199,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_conv_tc(const TcJob *__restri
 
   if (threadIdx.x == 0) {
     mbar_init(bar_load, 1);
-    mbar_init(bar_mma, 1);
+    mbar_init(bar_mma, kTcThreads / 32);   // one commit per issuing warp
     mbar_fence_init();
   }
   if (warp == 0) tmem_alloc(tslot, ncols);
@@ -230,7 +232,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_conv_tc(const TcJob *__restri
     }
     ok = __syncthreads_and(landed);
     if (!ok) break;
-    if (threadIdx.x == 0) {
+    if (lane == 0) {   // one issuing thread per warp: tiles warp, warp + 4, ... (each tile's chain in order)
       tc_fence_after();
       // The start-address field of a descriptor is (address >> 4) in its low 14 bits and
       // every operand lies below 2^18 bytes, so moving an operand by a 16-byte multiple off
@@ -240,7 +242,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_conv_tc(const TcJob *__restri
       const uint32_t a_hi = 2u * (uint32_t)S;           // planes 2, 3: 2 * plane_bytes >> 4
       const uint32_t b_tap = NQ * (uint32_t)J.n_pad;    // one tap of the bank: NQ * bq >> 4
       const uint32_t b_hi = 2u * (uint32_t)J.n_pad;     // planes 2, 3 of a tap
-      for (int i = 0; i < ntile; i++) {
+      for (int i = warp; i < ntile; i += kTcThreads / 32) {
         const uint32_t d = tmem + (uint32_t)(i * J.n_pad);
         uint32_t acc = ph ? 1u : 0u;
         for (int xp = 0; xp < ncol; xp++) {
@@ -255,7 +257,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_conv_tc(const TcJob *__restri
           }
         }
       }
-      tc_commit(bar_mma);
+      tc_commit(bar_mma);   // tracks this thread's MMAs (an immediate arrive if it issued none)
     }
     bool done = mbar_wait(bar_mma, (uint32_t)(ph & 1), kWaitNs);
     if (!done) {

@@ -33,7 +33,7 @@
 namespace geye {
 
 constexpr int kDtThreads = 256;
-constexpr int kDtElems = 2048;      // outputs per block (about)
+constexpr int kDtElems = 4096;      // outputs per block (about)
 constexpr int kDtPad = 64;          // largest window half-width served by the fast loop
 
 __device__ __forceinline__ float dt_f(float v, float a, float b, int t) {
@@ -98,47 +98,68 @@ __host__ __device__ __forceinline__ size_t dt_smem_bytes(int L, int n) {
          sizeof(int) * 2 * (size_t)L;
 }
 
-// Every output of lines l0, l0 + G, ... (G groups of n threads) or, for lines
-// longer than the block, outputs d, d + blockDim of every line: window
-// half-width KM (the block's largest K: candidates past a line's own K lose
-// to f_d(d) anyway, so the wider window returns the same leftmost minimum),
-// unrolled with the per-offset terms in registers.
+// Leftmost minimum of output d over the window |t| < KM of a padded line,
+// unrolled; At/Bt: (a*t)*t and b*t tabulated in shared memory (broadcast
+// reads).  KM may exceed the line's own K: candidates past K lose to f_d(d)
+// anyway, so a wider window returns the same leftmost minimum.
 template <int KM>
-__device__ __forceinline__ void dt_scan_block(const float *__restrict__ v_s, int stride, int n, int nl, float a, float b,
-                                              const int *__restrict__ K_s, float *__restrict__ o_s,
-                                              int *__restrict__ g_s) {
-  float At[2 * KM - 1], Bt[2 * KM - 1];
+__device__ __forceinline__ int dt_scan_fixed(const float *__restrict__ line, int d, const float *__restrict__ At,
+                                             const float *__restrict__ Bt, float &best) {
+  const float *v = line + d - (KM - 1);   // v[i] = line[d - t], t = KM-1-i: p ascending
+  best = INFINITY;
+  int s = -1;
 #pragma unroll
   for (int i = 0; i < 2 * KM - 1; i++) {
-    const float ft = (float)(KM - 1 - i);   // t = KM-1 .. 1-KM
-    At[i] = a * ft * ft;
-    Bt[i] = b * ft;
+    const float f = (v[i] + At[KM - 1 - i]) + Bt[KM - 1 - i];
+    if (f < best) { best = f; s = i; }
   }
-  auto scan = [&](int l, int d) {
-    const float *v = v_s + l * stride + d - (KM - 1);   // v[i] = line[d - t], t = KM-1-i: p ascending
-    float best = INFINITY;
-    int s = -1;
-#pragma unroll
-    for (int i = 0; i < 2 * KM - 1; i++) {
-      const float f = (v[i] + At[i]) + Bt[i];
-      if (f < best) { best = f; s = i; }
+  return s < 0 ? -1 : d - (KM - 1) + s;
+}
+
+// Every output of the tile, spread over all threads (e -> line e / n, output
+// e % n, the division by a precomputed reciprocal), each with its own line's
+// window: K rounded up to an unrolled size, a loop beyond 16, a bounds-checked
+// loop past the padding.
+__device__ __forceinline__ void dt_scan_tile(const float *__restrict__ v_s, int stride, int n, int nl, float a,
+                                             float b, const int *__restrict__ K_s, const float *__restrict__ At,
+                                             const float *__restrict__ Bt, float *__restrict__ o_s,
+                                             int *__restrict__ g_s, unsigned magic) {
+  const int cnt = nl * n;
+  for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
+    const int l = __umulhi((unsigned)e, magic), d = e - l * n;
+    const float *line = v_s + l * stride;
+    const int K = K_s[l];
+    float best;
+    int p;
+    if (K <= 3) p = dt_scan_fixed<3>(line, d, At, Bt, best);
+    else if (K <= 4) p = dt_scan_fixed<4>(line, d, At, Bt, best);
+    else if (K <= 5) p = dt_scan_fixed<5>(line, d, At, Bt, best);
+    else if (K <= 6) p = dt_scan_fixed<6>(line, d, At, Bt, best);
+    else if (K <= 8) p = dt_scan_fixed<8>(line, d, At, Bt, best);
+    else if (K <= 12) p = dt_scan_fixed<12>(line, d, At, Bt, best);
+    else if (K <= 16) p = dt_scan_fixed<16>(line, d, At, Bt, best);
+    else if (K <= kDtPad) {
+      best = INFINITY;
+      p = -1;
+      for (int t = K - 1; t > -K; t--) {   // p = d - t ascending
+        const float f = (line[d - t] + At[t]) + Bt[t];
+        if (f < best) { best = f; p = d - t; }
+      }
+    } else {
+      const int lo = max(0, d - K + 1), hi = min(n - 1, d + K - 1);
+      p = lo;
+      best = dt_f(line[lo], a, b, d - lo);
+      for (int q = lo + 1; q <= hi; q++) {
+        const float fq = dt_f(line[q], a, b, d - q);
+        if (best > fq) { best = fq; p = q; }
+      }
     }
-    int p = d - (KM - 1) + s;
-    if (s < 0) {   // every candidate was NaN: the reference keeps the window's first index
-      p = max(0, d - K_s[l] + 1);
-      best = dt_f(v_s[l * stride + p], a, b, d - p);
+    if (p < 0) {   // every candidate was NaN: the reference keeps the window's first index
+      p = max(0, d - K + 1);
+      best = dt_f(line[p], a, b, d - p);
     }
-    o_s[l * n + d] = best;
-    g_s[l * n + d] = p;
-  };
-  const int tid = threadIdx.x, nth = blockDim.x;
-  if (n <= nth) {
-    const int G = nth / n, l0 = tid / n, d = tid - l0 * n;
-    if (l0 < G)
-      for (int l = l0; l < nl; l += G) scan(l, d);
-  } else {
-    for (int l = 0; l < nl; l++)
-      for (int d = tid; d < n; d += nth) scan(l, d);
+    o_s[e] = best;
+    g_s[e] = p;
   }
 }
 
@@ -149,7 +170,6 @@ template <int PASS>
 __global__ void __launch_bounds__(kDtThreads) k_dt(const DtJob *__restrict__ jobs, float *__restrict__ arena,
                                                     int *__restrict__ arena_i, int *fallback_count) {
   extern __shared__ float dsm[];
-  __shared__ int kmax_s;
   const DtJob J = jobs[blockIdx.y];
   const int d0 = J.d0;
   const int n = PASS == 1 ? J.d0 : J.d1;           // line length
@@ -195,7 +215,6 @@ __global__ void __launch_bounds__(kDtThreads) k_dt(const DtJob *__restrict__ job
     At[t] = a * ft * ft;
     Bt[t] = b * ft;
   }
-  if (tid == 0) kmax_s = 0;
   __syncthreads();
 
   // per-line window bound
@@ -219,53 +238,12 @@ __global__ void __launch_bounds__(kDtThreads) k_dt(const DtJob *__restrict__ job
       const int K = dt_window(vmin, vmax, vabs, a, b, n);
       K_s[l] = K;
       bad_s[l] = 0;
-      atomicMax(&kmax_s, K);
     }
   }
   __syncthreads();
 
-  // leftmost minimum of every output's window: a fixed window of the block's
-  // largest K when that is small, else each line's own window
-  const int KM = kmax_s;
-  switch (KM <= 2 ? 2 : KM <= 3 ? 3 : KM <= 4 ? 4 : KM <= 5 ? 5 : KM <= 6 ? 6 : KM <= 8 ? 8 : 0) {
-    case 2: dt_scan_block<2>(v_s, stride, n, nl, a, b, K_s, o_s, g_s); break;
-    case 3: dt_scan_block<3>(v_s, stride, n, nl, a, b, K_s, o_s, g_s); break;
-    case 4: dt_scan_block<4>(v_s, stride, n, nl, a, b, K_s, o_s, g_s); break;
-    case 5: dt_scan_block<5>(v_s, stride, n, nl, a, b, K_s, o_s, g_s); break;
-    case 6: dt_scan_block<6>(v_s, stride, n, nl, a, b, K_s, o_s, g_s); break;
-    case 8: dt_scan_block<8>(v_s, stride, n, nl, a, b, K_s, o_s, g_s); break;
-    default:
-      for (int e = tid; e < cnt; e += nth) {
-        const int l = __umulhi((unsigned)e, magic), d = e - l * n;
-        const float *v = v_s + l * stride;
-        const int K = K_s[l];
-        float best;
-        int s;
-        if (K <= kDtPad) {
-          best = INFINITY;
-          s = -1;
-          for (int t = K - 1; t > -K; t--) {   // p = d - t ascending
-            const float f = (v[d - t] + At[t]) + Bt[t];
-            if (f < best) { best = f; s = d - t; }
-          }
-          if (s < 0) {   // every candidate was NaN: the reference keeps the window's first index
-            s = max(0, d - K + 1);
-            best = dt_f(v[s], a, b, d - s);
-          }
-        } else {
-          const int lo = max(0, d - K + 1), hi = min(n - 1, d + K - 1);
-          s = lo;
-          best = dt_f(v[lo], a, b, d - lo);
-          for (int p = lo + 1; p <= hi; p++) {
-            const float fp = dt_f(v[p], a, b, d - p);
-            if (best > fp) { best = fp; s = p; }
-          }
-        }
-        o_s[e] = best;
-        g_s[e] = s;
-      }
-      break;
-  }
+  // leftmost minimum of every output's window
+  dt_scan_tile(v_s, stride, n, nl, a, b, K_s, At, Bt, o_s, g_s, magic);
   __syncthreads();
   for (int e = tid; e < cnt; e += nth) {
     const int l = __umulhi((unsigned)e, magic), d = e - l * n;
