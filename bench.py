@@ -52,8 +52,9 @@ WORKLOADS = {
     "serve64_mixed_bf16": dict(w=640, h=480, models=("car", "person"), conv="bf16", sim=True, streams=64, fps=30.0,
                                sizes=((640, 480), (1280, 720), (1920, 1080)), seconds=6.0),
     # 64 cameras at 640x480 only (the served BF16 pipeline's latency target at 64 streams)
+    # (at most 16 slots: more frames in flight only lengthen each frame's share of the GPU)
     "serve64_640x480_bf16": dict(w=640, h=480, models=("car", "person"), conv="bf16", sim=True, streams=64, fps=30.0,
-                                 sizes=((640, 480),), seconds=6.0),
+                                 sizes=((640, 480),), seconds=6.0, slots=16),
     # a batch of 32 frames of mixed sizes as one CUDA graph (geye_batch_run)
     "batch32_mixed_fp32": dict(w=640, h=480, models=("car", "person"), conv="fp32", batch=32,
                                sizes=((320, 240), (640, 480), (1280, 720), (1920, 1080))),
@@ -607,10 +608,11 @@ def run_serve_sim(args, wl):
     for s in range(n):
         for k in range(2):
             frames[(s, k)] = synth.make_frame(*sizes[s], seed=1000 * s + k)
-    srv = g.Server(models, conv=g.CONV_BF16, hbm_budget=40 << 30, max_slots=64, track=True)
+    max_slots = args.slots or wl.get("slots", 64)
+    srv = g.Server(models, conv=g.CONV_BF16, hbm_budget=40 << 30, max_slots=max_slots, track=True)
     for sz in sorted(set(sizes)):   # slots, plans and graphs for every resolution before the clock starts
         s0 = sizes.index(sz)
-        for _ in range(64):
+        for _ in range(max_slots):
             srv.submit(s0, frames[(s0, 0)])
         srv.drain()
         srv.poll(1024)
@@ -660,7 +662,8 @@ def run_serve_sim(args, wl):
         "e2e": {"value": len(arrivals) / wall, "unit": "frames/s", "api": "geye_server_submit/poll",
                 "h2d_bytes_per_step": int(np.mean([a * b * 3 for a, b in sizes])), "d2h_bytes_per_step": 4 * (64 + 2 * 11 * 4096),
                 "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99))},
-        "server": {"slots": st["slots"], "bytes_held": st["bytes_held"], "live_tracks_end": tracks},
+        "server": {"slots": st["slots"], "max_slots": max_slots, "bytes_held": st["bytes_held"],
+                   "live_tracks_end": tracks},
         "clocks": clk.summary(),
     }
     print(json.dumps(line), flush=True)
