@@ -162,3 +162,65 @@ def test_car_and_person_1280x720(ctx, car, person):
         assert res["num"] == ref["K"]
         assert np.array_equal(res["point"], ref["point"])
         assert np.array_equal(bits(res["score"]), bits(ref["score"]))
+
+
+def _all_scores(om, fr):
+    S = O.Scores(om, O.Pyramid(om, fr))
+    return np.sort(np.concatenate([S.score(l, c).ravel() for l in range(S.interval, S.LEN) if not S.skipped[l]
+                                   for c in range(S.NoC)]))[::-1]
+
+
+@pytest.mark.parametrize("k", [0, 1, 2, 3, 50])
+def test_pipeline_few_detections(ctx, car, k):
+    """Thresholds that let exactly k root positions through (k = 0: none; 1: the
+    reference's NMS never emits a box that is alone at its turn)."""
+    gm, om = car
+    fr = synth.make_frame(320, 240, seed=9)
+    gm.reset_scales()
+    om.m.ini = 1
+    s = _all_scores(om, fr)
+    assert s[k] < s[k - 1] if k else True   # no tie at the cut
+    thresh = float(s[k])
+    om.m.ini = 1
+    ref = O.car_detection(om, fr, thresh, 0.5)
+    gm.reset_scales()
+    got = ctx.car_detection(fr, gm, thresh, None, 0.5)
+    assert got["num"] == ref["K"]
+    assert np.array_equal(got["point"], ref["point"])
+    assert np.array_equal(bits(got["score"]), bits(ref["score"]))
+
+
+def test_pipeline_trained_like_models(ctx, tmp_path):
+    """Models with the shapes and value statistics of the reference's trained car
+    and person models: sparse detections (a few per frame) instead of every
+    position, at a threshold that lets some through."""
+    import geye_gb300 as g
+    fr = synth.make_frame(640, 480, seed=3)
+    for spec in (synth.CAR_TRAINED_LIKE, synth.PERSON_TRAINED_LIKE):
+        paths = synth.write_model_csv(spec, str(tmp_path))
+        om = O.Model(*paths)
+        s = _all_scores(om, fr)
+        thresh = float(s[min(200, len(s) - 1)])
+        om.m.ini = 1
+        ref = O.car_detection(om, fr, thresh, 0.5)
+        gm = g.Model(ctx, *paths)
+        got = ctx.car_detection(fr, gm, thresh, None, 0.5)
+        gm.close()
+        assert got["num"] == ref["K"] > 0
+        assert np.array_equal(got["point"], ref["point"])
+        assert np.array_equal(got["type"], ref["type"])
+        assert np.array_equal(bits(got["score"]), bits(ref["score"]))
+
+
+@pytest.mark.parametrize("w,h", [(333, 251), (1920, 1080)])
+def test_pipeline_odd_and_large_frames(ctx, car, w, h):
+    gm, om = car
+    gm.reset_scales()
+    om.m.ini = 1
+    fr = synth.make_frame(w, h, seed=12)
+    got = ctx.car_detection(fr, gm, -0.5, None, 0.5)
+    ref = O.car_detection(om, fr, -0.5, 0.5)
+    assert got["num"] == ref["K"]
+    assert np.array_equal(got["point"], ref["point"])
+    assert np.array_equal(got["or_point"], ref["or_point"])
+    assert np.array_equal(bits(got["score"]), bits(ref["score"]))
