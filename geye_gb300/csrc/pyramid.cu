@@ -80,9 +80,11 @@ __global__ void __launch_bounds__(kResizeWarps * 32) k_resize_pass(const ResizeJ
     float *out = dst + (size_t)x * J.dst_h;
     if (vertical) {
       const float *col = src + (size_t)x * J.src_h;
-      for (int y = lane; y < J.dst_h; y += 32) {
-        float a0 = 0.0f, a1 = 0.0f, a2 = 0.0f;
+      for (int y = lane; y < J.dst_h; y += 64) {   // two outputs per lane in flight
+        const int y2 = y + 32;
+        float a0 = 0.0f, a1 = 0.0f, a2 = 0.0f, c0 = 0.0f, c1 = 0.0f, c2 = 0.0f;
         const int t1 = ts[y + 1];
+        const int u0 = y2 < J.dst_h ? ts[y2] : 0, u1 = y2 < J.dst_h ? ts[y2 + 1] : 0;
         for (int t = ts[y]; t < t1; t++) {
           const float w = al[t];
           const float *p = col + si[t];
@@ -90,9 +92,21 @@ __global__ void __launch_bounds__(kResizeWarps * 32) k_resize_pass(const ResizeJ
           a1 += w * p[src_plane];
           a2 += w * p[2 * src_plane];
         }
+        for (int t = u0; t < u1; t++) {
+          const float w = al[t];
+          const float *p = col + si[t];
+          c0 += w * p[0];
+          c1 += w * p[src_plane];
+          c2 += w * p[2 * src_plane];
+        }
         out[y] = a0;
         out[dst_plane + y] = a1;
         out[2 * dst_plane + y] = a2;
+        if (y2 < J.dst_h) {
+          out[y2] = c0;
+          out[dst_plane + y2] = c1;
+          out[2 * dst_plane + y2] = c2;
+        }
       }
     } else {
       // taps are uniform along the column: two outputs per lane in flight
@@ -202,12 +216,18 @@ __global__ void __launch_bounds__(kPixWarps * 32) k_hog_pix(const HogPixJob *__r
   uint8_t *bin = reinterpret_cast<uint8_t *>(arena + J.bin_off);
   const int lane = threadIdx.x & 31;
   for (int x = 1 + blockIdx.x * kPixWarps + (threadIdx.x >> 5); x < J.xe; x += gridDim.x * kPixWarps) {
-    for (int y = 1 + lane; y < J.ye; y += 32) {
-      int b;
-      float m;
+    for (int y = 1 + lane; y < J.ye; y += 64) {   // two pixels per lane in flight
+      const int y2 = y + 32;
+      int b, b2 = 0;
+      float m, m2 = 0.f;
       hog_pixel(img, J.h, J.w, x, y, b, m);
+      if (y2 < J.ye) hog_pixel(img, J.h, J.w, x, y2, b2, m2);
       mag[(size_t)x * J.Y + y] = m;
       bin[(size_t)x * J.Y + y] = (uint8_t)b;
+      if (y2 < J.ye) {
+        mag[(size_t)x * J.Y + y2] = m2;
+        bin[(size_t)x * J.Y + y2] = (uint8_t)b2;
+      }
     }
   }
 }

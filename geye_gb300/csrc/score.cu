@@ -110,18 +110,20 @@ void launch_scan_counts(int *counts, int n, int *total, cudaStream_t s) {
 // exact except the final rounding to float, so it is restated in float and
 // integer arithmetic with that one rounding (the FP64 pipe is narrow here):
 //   q0 = ((py - 2)/2 + 1) * scale  ==  (py * 0.5f) * scale   (exact product, one rounding)
-//   q2 = q0 + psize*scale/2 - 1     ==  one rounding of the exact sum (int64 below)
+//   q2 = q0 + psize*scale/2 - 1     ==  one rounding of the exact sum (below)
 
-// float(q + h - 1) with the sum taken exactly.  For |q|, |h| in [0.5, 2^28) the
-// double expression is exact before its rounding to float, and q, h, 1 are
-// multiples of 2^-24 whose scaled sum fits an int64; __ll2float_rn rounds it
-// to nearest even as the double-to-float conversion does.
+// float(q + h - 1) with the sum taken exactly.  For q, h in [0.5, 2^23) the
+// double expression is exact before its rounding to float.  In float:
+// s + e = q + h exactly (TwoSum; no contraction), s - 1 is exact for
+// 1 <= s < 2^24 (1 is a multiple of s's unit in the last place), so
+// (s - 1) + e is one correctly rounded addition of the exact q + h - 1.
+// (64-bit integer conversions would run on the narrow FP64 pipe.)
 __device__ __forceinline__ float sum_minus_one(float q, float h) {
-  const float aq = fabsf(q), ah = fabsf(h);
-  if (aq >= 0.5f && ah >= 0.5f && aq < 268435456.0f && ah < 268435456.0f) {
-    const long long Q = __float2ll_rn(q * 16777216.0f);
-    const long long H = __float2ll_rn(h * 16777216.0f);
-    return __ll2float_rn(Q + H - 16777216LL) * 5.9604644775390625e-08f;
+  if (q >= 0.5f && h >= 0.5f && q < 8388608.0f && h < 8388608.0f) {
+    const float s = q + h;
+    const float bb = s - q;
+    const float e = (q - (s - bb)) + (h - bb);
+    return (s - 1.0f) + e;
   }
   return (float)((double)q + (double)h - 1.0);
 }
