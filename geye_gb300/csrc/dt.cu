@@ -272,11 +272,17 @@ __global__ void __launch_bounds__(kDtThreads) k_dt(const DtJob *__restrict__ job
     for (int e = tid; e < (n << lgL); e += nth) {
       const int l = e & (L - 1), x = e >> lgL;
       if (l >= nl) continue;
-      const size_t o = (size_t)x * d0 + line0 + l;
+      const int y = line0 + l;
+      const bool mpos = (y & 1) == J.par_y && (x & 1) == J.par_x;
+      const bool ipos = (y & 1) != J.par_y && (x & 1) != J.par_x;
+      const bool wm = !J.samp_m || mpos, wi = !J.samp_i || ipos;
+      const size_t o = (size_t)x * d0 + y;
       const int ix = g_s[l * n + x];
-      M[o] = o_s[l * n + x];
-      Ix[o] = ix;
-      Iy[o] = tIy[(size_t)ix * d0 + line0 + l];
+      if (wm) M[o] = o_s[l * n + x];
+      if (wi) {
+        Ix[o] = ix;
+        Iy[o] = tIy[(size_t)ix * d0 + y];
+      }
     }
   }
 }

@@ -76,6 +76,12 @@ struct DtJob {             // one part map: DT of the negated map
   int M_off, Ix_off, Iy_off;
   float ax, bx, ay, by;
   int negate;              // 1: run on -map (inverse_Q of the pipeline); 0: plain dt()
+  // only what the pipeline reads is written (0: full maps, dt() itself):
+  // samp_m: M only where the score sum reads it (rows y = par_y, columns
+  // x = par_x mod 2); samp_i: Ix/Iy only where the part boxes probe (the other
+  // parity in both), set when every probe falls inside the map
+  int samp_m, samp_i;
+  int par_y, par_x;
 };
 
 struct ScoreJob {          // one (level, component) score map

@@ -374,6 +374,15 @@ static geye_status build_model_plan(geye_ctx *ctx, Plan &P, geye_model *mdl, int
         D.Iy_off = A.take((size_t)d0 * d1);
         D.ax = m.def[4 * di]; D.bx = m.def[4 * di + 1]; D.ay = m.def[4 * di + 2]; D.by = m.def[4 * di + 3];
         D.negate = 1;
+        // the score sum reads M at (anchor_y + 2y, anchor_x + 2x) (dt.cpp:38-55); the
+        // part boxes read Ix/Iy one row and column before (get_boxes.cpp:243-258)
+        D.samp_m = 1;
+        D.par_y = m.anchor[di * 2 + 1] & 1;
+        D.par_x = m.anchor[di * 2] & 1;
+        {   // the box probes (anchor - 1 + 2k) all inside the map: no linear wrap, no entry-0 reads
+          const int ay0 = m.anchor[di * 2 + 1] - 1, ax0 = m.anchor[di * 2] - 1;
+          D.samp_i = ay0 >= 0 && ax0 >= 0 && ay0 + 2 * (r0 - 1) < d0 && ax0 + 2 * (r1 - 1) < d1;
+        }
         mp->dt_jobs.push_back(D);
         mp->dt_max_d0 = std::max(mp->dt_max_d0, d0);
         mp->dt_max_d1 = std::max(mp->dt_max_d1, d1);
