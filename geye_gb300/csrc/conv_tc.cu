@@ -51,7 +51,7 @@ constexpr int kTcThreads = 128;
 constexpr int kTcM = 128;                        // positions per tile (TMEM lanes)
 constexpr int kTcMaxTiles = 16;                  // tiles per CTA, at most
 constexpr size_t kTcSmemBudget = 220 * 1024;     // dynamic shared memory per CTA, at most
-constexpr int kTcHead = 384;                    // barriers, TMEM address, map offsets and scales at the front
+constexpr int kTcHead = 640;                    // barriers, TMEM address, map offsets, scales, map dims
 constexpr unsigned long long kWaitNs = 1000000000ull;   // a wait gives up after 1 s (then 4 s for the drain)
 
 struct TcJob {
@@ -59,7 +59,7 @@ struct TcJob {
   int plane_cells;   // cells per plane
   int fs0, fs1;      // feature rows, columns
   int b0, b1;        // filter rows, columns
-  int c0, c1;        // output rows, columns
+  int c0, c1;        // output rows, columns computed (those of the group's smallest filter)
   int n, n_pad;      // filters; padded to 16 or 32
   int bank_off;      // byte offset of the group's bank in the model's bank buffer
   int out_tab;       // first entry of the job's map offsets
@@ -170,6 +170,7 @@ template <int NQ>
 __global__ void __launch_bounds__(kTcThreads, 1) k_conv_tc(const TcJob *__restrict__ jobs, const int4 *__restrict__ chunks,
                                                            const int *__restrict__ outs,
                                                            const float *__restrict__ inv_scale,
+                                                           const int2 *__restrict__ out_dims,
                                                            const uint8_t *__restrict__ arena16,
                                                            const uint8_t *__restrict__ bank, float *__restrict__ arena,
                                                            int *err) {
@@ -179,12 +180,14 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_conv_tc(const TcJob *__restri
   uint32_t *tslot = reinterpret_cast<uint32_t *>(sm + 16);
   int *out_s = reinterpret_cast<int *>(sm + 32);       // the job's map offsets (n <= 32)
   float *scl_s = reinterpret_cast<float *>(sm + 160);   // and output scales
+  int2 *dim_s = reinterpret_cast<int2 *>(sm + 288);     // and each map's rows, columns
   const int4 ch = chunks[blockIdx.x];
   const TcJob J = jobs[ch.x];
   const int tile0 = ch.y, ntile = ch.z, cs = ch.w;   // cs = filter columns per phase
   if (threadIdx.x < J.n) {
     out_s[threadIdx.x] = outs[J.out_tab + threadIdx.x];
     scl_s[threadIdx.x] = inv_scale[J.out_tab + threadIdx.x];
+    dim_s[threadIdx.x] = out_dims[J.out_tab + threadIdx.x];
   }
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int p_begin = tile0 * kTcM;
@@ -278,9 +281,11 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_conv_tc(const TcJob *__restri
       tc_wait_ld();
       if (valid) {
         for (int k = 0; k < 16 && c0 + k < J.n; k++) {
+          const int2 dk = dim_s[c0 + k];   // this filter's own map: rows dk.x, columns dk.y
+          if (x >= dk.y || y >= dk.x) continue;
           float v;
           memcpy(&v, &r[k], 4);
-          arena[(size_t)out_s[c0 + k] + (size_t)x * J.c0 + y] = v * scl_s[c0 + k];
+          arena[(size_t)out_s[c0 + k] + (size_t)x * dk.x + y] = v * scl_s[c0 + k];
         }
       }
     }
@@ -314,24 +319,33 @@ static uint16_t to_bf16(float f) {   // round to nearest even
 }
 
 // e4m3 bank from FP32 filters on the device (CUDA's own conversion, as for the
-// features): element (tap t, plane q, filter n, lane k) = channel 16q + k of
-// filter n at tap t times scale[n]
-__global__ void k_bank_e4m3(const float *const *__restrict__ filt, const float *__restrict__ scale, int n, int n_pad,
-                            int taps, uint8_t *__restrict__ out) {
+// features): element (tap t = xp*b0 + yp of the group's grid, plane q, filter
+// f, lane k) = channel 16q + k of filter f at (xp, yp) times scale[f], zero
+// outside the filter's own b1 x b0 (fdim[f] = {b0, b1})
+__global__ void k_bank_e4m3(const float *const *__restrict__ filt, const float *__restrict__ scale,
+                            const int2 *__restrict__ fdim, int n, int n_pad, int b0, int taps,
+                            uint8_t *__restrict__ out) {
   const int total = taps * 2 * n_pad * 16;
   for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x) {
     const int k = e % 16, f = (e / 16) % n_pad, q = (e / (16 * n_pad)) % 2, t = e / (32 * n_pad);
-    const int c = 16 * q + k;
+    const int c = 16 * q + k, xp = t / b0, yp = t - xp * b0;
     float v = 0.f;
-    if (f < n && c < kFeat) v = filt[f][(size_t)c * taps + t] * scale[f];
+    if (f < n && c < kFeat) {
+      const int fb0 = fdim[f].x, fb1 = fdim[f].y;
+      if (xp < fb1 && yp < fb0) v = filt[f][(size_t)c * fb0 * fb1 + xp * fb0 + yp] * scale[f];
+    }
     out[e] = (uint8_t)__nv_cvt_float_to_fp8(v, __NV_SATFINITE, __NV_E4M3);
   }
 }
 
-// filters of one size, one bank [tap][q][n_pad][16 B] each
+// A group's filters share one bank [tap][q][n_pad][16 B] over the group's tap
+// grid b1 x b0 (the largest of its filters); a smaller filter sits in the
+// grid's first rows and columns with zero weights around it, which add
+// nothing to its sums, and its map is its own size (c0, c1 of its b0, b1).
 struct BankGroup {
   int b0, b1, n, n_pad, bank_off, kind;
   std::vector<int> filt;      // indices into the caller's filter list
+  std::vector<int> fb0, fb1;  // each filter's own rows, columns
   std::vector<float> inv;     // per filter: factor that undoes the operand scaling
 };
 
@@ -345,26 +359,46 @@ static float e4m3_filter_scale(const float *F, size_t n) {
   return std::ldexp(1.0f, (int)std::floor(std::log2(448.0 / m)));
 }
 
-// groups filters by (kind, size), at most 32 per group; lays out their banks
-// (filter f is [31][b1][b0] as conv_fp32 reads it: element (c, xp, yp) at
-// c*b0*b1 + xp*b0 + yp).  BF16 banks are built here into bank16; for FP8
-// scale[f] is filled and the caller converts on the device.
+// tensor work of a grouping: every tile issues taps MMAs of N = n_pad
+static double group_cost(const std::vector<BankGroup> &gs) {
+  double c = 0;
+  for (auto &g : gs) c += (double)g.b0 * g.b1 * ((g.n <= 16 ? 16 : 32) + 16);
+  return c;
+}
+
+// groups the filters of each kind either by exact size or all together on the
+// largest grid (at most 32 a group), whichever issues less tensor work; lays
+// out the banks (filter f is [31][b1][b0] as conv_fp32 reads it: element
+// (c, xp, yp) at c*b0*b1 + xp*b0 + yp).  BF16 banks are built here into
+// bank16; for FP8 scale[f] is filled and the caller converts on the device.
 static void build_banks(const std::vector<const float *> &filt, const std::vector<int> &b0s,
                         const std::vector<int> &b1s, const std::vector<int> &kinds, geye_conv_mode mode,
                         std::vector<BankGroup> &groups, std::vector<uint16_t> &bank16, std::vector<float> &scale,
                         size_t &total) {
   const int NQ = tc_planes_of(mode);
   groups.clear();
-  for (size_t f = 0; f < filt.size(); f++) {
-    bool placed = false;
-    for (auto &g : groups)
-      if (g.kind == kinds[f] && g.b0 == b0s[f] && g.b1 == b1s[f] && g.n < 32) {
-        g.filt.push_back((int)f);
-        g.n++;
-        placed = true;
-        break;
-      }
-    if (!placed) groups.push_back(BankGroup{b0s[f], b1s[f], 1, 0, 0, kinds[f], {(int)f}, {}});
+  for (int kind = 0; kind <= 1; kind++) {
+    std::vector<BankGroup> exact, merged;
+    for (size_t f = 0; f < filt.size(); f++) {
+      if (kinds[f] != kind) continue;
+      bool placed = false;
+      for (auto &g : exact)
+        if (g.b0 == b0s[f] && g.b1 == b1s[f] && g.n < 32) {
+          g.filt.push_back((int)f); g.fb0.push_back(b0s[f]); g.fb1.push_back(b1s[f]);
+          g.n++;
+          placed = true;
+          break;
+        }
+      if (!placed) exact.push_back(BankGroup{b0s[f], b1s[f], 1, 0, 0, kind, {(int)f}, {b0s[f]}, {b1s[f]}, {}});
+      if (merged.empty() || merged.back().n == 32) merged.push_back(BankGroup{0, 0, 0, 0, 0, kind, {}, {}, {}, {}});
+      BankGroup &m = merged.back();
+      m.b0 = std::max(m.b0, b0s[f]);
+      m.b1 = std::max(m.b1, b1s[f]);
+      m.filt.push_back((int)f); m.fb0.push_back(b0s[f]); m.fb1.push_back(b1s[f]);
+      m.n++;
+    }
+    const auto &pick = group_cost(merged) < group_cost(exact) ? merged : exact;
+    groups.insert(groups.end(), pick.begin(), pick.end());
   }
   total = 0;
   for (auto &g : groups) {
@@ -373,23 +407,25 @@ static void build_banks(const std::vector<const float *> &filt, const std::vecto
     total += (size_t)g.b0 * g.b1 * NQ * g.n_pad * 16;
   }
   scale.assign(filt.size(), 1.f);
-  for (auto &g : groups) {
-    const int taps = g.b0 * g.b1;
-    for (int f : g.filt) {
-      if (mode == GEYE_CONV_FP8) scale[f] = e4m3_filter_scale(filt[f], (size_t)taps * kFeat);
+  for (auto &g : groups)
+    for (int k = 0; k < g.n; k++) {
+      const int f = g.filt[k];
+      if (mode == GEYE_CONV_FP8) scale[f] = e4m3_filter_scale(filt[f], (size_t)g.fb0[k] * g.fb1[k] * kFeat);
       g.inv.push_back(mode == GEYE_CONV_FP8 ? 1.0f / (scale[f] * kFp8FeatScale) : 1.0f);
     }
-  }
   if (mode == GEYE_CONV_FP8) return;
   bank16.assign(total / 2, 0);
   for (auto &g : groups) {
     uint16_t *dst = bank16.data() + g.bank_off / 2;
-    const int taps = g.b0 * g.b1;
     for (int n = 0; n < g.n; n++) {
       const float *F = filt[g.filt[n]];
-      for (int t = 0; t < taps; t++)
-        for (int c = 0; c < kFeat; c++)
-          dst[(((size_t)t * 4 + (c >> 3)) * g.n_pad + n) * 8 + (c & 7)] = to_bf16(F[(size_t)c * taps + t]);
+      const int fb0 = g.fb0[n], fb1 = g.fb1[n];
+      for (int xp = 0; xp < fb1; xp++)
+        for (int yp = 0; yp < fb0; yp++) {
+          const size_t t = (size_t)xp * g.b0 + yp;
+          for (int c = 0; c < kFeat; c++)
+            dst[((t * 4 + (c >> 3)) * g.n_pad + n) * 8 + (c & 7)] = to_bf16(F[(size_t)c * fb0 * fb1 + xp * fb0 + yp]);
+        }
     }
   }
 }
@@ -405,21 +441,30 @@ static geye_status upload_bank(const std::vector<BankGroup> &groups, geye_conv_m
   for (auto &g : groups) {
     std::vector<const float *> ptrs;
     std::vector<float> sc;
-    for (int f : g.filt) { ptrs.push_back(d_filt[f]); sc.push_back(scale[f]); }
+    std::vector<int2> dims;
+    for (int k = 0; k < g.n; k++) {
+      ptrs.push_back(d_filt[g.filt[k]]);
+      sc.push_back(scale[g.filt[k]]);
+      dims.push_back(make_int2(g.fb0[k], g.fb1[k]));
+    }
     const float **d_ptrs = nullptr;
     float *d_sc = nullptr;
+    int2 *d_dims = nullptr;
     CUDA_TRY(cudaMalloc(&d_ptrs, sizeof(float *) * ptrs.size()));
     cudaError_t e = cudaMalloc(&d_sc, sizeof(float) * sc.size());
+    if (e == cudaSuccess) e = cudaMalloc(&d_dims, sizeof(int2) * dims.size());
     if (e == cudaSuccess) e = cudaMemcpy(d_ptrs, ptrs.data(), sizeof(float *) * ptrs.size(), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(d_sc, sc.data(), sizeof(float) * sc.size(), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(d_dims, dims.data(), sizeof(int2) * dims.size(), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) {
       const int taps = g.b0 * g.b1, elems = taps * 2 * g.n_pad * 16;
       k_bank_e4m3<<<std::max(1, std::min((elems + 255) / 256, 1024)), 256, 0, s>>>(
-          d_ptrs, d_sc, g.n, g.n_pad, taps, static_cast<uint8_t *>(d_bank) + g.bank_off);
+          d_ptrs, d_sc, d_dims, g.n, g.n_pad, g.b0, taps, static_cast<uint8_t *>(d_bank) + g.bank_off);
       e = cudaStreamSynchronize(s);
     }
     cudaFree(d_ptrs);
     cudaFree(d_sc);
+    cudaFree(d_dims);
     if (e != cudaSuccess) {
       set_error(std::string("e4m3 filter bank: ") + cudaGetErrorString(e));
       return GEYE_ERR_CUDA;
@@ -433,28 +478,38 @@ struct TcTables {
   std::vector<int4> chunks;
   std::vector<int> outs;
   std::vector<float> inv;
+  std::vector<int2> dims;   // each map's rows, columns
   size_t max_smem = 0;
 };
 
 // one job: group g on a level whose planes start at plane_off; map_off[k] is
-// the float offset of filter k's output map.  False if it cannot fit in shared memory.
-// t_cap and budget: the largest tile run and shared memory a CTA may take (the
-// tile-shape candidates of the autotuner below).
+// the float offset of filter k's output map.  cells_avail: cells from the
+// start of plane 0 to the end of the planes' buffer (a slab may read past its
+// own plane into the next one or into the buffer's tail: those cells only
+// meet zero weights).  t_cap and budget: the largest tile run and shared
+// memory a CTA may take (the tile-shape candidates of the autotuner below).
+// False if it cannot fit in shared memory or the buffer.
 static bool add_tc_job(TcTables &T, int NQ, int plane_off, int fs0, int fs1, const BankGroup &g,
-                       const std::vector<int> &map_off, int t_cap = kTcMaxTiles, size_t budget = kTcSmemBudget) {
+                       const std::vector<int> &map_off, long long cells_avail, int t_cap = kTcMaxTiles,
+                       size_t budget = kTcSmemBudget) {
   TcJob J{};
   J.plane_off = plane_off;
   J.plane_cells = fs0 * fs1 + kTcPlanePad;
   J.fs0 = fs0; J.fs1 = fs1;
   J.b0 = g.b0; J.b1 = g.b1;
-  J.c0 = fs0 - g.b0 + 1; J.c1 = fs1 - g.b1 + 1;
+  int mb0 = g.b0, mb1 = g.b1;   // the smallest filter: the most outputs
+  for (int k = 0; k < g.n; k++) { mb0 = std::min(mb0, g.fb0[k]); mb1 = std::min(mb1, g.fb1[k]); }
+  J.c0 = fs0 - mb0 + 1; J.c1 = fs1 - mb1 + 1;
   if (J.c0 < 1 || J.c1 < 1) return false;
   J.n = g.n; J.n_pad = g.n_pad;
   J.bank_off = g.bank_off;
   J.out_tab = (int)T.outs.size();
   for (int k = 0; k < g.n; k++) {
+    const int c0k = fs0 - g.fb0[k] + 1, c1k = fs1 - g.fb1[k] + 1;
+    if (c0k < 1 || c1k < 1) return false;
     T.outs.push_back(map_off[k]);
     T.inv.push_back(g.inv[k]);
+    T.dims.push_back(make_int2(c0k, c1k));
   }
   const int P_valid = (J.c1 - 1) * J.fs0 + J.c0;
   J.ntiles = (P_valid + kTcM - 1) / kTcM;
@@ -478,7 +533,8 @@ static bool add_tc_job(TcTables &T, int NQ, int plane_off, int fs0, int fs1, con
   const long long reach = (long long)(g.b1 - 1) * fs0 + (g.b0 - 1);
   for (int t0 = 0; t0 < J.ntiles; t0 += T_cta) {
     const int nt = std::min(T_cta, J.ntiles - t0);
-    if ((long long)t0 * kTcM + nt * kTcM + reach > J.plane_cells) return false;   // slabs stay inside the planes
+    // the last plane's slab stays inside the buffer
+    if ((long long)(NQ - 1) * J.plane_cells + (long long)t0 * kTcM + nt * kTcM + reach > cells_avail) return false;
     T.chunks.push_back(make_int4(jid, t0, nt, cs));
     T.max_smem = std::max(T.max_smem, need(nt, cs));
   }
@@ -486,14 +542,14 @@ static bool add_tc_job(TcTables &T, int NQ, int plane_off, int fs0, int fs1, con
 }
 
 static void launch_conv_tc(int NQ, const TcJob *jobs, const int4 *chunks, int n_chunks, const int *outs,
-                           const float *inv, const uint8_t *planes, const uint8_t *bank, float *out, int *err,
-                           size_t smem, cudaStream_t s) {
+                           const float *inv, const int2 *dims, const uint8_t *planes, const uint8_t *bank, float *out,
+                           int *err, size_t smem, cudaStream_t s) {
   if (NQ == 4) {
     cudaFuncSetAttribute(k_conv_tc<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    k_conv_tc<4><<<n_chunks, kTcThreads, smem, s>>>(jobs, chunks, outs, inv, planes, bank, out, err);
+    k_conv_tc<4><<<n_chunks, kTcThreads, smem, s>>>(jobs, chunks, outs, inv, dims, planes, bank, out, err);
   } else {
     cudaFuncSetAttribute(k_conv_tc<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    k_conv_tc<2><<<n_chunks, kTcThreads, smem, s>>>(jobs, chunks, outs, inv, planes, bank, out, err);
+    k_conv_tc<2><<<n_chunks, kTcThreads, smem, s>>>(jobs, chunks, outs, inv, dims, planes, bank, out, err);
   }
 }
 
@@ -530,6 +586,7 @@ static geye_status ensure_bank(geye_ctx *ctx, geye_model *m, geye_conv_mode mode
 static geye_status build_tables(Plan &P, ModelPlan &mp, const std::vector<BankGroup> &groups, int NQ, int t_cap,
                                 size_t budget, TcTables &T) {
   const HostModel &h = mp.model->h;
+  const long long total_cells = (long long)(P.arena16.bytes / 16);
   const int NoC = h.numcomponent, NoP = h.NoP, interval = h.interval;
   for (int level = interval; level < mp.LEN; level++) {
     if (mp.skipped[level]) continue;
@@ -541,7 +598,8 @@ static geye_status build_tables(Plan &P, ModelPlan &mp, const std::vector<BankGr
       for (int v : map_off)
         if (v < 0) { set_error("tensor-core conv: filter map missing from the plan"); return GEYE_ERR_UNSUPPORTED; }
       const LevelInfo &L = root ? P.lv[level] : P.lv[Lv];
-      if (!add_tc_job(T, NQ, L.feat16_off, L.fs0, L.fs1, g, map_off, t_cap, budget)) {
+      const long long avail = total_cells - (long long)L.feat16_off * 2 / 16;
+      if (!add_tc_job(T, NQ, L.feat16_off, L.fs0, L.fs1, g, map_off, avail, t_cap, budget)) {
         set_error("tensor-core conv: a filter bank and its feature reach exceed shared memory");
         return GEYE_ERR_UNSUPPORTED;
       }
@@ -574,6 +632,11 @@ geye_status build_tc_jobs(geye_ctx *ctx, Plan &P, ModelPlan &mp) {
   GEYE_TRY(ensure_bank(ctx, m, mode, groups));
   const int NQ = tc_planes_of(mode);
   const void *bank = NQ == 2 ? m->d_bank8 : m->d_bank16;
+  mp.tc_planes = NQ;
+  if (!P.arena16.p) {   // a plan built from features has no planes: run_conv_tc reports it
+    mp.tc_chunks = 0;
+    return GEYE_OK;
+  }
   TcTables best;
   int best_shape = -1;
   float best_ms = 0.f;
@@ -611,14 +674,15 @@ geye_status build_tc_jobs(geye_ctx *ctx, Plan &P, ModelPlan &mp) {
       best_shape = si;
       break;
     }
-    DevBuf jobs, chunks, outs, inv;
+    DevBuf jobs, chunks, outs, inv, dims;
     GEYE_TRY(upload_bytes(ctx, jobs, T.jobs.data(), sizeof(TcJob) * T.jobs.size()));
     GEYE_TRY(upload_bytes(ctx, chunks, T.chunks.data(), sizeof(int4) * T.chunks.size()));
     GEYE_TRY(upload_bytes(ctx, outs, T.outs.data(), sizeof(int) * T.outs.size()));
     GEYE_TRY(upload_bytes(ctx, inv, T.inv.data(), sizeof(float) * T.inv.size()));
+    GEYE_TRY(upload_bytes(ctx, dims, T.dims.data(), sizeof(int2) * T.dims.size()));
     auto launch = [&]() {
       launch_conv_tc(NQ, jobs.as<TcJob>(), chunks.as<int4>(), (int)T.chunks.size(), outs.as<int>(), inv.as<float>(),
-                     P.arena16.as<uint8_t>(), static_cast<const uint8_t *>(bank), P.arena.as<float>(),
+                     dims.as<int2>(), P.arena16.as<uint8_t>(), static_cast<const uint8_t *>(bank), P.arena.as<float>(),
                      P.d_small.as<int>() + 130, T.max_smem, ctx->stream);
     };
     launch();
@@ -652,6 +716,7 @@ geye_status build_tc_jobs(geye_ctx *ctx, Plan &P, ModelPlan &mp) {
   GEYE_TRY(upload_bytes(ctx, mp.d_tc_chunks, best.chunks.data(), sizeof(int4) * best.chunks.size()));
   GEYE_TRY(upload_bytes(ctx, mp.d_tc_outs, best.outs.data(), sizeof(int) * best.outs.size()));
   GEYE_TRY(upload_bytes(ctx, mp.d_tc_inv, best.inv.data(), sizeof(float) * best.inv.size()));
+  GEYE_TRY(upload_bytes(ctx, mp.d_tc_dims, best.dims.data(), sizeof(int2) * best.dims.size()));
   return GEYE_OK;
 }
 
@@ -676,14 +741,14 @@ geye_status geye_conv_tuning(geye_ctx *ctx, const geye_model *m, int shape[3], f
 namespace geye {
 
 geye_status run_conv_tc(geye_ctx *ctx, Plan &P, ModelPlan &mp) {
-  if (mp.tc_chunks == 0) return GEYE_OK;
   if (!P.arena16.p) {
     set_error("tensor-core conv: the plan has no feature planes");
     return GEYE_ERR_UNSUPPORTED;
   }
+  if (mp.tc_chunks == 0) return GEYE_OK;
   const void *bank = mp.tc_planes == 2 ? mp.model->d_bank8 : mp.model->d_bank16;
   launch_conv_tc(mp.tc_planes, mp.d_tc_jobs.as<TcJob>(), mp.d_tc_chunks.as<int4>(), mp.tc_chunks,
-                 mp.d_tc_outs.as<int>(), mp.d_tc_inv.as<float>(), P.arena16.as<uint8_t>(),
+                 mp.d_tc_outs.as<int>(), mp.d_tc_inv.as<float>(), mp.d_tc_dims.as<int2>(), P.arena16.as<uint8_t>(),
                  static_cast<const uint8_t *>(bank), P.arena.as<float>(), P.d_small.as<int>() + 130, mp.tc_smem,
                  ctx->stream);
   ctx->launches++;
@@ -718,33 +783,40 @@ geye_status conv_tc_maps(geye_ctx *ctx, const float *d_feat, int a0, int a1, con
     GEYE_TRY(upload_bytes(ctx, *f, filters[i], sizeof(float) * n));
     d_filt.push_back(f->as<float>());
   }
+  // planes, then a zeroed tail that slabs of filters smaller than their group's grid may read
+  const int ncell = a0 * a1;
+  int mb0 = 1, mb1 = 1;
+  for (auto &g : groups) { mb0 = std::max(mb0, g.b0); mb1 = std::max(mb1, g.b1); }
+  const size_t tail_cells = (size_t)mb1 * a0 + mb0 + (size_t)kTcMaxTiles * kTcM;
+  const size_t plane_total = (size_t)NQ * (ncell + kTcPlanePad);
   TcTables T;
   for (auto &g : groups) {
     std::vector<int> map_off;
     for (int f : g.filt) map_off.push_back(out_off[f]);
-    if (!add_tc_job(T, NQ, 0, a0, a1, g, map_off)) {
+    if (!add_tc_job(T, NQ, 0, a0, a1, g, map_off, (long long)(plane_total + tail_cells))) {
       set_error("tensor-core conv: a filter bank and its feature reach exceed shared memory");
       return GEYE_ERR_UNSUPPORTED;
     }
   }
   DevBuf *planes = buf(), *d_bank = buf(), *d_jobs = buf(), *d_chunks = buf(), *d_outs = buf(), *d_inv = buf(),
-         *d_err = buf();
-  const int ncell = a0 * a1;
-  GEYE_TRY(planes->alloc(ctx, (size_t)NQ * (ncell + kTcPlanePad) * 16));
+         *d_dims = buf(), *d_err = buf();
+  GEYE_TRY(planes->alloc(ctx, (plane_total + tail_cells) * 16));
+  CUDA_TRY(cudaMemsetAsync(planes->as<uint8_t>() + plane_total * 16, 0, tail_cells * 16, ctx->stream));
   GEYE_TRY(d_bank->alloc(ctx, std::max<size_t>(total, 16)));
   GEYE_TRY(upload_bank(groups, mode, bank16, d_filt, scale, total, d_bank->p, ctx->stream));
   GEYE_TRY(upload_bytes(ctx, *d_jobs, T.jobs.data(), sizeof(TcJob) * T.jobs.size()));
   GEYE_TRY(upload_bytes(ctx, *d_chunks, T.chunks.data(), sizeof(int4) * T.chunks.size()));
   GEYE_TRY(upload_bytes(ctx, *d_outs, T.outs.data(), sizeof(int) * T.outs.size()));
   GEYE_TRY(upload_bytes(ctx, *d_inv, T.inv.data(), sizeof(float) * T.inv.size()));
+  GEYE_TRY(upload_bytes(ctx, *d_dims, T.dims.data(), sizeof(int2) * T.dims.size()));
   GEYE_TRY(d_err->alloc(ctx, 16));
   CUDA_TRY(cudaMemsetAsync(d_err->p, 0, 16, ctx->stream));
   const int grid = std::max(1, std::min((ncell + kTcPlanePad + 255) / 256, 1024));
   if (NQ == 4) k_feat_planes<4><<<grid, 256, 0, ctx->stream>>>(d_feat, ncell, planes->as<uint8_t>());
   else k_feat_planes<2><<<grid, 256, 0, ctx->stream>>>(d_feat, ncell, planes->as<uint8_t>());
   launch_conv_tc(NQ, d_jobs->as<TcJob>(), d_chunks->as<int4>(), (int)T.chunks.size(), d_outs->as<int>(),
-                 d_inv->as<float>(), planes->as<uint8_t>(), d_bank->as<uint8_t>(), d_out, d_err->as<int>(),
-                 T.max_smem, ctx->stream);
+                 d_inv->as<float>(), d_dims->as<int2>(), planes->as<uint8_t>(), d_bank->as<uint8_t>(), d_out,
+                 d_err->as<int>(), T.max_smem, ctx->stream);
   CUDA_TRY(cudaGetLastError());
   int errw = 0;
   CUDA_TRY(cudaMemcpyAsync(&errw, d_err->p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));

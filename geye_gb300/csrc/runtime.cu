@@ -576,6 +576,16 @@ static geye_status finish_plan(geye_ctx *ctx, Plan &P, ArenaAlloc &A) {
   P.arena_words = A.words + 64;
   GEYE_TRY(P.arena.alloc(ctx, P.arena_words * 4));
   if (P.arena16_elems) {
+    // after the last plane, a tail that slabs of filters smaller than their group's
+    // tap grid may read (the widest filter's columns of the largest level)
+    int fb0 = 1, fb1 = 1, fs0 = 1;
+    for (auto &mp : P.models) {
+      const HostModel &h = mp->model->h;
+      for (int r = 0; r < h.NoR; r++) { fb0 = std::max(fb0, h.root_size[3 * r]); fb1 = std::max(fb1, h.root_size[3 * r + 1]); }
+      for (int q = 0; q < h.NoP; q++) { fb0 = std::max(fb0, h.part_size[3 * q]); fb1 = std::max(fb1, h.part_size[3 * q + 1]); }
+    }
+    for (auto &L : P.lv) fs0 = std::max(fs0, L.fs0);
+    P.arena16_elems += ((size_t)fb1 * fs0 + fb0 + 16 * 128) * 8;
     GEYE_TRY(P.arena16.alloc(ctx, P.arena16_elems * 2));
     // plane tails are read (and their outputs discarded) but never written: keep them zero
     CUDA_TRY(cudaMemsetAsync(P.arena16.p, 0, P.arena16_elems * 2, ctx->stream));

@@ -91,7 +91,7 @@ struct ModelPlan {
   double conv_flops = 0, conv_bytes = 0, dt_bytes = 0, score_bytes = 0;
   // tensor-core convolution (conv_tc.cu): jobs, CTA chunks, map offsets and
   // per-map factors undoing the operand scaling; planes per position (4 bf16, 2 e4m3)
-  DevBuf d_tc_jobs, d_tc_chunks, d_tc_outs, d_tc_inv;
+  DevBuf d_tc_jobs, d_tc_chunks, d_tc_outs, d_tc_inv, d_tc_dims;
   // A_SCORE lookups: [job][image column] score-map column base, [job][image row] score row
   DevBuf d_as_col, d_as_row;
   int tc_chunks = 0, tc_planes = 0;
