@@ -3,7 +3,8 @@
 // order for equal scores (partition argument in nms_common.h).
 //
 //   k_qs_load: keys, the identity order and the first segment of each model.
-//   Levels, kLevels launches of three kernels (no-ops once nothing is left):
+//   Levels (twice the balanced depth to kNmsSegS, plus two: sort_levels), three
+//   kernels each (no-ops once nothing is left):
 //     k_qs_count   every segment above kNmsSegS is cut into tiles of kNmsTile
 //                  elements; a block counts its tile's values <= key and >= key;
 //     k_qs_scatter with the counts of the tiles before it, a block writes its
@@ -25,7 +26,6 @@
 
 namespace geye {
 
-constexpr int kLevels = 10;      // grid-wide partition levels launched per frame
 constexpr int kT = kNmsTile;     // elements per tile (4 per thread)
 constexpr int kWarpSeg = 1024;   // shared-memory kernel: block partitions above this
 constexpr int kWL = 256;         // its queue of warp segments
@@ -486,14 +486,24 @@ __global__ void __launch_bounds__(kNmsNT) k_qs_rest(int levels, int cap, int *si
   }
 }
 
+// grid-wide levels launched for a plan of cap boxes per model: quicksort splits are
+// uneven (ties, runs), so twice the balanced depth to kNmsSegS, plus two;
+// anything still above kNmsSegS afterwards is finished by k_qs_rest
+static int sort_levels(int cap) {
+  int depth = 0;
+  while (((long long)kNmsSegS << depth) < cap) depth++;
+  return std::max(4, std::min(24, 2 * depth + 2));
+}
+
 void launch_nms_sort(const float *boxes, const int *d_num, int n_models, int GL, int cap, int *si, float *sf,
                      int *err, long long *diag, cudaStream_t s) {
+  const int levels = sort_levels(cap);
   k_qs_load<<<dim3((cap + 255) / 256, n_models), 256, 0, s>>>(boxes, d_num, GL, cap, si, sf);
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   const int tiles = std::max(1, std::min(nms_tile_cap(cap), std::max(1, 2 * sms / std::max(1, n_models))));
-  for (int l = 0; l < kLevels; l++) {
+  for (int l = 0; l < levels; l++) {
     k_qs_count<<<dim3(tiles, n_models), kNmsNT, 0, s>>>(l, cap, si, sf);
     k_qs_scatter<<<dim3(tiles, n_models), kNmsNT, 0, s>>>(l, cap, si, sf);
     k_qs_swap<<<dim3(tiles, n_models), kNmsNT, 0, s>>>(l, cap, si, sf, err);
@@ -504,7 +514,7 @@ void launch_nms_sort(const float *boxes, const int *d_num, int n_models, int GL,
     attr = true;
   }
   k_qs_small<<<std::max(1, sms), kNmsNT, sizeof(SmallSmem), s>>>(n_models, cap, si, sf, err);
-  k_qs_rest<<<n_models, kNmsNT, 0, s>>>(kLevels, cap, si, sf, err, diag);
+  k_qs_rest<<<n_models, kNmsNT, 0, s>>>(levels, cap, si, sf, err, diag);
 }
 
 }  // namespace geye
