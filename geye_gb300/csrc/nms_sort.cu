@@ -3,7 +3,7 @@
 // order for equal scores (partition argument in nms_common.h).
 //
 //   k_qs_load: keys, the identity order and the first segment of each model.
-//   Levels (twice the balanced depth to kNmsSegS, plus two: sort_levels), three
+//   Levels (three times the balanced depth to kNmsSegS, plus three: sort_levels), three
 //   kernels each (no-ops once nothing is left):
 //     k_qs_count   every segment above kNmsSegS is cut into tiles of kNmsTile
 //                  elements; a block counts its tile's values <= key and >= key;
@@ -487,12 +487,13 @@ __global__ void __launch_bounds__(kNmsNT) k_qs_rest(int levels, int cap, int *si
 }
 
 // grid-wide levels launched for a plan of cap boxes per model: quicksort splits are
-// uneven (ties, runs), so twice the balanced depth to kNmsSegS, plus two;
-// anything still above kNmsSegS afterwards is finished by k_qs_rest
+// uneven (ties, runs), so three times the balanced depth to kNmsSegS, plus three
+// (a level with nothing left costs three empty launches; a segment still above
+// kNmsSegS afterwards costs k_qs_rest's single block per model far more)
 static int sort_levels(int cap) {
   int depth = 0;
   while (((long long)kNmsSegS << depth) < cap) depth++;
-  return std::max(4, std::min(24, 2 * depth + 2));
+  return std::max(4, std::min(30, 3 * depth + 3));
 }
 
 void launch_nms_sort(const float *boxes, const int *d_num, int n_models, int GL, int cap, int *si, float *sf,
