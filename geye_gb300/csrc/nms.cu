@@ -176,8 +176,10 @@ __device__ __forceinline__ bool nms_suppress(float Ay1, float Ax1, float Ay2, fl
   const float xx1 = Ax1 >= Bx1 ? Ax1 : Bx1;
   const float yy2 = Ay2 <= By2 ? Ay2 : By2;
   const float xx2 = Ax2 <= Bx2 ? Ax2 : Bx2;
-  const float w = xx2 - xx1 + 1.0;
-  const float h = yy2 - yy1 + 1.0;
+  // the reference adds the double 1.0 and stores a float: the float addition
+  // rounds the same exact sum once
+  const float w = xx2 - xx1 + 1.0f;
+  const float h = yy2 - yy1 + 1.0f;
   const float R_AREA = areaA <= areaB ? areaA : areaB;
   if (w > 0 && h > 0) {
     const float o = w * h / R_AREA;

@@ -248,8 +248,10 @@ __device__ __forceinline__ bool supp(float Ay1, float Ax1, float Ay2, float Ax2,
   const float xx1 = Ax1 >= Bx1 ? Ax1 : Bx1;
   const float yy2 = Ay2 <= By2 ? Ay2 : By2;
   const float xx2 = Ax2 <= Bx2 ? Ax2 : Bx2;
-  const float w = xx2 - xx1 + 1.0;
-  const float h = yy2 - yy1 + 1.0;
+  // nms.cpp adds the double 1.0 and stores a float: one rounding of the exact
+  // sum, which is what the float addition gives (no FP64 in the inner loop)
+  const float w = xx2 - xx1 + 1.0f;
+  const float h = yy2 - yy1 + 1.0f;
   const float R_AREA = aA <= aB ? aA : aB;
   if (w > 0 && h > 0) return w * h / R_AREA > overlap;
   if (Ay1 < By1 && Ax1 < Bx1 && Ay2 > By2 && Ax2 > Bx2) return true;

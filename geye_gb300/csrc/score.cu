@@ -251,7 +251,10 @@ __global__ void __launch_bounds__(kAsTile *kAsTile) k_ascore(const int *__restri
 __global__ void k_ascore_norm(float *__restrict__ a_score, int n, const unsigned *__restrict__ max_bits) {
   const float max_ac = __uint_as_float(*max_bits);
   if (!(max_ac > 0.0f)) return;
-  const float ac_ratio = 1.0 / max_ac;
+  // the reference's double reciprocal, once per warp (the FP64 pipe is narrow)
+  float ac_ratio = 0.f;
+  if ((threadIdx.x & 31) == 0) ac_ratio = 1.0 / max_ac;
+  ac_ratio = __shfl_sync(0xffffffffu, ac_ratio, 0);
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) a_score[i] *= ac_ratio;
 }
 
