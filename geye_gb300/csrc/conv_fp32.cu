@@ -8,25 +8,29 @@
 // and the output is 0 + add_val.  With -fmad=false this kernel repeats that
 // order exactly, so its maps are bit-identical to the oracle's.
 //
-// Tiling: a block computes a 32 (y) x 16 (x) output tile for G filters of the
-// same size.  Features arrive 8 channels at a time ([pos][32] layout, one
+// Tiling: a block computes an (8*CR) (y) x 16 (x) output tile for G filters of
+// the same size.  Features arrive 8 channels at a time ([pos][32] layout, one
 // 32-byte sector per cell) into shared memory; filter slices of the same 8
 // channels sit beside them and are read as warp-wide broadcasts.  Each thread
-// owns 4 consecutive y outputs x G filters.
+// owns CR consecutive y outputs x G filters.  Neither CR nor G changes any
+// output's summation order, so every shape gives the same bits; the shape per
+// plan (CR = 4 or 8, groups of up to 8 or 4 filters) is chosen by timing
+// (tune_conv_fp32).
 #include "internal.h"
 
 namespace geye {
 
-constexpr int kCTY = 32, kCTX = 16, kCR = 4;             // tile and outputs per thread along y
-constexpr int kCThreads = (kCTY / kCR) * kCTX;          // 128
+constexpr int kCTX = 16, kCYT = 8;                       // tile columns; threads along y
+constexpr int kCThreads = kCYT * kCTX;                   // 128
 constexpr int kChunk = 8;                               // channels per shared-memory stage
 
-template <int G>
+template <int G, int kCR>
 __global__ void __launch_bounds__(kCThreads) k_conv_fp32(const ConvJob *__restrict__ jobs,
                                                          const float *__restrict__ filters,
                                                          const int *__restrict__ filt_off,
                                                          const float *__restrict__ arena_in,
                                                          float *__restrict__ arena_out) {
+  constexpr int kCTY = kCYT * kCR;                       // tile rows
   extern __shared__ float sm[];
   const ConvJob J = jobs[blockIdx.y];
   const int tiles = J.tiles_y * J.tiles_x;
@@ -41,8 +45,8 @@ __global__ void __launch_bounds__(kCThreads) k_conv_fp32(const ConvJob *__restri
   const int BSQ = b0 * b1;
   const float *feat = arena_in + J.feat_off;
 
-  const int ty = threadIdx.x % (kCTY / kCR);             // 0..7
-  const int tx = threadIdx.x / (kCTY / kCR);             // 0..15
+  const int ty = threadIdx.x % kCYT;                     // 0..7
+  const int tx = threadIdx.x / kCYT;                     // 0..15
   float add[G][kCR];
 #pragma unroll
   for (int g = 0; g < G; g++)
@@ -118,36 +122,45 @@ __global__ void __launch_bounds__(kCThreads) k_conv_fp32(const ConvJob *__restri
   }
 }
 
-static size_t conv_smem(int b0, int b1, int G) {
-  const int RH = kCTY + b0 - 1, RW = kCTX + b1 - 1;
+static size_t conv_smem(int b0, int b1, int G, int CR) {
+  const int RH = kCYT * CR + b0 - 1, RW = kCTX + b1 - 1;
   return sizeof(float) * ((size_t)kChunk * RW * (RH | 1) + (size_t)G * kChunk * b0 * b1);
 }
 
-void launch_conv_fp32(const ConvJob *d_jobs, int n_jobs, int max_tiles_y, int max_tiles_x, const float *filters,
-                      const int *filt_off, const float *arena_in, float *arena_out, int max_b0, int max_b1,
-                      int max_group, cudaStream_t s) {
-  if (n_jobs <= 0) return;
-  dim3 grid(max_tiles_y * max_tiles_x, n_jobs);
-  int G = max_group <= 1 ? 1 : max_group <= 2 ? 2 : max_group <= 4 ? 4 : 8;
-  size_t smem = conv_smem(max_b0, max_b1, G);
+template <int CR>
+static void launch_cr(const ConvJob *d_jobs, int n_jobs, dim3 grid, const float *filters, const int *filt_off,
+                      const float *arena_in, float *arena_out, int max_b0, int max_b1, int G, cudaStream_t s) {
+  const size_t smem = conv_smem(max_b0, max_b1, G, CR);
   switch (G) {
     case 1:
-      cudaFuncSetAttribute(k_conv_fp32<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      k_conv_fp32<1><<<grid, kCThreads, smem, s>>>(d_jobs, filters, filt_off, arena_in, arena_out);
+      cudaFuncSetAttribute(k_conv_fp32<1, CR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      k_conv_fp32<1, CR><<<grid, kCThreads, smem, s>>>(d_jobs, filters, filt_off, arena_in, arena_out);
       break;
     case 2:
-      cudaFuncSetAttribute(k_conv_fp32<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      k_conv_fp32<2><<<grid, kCThreads, smem, s>>>(d_jobs, filters, filt_off, arena_in, arena_out);
+      cudaFuncSetAttribute(k_conv_fp32<2, CR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      k_conv_fp32<2, CR><<<grid, kCThreads, smem, s>>>(d_jobs, filters, filt_off, arena_in, arena_out);
       break;
     case 4:
-      cudaFuncSetAttribute(k_conv_fp32<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      k_conv_fp32<4><<<grid, kCThreads, smem, s>>>(d_jobs, filters, filt_off, arena_in, arena_out);
+      cudaFuncSetAttribute(k_conv_fp32<4, CR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      k_conv_fp32<4, CR><<<grid, kCThreads, smem, s>>>(d_jobs, filters, filt_off, arena_in, arena_out);
       break;
     default:
-      cudaFuncSetAttribute(k_conv_fp32<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      k_conv_fp32<8><<<grid, kCThreads, smem, s>>>(d_jobs, filters, filt_off, arena_in, arena_out);
+      cudaFuncSetAttribute(k_conv_fp32<8, CR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      k_conv_fp32<8, CR><<<grid, kCThreads, smem, s>>>(d_jobs, filters, filt_off, arena_in, arena_out);
       break;
   }
+}
+
+// rows per thread: 4 (tiles of 32 rows) or 8 (64 rows); jobs' tiles_y must be
+// ceil(c0 / (8 * cr))
+void launch_conv_fp32(const ConvJob *d_jobs, int n_jobs, int max_tiles_y, int max_tiles_x, const float *filters,
+                      const int *filt_off, const float *arena_in, float *arena_out, int max_b0, int max_b1,
+                      int max_group, cudaStream_t s, int cr) {
+  if (n_jobs <= 0) return;
+  dim3 grid(max_tiles_y * max_tiles_x, n_jobs);
+  const int G = max_group <= 1 ? 1 : max_group <= 2 ? 2 : max_group <= 4 ? 4 : 8;
+  if (cr == 8) launch_cr<8>(d_jobs, n_jobs, grid, filters, filt_off, arena_in, arena_out, max_b0, max_b1, G, s);
+  else launch_cr<4>(d_jobs, n_jobs, grid, filters, filt_off, arena_in, arena_out, max_b0, max_b1, G, s);
 }
 
 }  // namespace geye

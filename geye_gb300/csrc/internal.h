@@ -173,7 +173,7 @@ void launch_to_ref_layout(const float *feat, int fs0, int fs1, float *out, cudaS
 void launch_from_ref_layout(const float *ref, int fs0, int fs1, float *feat, cudaStream_t s);
 void launch_conv_fp32(const ConvJob *d_jobs, int n_jobs, int max_tiles_y, int max_tiles_x, const float *filters,
                       const int *filt_off, const float *arena_in, float *arena_out, int max_b0, int max_b1,
-                      int max_group, cudaStream_t s);
+                      int max_group, cudaStream_t s, int cr = 4);
 void launch_dt(const DtJob *d_jobs, int n_jobs, int max_d0, int max_d1, float *arena, int *arena_i,
                int *fallback_count, cudaStream_t s);
 void launch_score(const ScoreJob *d_jobs, int n_jobs, int max_r, float thresh, float *arena, int *block_counts,

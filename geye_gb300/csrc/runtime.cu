@@ -572,6 +572,106 @@ static geye_status build_pyramid_plan(geye_ctx *ctx, Plan &P, int width, int hei
   return GEYE_OK;
 }
 
+// FP32 conv shape tuner: job tables for rows per thread cr (4 or 8) and groups
+// of at most gmax filters, split from the plan's groups (maps of a group are
+// contiguous, so a split group writes the same places); each candidate is timed
+// on the plan's arena (CUDA events after one untimed launch), the fastest kept.
+// Every shape gives the same bits.
+static void conv_jobs_for(const std::vector<ConvJob> &in, int cr, int gmax, std::vector<ConvJob> &out, int &mty,
+                          int &mtx, int &mg) {
+  out.clear();
+  mty = mtx = 0;
+  mg = 1;
+  for (const ConvJob &J : in)
+    for (int k = 0; k < J.n_filt; k += gmax) {
+      ConvJob C = J;
+      C.filt_base = J.filt_base + k;
+      C.n_filt = std::min(gmax, J.n_filt - k);
+      C.out_off = J.out_off + k * J.c0 * J.c1;
+      C.tiles_y = (J.c0 + 8 * cr - 1) / (8 * cr);
+      C.tiles_x = (J.c1 + 15) / 16;
+      mty = std::max(mty, C.tiles_y);
+      mtx = std::max(mtx, C.tiles_x);
+      mg = std::max(mg, C.n_filt);
+      out.push_back(C);
+    }
+}
+
+static geye_status tune_conv_fp32(geye_ctx *ctx, Plan &P, ModelPlan &mp) {
+  geye_model *m = mp.model;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  CUDA_TRY(cudaEventCreate(&e0));
+  CUDA_TRY(cudaEventCreate(&e1));
+  geye_status st = GEYE_OK;
+  for (int kind = 0; kind < 2 && st == GEYE_OK; kind++) {
+    std::vector<ConvJob> &jobs = kind ? mp.part_jobs : mp.root_jobs;
+    if (jobs.empty()) continue;
+    const int b0 = kind ? mp.part_max_b0 : mp.root_max_b0, b1 = kind ? mp.part_max_b1 : mp.root_max_b1;
+    float best = 0.f;
+    std::vector<ConvJob> best_jobs;
+    int best_cr = 4, bty = 0, btx = 0, bg = 1, best_i = 0;
+    // a geometry this model was tuned at before reuses the choice without timing
+    const std::string key = std::string(kind ? "fp32p:" : "fp32r:") + std::to_string(P.width) + "x" +
+                            std::to_string(P.height) + "/" + std::to_string(mp.LEN);
+    int only = -1;
+    {
+      std::lock_guard<std::mutex> lk(m->tc_mu);
+      auto it = m->tc_tuned.find(key);
+      if (it != m->tc_tuned.end()) only = it->second.first;
+    }
+    for (int ci = 0; ci < 4; ci++) {
+      if (only >= 0 && ci != only) continue;
+      const int cr = ci < 2 ? 4 : 8, gmax = ci % 2 ? 4 : 8;
+      {
+        std::vector<ConvJob> cand;
+        int mty, mtx, mg;
+        conv_jobs_for(jobs, cr, gmax, cand, mty, mtx, mg);
+        DevBuf d;
+        st = upload(ctx, d, cand);
+        if (st != GEYE_OK) break;
+        auto launch = [&]() {
+          launch_conv_fp32(d.as<ConvJob>(), (int)cand.size(), mty, mtx, m->d_filters, m->d_filt_off,
+                           P.arena.as<float>(), P.arena.as<float>(), b0, b1, mg, ctx->stream, cr);
+        };
+        launch();
+        if (cudaEventRecord(e0, ctx->stream) != cudaSuccess) { st = GEYE_ERR_CUDA; break; }
+        for (int r = 0; r < 3; r++) launch();
+        float ms = 0.f;
+        cudaError_t e = cudaEventRecord(e1, ctx->stream);
+        if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+        if (e == cudaSuccess) e = cudaGetLastError();
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+        if (e != cudaSuccess) {
+          set_error(std::string("FP32 conv tuning: ") + cudaGetErrorString(e));
+          st = GEYE_ERR_CUDA;
+          break;
+        }
+        if (best_jobs.empty() || ms < best) {
+          best = ms;
+          best_jobs = cand;
+          best_cr = cr; bty = mty; btx = mtx; bg = mg; best_i = ci;
+        }
+      }
+    }
+    if (st != GEYE_OK) break;
+    if (only < 0) {
+      std::lock_guard<std::mutex> lk(m->tc_mu);
+      m->tc_tuned[key] = {best_i, best / 3.0f};
+    }
+    jobs = best_jobs;
+    if (kind) {
+      mp.part_cr = best_cr; mp.part_tiles_y = bty; mp.part_tiles_x = btx; mp.part_max_g = bg;
+      st = upload(ctx, mp.d_part_jobs, mp.part_jobs);
+    } else {
+      mp.root_cr = best_cr; mp.root_tiles_y = bty; mp.root_tiles_x = btx; mp.root_max_g = bg;
+      st = upload(ctx, mp.d_root_jobs, mp.root_jobs);
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  return st;
+}
+
 static geye_status finish_plan(geye_ctx *ctx, Plan &P, ArenaAlloc &A) {
   P.arena_words = A.words + 64;
   GEYE_TRY(P.arena.alloc(ctx, P.arena_words * 4));
@@ -672,8 +772,11 @@ static geye_status get_frame_plan(geye_ctx *ctx, geye_model *const *models, int 
   GEYE_TRY(build_pyramid_plan(ctx, *P, width, height, LEN, interval, sbin, A, tc_planes));
   for (int i = 0; i < n_models; i++) GEYE_TRY(build_model_plan(ctx, *P, models[i], LENs[i], A));
   GEYE_TRY(finish_plan(ctx, *P, A));
-  if (ctx->conv_mode != GEYE_CONV_FP32)   // after the arena exists: the tile shapes are tuned on it
+  // after the arena exists: the tile shapes are tuned on it
+  if (ctx->conv_mode != GEYE_CONV_FP32)
     for (auto &mp : P->models) GEYE_TRY(build_tc_jobs(ctx, *P, *mp));
+  else
+    for (auto &mp : P->models) GEYE_TRY(tune_conv_fp32(ctx, *P, *mp));
   GEYE_TRY(P->d_bgr.alloc(ctx, (size_t)width * height * 3 + 64));
   if (ctx->plans.size() > 32) ctx->plans.clear();
   *out = P.get();
@@ -750,13 +853,13 @@ geye_status run_conv(geye_ctx *ctx, Plan &P, ModelPlan &mp) {
   if (!mp.root_jobs.empty()) {
     launch_conv_fp32(mp.d_root_jobs.as<ConvJob>(), (int)mp.root_jobs.size(), mp.root_tiles_y, mp.root_tiles_x,
                      m->d_filters, m->d_filt_off, arena, arena, mp.root_max_b0, mp.root_max_b1, mp.root_max_g,
-                     ctx->stream);
+                     ctx->stream, mp.root_cr);
     GEYE_TRY(check_launch(ctx, "root conv"));
   }
   if (!mp.part_jobs.empty()) {
     launch_conv_fp32(mp.d_part_jobs.as<ConvJob>(), (int)mp.part_jobs.size(), mp.part_tiles_y, mp.part_tiles_x,
                      m->d_filters, m->d_filt_off, arena, arena, mp.part_max_b0, mp.part_max_b1, mp.part_max_g,
-                     ctx->stream);
+                     ctx->stream, mp.part_cr);
     GEYE_TRY(check_launch(ctx, "part conv"));
   }
   return GEYE_OK;

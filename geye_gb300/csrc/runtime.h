@@ -77,6 +77,7 @@ struct ModelPlan {
   std::vector<ConvJob> root_jobs, part_jobs;
   int root_max_b0 = 0, root_max_b1 = 0, root_max_g = 1, root_tiles_y = 0, root_tiles_x = 0;
   int part_max_b0 = 0, part_max_b1 = 0, part_max_g = 1, part_tiles_y = 0, part_tiles_x = 0;
+  int root_cr = 4, part_cr = 4;   // FP32 conv rows per thread (tuned per plan)
   std::vector<DtJob> dt_jobs;
   int dt_max_d0 = 0, dt_max_d1 = 0;
   std::vector<ScoreJob> score_jobs;
