@@ -9,9 +9,12 @@
 // GPU form.  Let g(d) be the leftmost global argmin of f_d over the whole
 // line.  If g is non-decreasing in d, the recursion returns g(d) for every d
 // (each node's range [s1, s2] then contains g(d), and no smaller index in it
-// reaches the minimum).  So every output of a line is computed in parallel,
-// g is checked to be non-decreasing, and only if it is not does one thread
-// replay the recursion exactly (counted in *fallback_count).
+// reaches the minimum).  So every output of a line is computed in parallel.
+// Where dt_monotone proves from the line's value range and (a, b) that the
+// computed g cannot decrease (the usual case: a >= 8 times the rounding bound),
+// nothing else is needed, and pass 2 computes only the entries it stores;
+// otherwise g is checked to be non-decreasing, and only if it is not does one
+// thread replay the recursion exactly (counted in *fallback_count).
 //
 // A block takes a tile of L consecutive lines (about kDtElems outputs) into
 // shared memory, each line padded with +inf, and spreads the tile's outputs
@@ -95,7 +98,7 @@ __host__ __device__ __forceinline__ int dt_lg_lines2(int n) {
 }
 __host__ __device__ __forceinline__ size_t dt_smem_bytes(int L, int n) {
   return sizeof(float) * ((size_t)kDtPad + (size_t)L * (n + kDtPad) + 2 * (size_t)L * n + 2 * (2 * kDtPad - 1)) +
-         sizeof(int) * 2 * (size_t)L;
+         sizeof(int) * (2 * (size_t)L + 1);
 }
 
 // Leftmost minimum of output d over the window |t| < KM of a padded line,
@@ -116,51 +119,78 @@ __device__ __forceinline__ int dt_scan_fixed(const float *__restrict__ line, int
   return s < 0 ? -1 : d - (KM - 1) + s;
 }
 
-// Every output of the tile, spread over all threads (e -> line e / n, output
-// e % n, the division by a precomputed reciprocal), each with its own line's
-// window: K rounded up to an unrolled size, a loop beyond 16, a bounds-checked
-// loop past the padding.
+// Leftmost minimum of output d over its line's window (K rounded up to an
+// unrolled size, a loop beyond 16, a bounds-checked loop past the padding).
+__device__ __forceinline__ int dt_full(const float *__restrict__ line, int d, int K, int n, float a, float b,
+                                       const float *__restrict__ At, const float *__restrict__ Bt, float &best) {
+  int p;
+  if (K <= 3) p = dt_scan_fixed<3>(line, d, At, Bt, best);
+  else if (K <= 4) p = dt_scan_fixed<4>(line, d, At, Bt, best);
+  else if (K <= 5) p = dt_scan_fixed<5>(line, d, At, Bt, best);
+  else if (K <= 6) p = dt_scan_fixed<6>(line, d, At, Bt, best);
+  else if (K <= 8) p = dt_scan_fixed<8>(line, d, At, Bt, best);
+  else if (K <= 12) p = dt_scan_fixed<12>(line, d, At, Bt, best);
+  else if (K <= 16) p = dt_scan_fixed<16>(line, d, At, Bt, best);
+  else if (K <= kDtPad) {
+    best = INFINITY;
+    p = -1;
+    for (int t = K - 1; t > -K; t--) {   // p = d - t ascending
+      const float f = (line[d - t] + At[t]) + Bt[t];
+      if (f < best) { best = f; p = d - t; }
+    }
+  } else {
+    const int lo = max(0, d - K + 1), hi = min(n - 1, d + K - 1);
+    p = lo;
+    best = dt_f(line[lo], a, b, d - lo);
+    for (int q = lo + 1; q <= hi; q++) {
+      const float fq = dt_f(line[q], a, b, d - q);
+      if (best > fq) { best = fq; p = q; }
+    }
+  }
+  if (p < 0) {   // every candidate was NaN: the reference keeps the window's first index
+    p = max(0, d - K + 1);
+    best = dt_f(line[p], a, b, d - p);
+  }
+  return p;
+}
+
+// Outputs d = c + q*i of every line of the tile, spread over all threads
+// (e -> line e / m, slot e % m, the division by a precomputed reciprocal), each
+// with its own line's window.  q = 1: every output (c = 0); q = 2: the parity
+// class c of line l that pass 2 writes (par_x on rows of parity par_y, the
+// other class on the other rows).
 __device__ __forceinline__ void dt_scan_tile(const float *__restrict__ v_s, int stride, int n, int nl, float a,
                                              float b, const int *__restrict__ K_s, const float *__restrict__ At,
                                              const float *__restrict__ Bt, float *__restrict__ o_s,
-                                             int *__restrict__ g_s, unsigned magic) {
-  const int cnt = nl * n;
-  for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
-    const int l = __umulhi((unsigned)e, magic), d = e - l * n;
-    const float *line = v_s + l * stride;
-    const int K = K_s[l];
+                                             int *__restrict__ g_s, int q, int y0, int par_y, int par_x) {
+  const int m = (n + q - 1) / q;
+  const unsigned mg = 0xFFFFFFFFu / (unsigned)m + 1u;   // e / m for e < 2^32 / m
+  for (int e = threadIdx.x; e < nl * m; e += blockDim.x) {
+    const int l = __umulhi((unsigned)e, mg), i = e - l * m;
+    const int c = q == 1 ? 0 : (((y0 + l) & 1) == par_y ? par_x : 1 - par_x);
+    const int d = c + q * i;
+    if (d >= n) continue;
     float best;
-    int p;
-    if (K <= 3) p = dt_scan_fixed<3>(line, d, At, Bt, best);
-    else if (K <= 4) p = dt_scan_fixed<4>(line, d, At, Bt, best);
-    else if (K <= 5) p = dt_scan_fixed<5>(line, d, At, Bt, best);
-    else if (K <= 6) p = dt_scan_fixed<6>(line, d, At, Bt, best);
-    else if (K <= 8) p = dt_scan_fixed<8>(line, d, At, Bt, best);
-    else if (K <= 12) p = dt_scan_fixed<12>(line, d, At, Bt, best);
-    else if (K <= 16) p = dt_scan_fixed<16>(line, d, At, Bt, best);
-    else if (K <= kDtPad) {
-      best = INFINITY;
-      p = -1;
-      for (int t = K - 1; t > -K; t--) {   // p = d - t ascending
-        const float f = (line[d - t] + At[t]) + Bt[t];
-        if (f < best) { best = f; p = d - t; }
-      }
-    } else {
-      const int lo = max(0, d - K + 1), hi = min(n - 1, d + K - 1);
-      p = lo;
-      best = dt_f(line[lo], a, b, d - lo);
-      for (int q = lo + 1; q <= hi; q++) {
-        const float fq = dt_f(line[q], a, b, d - q);
-        if (best > fq) { best = fq; p = q; }
-      }
-    }
-    if (p < 0) {   // every candidate was NaN: the reference keeps the window's first index
-      p = max(0, d - K + 1);
-      best = dt_f(line[p], a, b, d - p);
-    }
-    o_s[e] = best;
-    g_s[e] = p;
+    const int p = dt_full(v_s + l * stride, d, K_s[l], n, a, b, At, Bt, best);
+    o_s[l * n + d] = best;
+    g_s[l * n + d] = p;
   }
+}
+
+// True when the computed leftmost argmin g(d) of a line is certainly
+// non-decreasing in d.  For s < p, the exact terms give
+//   [f_d(s) - f_d(p)] - [f_{d-1}(s) - f_{d-1}(p)] = 2a(p - s) >= 2a,
+// and each computed f (four roundings, no FMA) is within
+// E = 4u(|v| + a t^2 + |b t|) of the exact one (u = 2^-24, |t| <= K for the
+// argmins of d and d - 1, which lie in their windows).  g(d) < g(d-1) needs
+// the computed bracket below zero, so 2a > 4E; a >= 8E rules it out with a
+// factor 4 to spare (the 1e-37 covers subnormal roundings).  NaN or infinite
+// values, a <= 0 and windows past the padding fail the test.
+__device__ __forceinline__ bool dt_monotone(float vabs, float a, float b, int K) {
+  if (!(a > 0.f) || K > kDtPad - 2 || !(vabs <= 3.0e38f)) return false;
+  const float T = (float)(K + 1);
+  const float E = 4.0f * 5.9604644775390625e-08f * (vabs + a * T * T + fabsf(b) * T) + 1e-37f;
+  return a >= 8.0f * E;
 }
 
 // PASS 1: along y (dim 0) of each column x of the negated part map -> tmpM, tmpI.
@@ -187,6 +217,7 @@ __global__ void __launch_bounds__(kDtThreads) k_dt(const DtJob *__restrict__ job
   float *Bt = At + (2 * kDtPad - 1);
   int *K_s = reinterpret_cast<int *>(Bt + kDtPad);
   int *bad_s = K_s + L;
+  int *mono_s = bad_s + L;   // every line's argmin certainly non-decreasing
   const float a = PASS == 1 ? J.ay : J.ax, b = PASS == 1 ? J.by : J.bx;
   const int tid = threadIdx.x, nth = blockDim.x;
   const int cnt = nl * n;
@@ -210,6 +241,7 @@ __global__ void __launch_bounds__(kDtThreads) k_dt(const DtJob *__restrict__ job
     const int l = i / kDtPad, k = i - l * kDtPad;
     v_s[l * stride - kDtPad + k] = INFINITY;   // pad before line l (l = nl: after the last line)
   }
+  if (tid == 0) *mono_s = 1;
   for (int t = tid - (kDtPad - 1); t < kDtPad; t += nth) {
     const float ft = (float)t;
     At[t] = a * ft * ft;
@@ -222,11 +254,13 @@ __global__ void __launch_bounds__(kDtThreads) k_dt(const DtJob *__restrict__ job
   for (int l = warp; l < nl; l += nth >> 5) {
     const float *v = v_s + l * stride;
     float vmin = INFINITY, vmax = -INFINITY, vabs = 0.f;
+    bool nan = false;   // fminf/fmaxf skip NaN
     for (int i = lane; i < n; i += 32) {
       const float x = v[i];
       vmin = fminf(vmin, x);
       vmax = fmaxf(vmax, x);
       vabs = fmaxf(vabs, fabsf(x));
+      nan |= x != x;
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
@@ -234,28 +268,39 @@ __global__ void __launch_bounds__(kDtThreads) k_dt(const DtJob *__restrict__ job
       vmax = fmaxf(vmax, __shfl_xor_sync(0xffffffffu, vmax, o));
       vabs = fmaxf(vabs, __shfl_xor_sync(0xffffffffu, vabs, o));
     }
+    nan = __any_sync(0xffffffffu, nan);
     if (lane == 0) {
       const int K = dt_window(vmin, vmax, vabs, a, b, n);
       K_s[l] = K;
       bad_s[l] = 0;
+      if (nan || !dt_monotone(vabs, a, b, K)) *mono_s = 0;
     }
   }
   __syncthreads();
 
-  // leftmost minimum of every output's window
-  dt_scan_tile(v_s, stride, n, nl, a, b, K_s, At, Bt, o_s, g_s, magic);
-  __syncthreads();
-  for (int e = tid; e < cnt; e += nth) {
-    const int l = __umulhi((unsigned)e, magic), d = e - l * n;
-    if (d + 1 < n && g_s[e] > g_s[e + 1]) bad_s[l] = 1;
-  }
-  __syncthreads();
-  for (int l = tid; l < nl; l += nth)
-    if (bad_s[l]) {
-      dt_replay(v_s + l * stride, n, a, b, o_s + (size_t)l * n, g_s + (size_t)l * n);
-      atomicAdd(fallback_count, 1);
+  // pass 2 computes only the entries it writes when both the score sum's and
+  // the part boxes' reads are sampled: one parity class of x per row
+  const int q = (PASS == 2 && J.samp_m && J.samp_i) ? 2 : 1;
+  if (*mono_s) {
+    // the order holds: no check, no replay
+    dt_scan_tile(v_s, stride, n, nl, a, b, K_s, At, Bt, o_s, g_s, q, line0, J.par_y, J.par_x);
+    __syncthreads();   // every output of the tile written before the stores read them
+  } else {
+    // every output's window, then the order check and the exact replay
+    dt_scan_tile(v_s, stride, n, nl, a, b, K_s, At, Bt, o_s, g_s, 1, 0, 0, 0);
+    __syncthreads();
+    for (int e = tid; e < cnt; e += nth) {
+      const int l = __umulhi((unsigned)e, magic), d = e - l * n;
+      if (d + 1 < n && g_s[e] > g_s[e + 1]) bad_s[l] = 1;
     }
-  __syncthreads();
+    __syncthreads();
+    for (int l = tid; l < nl; l += nth)
+      if (bad_s[l]) {
+        dt_replay(v_s + l * stride, n, a, b, o_s + (size_t)l * n, g_s + (size_t)l * n);
+        atomicAdd(fallback_count, 1);
+      }
+    __syncthreads();
+  }
 
   if (PASS == 1) {
     float *tm = arena + J.tmpM_off + (size_t)line0 * n;

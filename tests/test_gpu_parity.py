@@ -212,6 +212,31 @@ def test_pipeline_trained_like_models(ctx, tmp_path):
         assert np.array_equal(bits(got["score"]), bits(ref["score"]))
 
 
+def test_pipeline_flat_deformation(ctx, tmp_path):
+    """Deformation weights near zero and of either sign: the DT windows span
+    whole lines and the argmin order cannot be proven from the value range, so
+    the pipeline takes the checked path (order check, exact replay) with its
+    sampled stores."""
+    import dataclasses
+    import geye_gb300 as g
+    spec = dataclasses.replace(synth.CAR_TRAINED_LIKE, name="car_flat", seed=21,
+                               def_ranges=((-1e-6, 1e-6), (-0.01, 0.01), (-1e-6, 1e-6), (-0.01, 0.01)))
+    fr = synth.make_frame(320, 240, seed=4)
+    paths = synth.write_model_csv(spec, str(tmp_path))
+    om = O.Model(*paths)
+    s = _all_scores(om, fr)
+    thresh = float(s[min(100, len(s) - 1)])
+    om.m.ini = 1
+    ref = O.car_detection(om, fr, thresh, 0.5)
+    gm = g.Model(ctx, *paths)
+    got = ctx.car_detection(fr, gm, thresh, None, 0.5)
+    gm.close()
+    assert got["num"] == ref["K"] > 0
+    assert np.array_equal(got["point"], ref["point"])
+    assert np.array_equal(got["or_point"], ref["or_point"])
+    assert np.array_equal(bits(got["score"]), bits(ref["score"]))
+
+
 @pytest.mark.parametrize("w,h", [(333, 251), (1920, 1080)])
 def test_pipeline_odd_and_large_frames(ctx, car, w, h):
     gm, om = car
