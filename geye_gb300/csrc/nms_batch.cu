@@ -183,7 +183,9 @@ __device__ void resolve_batch(Slots &S, float overlap, ResolveSmem &R) {
     st.npb = np;
     st.scan_word = R.last_word;
     st.batches += 1;
-    if (nb == 0) st.done = 1;
+    // done once no alive box is left: none found, or this batch took every
+    // one up to the end of the bitmap (its pass would test nothing)
+    if (nb == 0 || R.last_word >= nwords) st.done = 1;
     R.done = nb == 0;
   }
   __syncthreads();
