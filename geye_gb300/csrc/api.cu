@@ -276,6 +276,17 @@ geye_status geye_model_info(const geye_model *m, int info[8]) {
   return GEYE_OK;
 }
 
+geye_status geye_model_sym(const geye_model *m, int *rootsym, int *part_partner, int *part_sym) {
+  ARG_CHECK(m, "model is null");
+  for (int i = 0; rootsym && i < m->h.NoR; i++) rootsym[i] = 1;   // load_model.cpp:373
+  for (int i = 0; i < m->h.NoP; i++) {
+    const int p = i < (int)m->h.part_partner.size() ? m->h.part_partner[i] : 0;
+    if (part_partner) part_partner[i] = p;                         // load_model.cpp:522
+    if (part_sym) part_sym[i] = p == 0 ? 1 : 0;                    // load_model.cpp:523-524
+  }
+  return GEYE_OK;
+}
+
 geye_status geye_model_reset_scales(geye_model *m) {
   ARG_CHECK(m, "model is null");
   m->ini = true;

@@ -170,6 +170,7 @@ void launch_resize_pass(const ResizeJob *d_jobs, int n_jobs, int max_cols, int v
 void launch_hog(const HogJob *d_jobs, int n_jobs, int max_b0, int max_b1, const HogPixJob *d_pix, int n_pix,
                 int max_xe, float *arena, void *arena16, cudaStream_t s);   // arena16: base of the tensor-core planes (bytes)
 void launch_to_ref_layout(const float *feat, int fs0, int fs1, float *out, cudaStream_t s);
+void launch_flip_feat(const float *feat, int n0, int n1, float *out, cudaStream_t s);
 void launch_from_ref_layout(const float *ref, int fs0, int fs1, float *feat, cudaStream_t s);
 void launch_conv_fp32(const ConvJob *d_jobs, int n_jobs, int max_tiles_y, int max_tiles_x, const float *filters,
                       const int *filt_off, const float *arena_in, float *arena_out, int max_b0, int max_b1,

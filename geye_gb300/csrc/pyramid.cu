@@ -454,6 +454,28 @@ __global__ void k_from_ref(const float *__restrict__ ref, int ncell, float *__re
   }
 }
 
+// flip_feat (get_boxes.cpp:121-178): output channel c, column x is source
+// channel ord[c] - 1, column n1 - 1 - x (a mirror along dim 1 with the signed
+// orientations reversed); a thread per output element, rows contiguous.
+__constant__ int c_flip_ord[kFeat] = {10, 9,  8,  7,  6,  5,  4,  3,  2,  1,  18, 17, 16, 15, 14, 13,
+                                      12, 11, 19, 27, 26, 25, 24, 23, 22, 21, 20, 30, 31, 28, 29};
+
+__global__ void k_flip_feat(const float *__restrict__ feat, int n0, int n1, float *__restrict__ out) {
+  const size_t plane = (size_t)n0 * n1, total = plane * kFeat;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+    const int c = (int)(i / plane);
+    const size_t r = i - (size_t)c * plane;
+    const int x = (int)(r / n0), y = (int)(r - (size_t)x * n0);
+    out[i] = feat[(size_t)(c_flip_ord[c] - 1) * plane + (size_t)(n1 - 1 - x) * n0 + y];
+  }
+}
+
+void launch_flip_feat(const float *feat, int n0, int n1, float *out, cudaStream_t s) {
+  const size_t total = (size_t)n0 * n1 * kFeat;
+  const int blocks = (int)std::min<size_t>((total + 255) / 256, 4096);
+  k_flip_feat<<<blocks, 256, 0, s>>>(feat, n0, n1, out);
+}
+
 void launch_to_ref_layout(const float *feat, int fs0, int fs1, float *out, cudaStream_t s) {
   int n = fs0 * fs1 * kFeat;
   if (n <= 0) return;

@@ -118,6 +118,36 @@ geye_status geye_resize(geye_ctx *ctx, const float *src, const int *sdims, int *
   return GEYE_OK;
 }
 
+geye_status geye_flip_feat(geye_ctx *ctx, const float *feat, const int *size, float **out) {
+  ARG_CHECK(ctx && feat && size && out, "null argument");
+  *out = nullptr;
+  ARG_CHECK(size[2] == kFeat, "flip_feat takes 31 feature channels");   // the reference's ORD table has 31 entries
+  ARG_CHECK(size[0] >= 0 && size[1] >= 0, "negative size");
+  const size_t n = (size_t)size[0] * size[1] * kFeat;
+  CUDA_TRY(cudaSetDevice(ctx->device));
+  float *h = static_cast<float *>(calloc(n ? n : 1, sizeof(float)));
+  ARG_CHECK(h, "host allocation failed");
+  if (n == 0) { *out = h; return GEYE_OK; }
+  geye_status st = GEYE_OK;
+  {
+    Scratch S(ctx);
+    float *d_in, *d_out;
+    if ((st = S.put(feat, n, &d_in)) == GEYE_OK && (st = S.get(n, &d_out)) == GEYE_OK) {
+      launch_flip_feat(d_in, size[0], size[1], d_out, ctx->stream);
+      cudaError_t e = cudaGetLastError();
+      if (e == cudaSuccess) e = cudaMemcpyAsync(h, d_out, sizeof(float) * n, cudaMemcpyDeviceToHost, ctx->stream);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+      if (e != cudaSuccess) {
+        set_error(std::string("flip_feat: ") + cudaGetErrorString(e));
+        st = GEYE_ERR_CUDA;
+      }
+    }
+  }
+  if (st != GEYE_OK) { free(h); return st; }
+  *out = h;
+  return GEYE_OK;
+}
+
 geye_status geye_calc_feature(geye_ctx *ctx, const float *src, const int *isize, int sbin, int *ftsize, float *feat) {
   ARG_CHECK(ctx && src && isize && ftsize && feat, "null argument");
   ARG_CHECK(sbin >= 1 && sbin <= 8, "sbin must be in 1..8");

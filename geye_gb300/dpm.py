@@ -66,6 +66,8 @@ def lib(build_if_missing: bool = True):
             "geye_fconv": [vp, vp, vp, vp, vp, i32, vp],
             "geye_resize": [vp, vp, vp, vp, C.c_float, vp],
             "geye_calc_feature": [vp, vp, vp, i32, vp, vp],
+            "geye_flip_feat": [vp, vp, vp, C.POINTER(fp)],
+            "geye_model_sym": [vp, vp, vp, vp],
             "geye_free": [vp],
             "geye_detect_device": [vp, vp, i32, vp, i32, i32, C.c_float, C.c_float],
             "geye_fetch_result": [vp, i32, vp, ip],
@@ -338,6 +340,17 @@ class Context:
                "calc_feature")
         return out
 
+    def flip_feat(self, feat: np.ndarray) -> np.ndarray:
+        """flip_feat (get_boxes.cpp:121-178): feat (31, n1, n0) -> mirrored along n1, channels reordered."""
+        f = np.ascontiguousarray(feat, np.float32)
+        c, n1, n0 = f.shape
+        op = C.POINTER(C.c_float)()
+        _check(lib().geye_flip_feat(self.h, _p(f), _p(np.array([n0, n1, c], np.int32)), C.byref(op)), "flip_feat")
+        n = c * n1 * n0
+        out = np.ctypeslib.as_array(op, shape=(max(n, 1),))[:n].reshape(c, n1, n0).copy()
+        lib().geye_free(C.cast(op, C.c_void_p))
+        return out
+
     # ---- device-resident path ---------------------------------------------
     def detect_device(self, d_bgr_ptr: int, width: int, height: int, models: list, thresh: float = -0.5,
                       overlap: float = 0.5):
@@ -525,6 +538,14 @@ class Model:
 
     def reset_scales(self):
         _check(lib().geye_model_reset_scales(self.h), "reset_scales")
+
+    def sym(self) -> dict:
+        """Symmetric information (load_model.cpp:279-373, 420-524): rootsym, part_partner, part_sym."""
+        rs = np.zeros(max(self.NoR, 1), np.int32)
+        pp = np.zeros(max(self.NoP, 1), np.int32)
+        ps = np.zeros(max(self.NoP, 1), np.int32)
+        _check(lib().geye_model_sym(self.h, _p(rs), _p(pp), _p(ps)), "model_sym")
+        return {"rootsym": rs[:self.NoR], "part_partner": pp[:self.NoP], "part_sym": ps[:self.NoP]}
 
     def close(self):
         if getattr(self, "h", None):

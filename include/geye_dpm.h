@@ -139,6 +139,18 @@ geye_status geye_resize(geye_ctx *ctx, const float *src, const int *sdims, int *
 geye_status geye_calc_feature(geye_ctx *ctx, const float *src, const int *isize, int sbin, int *ftsize,
                               float *feat);
 
+/* flip_feat (CAR_TRACKING/get_boxes.cpp:121-178): feat [size[2]][size[1]][size[0]]
+ * (reference layout, size[2] = 31 channels) mirrored along dim 1, channel ii
+ * taken from channel ORD[ii]-1 of the reference's table; *out is callee-allocated
+ * (geye_free), as the reference allocates its result. */
+geye_status geye_flip_feat(geye_ctx *ctx, const float *feat, const int *size, float **out);
+
+/* Symmetric information of a loaded model (CAR_TRACKING/load_model.cpp:279-373,
+ * 420-524): rootsym (NoR ints; the loader sets every one to 1), part_partner
+ * (NoP ints, the part CSV's partner field) and part_sym (NoP ints, 1 where the
+ * partner is 0).  Any pointer may be NULL. */
+geye_status geye_model_sym(const geye_model *model, int *rootsym, int *part_partner, int *part_sym);
+
 void geye_free(void *p);
 
 /* ---- device-resident path (benchmarks, batching) ------------------------ */

@@ -252,6 +252,19 @@ def dt(vals: np.ndarray, ax, bx, ay, by):
     return M, Ix, Iy
 
 
+# flip_feat (get_boxes.cpp:121-178): output channel c is input channel
+# FLIP_ORD[c] - 1 with dim 1 reversed (signed orientations mirrored, the
+# unsigned ones and the texture pairs swapped accordingly)
+FLIP_ORD = (10, 9, 8, 7, 6, 5, 4, 3, 2, 1, 18, 17, 16, 15, 14, 13, 12, 11, 19, 27, 26, 25, 24, 23, 22, 21, 20,
+            30, 31, 28, 29)
+
+
+def flip_feat(feat: np.ndarray) -> np.ndarray:
+    """feat (31, n1, n0) -> out[c, x, y] = feat[FLIP_ORD[c] - 1, n1 - 1 - x, y]."""
+    f = _f32(feat)
+    return np.ascontiguousarray(f[np.asarray(FLIP_ORD) - 1, ::-1, :])
+
+
 def quicksort(vals: np.ndarray):
     a = _f32(vals).copy()
     order = np.arange(len(a), dtype=np.int32)
@@ -426,6 +439,14 @@ def ref_resize(img: np.ndarray, scale: float) -> np.ndarray:
     od = _i32(resize_dims([h, w, c], scale))
     out = np.zeros((c, od[1], od[0]), np.float32)
     _R().ref_resize(_ptr(_f32(img).copy()), _ptr(sd), _ptr(od), C.c_float(scale), _ptr(out))
+    return out
+
+
+def ref_flip_feat(feat: np.ndarray) -> np.ndarray:
+    f = _f32(feat).copy()
+    c, n1, n0 = f.shape
+    out = np.zeros_like(f)
+    _R().ref_flip_feat(_ptr(f), _ptr(_i32([n0, n1, c])), _ptr(out))
     return out
 
 

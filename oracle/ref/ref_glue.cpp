@@ -21,6 +21,7 @@ FLOAT *partbox(int x, int y, int ax, int ay, FLOAT scale, int padx, int pady, in
 void calc_a_score(FLOAT *ac_score, FLOAT *score, int *ssize, int *rsize, Model_info *MI, FLOAT scale); /* :265 */
 FLOAT *nms(FLOAT *boxes, FLOAT overlap, int *num, MODEL *MO);                      /* nms.cpp:94 */
 void quickSort(FLOAT *ary, int *Order, int first_index, int last_index);          /* nms.cpp:70 */
+FLOAT *flip_feat(FLOAT *feat, int *size);                                          /* get_boxes.cpp:121 */
 
 extern "C" {
 
@@ -32,6 +33,15 @@ void ref_resize(float *src, int *sdims, int *odims, float scale, float *dst)
     FLOAT *r = resize(src, sdims, odims, scale);
     memcpy(dst, r, sizeof(FLOAT) * (size_t)odims[0] * odims[1] * odims[2]);
     free(r);
+}
+
+/* out holds size[0]*size[1]*size[2] floats; the reference's result is pinned
+ * memory on the GPU build (cuMemHostAlloc, a calloc stub here) */
+void ref_flip_feat(float *feat, int *size, float *out)
+{
+    FLOAT *f = flip_feat(feat, size);
+    memcpy(out, f, sizeof(FLOAT) * (size_t)size[0] * size[1] * size[2]);
+    free(f);
 }
 
 void ref_calc_feature(float *src, int *isize, int sbin, int *ftsize, float *feat)

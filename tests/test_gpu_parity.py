@@ -97,6 +97,29 @@ def test_dt(ctx, seed):
     assert np.array_equal(bits(M), bits(rM))
 
 
+def test_model_sym(ctx, tmp_path):
+    """rootsym (all 1), part_partner and part_sym as the reference's loader sets them."""
+    import geye_gb300 as g
+    comp, root, part = synth.write_model_csv(synth.CAR_SPEC, str(tmp_path))
+    vals = [v.strip() for v in open(part).read().split(",") if v.strip()]
+    n, pos, partners = int(float(vals[0])), 1, []
+    for i in range(n):
+        h, w, c = (int(float(v)) for v in vals[pos:pos + 3])
+        pos += 3 + h * w * c
+        partners.append([0, 2, 0, 5][i % 4])
+        vals[pos] = f"{partners[-1]:14.6f}"
+        pos += 1
+    with open(part, "w") as f:
+        f.write("".join(v + ",\n" for v in vals))
+    m = g.Model(ctx, comp, root, part)
+    s = m.sym()
+    nor = m.NoR
+    m.close()
+    assert list(s["rootsym"]) == [1] * nor
+    assert list(s["part_partner"]) == partners
+    assert list(s["part_sym"]) == [1 if p == 0 else 0 for p in partners]
+
+
 @pytest.mark.parametrize("seed", range(4))
 def test_nms_ties(ctx, seed):
     rng = np.random.default_rng(seed)

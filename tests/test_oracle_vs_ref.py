@@ -141,3 +141,9 @@ def test_pyramid_matches_reference_functions(car_paths):
         im = imgs[l] if l < 10 or l >= 20 else imgs[l - 10]
         f = O.ref_calc_feature(im, 4 if l < 10 else 8)
         assert np.array_equal(P.feat(l).view(np.int32), f.view(np.int32)), f"level {l}"
+
+
+@pytest.mark.parametrize("n0,n1", [(1, 1), (5, 7), (23, 40)])
+def test_flip_feat_bit_exact(n0, n1):
+    f = np.random.default_rng(n0 * 100 + n1).normal(size=(31, n1, n0)).astype(np.float32)
+    assert np.array_equal(O.flip_feat(f).view(np.int32), O.ref_flip_feat(f).view(np.int32))
