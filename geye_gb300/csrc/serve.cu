@@ -50,7 +50,7 @@ static geye_status enqueue_frame(geye_ctx *ctx, Plan &P, float thresh, float ove
   if (trk) {
     if (after) CUDA_TRY(cudaStreamWaitEvent(ctx->stream, after, 0));
     GEYE_TRY(tracker_update(*trk, stream, P.d_result.as<int>(), P.max_cap, P.d_small.as<int>() + 32, n_models,
-                            ctx->stream));
+                            P.d_ascore.as<float>(), P.width, P.height, ctx->stream));
     CUDA_TRY(cudaEventRecord(tracked, ctx->stream));
   }
   int *h = static_cast<int *>(P.h_res);

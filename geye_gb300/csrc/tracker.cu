@@ -5,10 +5,14 @@
 //     assignment in track order (highest IoU >= kAssocIoU, lowest index on
 //     ties), new tracks for detections left over, ends tracks missed too long.
 //   k_track_update (a block per track, a thread per particle): predict with
-//     Philox-driven Gaussian noise; with an assigned detection, weight by
-//     exp(-|corners - detection corners|^2 / (2 kLikeScale^2)), estimate as the
-//     weighted mean and resample systematically; a new track starts its
-//     particles around its detection.
+//     Philox-driven Gaussian noise; weight each particle, as the reference's
+//     calc_part_likelihood does (tracking.cpp:403-452: confidence = A_SCORE at
+//     the particle + an image likelihood), by the frame's A_SCORE at its
+//     centre (the largest over the models, 0 outside the image) plus
+//     exp(-|corners - detection corners|^2 / (2 kLikeScale^2)) for an assigned
+//     detection (1 without one); estimate as the weighted mean and, with a
+//     detection, resample systematically; a new track starts its particles
+//     around its detection.
 #include <math.h>
 #include <string.h>
 
@@ -134,7 +138,20 @@ __device__ __forceinline__ float block_sum512(float v, float *wbuf) {
   return t;
 }
 
-__global__ void __launch_bounds__(512) k_track_update(TrackState *S, uint32_t k0, uint32_t k1) {
+// A_SCORE[Y + X*H] (column-major, get_boxes.cpp:265-300) at the particle centre:
+// X = (int)cx and Y = (int)cy as the reference casts them, the largest over
+// the n_models maps; 0 when the point is outside the image or no map is given
+__device__ __forceinline__ float ascore_at(const float *__restrict__ asc, int n_models, int W, int H, float cx,
+                                           float cy) {
+  if (!asc || !(cx > -1.0f && cx < (float)W && cy > -1.0f && cy < (float)H)) return 0.f;
+  const size_t o = (size_t)(int)cx * H + (int)cy;
+  float v = asc[o];
+  for (int m = 1; m < n_models; m++) v = fmaxf(v, asc[(size_t)m * W * H + o]);
+  return v;
+}
+
+__global__ void __launch_bounds__(512) k_track_update(TrackState *S, uint32_t k0, uint32_t k1,
+                                                       const float *__restrict__ asc, int n_models, int W, int H) {
   __shared__ float q[6][kParticles];
   __shared__ float cum[512];
   __shared__ float wbuf[16];
@@ -173,12 +190,16 @@ __global__ void __launch_bounds__(512) k_track_update(TrackState *S, uint32_t k0
   }
   float b[4] = {s[0] - 0.5f * s[2], s[1] - 0.5f * s[3], s[0] + 0.5f * s[2], s[1] + 0.5f * s[3]};
   const int a = S->assign[t];
-  float w = mine ? 1.0f : 0.f;
-  if (a >= 0 && mine) {
-    const float *d = S->det[a];
-    float d2 = 0.f;
-    for (int c = 0; c < 4; c++) d2 += (b[c] - d[c]) * (b[c] - d[c]);
-    w = expf(-d2 / (2.0f * kLikeScale * kLikeScale));
+  float w = 0.f;
+  if (mine) {
+    float pro = 1.0f;
+    if (a >= 0) {
+      const float *d = S->det[a];
+      float d2 = 0.f;
+      for (int c = 0; c < 4; c++) d2 += (b[c] - d[c]) * (b[c] - d[c]);
+      pro = expf(-d2 / (2.0f * kLikeScale * kLikeScale));
+    }
+    w = ascore_at(asc, n_models, W, H, s[0], s[1]) + pro;
   }
   float total = block_sum512(w, wbuf);
   if (!(total > 0.f)) {   // every weight underflowed: uniform
@@ -239,7 +260,7 @@ void tracker_free(TrackerSet &T) {
 }
 
 geye_status tracker_update(TrackerSet &T, int stream, const int *d_result, int max_cap, const int *d_kept,
-                           int n_models, cudaStream_t s) {
+                           int n_models, const float *d_ascore, int width, int height, cudaStream_t s) {
   TrackState *S = nullptr;
   auto it = T.d.find(stream);
   if (it == T.d.end()) {
@@ -251,7 +272,7 @@ geye_status tracker_update(TrackerSet &T, int stream, const int *d_result, int m
   }
   const uint32_t k0 = (uint32_t)T.seed ^ (uint32_t)(stream * 0x9E3779B9u), k1 = (uint32_t)(T.seed >> 32) + (uint32_t)stream;
   k_track_assoc<<<1, 256, 0, s>>>(S, d_result, max_cap, d_kept, n_models);
-  k_track_update<<<kTracks, 512, 0, s>>>(S, k0, k1);
+  k_track_update<<<kTracks, 512, 0, s>>>(S, k0, k1, d_ascore, n_models, width, height);
   CUDA_TRY(cudaGetLastError());
   CUDA_TRY(cudaMemcpyAsync(T.h_count + stream, &S->n_alive, sizeof(int), cudaMemcpyDeviceToHost, s));
   return GEYE_OK;

@@ -44,9 +44,11 @@ struct TrackerSet {
 geye_status tracker_init(TrackerSet &T, unsigned long long seed);
 void tracker_free(TrackerSet &T);
 // one frame of `stream`: detections are the kept boxes of each model
-// (point arrays of d_result, model m at m*max_cap*11, counts d_kept[m])
+// (point arrays of d_result, model m at m*max_cap*11, counts d_kept[m]);
+// d_ascore holds the frame's n_models A_SCORE maps (width x height,
+// column-major, map m at m*width*height) or is NULL
 geye_status tracker_update(TrackerSet &T, int stream, const int *d_result, int max_cap, const int *d_kept,
-                           int n_models, cudaStream_t s);
+                           int n_models, const float *d_ascore, int width, int height, cudaStream_t s);
 int tracker_count(const TrackerSet &T, int stream);
 int tracker_streams(const TrackerSet &T);
 geye_status tracker_read(TrackerSet &T, int stream, int max, float *boxes, int *n);

@@ -4,7 +4,9 @@ Test infrastructure only.  Parity unpinned: the reference tracks with OpenCV's
 CvConDensation (CAR_TRACKING/tracking.cpp:321-850), which needs OpenCV 2.4 and
 does not build here; this file restates the project's own specification
 (constant velocity, Gaussian noise sigma 4 px / 1 px per frame, Philox4x32-10
-draws, greedy IoU association, Gaussian corner likelihood, systematic
+draws, greedy IoU association, a particle weight of A_SCORE at the particle
+plus a Gaussian corner likelihood as the reference's calc_part_likelihood adds
+A_SCORE to its image likelihood (tracking.cpp:403-452), systematic
 resampling) so the GPU kernels can be checked against it.
 
 Philox4x32-10 follows Salmon, Moraes, Dror and Shaw, "Parallel random numbers:
@@ -61,6 +63,18 @@ def iou(a, b):
     return inter / ua if ua > 0 else 0.0
 
 
+def ascore_at(ascore, cx, cy):
+    """Largest A_SCORE over the models at ((int)cx, (int)cy), C truncation; 0 outside the image."""
+    if ascore is None:
+        return 0.0
+    a = np.asarray(ascore, np.float32)
+    _, W, H = a.shape
+    inside = (cx > -1) & (cx < W) & (cy > -1) & (cy < H)
+    X = np.where(inside, np.trunc(cx), 0).astype(np.int64)
+    Y = np.where(inside, np.trunc(cy), 0).astype(np.int64)
+    return np.where(inside, a.max(0)[X, Y].astype(np.float64), 0.0)
+
+
 class StreamTracker:
     """One stream's tracker; step(dets) runs one frame (dets: (n, 4) x1 y1 x2 y2)."""
 
@@ -72,7 +86,8 @@ class StreamTracker:
         self.est = np.zeros((TRACKS, 4))
         self.p = np.zeros((TRACKS, 6, PARTICLES))
 
-    def step(self, dets: np.ndarray):
+    def step(self, dets: np.ndarray, ascore: np.ndarray | None = None):
+        """ascore: the frame's A_SCORE maps, (n_models, W, H) indexed [m, x, y], or None."""
         dets = np.asarray(dets, np.float64)[:MAX_DET]
         nd = len(dets)
         taken = np.zeros(nd, bool)
@@ -132,6 +147,7 @@ class StreamTracker:
             if assign[t] >= 0:
                 d = dets[assign[t]]
                 w = np.exp(-((b - d[:, None]) ** 2).sum(0) / (2 * LIKE_SCALE ** 2))
+            w = w + ascore_at(ascore, s[0], s[1])
             if not w.sum() > 0:
                 w = np.ones(PARTICLES)
             self.est[t] = (w * b).sum(1) / w.sum()

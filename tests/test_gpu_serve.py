@@ -92,7 +92,10 @@ def test_tracker_matches_its_restatement_and_isolates_streams(setup):
             solo.submit(0, f)
             solo.drain()
             d = solo.poll(4)[0]
-            ref.step(_dets(d["results"])[:TR.MAX_DET])
+            # the frame's A_SCORE maps (same conv mode, fresh -100 start, as the server's)
+            asc = [np.full((320, 240), -100, np.float32) for _ in models]
+            ctx.detect_multi(f, models, -0.5, 0.5, asc)
+            ref.step(_dets(d["results"])[:TR.MAX_DET], np.stack(asc))
             got = solo.tracks(0)
             assert d["n_tracks"] == len(got) == len(ref.boxes())
             if k < 2:   # start and first update: no resampling has happened yet

@@ -26,3 +26,20 @@ def test_tracker_follows_a_moving_box():
     for _ in range(TR.MAX_MISSED + 1):
         tr.step(np.zeros((0, 4)))
     assert len(tr.boxes()) == 0
+
+
+def test_ascore_weights_the_particles():
+    """A frame without an associated detection: particles on high A_SCORE pull
+    the estimate (the reference adds A_SCORE to each particle's confidence)."""
+    box = np.array([[100, 50, 160, 130]], float)
+    plain, lit = TR.StreamTracker(0), TR.StreamTracker(0)
+    for tr in (plain, lit):
+        tr.step(box)
+        tr.step(box)
+    asc = np.zeros((1, 320, 240), np.float32)
+    asc[0, 135:, :] = 1.0    # everything right of x = 135 scores 1
+    plain.step(np.zeros((0, 4)))
+    lit.step(np.zeros((0, 4)), asc)
+    assert lit.boxes()[0][0] > plain.boxes()[0][0] + 1.0
+    assert np.array_equal(TR.ascore_at(asc, np.array([-0.5, 134.9, 135.0, 320.0]), np.array([5.0, 5.0, 5.0, 5.0])),
+                          [0.0, 0.0, 1.0, 0.0])
