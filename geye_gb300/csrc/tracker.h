@@ -6,8 +6,10 @@
 // camera stream up to kTracks tracks of kParticles particles, state (cx, cy,
 // w, h, vx, vy) in FP32, constant-velocity motion with Gaussian noise
 // (sigma 4 px on position and size, 1 px/frame on velocity) drawn from a
-// per-stream Philox4x32-10 stream, a Gaussian likelihood on the box corners
-// of the associated detection, and systematic resampling.  Association is
+// per-stream Philox4x32-10 stream, particle weights of A_SCORE at the
+// particle plus a Gaussian likelihood on the box corners of the associated
+// detection (the reference adds A_SCORE to its template likelihood,
+// tracking.cpp:429-433), and systematic resampling.  Association is
 // greedy by IoU (>= 0.3) in track order; detections left over start tracks;
 // tracks missed kMaxMissed frames in a row end.
 #pragma once
