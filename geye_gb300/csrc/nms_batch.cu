@@ -199,7 +199,10 @@ __global__ void __launch_bounds__(kSortNT) k_nms_resolve(int cap, int *si, float
 }
 
 // ---------------------------------------------------------------------------
-// 3b. test the alive boxes against the batch's picks (warps own bitmap words)
+// 3b. test the alive boxes against the batch's picks (warps own bitmap words):
+// each alive box is removed by the first pick, in pick order, that suppresses
+// it, and that pick is flagged; sparse words take a box at a time against 32
+// picks a step, dense ones a pick at a time against 32 boxes a step
 // ---------------------------------------------------------------------------
 __device__ void pass_words(Slots &S, const float (*pk)[kBatch], int np, int pick_base, float overlap, int gwarp,
                            int nwarps) {
@@ -212,6 +215,21 @@ __device__ void pass_words(Slots &S, const float (*pk)[kBatch], int np, int pick
     const bool mine = (word >> lane) & 1u;
     const float e0 = mine ? S.y1[r] : 0.f, e1 = mine ? S.x1[r] : 0.f, e2 = mine ? S.y2[r] : 0.f,
                 e3 = mine ? S.x2[r] : 0.f, e4 = mine ? S.ar[r] : 0.f;
+    if (2 * __popc(word) * ((np + 31) >> 5) > np) {
+      // dense word: a lane per box walks the picks in order (about np steps for
+      // the warp instead of one 32-pick step per box and pick chunk)
+      int first = -1;
+      if (mine)
+        for (int t = 0; t < np; t++)
+          if (supp(pk[0][t], pk[1][t], pk[2][t], pk[3][t], pk[4][t], e0, e1, e2, e3, e4, overlap)) {
+            first = t;
+            break;
+          }
+      const unsigned gone = __ballot_sync(0xffffffffu, first >= 0);
+      if (first >= 0) S.flag[pick_base + first] = 1;
+      if (lane == 0 && gone) S.bits[w] = word & ~gone;
+      continue;
+    }
     unsigned out = word, rem = word;
     while (rem) {
       const int b = __ffs(rem) - 1;
