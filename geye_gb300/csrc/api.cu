@@ -69,6 +69,19 @@ geye_status geye_ctx_create(int device, void *cuda_stream, geye_ctx **out) {
     }
     ctx->own_stream = true;
   }
+  {
+    cudaError_t e = cudaStreamCreateWithFlags(&ctx->side, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming);
+    if (e != cudaSuccess) {
+      if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
+      if (ctx->side) cudaStreamDestroy(ctx->side);
+      if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
+      delete ctx;
+      set_error(std::string("side stream: ") + cudaGetErrorString(e));
+      return GEYE_ERR_CUDA;
+    }
+  }
   geye_status s = ctx->d_diag.alloc(ctx, 256);
   if (s != GEYE_OK) { delete ctx; return s; }
   cudaMemset(ctx->d_diag.p, 0, 256);
@@ -95,6 +108,12 @@ geye_status geye_ctx_destroy(geye_ctx *ctx) {
   for (auto &e : ctx->ev)
     if (e) cudaEventDestroy(e);
   if (ctx->h_pinned) cudaFreeHost(ctx->h_pinned);
+  if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
+  if (ctx->ev_join) cudaEventDestroy(ctx->ev_join);
+  if (ctx->side) {
+    cudaStreamSynchronize(ctx->side);
+    cudaStreamDestroy(ctx->side);
+  }
   if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
   return GEYE_OK;

@@ -906,21 +906,21 @@ static geye_status ascore_init(geye_ctx *ctx, Plan &P, int mi, const float *h_in
   return check_launch(ctx, "fill");
 }
 
-static geye_status ascore_compute(geye_ctx *ctx, Plan &P, ModelPlan &mp, int mi, float thresh) {
+static geye_status ascore_compute(geye_ctx *ctx, Plan &P, ModelPlan &mp, int mi, float thresh, cudaStream_t s) {
   float *a = P.d_ascore.as<float>() + (size_t)mi * P.width * P.height;
   const size_t n = (size_t)P.width * P.height;
   unsigned *maxb = reinterpret_cast<unsigned *>(P.d_small.as<int>() + 64 + mi);
-  CUDA_TRY(cudaMemsetAsync(maxb, 0, sizeof(unsigned), ctx->stream));
+  CUDA_TRY(cudaMemsetAsync(maxb, 0, sizeof(unsigned), s));
   launch_ascore(mp.d_as_col.as<int>(), mp.d_as_row.as<int>(), (int)mp.score_jobs.size(), P.arena.as<float>(), a,
-                P.width, P.height, thresh, maxb, ctx->stream);
+                P.width, P.height, thresh, maxb, s);
   GEYE_TRY(check_launch(ctx, "a_score"));
-  launch_ascore_normalize(a, (int)n, maxb, ctx->stream);
+  launch_ascore_normalize(a, (int)n, maxb, s);
   return check_launch(ctx, "a_score normalise");
 }
 
 geye_status run_ascore(geye_ctx *ctx, Plan &P, ModelPlan &mp, int mi, float thresh, const float *h_init) {
   GEYE_TRY(ascore_init(ctx, P, mi, h_init));
-  return ascore_compute(ctx, P, mp, mi, thresh);
+  return ascore_compute(ctx, P, mp, mi, thresh, ctx->stream);
 }
 
 geye_status run_nms(geye_ctx *ctx, Plan &P, int n_models, float overlap) {
@@ -957,12 +957,18 @@ static geye_status run_body(geye_ctx *ctx, Plan &P, float thresh, float overlap)
   T.mark(3);
   for (auto &mp : P.models) GEYE_TRY(run_dt(ctx, P, *mp));
   T.mark(4);
-  for (size_t mi = 0; mi < P.models.size(); mi++) {
-    GEYE_TRY(run_score(ctx, P, *P.models[mi], (int)mi, thresh));
-    GEYE_TRY(ascore_compute(ctx, P, *P.models[mi], (int)mi, thresh));
-  }
+  for (size_t mi = 0; mi < P.models.size(); mi++) GEYE_TRY(run_score(ctx, P, *P.models[mi], (int)mi, thresh));
   T.mark(5);
-  GEYE_TRY(run_nms(ctx, P, (int)P.models.size(), overlap));
+  // A_SCORE feeds nothing in the frame: it runs on the side stream beside NMS
+  CUDA_TRY(cudaEventRecord(ctx->ev_fork, ctx->stream));
+  CUDA_TRY(cudaStreamWaitEvent(ctx->side, ctx->ev_fork, 0));
+  geye_status st = GEYE_OK;
+  for (size_t mi = 0; mi < P.models.size() && st == GEYE_OK; mi++)
+    st = ascore_compute(ctx, P, *P.models[mi], (int)mi, thresh, ctx->side);
+  CUDA_TRY(cudaEventRecord(ctx->ev_join, ctx->side));
+  if (st == GEYE_OK) st = run_nms(ctx, P, (int)P.models.size(), overlap);
+  CUDA_TRY(cudaStreamWaitEvent(ctx->stream, ctx->ev_join, 0));   // joined on every path
+  GEYE_TRY(st);
   T.mark(6);
   return GEYE_OK;
 }

@@ -153,6 +153,10 @@ struct geye_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
   bool own_stream = false;
+  // A_SCORE runs beside NMS on this stream (forked after the score stage,
+  // joined before the frame ends)
+  cudaStream_t side = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   geye_conv_mode conv_mode = GEYE_CONV_FP32;
   std::map<std::string, std::unique_ptr<geye::Plan>> plans;
   int next_model_id = 1;
