@@ -51,7 +51,9 @@ constexpr int kTcThreads = 128;
 constexpr int kTcM = 128;                        // positions per tile (TMEM lanes)
 constexpr int kTcMaxTiles = 16;                  // tiles per CTA, at most
 constexpr size_t kTcSmemBudget = 220 * 1024;     // dynamic shared memory per CTA, at most
-constexpr int kTcHead = 640;                    // barriers, TMEM address, map offsets, scales, map dims
+constexpr int kTcMaxN = 64;                      // filters per group, at most (N of an MMA)
+constexpr int kTcHead = 1152;                    // barriers, TMEM address, map offsets, scales, map dims
+constexpr int kTcTmemCols = 512;                 // tiles per CTA x n_pad, at most
 constexpr unsigned long long kWaitNs = 1000000000ull;   // a wait gives up after 1 s (then 4 s for the drain)
 
 struct TcJob {
@@ -178,9 +180,9 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_conv_tc(const TcJob *__restri
   uint64_t *bar_load = reinterpret_cast<uint64_t *>(sm);
   uint64_t *bar_mma = reinterpret_cast<uint64_t *>(sm + 8);
   uint32_t *tslot = reinterpret_cast<uint32_t *>(sm + 16);
-  int *out_s = reinterpret_cast<int *>(sm + 32);       // the job's map offsets (n <= 32)
-  float *scl_s = reinterpret_cast<float *>(sm + 160);   // and output scales
-  int2 *dim_s = reinterpret_cast<int2 *>(sm + 288);     // and each map's rows, columns
+  int *out_s = reinterpret_cast<int *>(sm + 32);       // the job's map offsets (n <= kTcMaxN)
+  float *scl_s = reinterpret_cast<float *>(sm + 288);   // and output scales
+  int2 *dim_s = reinterpret_cast<int2 *>(sm + 544);     // and each map's rows, columns
   const int4 ch = chunks[blockIdx.x];
   const TcJob J = jobs[ch.x];
   const int tile0 = ch.y, ntile = ch.z, cs = ch.w;   // cs = filter columns per phase
@@ -362,7 +364,7 @@ static float e4m3_filter_scale(const float *F, size_t n) {
 // tensor work of a grouping: every tile issues taps MMAs of N = n_pad
 static double group_cost(const std::vector<BankGroup> &gs) {
   double c = 0;
-  for (auto &g : gs) c += (double)g.b0 * g.b1 * ((g.n <= 16 ? 16 : 32) + 16);
+  for (auto &g : gs) c += (double)g.b0 * g.b1 * (((g.n + 15) & ~15) + 16);
   return c;
 }
 
@@ -374,7 +376,7 @@ static double group_cost(const std::vector<BankGroup> &gs) {
 static void build_banks(const std::vector<const float *> &filt, const std::vector<int> &b0s,
                         const std::vector<int> &b1s, const std::vector<int> &kinds, geye_conv_mode mode,
                         std::vector<BankGroup> &groups, std::vector<uint16_t> &bank16, std::vector<float> &scale,
-                        size_t &total) {
+                        size_t &total, int cap = 32) {
   const int NQ = tc_planes_of(mode);
   groups.clear();
   for (int kind = 0; kind <= 1; kind++) {
@@ -383,14 +385,14 @@ static void build_banks(const std::vector<const float *> &filt, const std::vecto
       if (kinds[f] != kind) continue;
       bool placed = false;
       for (auto &g : exact)
-        if (g.b0 == b0s[f] && g.b1 == b1s[f] && g.n < 32) {
+        if (g.b0 == b0s[f] && g.b1 == b1s[f] && g.n < cap) {
           g.filt.push_back((int)f); g.fb0.push_back(b0s[f]); g.fb1.push_back(b1s[f]);
           g.n++;
           placed = true;
           break;
         }
       if (!placed) exact.push_back(BankGroup{b0s[f], b1s[f], 1, 0, 0, kind, {(int)f}, {b0s[f]}, {b1s[f]}, {}});
-      if (merged.empty() || merged.back().n == 32) merged.push_back(BankGroup{0, 0, 0, 0, 0, kind, {}, {}, {}, {}});
+      if (merged.empty() || merged.back().n == cap) merged.push_back(BankGroup{0, 0, 0, 0, 0, kind, {}, {}, {}, {}});
       BankGroup &m = merged.back();
       m.b0 = std::max(m.b0, b0s[f]);
       m.b1 = std::max(m.b1, b1s[f]);
@@ -402,7 +404,7 @@ static void build_banks(const std::vector<const float *> &filt, const std::vecto
   }
   total = 0;
   for (auto &g : groups) {
-    g.n_pad = g.n <= 16 ? 16 : 32;
+    g.n_pad = (g.n + 15) & ~15;   // N of the MMA: a multiple of 16
     g.bank_off = (int)total;
     total += (size_t)g.b0 * g.b1 * NQ * g.n_pad * 16;
   }
@@ -522,12 +524,22 @@ static bool add_tc_job(TcTables &T, int NQ, int plane_off, int fs0, int fs1, con
            ((size_t)Tc * kTcM + (size_t)(cs - 1) * fs0 + (g.b0 - 1)) * 16 * NQ;
   };
   int T_cta = 0, cs = 0;
-  for (int Tc = t_cap; Tc >= std::min(4, t_cap) && !T_cta; Tc /= 2)
+  const int t_max = std::max(1, std::min(t_cap, kTcTmemCols / g.n_pad));   // accumulators fit TMEM
+  for (int Tc = t_max; Tc >= std::min(4, t_max) && !T_cta; Tc /= 2)
     if (need(Tc, g.b1) <= budget) { T_cta = Tc; cs = g.b1; }
-  for (int Tc = std::min(8, t_cap); Tc >= 1 && !T_cta; Tc /= 2)
+  for (int Tc = std::min(8, t_max); Tc >= 1 && !T_cta; Tc /= 2)
     for (int c = g.b1; c >= 1; c--)
       if (need(Tc, c) <= budget) { T_cta = Tc; cs = c; break; }
   if (!T_cta) return false;
+  // the CTAs that share an SM (by shared memory) must fit their accumulators in
+  // its 512 TMEM columns together, or one's allocation waits for another to end
+  auto tmem_cols = [&](int Tc) {
+    uint32_t c = 32;
+    while (c < (uint32_t)(Tc * g.n_pad)) c <<= 1;
+    return (int)c;
+  };
+  auto per_sm = [&](int Tc) { return std::max<size_t>(1, (size_t)(228 * 1024) / (need(Tc, cs) + 1024)); };
+  while (T_cta > 1 && (size_t)tmem_cols(T_cta) * per_sm(T_cta) > (size_t)kTcTmemCols) T_cta /= 2;
   const int jid = (int)T.jobs.size();
   T.jobs.push_back(J);
   const long long reach = (long long)(g.b1 - 1) * fs0 + (g.b0 - 1);
@@ -581,6 +593,16 @@ static geye_status ensure_bank(geye_ctx *ctx, geye_model *m, geye_conv_mode mode
   return st;
 }
 
+// chunks ordered by cost (tiles x taps x N), heaviest first, so that the long
+// ones start in the first wave
+static void sort_chunks(TcTables &T) {
+  auto cost = [&](const int4 &c) {
+    const TcJob &J = T.jobs[c.x];
+    return (long long)c.z * J.b0 * J.b1 * J.n_pad;
+  };
+  std::stable_sort(T.chunks.begin(), T.chunks.end(), [&](const int4 &x, const int4 &y) { return cost(x) > cost(y); });
+}
+
 // job tables of one model for a tile-shape candidate; chunks ordered by cost,
 // heaviest first, so that the long ones start in the first wave
 static geye_status build_tables(Plan &P, ModelPlan &mp, const std::vector<BankGroup> &groups, int NQ, int t_cap,
@@ -605,11 +627,7 @@ static geye_status build_tables(Plan &P, ModelPlan &mp, const std::vector<BankGr
       }
     }
   }
-  auto cost = [&](const int4 &c) {
-    const TcJob &J = T.jobs[c.x];
-    return (long long)c.z * J.b0 * J.b1 * J.n_pad;
-  };
-  std::stable_sort(T.chunks.begin(), T.chunks.end(), [&](const int4 &x, const int4 &y) { return cost(x) > cost(y); });
+  sort_chunks(T);
   return GEYE_OK;
 }
 
@@ -776,7 +794,7 @@ geye_status conv_tc_maps(geye_ctx *ctx, const float *d_feat, int a0, int a1, con
   std::vector<uint16_t> bank16;
   std::vector<float> scale;
   size_t total = 0;
-  build_banks(filt, b0s, b1s, kinds, mode, groups, bank16, scale, total);
+  build_banks(filt, b0s, b1s, kinds, mode, groups, bank16, scale, total, kTcMaxN);
   for (int i = 0; i < n_filters; i++) {   // the FP8 bank is converted on the device from FP32 copies
     DevBuf *f = buf();
     const size_t n = (size_t)b0s[i] * b1s[i] * kFeat;

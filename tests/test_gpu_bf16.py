@@ -120,3 +120,14 @@ def test_conv_tile_shape_autotuner(tmp_path):
     for t in tuned:
         assert t["tiles_per_cta"] in (2, 4, 8, 16)
         assert 64 <= t["smem_kb"] <= 220 and t["ctas"] > 0 and t["ms"] > 0
+
+
+@pytest.mark.parametrize("n", [40, 64])
+def test_bf16_wide_filter_groups_bit_identical(ctx16, n):
+    """Groups of up to 64 filters (MMA N = 48, 64): exact-valued inputs give the FP32 maps bit for bit."""
+    rng = np.random.default_rng(n)
+    feat = (rng.integers(0, 5, size=(31, 30, 26)) * 0.25).astype(np.float32)
+    filters = [rng.integers(-2, 3, size=(31, 6, 6)).astype(np.float32) for _ in range(n)]
+    got = ctx16.fconvsMT(feat, filters)
+    for m, f in zip(got, filters):
+        assert np.array_equal(m.view(np.int32), O.fconv(feat, f).view(np.int32))
