@@ -354,9 +354,10 @@ __global__ void __launch_bounds__(kSortNT) k_nms_finish(const float *__restrict_
 }
 
 void launch_nms_batch(const float *boxes, const int *d_num, int n_models, int GL, float overlap, int cap, int *si,
-                      float *sf, float *out, int *d_kept, int *err, long long *diag, cudaStream_t s) {
+                      float *sf, float *out, int *d_kept, int *err, long long *diag, int levels, int *lv_used,
+                      cudaStream_t s) {
   if (n_models <= 0) return;
-  launch_nms_sort(boxes, d_num, n_models, GL, cap, si, sf, err, diag, s);
+  launch_nms_sort(boxes, d_num, n_models, GL, cap, si, sf, err, diag, levels, lv_used, s);
   k_nms_gather<<<dim3((cap + kPassNT - 1) / kPassNT, n_models), kPassNT, 0, s>>>(boxes, GL, cap, si, sf);
   const int words = (cap + 31) / 32;
   const int pass_blocks = std::max(1, std::min((words + kPassNT / 32 - 1) / (kPassNT / 32), 512));

@@ -260,8 +260,10 @@ __device__ __forceinline__ bool supp(float Ay1, float Ax1, float Ay2, float Ax2,
 }
 
 // sort stage (nms_sort.cu): leaves val/ord sorted for every model and the
-// BatchState initialised; diag[8m + 1] gets the segments left to k_qs_rest
+// BatchState initialised; diag[8m + 1] gets the segments left to k_qs_rest.
+// levels: grid-wide partition levels to launch (<= 0: nms_sort_levels(cap));
+// *lv_used (optional) gets the deepest level that had a segment to partition
 void launch_nms_sort(const float *boxes, const int *d_num, int n_models, int GL, int cap, int *si, float *sf,
-                     int *err, long long *diag, cudaStream_t s);
+                     int *err, long long *diag, int levels, int *lv_used, cudaStream_t s);
 
 }  // namespace geye

@@ -3,7 +3,8 @@
 // order for equal scores (partition argument in nms_common.h).
 //
 //   k_qs_load: keys, the identity order and the first segment of each model.
-//   Levels (three times the balanced depth to kNmsSegS, plus three: sort_levels), three
+//   Levels (by default three times the balanced depth to kNmsSegS, plus three:
+//   nms_sort_levels; a plan may launch fewer once it has seen its frames' depth), three
 //   kernels each (no-ops once nothing is left):
 //     k_qs_count   every segment above kNmsSegS is cut into tiles of kNmsTile
 //                  elements; a block counts its tile's values <= key and >= key;
@@ -127,13 +128,14 @@ __device__ __forceinline__ void tile_prefix(const Slots &S, const TileRef &r, in
   total = block_sum2(al, ar, wbuf);
 }
 
-__global__ void __launch_bounds__(kNmsNT) k_qs_count(int level, int cap, int *si, float *sf) {
+__global__ void __launch_bounds__(kNmsNT) k_qs_count(int level, int cap, int *si, float *sf, int *lv_used) {
   __shared__ int2 wbuf[kNmsNT / 32];
   Slots S = slots(si, sf, blockIdx.y, cap);
   const int cur = level & 1;
   if (blockIdx.x == 0 && threadIdx.x == 0) S.ss->big_n[cur ^ 1] = 0;   // the next level's queue
   const int n = S.ss->big_n[cur];
   if (n == 0) return;
+  if (lv_used && blockIdx.x == 0 && threadIdx.x == 0) atomicMax(lv_used, level + 1);   // levels with work
   const int ntot = total_tiles(S, cur, n);
   for (int g = blockIdx.x; g < ntot; g += gridDim.x) {
     TileRef r;
@@ -490,22 +492,22 @@ __global__ void __launch_bounds__(kNmsNT) k_qs_rest(int levels, int cap, int *si
 // uneven (ties, runs), so three times the balanced depth to kNmsSegS, plus three
 // (a level with nothing left costs three empty launches; a segment still above
 // kNmsSegS afterwards costs k_qs_rest's single block per model far more)
-static int sort_levels(int cap) {
+int nms_sort_levels(int cap) {
   int depth = 0;
   while (((long long)kNmsSegS << depth) < cap) depth++;
   return std::max(4, std::min(30, 3 * depth + 3));
 }
 
 void launch_nms_sort(const float *boxes, const int *d_num, int n_models, int GL, int cap, int *si, float *sf,
-                     int *err, long long *diag, cudaStream_t s) {
-  const int levels = sort_levels(cap);
+                     int *err, long long *diag, int levels, int *lv_used, cudaStream_t s) {
+  if (levels <= 0) levels = nms_sort_levels(cap);
   k_qs_load<<<dim3((cap + 255) / 256, n_models), 256, 0, s>>>(boxes, d_num, GL, cap, si, sf);
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   const int tiles = std::max(1, std::min(nms_tile_cap(cap), std::max(1, 2 * sms / std::max(1, n_models))));
   for (int l = 0; l < levels; l++) {
-    k_qs_count<<<dim3(tiles, n_models), kNmsNT, 0, s>>>(l, cap, si, sf);
+    k_qs_count<<<dim3(tiles, n_models), kNmsNT, 0, s>>>(l, cap, si, sf, lv_used);
     k_qs_scatter<<<dim3(tiles, n_models), kNmsNT, 0, s>>>(l, cap, si, sf);
     k_qs_swap<<<dim3(tiles, n_models), kNmsNT, 0, s>>>(l, cap, si, sf, err);
   }

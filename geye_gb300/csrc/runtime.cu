@@ -923,13 +923,39 @@ geye_status run_ascore(geye_ctx *ctx, Plan &P, ModelPlan &mp, int mi, float thre
   return ascore_compute(ctx, P, mp, mi, thresh, ctx->stream);
 }
 
+// After a frame of the plan has completed: `used` is the deepest grid-wide sort
+// level that had a segment to partition.  The first frame launches the
+// default count (nms_sort_levels); if it needed at most that minus four, the
+// plan launches three more than it needed from then on (each empty level
+// costs three launches on the frame's path).  A frame whose last launched
+// level still had work left its remaining segments to the single-block
+// fallback (exact, slower): the plan goes back to the default for good.
+// A change drops the plan's frame graphs after its stream has drained; the
+// next frame captures them again.
+void note_sort_levels(geye_ctx *ctx, Plan &P, int used) {
+  const int full = nms_sort_levels(P.max_cap);
+  const int launched = P.sort_levels > 0 ? P.sort_levels : full;
+  int next = P.sort_levels;
+  if (used >= launched) {
+    if (P.sort_levels > 0) { next = 0; P.sort_levels_fixed = true; }
+  } else if (!P.sort_levels_fixed && P.sort_levels == 0 && used + 3 < full) {
+    next = std::max(4, used + 3);
+  }
+  if (next == P.sort_levels) return;
+  P.sort_levels = next;
+  cudaStreamSynchronize(ctx->stream);
+  for (auto &g : P.graphs)
+    if (g.second.exec) cudaGraphExecDestroy(g.second.exec);
+  P.graphs.clear();
+}
+
 geye_status run_nms(geye_ctx *ctx, Plan &P, int n_models, float overlap) {
   int *d_num = P.d_small.as<int>();
   int *d_kept = d_num + 32;
   int *err = d_num + 128;
   launch_nms_batch(P.d_boxes.as<float>(), d_num, n_models, P.gl, overlap, P.max_cap, P.d_nms_i.as<int>(),
                    P.d_nms_f.as<float>(), P.d_kept_boxes.as<float>(), d_kept, err,
-                   reinterpret_cast<long long *>(d_num + 512), ctx->stream);
+                   reinterpret_cast<long long *>(d_num + 512), P.sort_levels, d_num + kSortLevelsUsed, ctx->stream);
   GEYE_TRY(check_launch(ctx, "nms"));
   for (int mi = 0; mi < n_models; mi++) {
     ModelPlan &mp = *P.models[mi];

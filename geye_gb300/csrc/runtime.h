@@ -44,6 +44,9 @@ struct ModelPlan;
 geye_status upload_bytes(geye_ctx *ctx, DevBuf &buf, const void *src, size_t n);
 // tensor-core convolution job tables of one model of a plan (conv_tc.cu)
 geye_status build_tc_jobs(geye_ctx *ctx, Plan &P, ModelPlan &mp);
+// d_small[kSortLevelsUsed]: the deepest NMS sort level with work in the frame
+constexpr int kSortLevelsUsed = 48;
+void note_sort_levels(geye_ctx *ctx, Plan &P, int used);
 // tensor-core fconvsMT of one feature map ([pos][32] float on the device) for the stage entry point
 geye_status conv_tc_maps(geye_ctx *ctx, const float *d_feat, int a0, int a1, const float *const *filters,
                          const int *b_dims, int n_filters, float *d_out, const std::vector<int> &out_off,
@@ -134,6 +137,10 @@ struct Plan {
     int kernels = 0;
   };
   std::map<std::string, FrameGraph> graphs;
+  // grid-wide NMS sort levels launched per frame (0: the default for max_cap),
+  // adapted once to the depth the plan's frames need (note_sort_levels)
+  int sort_levels = 0;
+  bool sort_levels_fixed = false;
   // asynchronous submission (serve.cu): pinned frame staging, pinned result
   // block (counts, then per model kHostRes records) and the completion event
   void *h_bgr = nullptr, *h_res = nullptr;

@@ -79,11 +79,14 @@ static geye_status ensure_staging(Plan &P) {
   return GEYE_OK;
 }
 
+// wait: the frame's own graph (submit and server slots; the plan's sort level
+// count may then adapt); false: a lane of a batch graph, already complete
 static geye_status collect_frame(geye_ctx *ctx, geye_result *out, bool wait = true) {
   Plan &P = *ctx->pending;
   if (wait) CUDA_TRY(cudaEventSynchronize(P.ev_done));
   const int n_models = (int)P.models.size();
   const int *h = static_cast<const int *>(P.h_res);
+  if (wait) note_sort_levels(ctx, P, h[kSortLevelsUsed]);
   geye_status st = GEYE_OK;
   for (int mi = 0; mi < n_models && out; mi++) {
     const int K = h[32 + mi];

@@ -272,3 +272,30 @@ def test_pipeline_odd_and_large_frames(ctx, car, w, h):
     assert np.array_equal(got["point"], ref["point"])
     assert np.array_equal(got["or_point"], ref["or_point"])
     assert np.array_equal(bits(got["score"]), bits(ref["score"]))
+
+
+def test_nms_sort_levels_adapt_and_fall_back(tmp_path):
+    """A plan fits its NMS sort levels to the depth its frames need (a shallow
+    frame first: few boxes) and returns to the default when a later frame
+    needs more (the leftover segments take the exact single-block fallback):
+    every result equals a fresh context's, which launches the default levels."""
+    import geye_gb300 as g
+    paths = [synth.write_model_csv(s, str(tmp_path)) for s in (synth.CAR_SPEC, synth.PERSON_SPEC)]
+    fr = synth.make_frame(640, 480, seed=6)
+    c1 = g.Context(0)
+    m1 = [g.Model(c1, *p) for p in paths]
+    for thresh in (0.9, 0.9, -0.5, -0.5):
+        got = c1.detect_multi(fr, m1, thresh, 0.5)
+        c2 = g.Context(0)
+        m2 = [g.Model(c2, *p) for p in paths]
+        want = c2.detect_multi(fr, m2, thresh, 0.5)
+        for m in m2:
+            m.close()
+        c2.close()
+        for x, y in zip(got, want):
+            assert x["num"] == y["num"]
+            assert np.array_equal(x["point"], y["point"]) and np.array_equal(x["type"], y["type"])
+            assert np.array_equal(bits(x["score"]), bits(y["score"]))
+    for m in m1:
+        m.close()
+    c1.close()
