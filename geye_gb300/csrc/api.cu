@@ -318,15 +318,15 @@ geye_status geye_model_reset_scales(geye_model *m) {
 // ---------------------------------------------------------------------------
 static geye_status fetch_model_result(geye_ctx *ctx, Plan &P, int mi, geye_result *out, int *D_out,
                                       float **kept_out) {
-  int counts[3] = {0, 0, 0};
+  int counts[4] = {0, 0, 0, 0};
   CUDA_TRY(cudaMemcpyAsync(&counts[0], P.d_small.as<int>() + mi, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
   CUDA_TRY(cudaMemcpyAsync(&counts[1], P.d_small.as<int>() + 32 + mi, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
   if (mi == 0)
-    CUDA_TRY(cudaMemcpyAsync(&counts[2], P.d_small.as<int>() + kSortLevelsUsed, sizeof(int), cudaMemcpyDeviceToHost,
-                             ctx->stream));
+    CUDA_TRY(cudaMemcpyAsync(&counts[2], P.d_small.as<int>() + kSortLevelsUsed, 2 * sizeof(int),
+                             cudaMemcpyDeviceToHost, ctx->stream));
   CUDA_TRY(cudaStreamSynchronize(ctx->stream));
   const int D = counts[0], K = counts[1];
-  if (mi == 0 && !P.from_features) note_sort_levels(ctx, P, counts[2]);
+  if (mi == 0 && !P.from_features) note_sort_levels(ctx, P, counts[2], counts[3]);
   if (D_out) *D_out = D;
   P.last_D[mi] = D;
   P.last_K[mi] = K;

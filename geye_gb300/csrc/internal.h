@@ -202,10 +202,13 @@ __host__ __device__ inline size_t nms_model_words(int cap) {
 }
 // diag (optional): per model m, diag[8m+1..8m+4] = sort segments left to the fallback, batches, picks,
 // whether the finish kernel ran rounds itself
-// levels, lv_used: as for launch_nms_sort (nms_common.h)
+// levels, lv_used: as for launch_nms_sort (nms_common.h); rounds: resolve/pass
+// rounds launched before the finish kernel (<= 0: kNmsRounds), *rounds_used
+// (optional) gets the batches the frame took, the finish kernel's included
+constexpr int kNmsRounds = 8;
 void launch_nms_batch(const float *boxes, const int *d_num, int n_models, int GL, float overlap, int cap, int *si,
                       float *sf, float *out, int *d_kept, int *err, long long *diag, int levels, int *lv_used,
-                      cudaStream_t s);
+                      int rounds, int *rounds_used, cudaStream_t s);
 int nms_sort_levels(int cap);   // the default number of grid-wide sort levels for cap boxes
 void launch_new_rects(const float *kept, const int *d_kept, int GL, int np, const float *coef, int img_w,
                       int img_h, float ratio, int *point, int *or_point, int *type, float *scale, float *score,

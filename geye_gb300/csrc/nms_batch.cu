@@ -32,7 +32,6 @@ constexpr int kSortNT = kNmsNT;   // threads of the resolve and finish blocks
 constexpr int kBatch = kNmsBatch;
 constexpr int kBW = kBatch / 32;   // words of a suppression row
 constexpr int kPassNT = 256;
-constexpr int kRounds = 8;         // resolve/pass rounds launched before the finish kernel
 constexpr int kRankSortMax = 4096; // kept boxes ordered by ranking in shared memory up to this many
 
 // ---------------------------------------------------------------------------
@@ -270,7 +269,7 @@ __global__ void __launch_bounds__(kPassNT) k_nms_pass(int cap, int *si, float *s
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(kSortNT) k_nms_finish(const float *__restrict__ boxes_all, int GL, int cap,
                                                         int *si, float *sf, float overlap, float *out_all,
-                                                        int *d_kept, int *err, long long *diag) {
+                                                        int *d_kept, int *err, long long *diag, int *rounds_used) {
   __shared__ ResolveSmem R;
   __shared__ float pk[5][kBatch];
   __shared__ int wcnt[kSortNT / 32];
@@ -345,6 +344,7 @@ __global__ void __launch_bounds__(kSortNT) k_nms_finish(const float *__restrict_
   }
   if (threadIdx.x == 0) {
     d_kept[m] = written;
+    if (rounds_used) atomicMax(rounds_used, st.batches);   // batches this frame took, grid rounds and any here
     if (diag) {
       diag[8 * m + 2] = st.batches;
       diag[8 * m + 3] = npk;
@@ -355,17 +355,18 @@ __global__ void __launch_bounds__(kSortNT) k_nms_finish(const float *__restrict_
 
 void launch_nms_batch(const float *boxes, const int *d_num, int n_models, int GL, float overlap, int cap, int *si,
                       float *sf, float *out, int *d_kept, int *err, long long *diag, int levels, int *lv_used,
-                      cudaStream_t s) {
+                      int rounds, int *rounds_used, cudaStream_t s) {
   if (n_models <= 0) return;
   launch_nms_sort(boxes, d_num, n_models, GL, cap, si, sf, err, diag, levels, lv_used, s);
   k_nms_gather<<<dim3((cap + kPassNT - 1) / kPassNT, n_models), kPassNT, 0, s>>>(boxes, GL, cap, si, sf);
   const int words = (cap + 31) / 32;
   const int pass_blocks = std::max(1, std::min((words + kPassNT / 32 - 1) / (kPassNT / 32), 512));
-  for (int r = 0; r < kRounds; r++) {
+  if (rounds <= 0) rounds = kNmsRounds;
+  for (int r = 0; r < rounds; r++) {
     k_nms_resolve<<<n_models, kSortNT, 0, s>>>(cap, si, sf, overlap);
     k_nms_pass<<<dim3(pass_blocks, n_models), kPassNT, 0, s>>>(cap, si, sf, overlap);
   }
-  k_nms_finish<<<n_models, kSortNT, 0, s>>>(boxes, GL, cap, si, sf, overlap, out, d_kept, err, diag);
+  k_nms_finish<<<n_models, kSortNT, 0, s>>>(boxes, GL, cap, si, sf, overlap, out, d_kept, err, diag, rounds_used);
 }
 
 }  // namespace geye

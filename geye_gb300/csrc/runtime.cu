@@ -924,25 +924,30 @@ geye_status run_ascore(geye_ctx *ctx, Plan &P, ModelPlan &mp, int mi, float thre
 }
 
 // After a frame of the plan has completed: `used` is the deepest grid-wide sort
-// level that had a segment to partition.  The first frame launches the
-// default count (nms_sort_levels); if it needed at most that minus four, the
-// plan launches three more than it needed from then on (each empty level
-// costs three launches on the frame's path).  A frame whose last launched
-// level still had work left its remaining segments to the single-block
-// fallback (exact, slower): the plan goes back to the default for good.
-// A change drops the plan's frame graphs after its stream has drained; the
-// next frame captures them again.
-void note_sort_levels(geye_ctx *ctx, Plan &P, int used) {
+// level that had a segment to partition, `rounds` the greedy batches the frame
+// took.  The first frame launches the default counts (nms_sort_levels,
+// kNmsRounds); if it needed fewer, the plan launches three levels and one
+// round more than it needed from then on (each empty level costs three
+// launches on the frame's path, each empty round two).  A frame whose last
+// launched level still had work left its remaining segments to the
+// single-block sort fallback, and one that took more batches than the rounds
+// launched ran them in the finish kernel (both exact, slower): the plan goes
+// back to the default counts for good.  A change drops the plan's frame
+// graphs after its stream has drained; the next frame captures them again.
+void note_sort_levels(geye_ctx *ctx, Plan &P, int used, int rounds) {
   const int full = nms_sort_levels(P.max_cap);
   const int launched = P.sort_levels > 0 ? P.sort_levels : full;
-  int next = P.sort_levels;
-  if (used >= launched) {
-    if (P.sort_levels > 0) { next = 0; P.sort_levels_fixed = true; }
-  } else if (!P.sort_levels_fixed && P.sort_levels == 0 && used + 3 < full) {
-    next = std::max(4, used + 3);
+  const int r_launched = P.nms_rounds > 0 ? P.nms_rounds : kNmsRounds;
+  int next = P.sort_levels, r_next = P.nms_rounds;
+  if (used >= launched || rounds > r_launched) {
+    if (P.sort_levels > 0 || P.nms_rounds > 0) { next = 0; r_next = 0; P.sort_levels_fixed = true; }
+  } else if (!P.sort_levels_fixed && P.sort_levels == 0 && P.nms_rounds == 0) {
+    if (used + 3 < full) next = std::max(4, used + 3);
+    if (rounds + 1 < kNmsRounds) r_next = std::max(2, rounds + 1);
   }
-  if (next == P.sort_levels) return;
+  if (next == P.sort_levels && r_next == P.nms_rounds) return;
   P.sort_levels = next;
+  P.nms_rounds = r_next;
   cudaStreamSynchronize(ctx->stream);
   for (auto &g : P.graphs)
     if (g.second.exec) cudaGraphExecDestroy(g.second.exec);
@@ -955,7 +960,8 @@ geye_status run_nms(geye_ctx *ctx, Plan &P, int n_models, float overlap) {
   int *err = d_num + 128;
   launch_nms_batch(P.d_boxes.as<float>(), d_num, n_models, P.gl, overlap, P.max_cap, P.d_nms_i.as<int>(),
                    P.d_nms_f.as<float>(), P.d_kept_boxes.as<float>(), d_kept, err,
-                   reinterpret_cast<long long *>(d_num + 512), P.sort_levels, d_num + kSortLevelsUsed, ctx->stream);
+                   reinterpret_cast<long long *>(d_num + 512), P.sort_levels, d_num + kSortLevelsUsed, P.nms_rounds,
+                   d_num + kNmsRoundsUsed, ctx->stream);
   GEYE_TRY(check_launch(ctx, "nms"));
   for (int mi = 0; mi < n_models; mi++) {
     ModelPlan &mp = *P.models[mi];

@@ -44,9 +44,10 @@ struct ModelPlan;
 geye_status upload_bytes(geye_ctx *ctx, DevBuf &buf, const void *src, size_t n);
 // tensor-core convolution job tables of one model of a plan (conv_tc.cu)
 geye_status build_tc_jobs(geye_ctx *ctx, Plan &P, ModelPlan &mp);
-// d_small[kSortLevelsUsed]: the deepest NMS sort level with work in the frame
-constexpr int kSortLevelsUsed = 48;
-void note_sort_levels(geye_ctx *ctx, Plan &P, int used);
+// d_small[kSortLevelsUsed]: the deepest NMS sort level with work in the frame;
+// d_small[kNmsRoundsUsed]: the greedy batches it took
+constexpr int kSortLevelsUsed = 48, kNmsRoundsUsed = 49;
+void note_sort_levels(geye_ctx *ctx, Plan &P, int used, int rounds);
 // tensor-core fconvsMT of one feature map ([pos][32] float on the device) for the stage entry point
 geye_status conv_tc_maps(geye_ctx *ctx, const float *d_feat, int a0, int a1, const float *const *filters,
                          const int *b_dims, int n_filters, float *d_out, const std::vector<int> &out_off,
@@ -140,6 +141,7 @@ struct Plan {
   // grid-wide NMS sort levels launched per frame (0: the default for max_cap),
   // adapted once to the depth the plan's frames need (note_sort_levels)
   int sort_levels = 0;
+  int nms_rounds = 0;   // greedy resolve/pass rounds per frame (0: kNmsRounds), adapted with the levels
   bool sort_levels_fixed = false;
   // asynchronous submission (serve.cu): pinned frame staging, pinned result
   // block (counts, then per model kHostRes records) and the completion event

@@ -86,7 +86,7 @@ static geye_status collect_frame(geye_ctx *ctx, geye_result *out, bool wait = tr
   if (wait) CUDA_TRY(cudaEventSynchronize(P.ev_done));
   const int n_models = (int)P.models.size();
   const int *h = static_cast<const int *>(P.h_res);
-  if (wait) note_sort_levels(ctx, P, h[kSortLevelsUsed]);
+  if (wait) note_sort_levels(ctx, P, h[kSortLevelsUsed], h[kNmsRoundsUsed]);
   geye_status st = GEYE_OK;
   for (int mi = 0; mi < n_models && out; mi++) {
     const int K = h[32 + mi];
