@@ -192,7 +192,7 @@ void launch_nms(const float *boxes, const int *d_num, int n_models, int GL, floa
 // pipeline NMS (nms_sort.cu, nms_batch.cu): per model nms_model_words(cap) ints
 // of scratch and 5 * cap floats (the boxes in sorted order)
 constexpr int kNmsBatch = 256;     // boxes resolved per round
-constexpr int kNmsSegS = 8192;     // sort segments finished in shared memory
+constexpr int kNmsSegS = 16384;    // sort segments finished in shared memory (one block, ~203 KB)
 constexpr int kNmsTile = 4096;     // elements per block in the sort's grid-wide partitions
 __host__ __device__ inline int nms_big_cap(int cap) { return cap / kNmsSegS + 2; }
 __host__ __device__ inline int nms_tile_cap(int cap) { return cap / kNmsTile + nms_big_cap(cap) + 1; }
