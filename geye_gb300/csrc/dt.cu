@@ -36,7 +36,7 @@
 namespace geye {
 
 constexpr int kDtThreads = 256;
-constexpr int kDtElems = 4096;      // outputs per block (about)
+constexpr int kDtElems = 2048;      // outputs per block (about)
 constexpr int kDtPad = 64;          // largest window half-width served by the fast loop
 
 __device__ __forceinline__ float dt_f(float v, float a, float b, int t) {

@@ -61,7 +61,7 @@ void launch_ingest(const uint8_t *bgr, int width, int height, int width_step, fl
 // no index division per element, and each tap is loaded once for the three
 // channels (vertical) or once per column (horizontal).
 // ----------------------------------------------------------------------------
-constexpr int kResizeWarps = 8;
+constexpr int kResizeWarps = 4;
 
 __global__ void __launch_bounds__(kResizeWarps * 32) k_resize_pass(const ResizeJob *__restrict__ jobs, int vertical,
                                                                    const int *__restrict__ tap_start,
