@@ -488,10 +488,11 @@ __global__ void __launch_bounds__(kNmsNT) k_qs_rest(int levels, int cap, int *si
   }
 }
 
-// grid-wide levels launched for a plan of cap boxes per model: quicksort splits are
-// uneven (ties, runs), so three times the balanced depth to kNmsSegS, plus three
-// (a level with nothing left costs three empty launches; a segment still above
-// kNmsSegS afterwards costs k_qs_rest's single block per model far more)
+// the default number of grid-wide levels for cap boxes per model: quicksort
+// splits are uneven (ties, runs), so three times the balanced depth to
+// kNmsSegS, plus three (a level with nothing left costs three empty launches; a
+// segment still above kNmsSegS afterwards costs k_qs_rest's single block per
+// model far more).  Plans then fit the count to their frames' depth on the host.
 int nms_sort_levels(int cap) {
   int depth = 0;
   while (((long long)kNmsSegS << depth) < cap) depth++;

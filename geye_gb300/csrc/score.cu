@@ -228,7 +228,7 @@ __global__ void __launch_bounds__(kAsTile *kAsTile) k_ascore(const int *__restri
     const size_t idx = (size_t)X * im_h + Y;
     float a = a_score[idx];
     const int *tc = tab_s + tx, *tr = tab_s + n_jobs * kAsTile + ty;
-#pragma unroll 2
+#pragma unroll 8   // eight gathers in flight per thread (the maximum is exact in any order)
     for (int j = 0; j < n_jobs; j++) {
       const int c = tc[j * kAsTile], r = tr[j * kAsTile];
       if ((c | r) >= 0) {
