@@ -85,6 +85,7 @@ __global__ void __launch_bounds__(kResizeWarps * 32) k_resize_pass(const ResizeJ
         float a0 = 0.0f, a1 = 0.0f, a2 = 0.0f, c0 = 0.0f, c1 = 0.0f, c2 = 0.0f;
         const int t1 = ts[y + 1];
         const int u0 = y2 < J.dst_h ? ts[y2] : 0, u1 = y2 < J.dst_h ? ts[y2 + 1] : 0;
+#pragma unroll 4
         for (int t = ts[y]; t < t1; t++) {
           const float w = al[t];
           const float *p = col + si[t];
@@ -92,6 +93,7 @@ __global__ void __launch_bounds__(kResizeWarps * 32) k_resize_pass(const ResizeJ
           a1 += w * p[src_plane];
           a2 += w * p[2 * src_plane];
         }
+#pragma unroll 4
         for (int t = u0; t < u1; t++) {
           const float w = al[t];
           const float *p = col + si[t];
