@@ -985,11 +985,34 @@ static geye_status run_body(geye_ctx *ctx, Plan &P, float thresh, float overlap)
   T.mark(1);
   GEYE_TRY(run_hog(ctx, P));
   T.mark(2);
-  for (auto &mp : P.models) GEYE_TRY(run_conv(ctx, P, *mp));
-  T.mark(3);
-  for (auto &mp : P.models) GEYE_TRY(run_dt(ctx, P, *mp));
-  T.mark(4);
-  for (size_t mi = 0; mi < P.models.size(); mi++) GEYE_TRY(run_score(ctx, P, *P.models[mi], (int)mi, thresh));
+  if (ctx->timing || P.models.size() < 2) {   // stage by stage (per-stage times)
+    for (auto &mp : P.models) GEYE_TRY(run_conv(ctx, P, *mp));
+    T.mark(3);
+    for (auto &mp : P.models) GEYE_TRY(run_dt(ctx, P, *mp));
+    T.mark(4);
+    for (size_t mi = 0; mi < P.models.size(); mi++) GEYE_TRY(run_score(ctx, P, *P.models[mi], (int)mi, thresh));
+  } else {
+    // each model's conv -> DT -> score chain reads only the shared features and
+    // writes only its own maps and records: models 1.. run on the side stream
+    // beside model 0 (their kernels take the context's stream, swapped while
+    // they are issued), joined before NMS
+    auto chain = [&](size_t mi) -> geye_status {
+      GEYE_TRY(run_conv(ctx, P, *P.models[mi]));
+      GEYE_TRY(run_dt(ctx, P, *P.models[mi]));
+      return run_score(ctx, P, *P.models[mi], (int)mi, thresh);
+    };
+    CUDA_TRY(cudaEventRecord(ctx->ev_fork, ctx->stream));
+    CUDA_TRY(cudaStreamWaitEvent(ctx->side, ctx->ev_fork, 0));
+    std::swap(ctx->stream, ctx->side);
+    geye_status st1 = GEYE_OK;
+    for (size_t mi = 1; mi < P.models.size() && st1 == GEYE_OK; mi++) st1 = chain(mi);
+    std::swap(ctx->stream, ctx->side);
+    CUDA_TRY(cudaEventRecord(ctx->ev_join, ctx->side));
+    const geye_status st0 = chain(0);
+    CUDA_TRY(cudaStreamWaitEvent(ctx->stream, ctx->ev_join, 0));   // joined on every path
+    GEYE_TRY(st0);
+    GEYE_TRY(st1);
+  }
   T.mark(5);
   // A_SCORE feeds nothing in the frame: it runs on the side stream beside NMS
   CUDA_TRY(cudaEventRecord(ctx->ev_fork, ctx->stream));
