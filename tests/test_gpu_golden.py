@@ -59,3 +59,12 @@ def test_nms(ctx, V):
         want = boxes[V[f"nms_keep{k}"].astype(bool)]
         got = ctx.nms(boxes, 0.5, 8)
         assert got.shape == want.shape and np.array_equal(_bits(got), _bits(want)), f"case {k}"
+
+
+def test_flip_feat_edges(ctx):
+    """Empty maps give an empty result; a channel count other than 31 is rejected (the reference's ORD table has 31)."""
+    import geye_gb300 as g
+    out = ctx.flip_feat(np.zeros((31, 0, 5), np.float32))
+    assert out.shape == (31, 0, 5)
+    with pytest.raises(g.GeyeError):
+        ctx.flip_feat(np.zeros((30, 4, 4), np.float32))
