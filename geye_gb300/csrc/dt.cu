@@ -323,10 +323,11 @@ __global__ void __launch_bounds__(kDtThreads) k_dt(const DtJob *__restrict__ job
       const bool wm = !J.samp_m || mpos, wi = !J.samp_i || ipos;
       const size_t o = (size_t)x * d0 + y;
       const int ix = g_s[l * n + x];
-      if (wm) M[o] = o_s[l * n + x];
+      if (wm) M[J.cm0 ? (size_t)((x - J.par_x) >> 1) * J.cm0 + ((y - J.par_y) >> 1) : o] = o_s[l * n + x];
       if (wi) {
-        Ix[o] = ix;
-        Iy[o] = tIy[(size_t)ix * d0 + y];
+        const size_t oi = J.ci0 ? (size_t)((x - 1 + J.par_x) >> 1) * J.ci0 + ((y - 1 + J.par_y) >> 1) : o;
+        Ix[oi] = ix;
+        Iy[oi] = tIy[(size_t)ix * d0 + y];
       }
     }
   }

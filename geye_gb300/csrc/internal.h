@@ -82,6 +82,10 @@ struct DtJob {             // one part map: DT of the negated map
   // parity in both), set when every probe falls inside the map
   int samp_m, samp_i;
   int par_y, par_x;
+  // sampled entries stored compactly: M of (x, y) in its class at
+  // ((x - par_x) / 2) * cm0 + (y - par_y) / 2, Ix/Iy likewise with the other
+  // parity and ci0 rows (cm0 / ci0 = the class's rows; 0: full layout)
+  int cm0, ci0;
 };
 
 struct ScoreJob {          // one (level, component) score map
@@ -104,6 +108,8 @@ struct ScoreJob {          // one (level, component) score map
   int ay[kMaxParts];
   int psize0[kMaxParts];   // part box size (component file)
   int psize1[kMaxParts];
+  int part_cm0[kMaxParts]; // DtJob.cm0 / ci0: the parts' compact layouts (0: full)
+  int part_ci0[kMaxParts];
 };
 
 // Root box of position (x, y) of a score map (get_boxes.cpp:227-235, pad = 0).

@@ -369,9 +369,6 @@ static geye_status build_model_plan(geye_ctx *ctx, Plan &P, geye_model *mdl, int
         D.d0 = d0; D.d1 = d1;
         D.tmpM_off = A.take((size_t)d0 * d1);
         D.tmpI_off = A.take((size_t)d0 * d1);
-        D.M_off = A.take((size_t)d0 * d1);
-        D.Ix_off = A.take((size_t)d0 * d1);
-        D.Iy_off = A.take((size_t)d0 * d1);
         D.ax = m.def[4 * di]; D.bx = m.def[4 * di + 1]; D.ay = m.def[4 * di + 2]; D.by = m.def[4 * di + 3];
         D.negate = 1;
         // the score sum reads M at (anchor_y + 2y, anchor_x + 2x) (dt.cpp:38-55); the
@@ -383,12 +380,21 @@ static geye_status build_model_plan(geye_ctx *ctx, Plan &P, geye_model *mdl, int
           const int ay0 = m.anchor[di * 2 + 1] - 1, ax0 = m.anchor[di * 2] - 1;
           D.samp_i = ay0 >= 0 && ax0 >= 0 && ay0 + 2 * (r0 - 1) < d0 && ax0 + 2 * (r1 - 1) < d1;
         }
+        // the sampled entries, stored compactly (a quarter of the map each)
+        const int qy = 1 - D.par_y, qx = 1 - D.par_x;
+        D.cm0 = (d0 - D.par_y + 1) >> 1;
+        D.ci0 = D.samp_i ? (d0 - qy + 1) >> 1 : 0;
+        D.M_off = A.take((size_t)D.cm0 * ((d1 - D.par_x + 1) >> 1));
+        const size_t ni = D.samp_i ? (size_t)D.ci0 * ((d1 - qx + 1) >> 1) : (size_t)d0 * d1;
+        D.Ix_off = A.take(ni);
+        D.Iy_off = A.take(ni);
         mp->dt_jobs.push_back(D);
         mp->dt_max_d0 = std::max(mp->dt_max_d0, d0);
         mp->dt_max_d1 = std::max(mp->dt_max_d1, d1);
         mp->dt_bytes += 16.0 * d0 * d1;
         S.part_M[k] = D.M_off; S.part_Ix[k] = D.Ix_off; S.part_Iy[k] = D.Iy_off;
         S.part_d0[k] = d0; S.part_d1[k] = d1;
+        S.part_cm0[k] = D.cm0; S.part_ci0[k] = D.ci0;
         S.ax[k] = m.anchor[di * 2] + 1;
         S.ay[k] = m.anchor[di * 2 + 1] + 1;
         S.psize0[k] = m.psize[c][2 * k];

@@ -32,7 +32,10 @@ __device__ __forceinline__ float assemble(const ScoreJob &J, const float *__rest
   float s = arena[J.root_off + i];
   s += J.off;
   for (int k = 0; k < J.np; k++) {
-    const int idx = (J.ay[k] + 2 * y - 1) + (J.ax[k] - 1 + 2 * x) * J.part_d0[k];
+    // M at (ax - 1 + 2x, ay - 1 + 2y); compact: its class entry ((ax - 1) / 2 + x, (ay - 1) / 2 + y)
+    const int cm0 = J.part_cm0[k];
+    const int idx = cm0 ? ((J.ax[k] - 1) / 2 + x) * cm0 + ((J.ay[k] - 1) / 2 + y)
+                        : (J.ay[k] + 2 * y - 1) + (J.ax[k] - 1 + 2 * x) * J.part_d0[k];
     s -= arena[J.part_M[k] + idx];
   }
   return s;
@@ -164,9 +167,14 @@ __global__ void __launch_bounds__(kScoreThreads) k_boxes(const ScoreJob *__restr
     for (int k = 0; k < J.np; k++) {
       const int probex = (x - 1) * 2 + J.ax[k];
       const int probey = (y - 1) * 2 + J.ay[k];
-      long Pi = probey + (long)probex * J.part_d0[k];
-      // the reference reads outside the map here (undefined); use entry 0 instead
-      if (Pi < 0 || Pi >= (long)J.part_d0[k] * J.part_d1[k]) Pi = 0;
+      long Pi;
+      if (const int ci0 = J.part_ci0[k]) {   // compact: every probe is inside and in the stored class
+        Pi = (long)(probex >> 1) * ci0 + (probey >> 1);
+      } else {
+        Pi = probey + (long)probex * J.part_d0[k];
+        // the reference reads outside the map here (undefined); use entry 0 instead
+        if (Pi < 0 || Pi >= (long)J.part_d0[k] * J.part_d1[k]) Pi = 0;
+      }
       const float px = (float)arena_i[J.part_Ix[k] + Pi] + 1.0f;   // an integer: exact
       const float py = (float)arena_i[J.part_Iy[k] + Pi] + 1.0f;
       const float q0 = (py * 0.5f) * scale;
