@@ -133,19 +133,19 @@ static void launch_cr(const ConvJob *d_jobs, int n_jobs, dim3 grid, const float 
   const size_t smem = conv_smem(max_b0, max_b1, G, CR);
   switch (G) {
     case 1:
-      cudaFuncSetAttribute(k_conv_fp32<1, CR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      { static SmemAttr a; raise_smem(a, k_conv_fp32<1, CR>, smem); }
       k_conv_fp32<1, CR><<<grid, kCThreads, smem, s>>>(d_jobs, filters, filt_off, arena_in, arena_out);
       break;
     case 2:
-      cudaFuncSetAttribute(k_conv_fp32<2, CR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      { static SmemAttr a; raise_smem(a, k_conv_fp32<2, CR>, smem); }
       k_conv_fp32<2, CR><<<grid, kCThreads, smem, s>>>(d_jobs, filters, filt_off, arena_in, arena_out);
       break;
     case 4:
-      cudaFuncSetAttribute(k_conv_fp32<4, CR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      { static SmemAttr a; raise_smem(a, k_conv_fp32<4, CR>, smem); }
       k_conv_fp32<4, CR><<<grid, kCThreads, smem, s>>>(d_jobs, filters, filt_off, arena_in, arena_out);
       break;
     default:
-      cudaFuncSetAttribute(k_conv_fp32<8, CR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      { static SmemAttr a; raise_smem(a, k_conv_fp32<8, CR>, smem); }
       k_conv_fp32<8, CR><<<grid, kCThreads, smem, s>>>(d_jobs, filters, filt_off, arena_in, arena_out);
       break;
   }

@@ -557,10 +557,12 @@ static void launch_conv_tc(int NQ, const TcJob *jobs, const int4 *chunks, int n_
                            const float *inv, const int2 *dims, const uint8_t *planes, const uint8_t *bank, float *out,
                            int *err, size_t smem, cudaStream_t s) {
   if (NQ == 4) {
-    cudaFuncSetAttribute(k_conv_tc<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    static SmemAttr a4;
+    raise_smem(a4, k_conv_tc<4>, smem);
     k_conv_tc<4><<<n_chunks, kTcThreads, smem, s>>>(jobs, chunks, outs, inv, dims, planes, bank, out, err);
   } else {
-    cudaFuncSetAttribute(k_conv_tc<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    static SmemAttr a2;
+    raise_smem(a2, k_conv_tc<2>, smem);
     k_conv_tc<2><<<n_chunks, kTcThreads, smem, s>>>(jobs, chunks, outs, inv, dims, planes, bank, out, err);
   }
 }

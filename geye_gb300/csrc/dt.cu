@@ -341,15 +341,9 @@ void launch_dt(const DtJob *d_jobs, int n_jobs, int max_d0, int max_d1, float *a
   size_t smem1 = 0, smem2 = 0;
   for (int n = 1; n <= max_d0; n++) smem1 = std::max(smem1, dt_smem_bytes(dt_lines1(n), n));
   for (int n = 1; n <= max_d1; n++) smem2 = std::max(smem2, dt_smem_bytes(1 << dt_lg_lines2(n), n));
-  static size_t set1 = 0, set2 = 0;
-  if (smem1 > set1) {
-    cudaFuncSetAttribute(k_dt<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem1);
-    set1 = smem1;
-  }
-  if (smem2 > set2) {
-    cudaFuncSetAttribute(k_dt<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem2);
-    set2 = smem2;
-  }
+  static SmemAttr a1, a2;
+  raise_smem(a1, k_dt<1>, smem1);
+  raise_smem(a2, k_dt<2>, smem2);
   k_dt<1><<<dim3((max_d1 + L1 - 1) / L1, n_jobs), kDtThreads, smem1, s>>>(d_jobs, arena, arena_i, fallback_count);
   k_dt<2><<<dim3((max_d0 + L2 - 1) / L2, n_jobs), kDtThreads, smem2, s>>>(d_jobs, arena, arena_i, fallback_count);
 }

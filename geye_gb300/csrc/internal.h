@@ -24,6 +24,26 @@ constexpr int kFeatPad = 32;    // channel stride in device feature buffers
 constexpr int kMaxParts = 32;   // parts per component supported by the kernels
 constexpr int kTcPlanePad = 128;   // cells after each bf16 feature plane (reach of a 128-position tile)
 
+// Raises a kernel's dynamic shared-memory limit to at least `smem` bytes on the
+// current device. The attribute belongs to the device, so the record of the largest
+// size set is kept per device; raises are serialised, so a concurrent smaller raise
+// never lowers a limit another thread's launch relies on.
+constexpr int kSmemAttrDevices = 64;
+struct SmemAttr {
+  size_t set[kSmemAttrDevices] = {};
+  std::mutex mu;
+};
+template <typename K>
+inline void raise_smem(SmemAttr &A, K *kernel, size_t smem) {
+  if (smem <= 48 * 1024) return;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  std::lock_guard<std::mutex> g(A.mu);
+  if (dev >= 0 && dev < kSmemAttrDevices && A.set[dev] >= smem) return;
+  cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (dev >= 0 && dev < kSmemAttrDevices) A.set[dev] = smem;
+}
+
 // ----------------------------------------------------------------------------
 // job descriptors (device-readable, plain structs)
 // ----------------------------------------------------------------------------

@@ -512,11 +512,8 @@ void launch_nms_sort(const float *boxes, const int *d_num, int n_models, int GL,
     k_qs_scatter<<<dim3(tiles, n_models), kNmsNT, 0, s>>>(l, cap, si, sf);
     k_qs_swap<<<dim3(tiles, n_models), kNmsNT, 0, s>>>(l, cap, si, sf, err);
   }
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(k_qs_small, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SmallSmem));
-    attr = true;
-  }
+  static SmemAttr attr;
+  raise_smem(attr, k_qs_small, sizeof(SmallSmem));
   k_qs_small<<<std::max(1, sms), kNmsNT, sizeof(SmallSmem), s>>>(n_models, cap, si, sf, err);
   k_qs_rest<<<n_models, kNmsNT, 0, s>>>(levels, cap, si, sf, err, diag);
 }

@@ -199,11 +199,8 @@ void launch_boxes(const ScoreJob *d_jobs, int n_jobs, int max_r, float thresh, c
   if (n_jobs <= 0) return;
   dim3 grid((max_r + kScoreThreads - 1) / kScoreThreads, n_jobs);
   const size_t smem = sizeof(float) * kScoreThreads * GL;
-  static size_t set = 0;
-  if (smem > set && smem > 48 * 1024) {
-    cudaFuncSetAttribute(k_boxes, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    set = smem;
-  }
+  static SmemAttr attr;
+  raise_smem(attr, k_boxes, smem);
   k_boxes<<<grid, kScoreThreads, smem, s>>>(d_jobs, thresh, arena, arena_i, block_offsets, stride, GL, boxes);
 }
 
@@ -270,11 +267,8 @@ void launch_ascore(const int *col, const int *row, int n_jobs, const float *aren
                   int im_h, float thresh, unsigned *max_bits, cudaStream_t s) {
   dim3 grid((im_h + kAsTile - 1) / kAsTile, (im_w + kAsTile - 1) / kAsTile);
   const size_t smem = sizeof(int) * 2 * kAsTile * (size_t)std::max(n_jobs, 1);
-  static size_t set = 0;
-  if (smem > 48 * 1024 && smem > set) {
-    cudaFuncSetAttribute(k_ascore, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    set = smem;
-  }
+  static SmemAttr attr;
+  raise_smem(attr, k_ascore, smem);
   k_ascore<<<grid, kAsTile * kAsTile, smem, s>>>(col, row, n_jobs, arena, a_score, im_w, im_h, thresh, max_bits);
 }
 
