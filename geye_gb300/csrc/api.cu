@@ -369,7 +369,7 @@ geye_status geye_detect_multi(geye_ctx *ctx, geye_model *const *models, int n_mo
                               geye_result *out) {
   ARG_CHECK(ctx && models && bgr && out, "null argument");
   ARG_CHECK(width >= 16 && height >= 16 && width_step >= 3 * width, "bad frame size");
-  for (int i = 0; i < n_models; i++) ARG_CHECK(models[i], "null model");
+  for (int i = 0; i < n_models; i++) MODEL_CHECK(models[i], ctx->device);
   CUDA_TRY(cudaSetDevice(ctx->device));
   Plan *P = nullptr;
   GEYE_TRY(frame_plan(ctx, models, n_models, width, height, &P));
@@ -407,6 +407,7 @@ geye_status geye_detect_device(geye_ctx *ctx, geye_model *const *models, int n_m
                                int width, int height, float thresh, float overlap) {
   ARG_CHECK(ctx && models && d_bgr, "null argument");
   ARG_CHECK(width >= 16 && height >= 16, "bad frame size");
+  for (int i = 0; i < n_models; i++) MODEL_CHECK(models[i], ctx->device);
   CUDA_TRY(cudaSetDevice(ctx->device));
   Plan *P = nullptr;
   GEYE_TRY(frame_plan(ctx, models, n_models, width, height, &P));

@@ -31,6 +31,14 @@
       return GEYE_ERR_ARG;     \
     }                          \
   } while (0)
+// a model's filters live on the device of the context that loaded it, and are freed
+// with that context: it runs only there, and only while that context lives
+#define MODEL_CHECK(m, dev)                                                          \
+  do {                                                                               \
+    ARG_CHECK((m), "null model");                                                    \
+    ARG_CHECK((m)->ctx, "the model's context was destroyed");                        \
+    ARG_CHECK((m)->ctx->device == (dev), "the model was loaded on another device");  \
+  } while (0)
 
 namespace geye {
 

@@ -142,7 +142,7 @@ geye_status geye_detect_submit(geye_ctx *ctx, geye_model *const *models, int n_m
   ARG_CHECK(ctx && models && bgr && n_models > 0, "null argument");
   ARG_CHECK(width >= 16 && height >= 16 && width_step >= 3 * width, "bad frame size");
   ARG_CHECK(!ctx->pending, "a submitted frame has not been collected");
-  for (int i = 0; i < n_models; i++) ARG_CHECK(models[i], "null model");
+  for (int i = 0; i < n_models; i++) MODEL_CHECK(models[i], ctx->device);
   CUDA_TRY(cudaSetDevice(ctx->device));
   Plan *P = nullptr;
   GEYE_TRY(frame_plan(ctx, models, n_models, width, height, &P));
@@ -333,7 +333,7 @@ geye_status geye_server_create(int device, geye_model *const *models, int n_mode
                                size_t hbm_budget, int max_slots, float thresh, float overlap, int track,
                                geye_server **out) {
   ARG_CHECK(out && models && n_models > 0 && max_slots > 0, "bad argument");
-  for (int i = 0; i < n_models; i++) ARG_CHECK(models[i], "null model");
+  for (int i = 0; i < n_models; i++) MODEL_CHECK(models[i], device);
   CUDA_TRY(cudaSetDevice(device));
   geye_server *s = new geye_server();
   s->device = device;
@@ -481,7 +481,7 @@ geye_status geye_batch_create(int device, geye_model *const *models, int n_model
   ARG_CHECK(models && n_models > 0 && n_models <= 16 && out, "bad argument");
   ARG_CHECK(max_frames >= 1 && max_frames <= 256, "max_frames must be in 1..256");
   ARG_CHECK(mode == GEYE_CONV_FP32 || mode == GEYE_CONV_BF16 || mode == GEYE_CONV_FP8, "unknown conv mode");
-  for (int i = 0; i < n_models; i++) ARG_CHECK(models[i], "null model");
+  for (int i = 0; i < n_models; i++) MODEL_CHECK(models[i], device);
   CUDA_TRY(cudaSetDevice(device));
   auto *b = new geye_batch();
   b->device = device;

@@ -193,6 +193,7 @@ geye_status geye_calc_feature(geye_ctx *ctx, const float *src, const int *isize,
 geye_status geye_calc_f_pyramid(geye_ctx *ctx, geye_model *model, const uint8_t *bgr, int width, int height,
                                 int width_step, int *n_levels, float **features, int **ftsize, float **scales) {
   ARG_CHECK(ctx && model && bgr && n_levels && features && ftsize && scales, "null argument");
+  MODEL_CHECK(model, ctx->device);
   ARG_CHECK(width >= 16 && height >= 16 && width_step >= 3 * width, "bad frame size");
   CUDA_TRY(cudaSetDevice(ctx->device));
   geye_model *ms[1] = {model};
@@ -243,6 +244,7 @@ geye_status geye_get_boxes(geye_ctx *ctx, geye_model *model, const float *featur
                            const int *ftsize, int n_levels, int img_width, int img_height, float thresh,
                            float *a_score, float **boxes, int *dnum) {
   ARG_CHECK(ctx && model && features && scales && ftsize && boxes && dnum, "null argument");
+  MODEL_CHECK(model, ctx->device);
   ARG_CHECK(n_levels > model->h.interval, "need more levels than the interval");
   CUDA_TRY(cudaSetDevice(ctx->device));
   Plan *P = nullptr;
@@ -329,6 +331,7 @@ geye_status geye_get_new_rects(geye_ctx *ctx, const geye_model *model, const flo
                                int img_height, geye_result *out) {
   ARG_CHECK(ctx && model && out, "null argument");
   ARG_CHECK(num >= 0, "num < 0");
+  MODEL_CHECK(model, ctx->device);
   memset(out, 0, sizeof(*out));
   const size_t k = std::max(num, 1);
   out->num = num;

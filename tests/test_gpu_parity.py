@@ -299,3 +299,19 @@ def test_nms_sort_levels_adapt_and_fall_back(tmp_path):
     for m in m1:
         m.close()
     c1.close()
+
+
+def test_model_of_destroyed_context_is_refused(car_paths):
+    """A model's filters are freed with the context that loaded it: detecting with
+    it afterwards is an argument error on the host, raised before any launch."""
+    import geye_gb300 as g
+    a = g.Context(0)
+    m = g.Model(a, *car_paths)
+    a.close()
+    frame = np.zeros((48, 64, 3), np.uint8)
+    with g.Context(0) as b:
+        with pytest.raises(g.GeyeError, match="destroyed"):
+            b.car_detection(frame, m)
+        with pytest.raises(g.GeyeError, match="destroyed"):
+            b.detect_multi(frame, [m])
+    m.close()
