@@ -374,6 +374,7 @@ geye_status geye_server_submit(geye_server *s, int stream, const uint8_t *bgr, i
   ARG_CHECK(s && bgr && ticket, "null argument");
   ARG_CHECK(width >= 16 && height >= 16 && width_step >= 3 * width, "bad frame size");
   ARG_CHECK(stream >= 0 && stream < kTrackerStreams, "stream id out of range");
+  for (geye_model *m : s->models) MODEL_CHECK(m, s->device);
   CUDA_TRY(cudaSetDevice(s->device));
   geye_server::Req r;
   r.ticket = s->next_ticket++;
@@ -443,6 +444,7 @@ geye_status geye_server_tracks(geye_server *s, int stream, int max, float *boxes
   ARG_CHECK(s && n && (max == 0 || boxes), "null argument");
   ARG_CHECK(s->track, "the server was created without trackers");
   ARG_CHECK(stream >= 0 && stream < kTrackerStreams, "stream id out of range");
+  for (geye_model *m : s->models) MODEL_CHECK(m, s->device);
   CUDA_TRY(cudaSetDevice(s->device));
   for (auto &sl : s->slots)
     if (sl.ctx) CUDA_TRY(cudaStreamSynchronize(sl.ctx->stream));
@@ -525,6 +527,7 @@ geye_status geye_batch_run(geye_batch *b, int n_frames, const uint8_t *const *bg
                            geye_result *results) {
   ARG_CHECK(b && bgr && widths && heights && width_steps && results, "null argument");
   ARG_CHECK(n_frames >= 1 && n_frames <= b->max_frames, "n_frames out of range");
+  for (geye_model *m : b->models) MODEL_CHECK(m, b->device);
   CUDA_TRY(cudaSetDevice(b->device));
   const int nm = (int)b->models.size();
   std::string key;
