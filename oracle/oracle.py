@@ -20,7 +20,10 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libdpm_oracle.so")
 REF_LIB_PATH = os.path.join(HERE, "_ref", "libgeye_ref.so")
-REF_SRC_DIR = os.environ.get("GEYE_REF_DIR", "/root/reference/CAR_TRACKING")
+# the reference's CAR_TRACKING sources: GEYE_REF_DIR, else a checkout named
+# "reference" beside this repository; absent on machines that only run the tests
+REF_SRC_DIR = os.environ.get("GEYE_REF_DIR") or os.path.normpath(
+    os.path.join(HERE, "..", "..", "reference", "CAR_TRACKING"))
 
 _fp = C.POINTER(C.c_float)
 _ip = C.POINTER(C.c_int)
@@ -516,6 +519,18 @@ def ref_nms_keep(boxes: np.ndarray, numpart0: int, overlap: float):
     keep = np.zeros(max(D, 1), np.int32)
     k = _R().ref_nms(_ptr(b), D, numpart0, C.c_float(overlap), _ptr(keep))
     return keep[:D].astype(bool), k
+
+
+def ref_load_model(comp: str, root: str, part: str) -> np.ndarray:
+    """Every field the reference's loader (load_model.cpp:57-530) parses from a CSV
+    triple, flattened in the order ref_load_model_dump (ref_glue.cpp) writes them."""
+    R = _R()
+    R.ref_load_model_dump.restype = C.c_int
+    R.ref_load_model_dump.argtypes = [C.c_char_p, C.c_char_p, C.c_char_p, C.c_void_p, C.c_int]
+    n = R.ref_load_model_dump(comp.encode(), root.encode(), part.encode(), None, 0)
+    out = np.zeros(n, np.float32)
+    R.ref_load_model_dump(comp.encode(), root.encode(), part.encode(), _ptr(out), n)
+    return out
 
 
 def ref_quicksort(vals: np.ndarray):

@@ -22,6 +22,10 @@ void calc_a_score(FLOAT *ac_score, FLOAT *score, int *ssize, int *rsize, Model_i
 FLOAT *nms(FLOAT *boxes, FLOAT overlap, int *num, MODEL *MO);                      /* nms.cpp:94 */
 void quickSort(FLOAT *ary, int *Order, int first_index, int last_index);          /* nms.cpp:70 */
 FLOAT *flip_feat(FLOAT *feat, int *size);                                          /* get_boxes.cpp:121 */
+Model_info *load_modelinfo(char *filename);                                        /* load_model.cpp:57 */
+Rootfilters *load_rootfilter(char *filename);                                      /* load_model.cpp:250 */
+Partfilters *load_partfilter(char *filename);                                      /* load_model.cpp:390 */
+extern int sum_size_def_array;                                                     /* load_model.cpp:25, set at :178 */
 
 extern "C" {
 
@@ -140,5 +144,61 @@ int ref_nms(float *boxes, int num, int numpart0, float overlap, int *keep)
 }
 
 void ref_quicksort(float *ary, int *order, int first, int last) { quickSort(ary, order, first, last); }
+
+/* Loads a model CSV triple with the reference's own loader functions and
+ * writes every parsed field, in a fixed order, into out[] as floats (the
+ * integers are small, so exact):
+ *   numcomponent sbin interval max_Y max_X padx pady
+ *   per component: ridx oidx offw rsize[0] rsize[1] numpart,
+ *                  then per part: pidx didx psize[0] psize[1]
+ *   DefL, def[4*DefL], anchor[2*DefL]
+ *   per component: x1[GL] y1[GL] x2[GL] y2[GL]   (GL = 1+2*(1+numpart))
+ *   NoR, per root: size[3] rootsym weights[size0*size1*size2]
+ *   NoP, per part: size[3] part_partner part_sym weights[...]
+ * Returns the number of floats (written only while below cap). */
+int ref_load_model_dump(const char *comp, const char *root, const char *part, float *out, int cap)
+{
+    Model_info *MI = load_modelinfo((char *)comp);
+    Rootfilters *RF = load_rootfilter((char *)root);
+    Partfilters *PF = load_partfilter((char *)part);
+    int n = 0;
+#define PUT(v) do { if (n < cap) out[n] = (float)(v); n++; } while (0)
+    PUT(MI->numcomponent); PUT(MI->sbin); PUT(MI->interval); PUT(MI->max_Y); PUT(MI->max_X);
+    PUT(MI->padx); PUT(MI->pady);
+    for (int c = 0; c < MI->numcomponent; c++) {
+        PUT(MI->ridx[c]); PUT(MI->oidx[c]); PUT(MI->offw[c]); PUT(MI->rsize[2 * c]); PUT(MI->rsize[2 * c + 1]);
+        PUT(MI->numpart[c]);
+        for (int k = 0; k < MI->numpart[c]; k++) {
+            PUT(MI->pidx[c][k]); PUT(MI->didx[c][k]); PUT(MI->psize[c][2 * k]); PUT(MI->psize[c][2 * k + 1]);
+        }
+    }
+    /* DefL is not kept in Model_info; the loader leaves 4*DefL floats' bytes in this global */
+    const int defl = sum_size_def_array / (int)(4 * sizeof(FLOAT));
+    PUT(defl);
+    for (int i = 0; i < 4 * defl; i++) PUT(MI->def[i]);
+    for (int i = 0; i < 2 * defl; i++) PUT(MI->anchor[i]);
+    for (int c = 0; c < MI->numcomponent; c++) {
+        const int GL = 1 + 2 * (1 + MI->numpart[c]);
+        for (int j = 0; j < GL; j++) PUT(MI->x1[c][j]);
+        for (int j = 0; j < GL; j++) PUT(MI->y1[c][j]);
+        for (int j = 0; j < GL; j++) PUT(MI->x2[c][j]);
+        for (int j = 0; j < GL; j++) PUT(MI->y2[c][j]);
+    }
+    PUT(RF->NoR);
+    for (int r = 0; r < RF->NoR; r++) {
+        const int *sz = RF->root_size[r];
+        PUT(sz[0]); PUT(sz[1]); PUT(sz[2]); PUT(RF->rootsym[r]);
+        for (int i = 0; i < sz[0] * sz[1] * sz[2]; i++) PUT(RF->rootfilter[r][i]);
+    }
+    PUT(PF->NoP);
+    for (int p = 0; p < PF->NoP; p++) {
+        const int *sz = PF->part_size[p];
+        PUT(sz[0]); PUT(sz[1]); PUT(sz[2]); PUT(PF->part_partner[p]); PUT(PF->part_sym[p]);
+        for (int i = 0; i < sz[0] * sz[1] * sz[2]; i++) PUT(PF->partfilter[p][i]);
+    }
+#undef PUT
+    /* the loader's allocations are left to the process: a test helper, called a few times */
+    return n;
+}
 
 }
