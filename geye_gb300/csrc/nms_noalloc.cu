@@ -18,9 +18,15 @@
 // Host code cannot use the array's name as a device address (there it names a
 // host-side stand-in), so the first call on each device, with that device
 // current, looks the address up with cudaGetSymbolAddress and caches it; make
-// that first call before any stream capture.
-#include <mutex>
+// that first call before any stream capture.  The cache is keyed on the
+// current CUDA context's unique id (cuCtxGetId), not on the device ordinal: a
+// context created after cudaDeviceReset, or a caller's own non-primary context
+// on the same device, has its own copy of the array at its own address, and
+// its first call looks that address up again.
+#include <cuda.h>
 
+#include <map>
+#include <mutex>
 #include <string>
 
 #include "runtime.h"
@@ -45,7 +51,38 @@ __global__ void k_noalloc_end(const int *counters, int *d_kept) {
 }
 
 std::mutex g_mu;
-float *g_base[128] = {};
+std::map<unsigned long long, float *> g_base;   // context id -> the array's device address there
+
+// the current context's unique id (making the device's primary context current
+// through the runtime when the thread has none yet).  The two driver calls are
+// looked up through the runtime, so the library keeps no link-time dependency
+// on the driver library (it loads on machines without a GPU driver).
+using CtxGetCurrentFn = CUresult (*)(CUcontext *);
+using CtxGetIdFn = CUresult (*)(CUcontext, unsigned long long *);
+geye_status current_context_id(unsigned long long *id) {
+  static CtxGetCurrentFn get_current = nullptr;
+  static CtxGetIdFn get_id = nullptr;
+  if (!get_current || !get_id) {
+    void *f1 = nullptr, *f2 = nullptr;
+    cudaDriverEntryPointQueryResult q1, q2;
+    // the driver ABI of CUDA 12.0, where cuCtxGetId first appeared
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 12000, cudaEnableDefault, &q1) != cudaSuccess ||
+        q1 != cudaDriverEntryPointSuccess ||
+        cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, &q2) != cudaSuccess ||
+        q2 != cudaDriverEntryPointSuccess)
+      return GEYE_ERR_CUDA;
+    get_current = reinterpret_cast<CtxGetCurrentFn>(f1);
+    get_id = reinterpret_cast<CtxGetIdFn>(f2);
+  }
+  CUcontext cur = nullptr;
+  if (get_current(&cur) != CUDA_SUCCESS) return GEYE_ERR_CUDA;
+  if (!cur) {
+    void *p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_nms_noalloc_scratch) != cudaSuccess) return GEYE_ERR_CUDA;
+    if (get_current(&cur) != CUDA_SUCCESS || !cur) return GEYE_ERR_CUDA;
+  }
+  return get_id(cur, id) == CUDA_SUCCESS ? GEYE_OK : GEYE_ERR_CUDA;
+}
 
 }  // namespace
 
@@ -60,25 +97,26 @@ extern "C" geye_status geye_nms_noalloc(const float *d_boxes, int num, int numpa
                     std::to_string(kMaxBoxes));
     return GEYE_ERR_ARG;
   }
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess || dev < 0 || dev >= 128) {
-    geye::set_error(std::string("geye_nms_noalloc: cudaGetDevice: ") + cudaGetErrorString(e));
+  unsigned long long ctx_id = 0;
+  std::lock_guard<std::mutex> lock(g_mu);
+  if (current_context_id(&ctx_id) != GEYE_OK) {
+    geye::set_error("geye_nms_noalloc: no usable CUDA context on the current device");
     return GEYE_ERR_CUDA;
   }
+  cudaError_t e = cudaSuccess;
   float *base = nullptr;
   {
-    std::lock_guard<std::mutex> lock(g_mu);
-    if (!g_base[dev]) {
+    auto it = g_base.find(ctx_id);
+    if (it == g_base.end()) {
       void *p = nullptr;
       e = cudaGetSymbolAddress(&p, g_nms_noalloc_scratch);
       if (e != cudaSuccess || !p) {
         geye::set_error(std::string("geye_nms_noalloc: cudaGetSymbolAddress: ") + cudaGetErrorString(e));
         return GEYE_ERR_CUDA;
       }
-      g_base[dev] = static_cast<float *>(p);
+      it = g_base.emplace(ctx_id, static_cast<float *>(p)).first;
     }
-    base = g_base[dev];
+    base = it->second;
   }
   cudaStream_t s = reinterpret_cast<cudaStream_t>(cuda_stream);
   float *scratch_f = base;

@@ -204,6 +204,11 @@ struct geye_server {
   geye::TrackerSet trk;
   std::map<int, cudaEvent_t> last_tracked;   // per stream: the event of its latest dispatched tracker update
   std::map<int, long long> stream_busy;      // per stream: frames dispatched and not finished
+  // admission (geye_server_set_admission): queued frames a stream may hold, the
+  // longest a frame may wait for a slot; 0 = no limit
+  int max_queued = 0;
+  long long max_wait_ns = 0;
+  long long dropped = 0;
 };
 
 namespace {
@@ -225,9 +230,28 @@ geye_status new_slot(geye_server *s, int *idx) {
   return GEYE_OK;
 }
 
+// a queued frame that will not run: reported by poll with dropped = 1 and empty results
+void drop_request(geye_server *s, const geye_server::Req &r) {
+  geye_server::Done d;
+  d.info = geye_served{};
+  d.info.ticket = r.ticket;
+  d.info.stream = r.stream;
+  d.info.queued_ns = now_ns() - r.t_submit;
+  d.info.latency_ns = d.info.queued_ns;
+  d.info.dropped = 1;
+  d.res.assign(s->models.size(), geye_result{});
+  s->done.push_back(std::move(d));
+  s->dropped++;
+}
+
 // dispatch the queue head into a slot; false when nothing fits right now
 geye_status dispatch_one(geye_server *s, bool *dispatched) {
   *dispatched = false;
+  // frames that waited past the limit are dropped rather than served late
+  while (s->max_wait_ns > 0 && !s->queue.empty() && now_ns() - s->queue.front().t_submit > s->max_wait_ns) {
+    drop_request(s, s->queue.front());
+    s->queue.pop_front();
+  }
   if (s->queue.empty()) return GEYE_OK;
   geye_server::Req &r = s->queue.front();
   int pick = -1;
@@ -275,6 +299,14 @@ geye_status dispatch_one(geye_server *s, bool *dispatched) {
 }
 
 geye_status pump(geye_server *s) {
+  // a model whose loading context was destroyed has freed filters: no queued
+  // frame can run any more, so every queued frame fails before any launch
+  for (geye_model *m : s->models)
+    if (!s->queue.empty() && (!m || !m->ctx || m->ctx->device != s->device)) {
+      for (const auto &r : s->queue) drop_request(s, r);
+      s->queue.clear();
+      MODEL_CHECK(m, s->device);
+    }
   for (;;) {
     bool d = false;
     GEYE_TRY(dispatch_one(s, &d));
@@ -287,6 +319,7 @@ geye_status complete(geye_server *s, geye_server::Slot &sl) {
   d.res.resize(s->models.size());
   GEYE_TRY(collect_frame(sl.ctx, d.res.data()));
   const long long t = now_ns();
+  d.info = geye_served{};
   d.info.ticket = sl.ticket;
   d.info.stream = sl.stream;
   d.info.queued_ns = sl.t_dispatch - sl.t_submit;
@@ -319,10 +352,10 @@ namespace geye {
 size_t plan_device_bytes(const Plan &P) {
   size_t b = P.arena.bytes + P.arena16.bytes + P.d_bgr.bytes + P.d_boxes.bytes + P.d_kept_boxes.bytes +
              P.d_nms_f.bytes + P.d_nms_i.bytes + P.d_small.bytes + P.d_ascore.bytes + P.d_result.bytes;
+  b += P.tc.d_bank.bytes + P.tc.d_jobs.bytes + P.tc.d_chunks.bytes + P.tc.d_cols.bytes + P.tc.d_sums.bytes;
   for (auto &mp : P.models)
     b += mp->d_root_jobs.bytes + mp->d_part_jobs.bytes + mp->d_dt_jobs.bytes + mp->d_score_jobs.bytes +
-         mp->d_counts.bytes + mp->d_tc_jobs.bytes + mp->d_tc_chunks.bytes + mp->d_tc_outs.bytes +
-         mp->d_tc_inv.bytes + mp->d_as_col.bytes + mp->d_as_row.bytes;
+         mp->d_counts.bytes + mp->d_as_col.bytes + mp->d_as_row.bytes;
   return b;
 }
 }  // namespace geye
@@ -387,8 +420,28 @@ geye_status geye_server_submit(geye_server *s, int stream, const uint8_t *bgr, i
     memcpy(r.bgr.data() + (size_t)y * 3 * width, bgr + (size_t)y * width_step, (size_t)3 * width);
   *ticket = r.ticket;
   s->queue.push_back(std::move(r));
+  if (s->max_queued > 0) {   // the stream's oldest queued frames make way for its newest
+    int n = 0;
+    for (const auto &q : s->queue) n += q.stream == stream;
+    for (auto it = s->queue.begin(); n > s->max_queued && it != s->queue.end();) {
+      if (it->stream == stream) {
+        drop_request(s, *it);
+        it = s->queue.erase(it);
+        n--;
+      } else {
+        ++it;
+      }
+    }
+  }
   GEYE_TRY(reap(s, false));
   return pump(s);
+}
+
+geye_status geye_server_set_admission(geye_server *s, int max_queued_per_stream, long long max_wait_ns) {
+  ARG_CHECK(s && max_queued_per_stream >= 0 && max_wait_ns >= 0, "bad argument");
+  s->max_queued = max_queued_per_stream;
+  s->max_wait_ns = max_wait_ns;
+  return GEYE_OK;
 }
 
 geye_status geye_server_poll(geye_server *s, int max, geye_served *info, geye_result *results, int *n) {
@@ -436,7 +489,7 @@ geye_status geye_server_stats(geye_server *s, long long out[8]) {
   out[4] = (long long)s->held;
   out[5] = s->completed;
   out[6] = s->track ? tracker_streams(s->trk) : 0;
-  out[7] = 0;
+  out[7] = s->dropped;
   return GEYE_OK;
 }
 

@@ -90,6 +90,7 @@ def lib(build_if_missing: bool = True):
             "geye_server_submit": [vp, i32, vp, i32, i32, i32, C.POINTER(C.c_longlong)],
             "geye_server_poll": [vp, i32, vp, vp, ip],
             "geye_server_drain": [vp],
+            "geye_server_set_admission": [vp, i32, C.c_longlong],
             "geye_server_stats": [vp, vp],
             "geye_server_tracks": [vp, i32, i32, vp, ip],
         }
@@ -406,7 +407,7 @@ class Context:
 
 class _Served(C.Structure):
     _fields_ = [("ticket", C.c_longlong), ("stream", C.c_int), ("n_tracks", C.c_int), ("queued_ns", C.c_longlong),
-                ("latency_ns", C.c_longlong)]
+                ("latency_ns", C.c_longlong), ("dropped", C.c_int), ("reserved", C.c_int)]
 
 
 class Server:
@@ -437,7 +438,7 @@ class Server:
         out = []
         for i in range(n.value):
             d = dict(ticket=info[i].ticket, stream=info[i].stream, n_tracks=info[i].n_tracks,
-                     queued_ns=info[i].queued_ns, latency_ns=info[i].latency_ns)
+                     queued_ns=info[i].queued_ns, latency_ns=info[i].latency_ns, dropped=bool(info[i].dropped))
             if with_results:
                 d["results"] = [_result_to_dict(res[i * self.n_models + m]) for m in range(self.n_models)]
             out.append(d)
@@ -446,11 +447,17 @@ class Server:
     def drain(self):
         _check(lib().geye_server_drain(self.h), "server_drain")
 
+    def set_admission(self, max_queued_per_stream: int = 0, max_wait_ms: float = 0.0):
+        """Per-stream queue cap (a newer frame drops the stream's oldest waiting one)
+        and the longest a frame may wait for a slot; 0 = no limit."""
+        _check(lib().geye_server_set_admission(self.h, max_queued_per_stream, int(max_wait_ms * 1e6)),
+               "server_set_admission")
+
     def stats(self) -> dict:
         o = np.zeros(8, np.int64)
         _check(lib().geye_server_stats(self.h, _p(o)), "server_stats")
-        keys = ["slots", "busy", "queued", "finished", "bytes_held", "completed", "tracked_streams"]
-        return dict(zip(keys, [int(v) for v in o[:7]]))
+        keys = ["slots", "busy", "queued", "finished", "bytes_held", "completed", "tracked_streams", "dropped"]
+        return dict(zip(keys, [int(v) for v in o]))
 
     def tracks(self, stream: int, max_tracks: int = 64) -> np.ndarray:
         b = np.zeros((max_tracks, 4), np.float32)

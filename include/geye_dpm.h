@@ -177,7 +177,10 @@ geye_status geye_fetch_result(geye_ctx *ctx, int model_index, geye_result *out, 
  * GEYE_ERR_ARG.  All calls share that array and it keeps the last call's
  * contents, so calls that overlap on the GPU race.  The first call on each
  * device looks up the array's device address (cudaGetSymbolAddress); make that
- * first call before any stream capture. */
+ * first call before any stream capture.  The address is remembered per CUDA
+ * context (its unique id), so after cudaDeviceReset, or in a caller's own
+ * non-primary context, the first call there looks it up again.
+ * On success *d_kept is the kept count (0 for num = 0). */
 #define GEYE_NMS_NOALLOC_MAX_BOXES 65536
 geye_status geye_nms_noalloc(const float *d_boxes, int num, int numpart0, float overlap, float *d_out,
                              int *d_kept, void *cuda_stream);
@@ -202,13 +205,16 @@ geye_status geye_detect_collect(geye_ctx *ctx, geye_result *out);
  * different resolutions and streams overlap on the GPU.  Each stream's frames
  * are dispatched in submission order.  When track is nonzero every stream
  * keeps a device-resident particle-filter tracker fed with its detections. */
-typedef struct geye_server geye_server;
+typedef struct geye_server geye_server;   /* the models must outlive the server */
 typedef struct {
     long long ticket;        /* from geye_server_submit                         */
     int stream;              /* camera stream id                                */
     int n_tracks;            /* live tracks of the stream after this frame      */
     long long queued_ns;     /* submit -> dispatch to a slot                     */
     long long latency_ns;    /* submit -> results on the host                    */
+    int dropped;             /* 1: never run (admission limit, or its model's
+                                context was destroyed); its results are empty  */
+    int reserved;
 } geye_served;
 geye_status geye_server_create(int device, geye_model *const *models, int n_models, geye_conv_mode mode,
                                size_t hbm_budget, int max_slots, float thresh, float overlap, int track,
@@ -223,8 +229,18 @@ geye_status geye_server_submit(geye_server *s, int stream, const uint8_t *bgr, i
 geye_status geye_server_poll(geye_server *s, int max, geye_served *info, geye_result *results, int *n);
 /* Blocks until every submitted frame has finished (collect them with poll). */
 geye_status geye_server_drain(geye_server *s);
+/* Latency-aware admission, for cameras that together offer more frames than the
+ * GPU serves: a stream holds at most max_queued_per_stream frames waiting for a
+ * slot (a newer frame drops the stream's oldest waiting one), and a frame that
+ * has waited more than max_wait_ns for a slot is dropped instead of run.  0 turns
+ * a limit off (the default: every frame is served).  Dropped frames come back
+ * from poll with dropped = 1 and empty results.  Before any launch, every
+ * submit and poll also drops all waiting frames and returns GEYE_ERR_ARG when a
+ * model's loading context has been destroyed; models must outlive the server. */
+geye_status geye_server_set_admission(geye_server *s, int max_queued_per_stream, long long max_wait_ns);
 /* out[0..7]: slots, busy slots, queued frames, finished not yet polled,
- * device bytes held by slots, frames completed, streams with trackers, 0. */
+ * device bytes held by slots, frames completed, streams with trackers,
+ * frames dropped. */
 geye_status geye_server_stats(geye_server *s, long long out[8]);
 /* Copies stream `stream`'s live tracks (up to max) as x1, y1, x2, y2 floats into
  * boxes[4*i]; *n = count. */
@@ -238,7 +254,7 @@ geye_status geye_server_tracks(geye_server *s, int stream, int max, float *boxes
  * frames into the lanes' pinned buffers, launches the graph, waits, and fills
  * results[i * n_models + m] (free each with geye_result_free); every result is
  * the one geye_detect_multi gives for that frame alone. */
-typedef struct geye_batch geye_batch;
+typedef struct geye_batch geye_batch;     /* the models must outlive the batch */
 geye_status geye_batch_create(int device, geye_model *const *models, int n_models, geye_conv_mode mode,
                               int max_frames, geye_batch **out);
 geye_status geye_batch_destroy(geye_batch *b);

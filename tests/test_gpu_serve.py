@@ -128,3 +128,54 @@ def test_batch_graph_matches_single_frames(tmp_path, conv):
             assert st["lanes"] == len(frames) and st["graphs"] == 1 and st["kernels"] > 0 and st["last_ms"] > 0
         for m in ms:
             m.close()
+
+
+def test_server_per_stream_queue_cap_drops_stale_frames(tmp_path):
+    """One slot, FP32 1080p frames (several ms each): frames of one stream
+    submitted while the slot is busy replace each other in the queue; the first
+    and the newest are served, the ones in between come back dropped."""
+    import geye_gb300 as g
+    from geye_gb300 import synth
+    with g.Context(0) as c:
+        ms = [g.Model(c, *synth.write_model_csv(synth.CAR_SPEC, str(tmp_path)))]
+        frames = [synth.make_frame(1920, 1080, seed=70 + k) for k in range(5)]
+        with g.Server(ms, conv=g.CONV_FP32, max_slots=1) as srv:
+            srv.set_admission(max_queued_per_stream=1)
+            tickets = [srv.submit(0, f) for f in frames]
+            srv.drain()
+            done = {d["ticket"]: d for d in srv.poll(16)}
+            assert sorted(done) == tickets
+            assert not done[tickets[0]]["dropped"] and not done[tickets[-1]]["dropped"]
+            dropped = [t for t in tickets if done[t]["dropped"]]
+            assert 1 <= len(dropped) <= 3 and srv.stats()["dropped"] == len(dropped)
+            for t in dropped:
+                assert all(r["num"] == 0 for r in done[t]["results"])
+            alone = c.detect_multi(frames[-1], ms, -0.5, 0.5, None)
+            assert same(done[tickets[-1]]["results"], alone)
+        for m in ms:
+            m.close()
+
+
+def test_server_refuses_queued_frames_once_a_models_context_is_gone(tmp_path):
+    """Destroying the context that loaded a model frees its filters: queued frames
+    are dropped and the call reports GEYE_ERR_ARG before anything is launched;
+    the frame already on the GPU finishes first (the destroy waits for it)."""
+    import geye_gb300 as g
+    from geye_gb300 import synth
+    load = g.Context(0)
+    ms = [g.Model(load, *synth.write_model_csv(synth.CAR_SPEC, str(tmp_path)))]
+    frames = [synth.make_frame(1920, 1080, seed=80 + k) for k in range(4)]
+    with g.Server(ms, conv=g.CONV_FP32, max_slots=1) as srv:
+        tickets = [srv.submit(0, f) for f in frames]
+        queued = srv.stats()["queued"]
+        load.close()
+        if queued:
+            with pytest.raises(g.GeyeError):
+                srv.poll(16)
+        done = {d["ticket"]: d for d in srv.poll(16)}
+        srv.drain()
+        done.update({d["ticket"]: d for d in srv.poll(16)})
+        assert sorted(done) == tickets
+        assert sum(d["dropped"] for d in done.values()) == queued >= 1
+        with pytest.raises(g.GeyeError):
+            srv.submit(0, frames[0])
