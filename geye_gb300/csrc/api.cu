@@ -93,14 +93,15 @@ geye_status geye_ctx_destroy(geye_ctx *ctx) {
   if (!ctx) return GEYE_OK;
   cudaSetDevice(ctx->device);
   cudaStreamSynchronize(ctx->stream);
+  // the models loaded here may be read by other contexts' work in flight (server
+  // slots, batch lanes): wait for the device before their filters are freed
+  if (!ctx->models.empty()) cudaDeviceSynchronize();
   ctx->plans.clear();
   for (geye_model *m : ctx->models) {
     if (m->d_filters) cudaFree(m->d_filters);
     if (m->d_filt_off) cudaFree(m->d_filt_off);
     if (m->d_coef) cudaFree(m->d_coef);
-    if (m->d_bank16) cudaFree(m->d_bank16);
-    if (m->d_bank8) cudaFree(m->d_bank8);
-    m->d_filters = nullptr; m->d_filt_off = nullptr; m->d_coef = nullptr; m->d_bank16 = nullptr; m->d_bank8 = nullptr;
+    m->d_filters = nullptr; m->d_filt_off = nullptr; m->d_coef = nullptr;
     m->ctx = nullptr;
   }
   ctx->models.clear();
@@ -276,8 +277,6 @@ geye_status geye_model_free(geye_model *m) {
   if (m->d_filters) cudaFree(m->d_filters);
   if (m->d_filt_off) cudaFree(m->d_filt_off);
   if (m->d_coef) cudaFree(m->d_coef);
-  if (m->d_bank16) cudaFree(m->d_bank16);
-  if (m->d_bank8) cudaFree(m->d_bank8);
   delete m;
   return GEYE_OK;
 }

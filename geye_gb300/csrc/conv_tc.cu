@@ -13,25 +13,35 @@
 // positions p is the slab rows p + xp*fs0 + yp of the staged planes: one
 // shared-memory descriptor per tap, LBO = the plane stride (next chunk of
 // channels), SBO = 128 B (next 8 rows).  An MMA takes two planes (K = 16 bf16
-// or 32 e4m3), so a tap is 2 MMAs in BF16 and 1 in FP8.  Positions whose
-// window crosses a column edge are computed and discarded ((b0-1)/fs0 of the work).
+// or 32 e4m3), so a tap is 2 MMAs in BF16 and 1 in FP8.
 //
-// B (the filters) is precomputed per model as [tap][q][n][16 B] (N padded to 16
-// or 32), one descriptor per (tap, plane pair) as well.  FP8 filters are scaled
-// per filter by the power of two that brings their absolute maximum under 448;
-// the epilogue multiplies by the exact inverse of both scales.
+// One launch covers every model of a plan.  The filters of all models share
+// one bank [tap][q][row][16 B] over one tap grid (the largest part filter):
+// each part filter is a row (zero weights around it in the grid), and each
+// root filter is cut into blocks of the grid, one row per block.  A level's
+// job multiplies its feature planes by every row the level uses in one MMA
+// chain (N = all of them), so the root filters cost no extra pass over the
+// features: block (a, b) of a root, evaluated at position p + a*gx*fs0 + b*gy,
+// is that root's partial sum over the block's taps, and k_root_sum adds a
+// root's blocks back into its map.  In BF16 mode the root blocks run on split
+// operands: the features' BF16 remainder planes (f - bf16(f)) and each block's
+// BF16 remainder row (w - bf16(w)) add the products hi*lo and lo*hi to hi*hi
+// (a second MMA chain accumulates lo*hi into the same TMEM columns), about 16
+// significant bits per operand for the roots, whose rounding decides most
+// detections; part filters stay plain BF16.
 //
-// A CTA (4 warps) owns a run of up to 16 tiles of 128 positions of one (level,
-// filter group), each tile with its own TMEM accumulator.  The filter is walked
-// in column phases whose bank columns and feature slab fit in shared memory:
-// one thread bulk-copies them (cp.async.bulk, completion on an mbarrier); one
-// thread per warp issues the MMAs of every fourth tile (each tile's chain from
-// one thread, in order) and commits them to a second mbarrier that expects the
-// four warps' commits; after the last
-// phase the four warps read the accumulators with tcgen05.ld (warp w owns TMEM
-// lanes 32w..32w+31) and write the maps in the reference layout.  Every
-// mbarrier wait is bounded; a timeout sets an error bit and the CTA still
-// waits (bounded) for its own copies and MMAs before it frees TMEM and leaves.
+// A CTA (4 warps) owns a run of up to 8 tiles of 128 positions of one job, each
+// tile with its own TMEM accumulator.  The run's feature slab stays in shared
+// memory while the bank streams through a ring of stages, one tap per stage:
+// lane 0 of warp 0 bulk-copies (cp.async.bulk, mbarrier completion), lane 0
+// of warp 1 issues the tap's MMAs for every tile and commits them to the
+// stage's "free" mbarrier, so the copy of tap t+stages overlaps the MMAs of
+// tap t.  Grids wider than the slab allows are walked in column phases (the
+// slab reloaded per phase).  After the last MMA the four warps read the
+// accumulators with tcgen05.ld (warp w owns TMEM lanes 32w..32w+31) and write
+// part maps in the reference layout and root blocks by position.  Every
+// mbarrier wait is bounded; a timeout sets an error bit, and the CTA waits
+// (bounded) for its own copies and MMAs before it frees TMEM and leaves.
 #include <stdint.h>
 #include <stdlib.h>
 #include <string.h>
@@ -49,24 +59,17 @@ namespace geye {
 
 constexpr int kTcThreads = 128;
 constexpr int kTcM = 128;                        // positions per tile (TMEM lanes)
-constexpr int kTcMaxTiles = 16;                  // tiles per CTA, at most
-constexpr size_t kTcSmemBudget = 220 * 1024;     // dynamic shared memory per CTA, at most
-constexpr int kTcMaxN = 64;                      // filters per group, at most (N of an MMA)
-constexpr int kTcHead = 1152;                    // barriers, TMEM address, map offsets, scales, map dims
-constexpr int kTcTmemCols = 512;                 // tiles per CTA x n_pad, at most
+constexpr int kTcMaxTiles = 8;                   // tiles per CTA, at most
+constexpr int kTcMaxStages = 8;                  // bank stages in the ring, at most
+constexpr int kTcHead = 256;                     // mbarriers and the TMEM address
+constexpr int kTcMaxN = 256;                     // N of an MMA, at most
+constexpr int kTcTmemCols = 512;                 // tiles per CTA x N, at most
 constexpr unsigned long long kWaitNs = 1000000000ull;   // a wait gives up after 1 s (then 4 s for the drain)
 
-struct TcJob {
-  int plane_off;     // offset of plane 0 in arena16, in 2-byte units
-  int plane_cells;   // cells per plane
-  int fs0, fs1;      // feature rows, columns
-  int b0, b1;        // filter rows, columns
-  int c0, c1;        // output rows, columns computed (those of the group's smallest filter)
-  int n, n_pad;      // filters; padded to 16 or 32
-  int bank_off;      // byte offset of the group's bank in the model's bank buffer
-  int out_tab;       // first entry of the job's map offsets
-  int ntiles;        // 128-position tiles up to the last valid output
-};
+// mbarriers in the head: slab landed, slab free, all MMAs done, then per stage
+// "landed" and "free"
+constexpr int kBarSlabFull = 0, kBarSlabFree = 1, kBarDone = 2, kBarStageFull = 3,
+              kBarStageFree = 3 + kTcMaxStages;
 
 // ---------------------------------------------------------------------------
 // PTX wrappers
@@ -168,43 +171,34 @@ __host__ __device__ constexpr uint32_t idesc_e4m3(int M, int N) {
 // ---------------------------------------------------------------------------
 // kernel
 // ---------------------------------------------------------------------------
+// Chunk (job, first tile, tiles, tap columns per phase) -> one CTA.
 template <int NQ>
-__global__ void __launch_bounds__(kTcThreads, 1) k_conv_tc(const TcJob *__restrict__ jobs, const int4 *__restrict__ chunks,
-                                                           const int *__restrict__ outs,
-                                                           const float *__restrict__ inv_scale,
-                                                           const int2 *__restrict__ out_dims,
-                                                           const uint8_t *__restrict__ arena16,
-                                                           const uint8_t *__restrict__ bank, float *__restrict__ arena,
-                                                           int *err) {
+__global__ void __launch_bounds__(kTcThreads, 1)
+    k_conv_tc(const TcJob *__restrict__ jobs, const int4 *__restrict__ chunks, const TcCol *__restrict__ cols,
+              const uint8_t *__restrict__ arena16, const uint8_t *__restrict__ bank, int bank_rows, int n_stages,
+              float *__restrict__ arena, int *err) {
   extern __shared__ __align__(128) uint8_t sm[];
-  uint64_t *bar_load = reinterpret_cast<uint64_t *>(sm);
-  uint64_t *bar_mma = reinterpret_cast<uint64_t *>(sm + 8);
-  uint32_t *tslot = reinterpret_cast<uint32_t *>(sm + 16);
-  int *out_s = reinterpret_cast<int *>(sm + 32);       // the job's map offsets (n <= kTcMaxN)
-  float *scl_s = reinterpret_cast<float *>(sm + 288);   // and output scales
-  int2 *dim_s = reinterpret_cast<int2 *>(sm + 544);     // and each map's rows, columns
+  uint64_t *bar = reinterpret_cast<uint64_t *>(sm);
+  uint32_t *tslot = reinterpret_cast<uint32_t *>(sm + 8 * (3 + 2 * kTcMaxStages));
   const int4 ch = chunks[blockIdx.x];
   const TcJob J = jobs[ch.x];
-  const int tile0 = ch.y, ntile = ch.z, cs = ch.w;   // cs = filter columns per phase
-  if (threadIdx.x < J.n) {
-    out_s[threadIdx.x] = outs[J.out_tab + threadIdx.x];
-    scl_s[threadIdx.x] = inv_scale[J.out_tab + threadIdx.x];
-    dim_s[threadIdx.x] = out_dims[J.out_tab + threadIdx.x];
-  }
+  const int tile0 = ch.y, ntile = ch.z, cs = ch.w;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int NS = n_stages;
   const int p_begin = tile0 * kTcM;
-  const uint32_t bq = (uint32_t)J.n_pad * 16u;                 // one (tap, q) slice of the bank
-  const uint32_t col_bytes = (uint32_t)J.b0 * NQ * bq;         // one filter column of the bank
-  const uint32_t bank_room = ((uint32_t)cs * col_bytes + 127u) & ~127u;
-  uint8_t *sB = sm + kTcHead;
-  uint8_t *sA = sB + bank_room;
-  // accumulators: tile i at TMEM columns i*n_pad .. i*n_pad + n_pad - 1
+  const int S = ntile * kTcM + (cs - 1) * J.fs0 + (J.b0 - 1);   // slab cells per plane
+  const uint32_t plane_bytes = (uint32_t)S * 16u;
+  const bool split = J.n_lo > 0;
+  uint8_t *slab = sm + kTcHead;
+  uint8_t *slab_lo = slab + (size_t)NQ * plane_bytes;
+  const size_t slab_end = kTcHead + (size_t)NQ * plane_bytes * (split ? 2 : 1);
+  uint8_t *stages = sm + ((slab_end + 127) & ~(size_t)127);
+  const uint32_t stage_bytes = (uint32_t)NQ * (uint32_t)J.n * 16u;
   uint32_t ncols = 32;
-  while (ncols < (uint32_t)(ntile * J.n_pad)) ncols <<= 1;
+  while (ncols < (uint32_t)(ntile * J.n)) ncols <<= 1;
 
   if (threadIdx.x == 0) {
-    mbar_init(bar_load, 1);
-    mbar_init(bar_mma, kTcThreads / 32);   // one commit per issuing warp
+    for (int i = 0; i < 3 + 2 * kTcMaxStages; i++) mbar_init(&bar[i], 1);
     mbar_fence_init();
   }
   if (warp == 0) tmem_alloc(tslot, ncols);
@@ -212,82 +206,135 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_conv_tc(const TcJob *__restri
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = *tslot;
-
-  const uint32_t idesc = NQ == 4 ? idesc_bf16(kTcM, J.n_pad) : idesc_e4m3(kTcM, J.n_pad);
-  const uint32_t sA_addr = smem_u32(sA), sB_addr = smem_u32(sB);
   const int phases = (J.b1 + cs - 1) / cs;
-  bool ok = true;   // uniform across the CTA (every wait outcome is combined with __syncthreads_and)
-  for (int ph = 0; ph < phases && ok; ph++) {
-    const int xp0 = ph * cs, ncol = min(cs, J.b1 - xp0);
-    const int S = ntile * kTcM + (ncol - 1) * J.fs0 + (J.b0 - 1);   // slab cells per plane this phase
-    const uint32_t plane_bytes = (uint32_t)S * 16u;
-    if (threadIdx.x == 0) {
-      mbar_expect_tx(bar_load, (uint32_t)ncol * col_bytes + NQ * plane_bytes);
-      bulk_g2s(sB, bank + J.bank_off + (size_t)xp0 * col_bytes, (uint32_t)ncol * col_bytes, bar_load);
+  bool ok = true;
+
+  if (warp == 0 && lane == 0) {
+    // ---- producer: the phase's slab, then one bank tap per stage
+    int issued = 0, slabs = 0;
+    for (int ph = 0; ph < phases && ok; ph++) {
+      const int xp0 = ph * cs, ncol = min(cs, J.b1 - xp0);
+      if (ph > 0 && !mbar_wait(&bar[kBarSlabFree], (uint32_t)((ph - 1) & 1), kWaitNs)) { ok = false; break; }
+      mbar_expect_tx(&bar[kBarSlabFull], (uint32_t)NQ * plane_bytes * (split ? 2u : 1u));
+      const size_t cell0 = (size_t)p_begin + (size_t)xp0 * J.fs0;
       for (int q = 0; q < NQ; q++)
-        bulk_g2s(sA + (size_t)q * plane_bytes,
-                 arena16 + 2 * (size_t)J.plane_off +
-                     ((size_t)q * J.plane_cells + (size_t)p_begin + (size_t)xp0 * J.fs0) * 16,
-                 plane_bytes, bar_load);
-    }
-    bool landed = mbar_wait(bar_load, (uint32_t)(ph & 1), kWaitNs);
-    if (!landed) {
-      atomicOr(err, 1);
-      mbar_wait(bar_load, (uint32_t)(ph & 1), 4 * kWaitNs);   // the copies must land before the CTA leaves
-    }
-    ok = __syncthreads_and(landed);
-    if (!ok) break;
-    if (lane == 0) {   // one issuing thread per warp: tiles warp, warp + 4, ... (each tile's chain in order)
-      tc_fence_after();
-      // The start-address field of a descriptor is (address >> 4) in its low 14 bits and
-      // every operand lies below 2^18 bytes, so moving an operand by a 16-byte multiple off
-      // is adding off >> 4 to the descriptor: A moves by cells (16 B), B by (tap, q) slices.
-      const uint64_t a_base = sdesc(sA_addr, plane_bytes, 128u);
-      const uint64_t b_base = sdesc(sB_addr, bq, 128u);
-      const uint32_t a_hi = 2u * (uint32_t)S;           // planes 2, 3: 2 * plane_bytes >> 4
-      const uint32_t b_tap = NQ * (uint32_t)J.n_pad;    // one tap of the bank: NQ * bq >> 4
-      const uint32_t b_hi = 2u * (uint32_t)J.n_pad;     // planes 2, 3 of a tap
-      for (int i = warp; i < ntile; i += kTcThreads / 32) {
-        const uint32_t d = tmem + (uint32_t)(i * J.n_pad);
-        uint32_t acc = ph ? 1u : 0u;
-        for (int xp = 0; xp < ncol; xp++) {
-          const uint32_t cell0 = (uint32_t)(i * kTcM + xp * J.fs0);
-          const uint32_t tap0 = (uint32_t)(xp * J.b0) * b_tap;
-          for (int yp = 0; yp < J.b0; yp++) {
-            const uint64_t ad = a_base + (cell0 + (uint32_t)yp);
-            const uint64_t bd = b_base + (tap0 + (uint32_t)yp * b_tap);
-            tc_mma<NQ>(d, ad, bd, idesc, acc);
-            if constexpr (NQ == 4) tc_mma<NQ>(d, ad + a_hi, bd + b_hi, idesc, 1u);
-            acc = 1u;
+        bulk_g2s(slab + (size_t)q * plane_bytes,
+                 arena16 + 2 * (size_t)J.plane_off + ((size_t)q * J.plane_cells + cell0) * 16, plane_bytes,
+                 &bar[kBarSlabFull]);
+      if (split)
+        for (int q = 0; q < NQ; q++)
+          bulk_g2s(slab_lo + (size_t)q * plane_bytes,
+                   arena16 + 2 * (size_t)J.lo_off + ((size_t)q * J.plane_cells + cell0) * 16, plane_bytes,
+                   &bar[kBarSlabFull]);
+      slabs++;
+      for (int xp = xp0; xp < xp0 + ncol && ok; xp++)
+        for (int yp = 0; yp < J.b0; yp++) {
+          const int s = issued % NS;
+          if (issued >= NS && !mbar_wait(&bar[kBarStageFree + s], (uint32_t)((issued / NS - 1) & 1), kWaitNs)) {
+            ok = false;
+            break;
           }
+          const int t = xp * J.b0 + yp;
+          uint8_t *dst = stages + (size_t)s * stage_bytes;
+          mbar_expect_tx(&bar[kBarStageFull + s], stage_bytes);
+          for (int q = 0; q < NQ; q++)
+            bulk_g2s(dst + (size_t)q * J.n * 16, bank + ((size_t)(t * NQ + q) * bank_rows + J.row0) * 16,
+                     (uint32_t)J.n * 16u, &bar[kBarStageFull + s]);
+          issued++;
         }
+    }
+    if (!ok) {
+      atomicOr(err, 1);
+      // every copy issued lands before the CTA leaves
+      if (slabs) mbar_wait(&bar[kBarSlabFull], (uint32_t)((slabs - 1) & 1), 4 * kWaitNs);
+      for (int s = 0; s < NS && s < issued; s++) {
+        const int last = issued - 1 - ((issued - 1 - s) % NS);
+        mbar_wait(&bar[kBarStageFull + s], (uint32_t)((last / NS) & 1), 4 * kWaitNs);
       }
-      tc_commit(bar_mma);   // tracks this thread's MMAs (an immediate arrive if it issued none)
     }
-    bool done = mbar_wait(bar_mma, (uint32_t)(ph & 1), kWaitNs);
-    if (!done) {
-      atomicOr(err, 2);
-      mbar_wait(bar_mma, (uint32_t)(ph & 1), 4 * kWaitNs);   // the MMAs must finish before smem or TMEM is reused
+  } else if (warp == 1 && lane == 0) {
+    // ---- MMA issue: per tap, every tile's chain (and the split chain of the root blocks)
+    // The start-address field of a descriptor is (address >> 4) in its low 14 bits and
+    // every operand lies below 2^18 bytes, so moving an operand by a 16-byte multiple off
+    // is adding off >> 4 to the descriptor: A moves by cells (16 B), B by rows (16 B).
+    const uint32_t idesc = NQ == 4 ? idesc_bf16(kTcM, J.n) : idesc_e4m3(kTcM, J.n);
+    const uint32_t idesc_lo = idesc_bf16(kTcM, split ? J.n_lo : 16);
+    const uint64_t a_base = sdesc(smem_u32(slab), plane_bytes, 128u);
+    const uint64_t alo_base = sdesc(smem_u32(slab_lo), plane_bytes, 128u);
+    const uint32_t a_k1 = 2u * (uint32_t)S;     // planes 2, 3: 2 * plane_bytes >> 4
+    const uint32_t b_k1 = 2u * (uint32_t)J.n;   // planes 2, 3 of a stage
+    int used = 0;
+    for (int ph = 0; ph < phases && ok; ph++) {
+      const int xp0 = ph * cs, ncol = min(cs, J.b1 - xp0);
+      if (!mbar_wait(&bar[kBarSlabFull], (uint32_t)(ph & 1), kWaitNs)) { ok = false; break; }
+      for (int xp = xp0; xp < xp0 + ncol && ok; xp++)
+        for (int yp = 0; yp < J.b0; yp++) {
+          const int s = used % NS;
+          if (!mbar_wait(&bar[kBarStageFull + s], (uint32_t)((used / NS) & 1), kWaitNs)) { ok = false; break; }
+          tc_fence_after();
+          const uint64_t b_base = sdesc(smem_u32(stages + (size_t)s * stage_bytes), (uint32_t)J.n * 16u, 128u);
+          const uint32_t acc = (xp > 0 || yp > 0) ? 1u : 0u;
+          const uint32_t shift = (uint32_t)((xp - xp0) * J.fs0 + yp);
+          for (int i = 0; i < ntile; i++) {
+            const uint32_t d = tmem + (uint32_t)(i * J.n);
+            const uint64_t ad = a_base + ((uint32_t)(i * kTcM) + shift);
+            tc_mma<NQ>(d, ad, b_base, idesc, acc);
+            if constexpr (NQ == 4) {
+              tc_mma<NQ>(d, ad + a_k1, b_base + b_k1, idesc, 1u);
+              if (split) {
+                const uint64_t al = alo_base + ((uint32_t)(i * kTcM) + shift);
+                const uint64_t bl = b_base + (uint32_t)J.lo_row;
+                tc_mma<NQ>(d + (uint32_t)J.lo_row, al, bl, idesc_lo, 1u);
+                tc_mma<NQ>(d + (uint32_t)J.lo_row, al + a_k1, bl + b_k1, idesc_lo, 1u);
+              }
+            }
+          }
+          tc_commit(&bar[kBarStageFree + s]);   // the stage is free once these MMAs are done
+          used++;
+        }
+      tc_commit(&bar[kBarSlabFree]);   // and the slab once the phase's MMAs are
     }
-    ok = __syncthreads_and(done);
+    if (!ok) atomicOr(err, 2);
+    tc_commit(&bar[kBarDone]);   // tracks every MMA issued above
   }
+  __syncthreads();
+  bool done = mbar_wait(&bar[kBarDone], 0u, kWaitNs);
+  if (!done) {
+    atomicOr(err, 4);
+    mbar_wait(&bar[kBarDone], 0u, 4 * kWaitNs);   // the MMAs must finish before TMEM is read or freed
+  }
+  ok = __syncthreads_and(done && ok);
   tc_fence_after();
-  // epilogue: row r of a tile is TMEM lane r; this thread owns row 32*warp + lane of every tile
+  // ---- epilogue: row r of a tile is TMEM lane r; this thread owns row 32*warp + lane of every tile
+  const int ncell = J.fs0 * J.fs1;
   for (int i = 0; i < ntile; i++) {
     const int p = p_begin + i * kTcM + warp * 32 + lane;
     const int x = p / J.fs0, y = p - x * J.fs0;
-    const bool valid = ok && x < J.c1 && y < J.c0;
-    for (int c0 = 0; c0 < J.n_pad; c0 += 16) {
-      uint32_t r[16];
-      tc_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(i * J.n_pad + c0), r);
+    const uint32_t row_addr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(i * J.n);
+    for (int c0 = 0; c0 < J.n; c0 += 16) {
+      const TcCol head = cols[J.col_tab + c0];   // a 16-column chunk lies inside one section
+      if (head.kind == 0) continue;               // (uniform across the warp: the loads below are collective)
+      uint32_t r[16], r2[16];
+      __syncwarp();
+      tc_ld16(row_addr + (uint32_t)c0, r);
+      if (head.kind == 2 && head.pair) tc_ld16(row_addr + (uint32_t)(c0 + head.pair), r2);
       tc_wait_ld();
-      if (valid) {
-        for (int k = 0; k < 16 && c0 + k < J.n; k++) {
-          const int2 dk = dim_s[c0 + k];   // this filter's own map: rows dk.x, columns dk.y
-          if (x >= dk.y || y >= dk.x) continue;
+      if (ok && p < ncell) {
+#pragma unroll
+        for (int k = 0; k < 16; k++) {
+          const TcCol c = cols[J.col_tab + c0 + k];
           float v;
           memcpy(&v, &r[k], 4);
-          arena[(size_t)out_s[c0 + k] + (size_t)x * dk.x + y] = v * scl_s[c0 + k];
+          if (c.kind == 1) {
+            if (x < c.cols && y < c.rows) arena[(size_t)c.off + (size_t)x * c.rows + y] = v * c.inv;
+          } else if (c.kind == 2) {
+            if (c.pair) {
+              float w;
+              memcpy(&w, &r2[k], 4);
+              v += w;
+            }
+            arena[(size_t)c.off + p] = v * c.inv;
+          }
         }
       }
     }
@@ -295,6 +342,20 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_conv_tc(const TcJob *__restri
   tc_fence_before();
   __syncthreads();
   if (warp == 0) tmem_dealloc(tmem, ncols);
+}
+
+// Root maps from their blocks: root[x][y] = sum_k block_k[x*fs0 + y + shift_k],
+// the blocks in row order.
+__global__ void k_root_sum(const RootSumJob *__restrict__ jobs, float *__restrict__ arena) {
+  const RootSumJob &J = jobs[blockIdx.y];
+  const int r0 = J.r0, n = J.r0 * J.r1, fs0 = J.fs0, nblk = J.nblk, out = J.out_off;
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
+    const int x = e / r0, y = e - x * r0;
+    const int p = x * fs0 + y;
+    float v = 0.f;
+    for (int k = 0; k < nblk; k++) v += arena[(size_t)J.blk[k] + p + J.shift[k]];
+    arena[(size_t)out + e] = v;
+  }
 }
 
 // feature planes for a standalone call: [pos][32] float -> NQ planes [ncell + pad][16 B]
@@ -309,7 +370,7 @@ __global__ void k_feat_planes(const float *__restrict__ feat, int ncell, uint8_t
 }
 
 // ---------------------------------------------------------------------------
-// host: filter banks and job tables
+// host: the filter bank
 // ---------------------------------------------------------------------------
 static uint16_t to_bf16(float f) {   // round to nearest even
   uint32_t u;
@@ -319,39 +380,15 @@ static uint16_t to_bf16(float f) {   // round to nearest even
   u += 0x7fffu + lsb;
   return (uint16_t)(u >> 16);
 }
-
-// e4m3 bank from FP32 filters on the device (CUDA's own conversion, as for the
-// features): element (tap t = xp*b0 + yp of the group's grid, plane q, filter
-// f, lane k) = channel 16q + k of filter f at (xp, yp) times scale[f], zero
-// outside the filter's own b1 x b0 (fdim[f] = {b0, b1})
-__global__ void k_bank_e4m3(const float *const *__restrict__ filt, const float *__restrict__ scale,
-                            const int2 *__restrict__ fdim, int n, int n_pad, int b0, int taps,
-                            uint8_t *__restrict__ out) {
-  const int total = taps * 2 * n_pad * 16;
-  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x) {
-    const int k = e % 16, f = (e / 16) % n_pad, q = (e / (16 * n_pad)) % 2, t = e / (32 * n_pad);
-    const int c = 16 * q + k, xp = t / b0, yp = t - xp * b0;
-    float v = 0.f;
-    if (f < n && c < kFeat) {
-      const int fb0 = fdim[f].x, fb1 = fdim[f].y;
-      if (xp < fb1 && yp < fb0) v = filt[f][(size_t)c * fb0 * fb1 + xp * fb0 + yp] * scale[f];
-    }
-    out[e] = (uint8_t)__nv_cvt_float_to_fp8(v, __NV_SATFINITE, __NV_E4M3);
-  }
+static float from_bf16(uint16_t h) {
+  const uint32_t u = (uint32_t)h << 16;
+  float f;
+  memcpy(&f, &u, 4);
+  return f;
 }
 
-// A group's filters share one bank [tap][q][n_pad][16 B] over the group's tap
-// grid b1 x b0 (the largest of its filters); a smaller filter sits in the
-// grid's first rows and columns with zero weights around it, which add
-// nothing to its sums, and its map is its own size (c0, c1 of its b0, b1).
-struct BankGroup {
-  int b0, b1, n, n_pad, bank_off, kind;
-  std::vector<int> filt;      // indices into the caller's filter list
-  std::vector<int> fb0, fb1;  // each filter's own rows, columns
-  std::vector<float> inv;     // per filter: factor that undoes the operand scaling
-};
-
 static int tc_planes_of(geye_conv_mode mode) { return mode == GEYE_CONV_FP8 ? 2 : 4; }
+static int pad16(int n) { return (n + 15) & ~15; }
 
 // power of two that brings a filter's absolute maximum under e4m3's 448
 static float e4m3_filter_scale(const float *F, size_t n) {
@@ -361,349 +398,407 @@ static float e4m3_filter_scale(const float *F, size_t n) {
   return std::ldexp(1.0f, (int)std::floor(std::log2(448.0 / m)));
 }
 
-// tensor work of a grouping: every tile issues taps MMAs of N = n_pad
-static double group_cost(const std::vector<BankGroup> &gs) {
-  double c = 0;
-  for (auto &g : gs) c += (double)g.b0 * g.b1 * (((g.n + 15) & ~15) + 16);
-  return c;
-}
+// One bank row: filter f ([31][fb1][fb0], element (c, x, y) at c*fb0*fb1 + x*fb0 + y)
+// from its row y0, column x0 on (a whole filter: 0, 0), or the BF16 remainder of
+// those weights (lo).  Padding rows have no filter.
+struct BankRow {
+  const float *h = nullptr;   // host copy
+  const float *d = nullptr;   // device copy (FP8 banks are converted on the device)
+  int fb0 = 0, fb1 = 0, y0 = 0, x0 = 0, lo = 0;
+  float scale = 1.f;          // FP8: the filter's power-of-two scale
+};
 
-// groups the filters of each kind either by exact size or all together on the
-// largest grid (at most 32 a group), whichever issues less tensor work; lays
-// out the banks (filter f is [31][b1][b0] as conv_fp32 reads it: element
-// (c, xp, yp) at c*b0*b1 + xp*b0 + yp).  BF16 banks are built here into
-// bank16; for FP8 scale[f] is filled and the caller converts on the device.
-static void build_banks(const std::vector<const float *> &filt, const std::vector<int> &b0s,
-                        const std::vector<int> &b1s, const std::vector<int> &kinds, geye_conv_mode mode,
-                        std::vector<BankGroup> &groups, std::vector<uint16_t> &bank16, std::vector<float> &scale,
-                        size_t &total, int cap = 32) {
-  const int NQ = tc_planes_of(mode);
-  groups.clear();
-  for (int kind = 0; kind <= 1; kind++) {
-    std::vector<BankGroup> exact, merged;
-    for (size_t f = 0; f < filt.size(); f++) {
-      if (kinds[f] != kind) continue;
-      bool placed = false;
-      for (auto &g : exact)
-        if (g.b0 == b0s[f] && g.b1 == b1s[f] && g.n < cap) {
-          g.filt.push_back((int)f); g.fb0.push_back(b0s[f]); g.fb1.push_back(b1s[f]);
-          g.n++;
-          placed = true;
-          break;
-        }
-      if (!placed) exact.push_back(BankGroup{b0s[f], b1s[f], 1, 0, 0, kind, {(int)f}, {b0s[f]}, {b1s[f]}, {}});
-      if (merged.empty() || merged.back().n == cap) merged.push_back(BankGroup{0, 0, 0, 0, 0, kind, {}, {}, {}, {}});
-      BankGroup &m = merged.back();
-      m.b0 = std::max(m.b0, b0s[f]);
-      m.b1 = std::max(m.b1, b1s[f]);
-      m.filt.push_back((int)f); m.fb0.push_back(b0s[f]); m.fb1.push_back(b1s[f]);
-      m.n++;
+struct DevRow {
+  const float *f;
+  int fb0, fb1, y0, x0;
+  float scale;
+};
+
+// e4m3 bank [tap][2][rows][16]: element (tap t = xp*b0 + yp, plane q, row r, lane k)
+// = channel 16q + k of row r's filter at (x0 + xp, y0 + yp) times its scale, CUDA's
+// own conversion (as for the features); zero outside the filter
+__global__ void k_bank_e4m3(const DevRow *__restrict__ rows, int n_rows, int R, int b0, int taps,
+                            uint8_t *__restrict__ out) {
+  const size_t total = (size_t)taps * 2 * R * 16;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
+    const int k = (int)(e % 16), r = (int)((e / 16) % R), q = (int)((e / (16 * (size_t)R)) % 2);
+    const int t = (int)(e / (32 * (size_t)R));
+    const int c = 16 * q + k, xp = t / b0, yp = t - (t / b0) * b0;
+    float v = 0.f;
+    if (r < n_rows && c < kFeat) {
+      const DevRow D = rows[r];
+      const int x = D.x0 + xp, y = D.y0 + yp;
+      if (D.f && x < D.fb1 && y < D.fb0) v = D.f[(size_t)c * D.fb0 * D.fb1 + (size_t)x * D.fb0 + y] * D.scale;
     }
-    const auto &pick = group_cost(merged) < group_cost(exact) ? merged : exact;
-    groups.insert(groups.end(), pick.begin(), pick.end());
-  }
-  total = 0;
-  for (auto &g : groups) {
-    g.n_pad = (g.n + 15) & ~15;   // N of the MMA: a multiple of 16
-    g.bank_off = (int)total;
-    total += (size_t)g.b0 * g.b1 * NQ * g.n_pad * 16;
-  }
-  scale.assign(filt.size(), 1.f);
-  for (auto &g : groups)
-    for (int k = 0; k < g.n; k++) {
-      const int f = g.filt[k];
-      if (mode == GEYE_CONV_FP8) scale[f] = e4m3_filter_scale(filt[f], (size_t)g.fb0[k] * g.fb1[k] * kFeat);
-      g.inv.push_back(mode == GEYE_CONV_FP8 ? 1.0f / (scale[f] * kFp8FeatScale) : 1.0f);
-    }
-  if (mode == GEYE_CONV_FP8) return;
-  bank16.assign(total / 2, 0);
-  for (auto &g : groups) {
-    uint16_t *dst = bank16.data() + g.bank_off / 2;
-    for (int n = 0; n < g.n; n++) {
-      const float *F = filt[g.filt[n]];
-      const int fb0 = g.fb0[n], fb1 = g.fb1[n];
-      for (int xp = 0; xp < fb1; xp++)
-        for (int yp = 0; yp < fb0; yp++) {
-          const size_t t = (size_t)xp * g.b0 + yp;
-          for (int c = 0; c < kFeat; c++)
-            dst[((t * 4 + (c >> 3)) * g.n_pad + n) * 8 + (c & 7)] = to_bf16(F[(size_t)c * fb0 * fb1 + xp * fb0 + yp]);
-        }
-    }
+    out[e] = (uint8_t)__nv_cvt_float_to_fp8(v, __NV_SATFINITE, __NV_E4M3);
   }
 }
 
-// device bank of the groups (d_bank sized total); d_filt: the filters on the device
-static geye_status upload_bank(const std::vector<BankGroup> &groups, geye_conv_mode mode,
-                               const std::vector<uint16_t> &bank16, const std::vector<const float *> &d_filt,
-                               const std::vector<float> &scale, size_t total, void *d_bank, cudaStream_t s) {
-  if (mode != GEYE_CONV_FP8) {
-    CUDA_TRY(cudaMemcpyAsync(d_bank, bank16.data(), total, cudaMemcpyHostToDevice, s));
+// uploads the bank of `rows` over the b0 x b1 grid into dst (sized by bank_bytes)
+static size_t bank_bytes(int NQ, int b0, int b1, int R) { return (size_t)b0 * b1 * NQ * R * 16; }
+
+static geye_status upload_bank(geye_ctx *ctx, const std::vector<BankRow> &rows, int NQ, int b0, int b1, int R,
+                               DevBuf &dst) {
+  GEYE_TRY(dst.alloc(ctx, std::max<size_t>(bank_bytes(NQ, b0, b1, R), 16)));
+  if (NQ == 4) {
+    std::vector<uint16_t> bank((size_t)b0 * b1 * 4 * R * 8, 0);
+    for (int xp = 0; xp < b1; xp++)
+      for (int yp = 0; yp < b0; yp++) {
+        const size_t t = (size_t)xp * b0 + yp;
+        for (size_t r = 0; r < rows.size(); r++) {
+          const BankRow &B = rows[r];
+          const int x = B.x0 + xp, y = B.y0 + yp;
+          if (!B.h || x >= B.fb1 || y >= B.fb0) continue;
+          for (int c = 0; c < kFeat; c++) {
+            const float w = B.h[(size_t)c * B.fb0 * B.fb1 + (size_t)x * B.fb0 + y];
+            const uint16_t hi = to_bf16(w);
+            bank[((t * 4 + (c >> 3)) * R + r) * 8 + (c & 7)] = B.lo ? to_bf16(w - from_bf16(hi)) : hi;
+          }
+        }
+      }
+    CUDA_TRY(cudaMemcpyAsync(dst.p, bank.data(), bank.size() * 2, cudaMemcpyHostToDevice, ctx->stream));
+    CUDA_TRY(cudaStreamSynchronize(ctx->stream));
     return GEYE_OK;
   }
-  for (auto &g : groups) {
-    std::vector<const float *> ptrs;
-    std::vector<float> sc;
-    std::vector<int2> dims;
-    for (int k = 0; k < g.n; k++) {
-      ptrs.push_back(d_filt[g.filt[k]]);
-      sc.push_back(scale[g.filt[k]]);
-      dims.push_back(make_int2(g.fb0[k], g.fb1[k]));
-    }
-    const float **d_ptrs = nullptr;
-    float *d_sc = nullptr;
-    int2 *d_dims = nullptr;
-    CUDA_TRY(cudaMalloc(&d_ptrs, sizeof(float *) * ptrs.size()));
-    cudaError_t e = cudaMalloc(&d_sc, sizeof(float) * sc.size());
-    if (e == cudaSuccess) e = cudaMalloc(&d_dims, sizeof(int2) * dims.size());
-    if (e == cudaSuccess) e = cudaMemcpy(d_ptrs, ptrs.data(), sizeof(float *) * ptrs.size(), cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) e = cudaMemcpy(d_sc, sc.data(), sizeof(float) * sc.size(), cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) e = cudaMemcpy(d_dims, dims.data(), sizeof(int2) * dims.size(), cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) {
-      const int taps = g.b0 * g.b1, elems = taps * 2 * g.n_pad * 16;
-      k_bank_e4m3<<<std::max(1, std::min((elems + 255) / 256, 1024)), 256, 0, s>>>(
-          d_ptrs, d_sc, d_dims, g.n, g.n_pad, g.b0, taps, static_cast<uint8_t *>(d_bank) + g.bank_off);
-      e = cudaStreamSynchronize(s);
-    }
-    cudaFree(d_ptrs);
-    cudaFree(d_sc);
-    cudaFree(d_dims);
-    if (e != cudaSuccess) {
-      set_error(std::string("e4m3 filter bank: ") + cudaGetErrorString(e));
-      return GEYE_ERR_CUDA;
-    }
-  }
+  std::vector<DevRow> dr;
+  for (const BankRow &B : rows) dr.push_back(DevRow{B.d, B.fb0, B.fb1, B.y0, B.x0, B.scale});
+  DevBuf d_rows;
+  GEYE_TRY(upload_bytes(ctx, d_rows, dr.data(), sizeof(DevRow) * std::max<size_t>(dr.size(), 1)));
+  const int taps = b0 * b1;
+  const size_t elems = (size_t)taps * 2 * R * 16;
+  k_bank_e4m3<<<(int)std::max<size_t>(1, std::min<size_t>((elems + 255) / 256, 2048)), 256, 0, ctx->stream>>>(
+      d_rows.as<DevRow>(), (int)dr.size(), R, b0, taps, dst.as<uint8_t>());
+  CUDA_TRY(cudaGetLastError());
+  CUDA_TRY(cudaStreamSynchronize(ctx->stream));
   return GEYE_OK;
 }
 
-struct TcTables {
-  std::vector<TcJob> jobs;
-  std::vector<int4> chunks;
-  std::vector<int> outs;
-  std::vector<float> inv;
-  std::vector<int2> dims;   // each map's rows, columns
-  size_t max_smem = 0;
+// ---------------------------------------------------------------------------
+// host: chunks (tile runs) of the jobs for a tile shape
+// ---------------------------------------------------------------------------
+struct TcShape {
+  int t_cap;        // tiles per CTA, at most
+  size_t budget;    // dynamic shared memory per CTA, at most
+  int stages;       // bank stages in the ring
 };
+static const TcShape kTcShapes[] = {{4, 220 * 1024, 6}, {8, 220 * 1024, 4}, {2, 110 * 1024, 4},
+                                    {4, 110 * 1024, 3}, {1, 72 * 1024, 4},  {2, 72 * 1024, 3},
+                                    {8, 220 * 1024, 8}};
+constexpr int kTcNumShapes = (int)(sizeof(kTcShapes) / sizeof(kTcShapes[0]));
 
-// one job: group g on a level whose planes start at plane_off; map_off[k] is
-// the float offset of filter k's output map.  cells_avail: cells from the
-// start of plane 0 to the end of the planes' buffer (a slab may read past its
-// own plane into the next one or into the buffer's tail: those cells only
-// meet zero weights).  t_cap and budget: the largest tile run and shared
-// memory a CTA may take (the tile-shape candidates of the autotuner below).
-// False if it cannot fit in shared memory or the buffer.
-static bool add_tc_job(TcTables &T, int NQ, int plane_off, int fs0, int fs1, const BankGroup &g,
-                       const std::vector<int> &map_off, long long cells_avail, int t_cap = kTcMaxTiles,
-                       size_t budget = kTcSmemBudget) {
-  TcJob J{};
-  J.plane_off = plane_off;
-  J.plane_cells = fs0 * fs1 + kTcPlanePad;
-  J.fs0 = fs0; J.fs1 = fs1;
-  J.b0 = g.b0; J.b1 = g.b1;
-  int mb0 = g.b0, mb1 = g.b1;   // the smallest filter: the most outputs
-  for (int k = 0; k < g.n; k++) { mb0 = std::min(mb0, g.fb0[k]); mb1 = std::min(mb1, g.fb1[k]); }
-  J.c0 = fs0 - mb0 + 1; J.c1 = fs1 - mb1 + 1;
-  if (J.c0 < 1 || J.c1 < 1) return false;
-  J.n = g.n; J.n_pad = g.n_pad;
-  J.bank_off = g.bank_off;
-  J.out_tab = (int)T.outs.size();
-  for (int k = 0; k < g.n; k++) {
-    const int c0k = fs0 - g.fb0[k] + 1, c1k = fs1 - g.fb1[k] + 1;
-    if (c0k < 1 || c1k < 1) return false;
-    T.outs.push_back(map_off[k]);
-    T.inv.push_back(g.inv[k]);
-    T.dims.push_back(make_int2(c0k, c1k));
+static size_t tc_need(const TcJob &J, int NQ, int T, int cs, int NS) {
+  const size_t S = (size_t)T * kTcM + (size_t)(cs - 1) * J.fs0 + (J.b0 - 1);
+  const size_t slab = kTcHead + (size_t)NQ * S * 16 * (J.n_lo > 0 ? 2 : 1);
+  return ((slab + 127) & ~(size_t)127) + (size_t)NS * NQ * J.n * 16;
+}
+
+static int tmem_cols(int c) {
+  int n = 32;
+  while (n < c) n <<= 1;
+  return n;
+}
+
+// chunks of every job for a shape; false when a job fits no CTA or a slab would
+// read past the planes' buffer (cells_total cells of 16 B)
+static bool chunk_jobs(const std::vector<TcJob> &jobs, int NQ, const TcShape &sh, long long cells_total,
+                       std::vector<int4> &chunks, size_t &max_smem) {
+  chunks.clear();
+  max_smem = 0;
+  for (size_t j = 0; j < jobs.size(); j++) {
+    const TcJob &J = jobs[j];
+    const int t_max = std::max(1, std::min(sh.t_cap, kTcTmemCols / J.n));
+    int T = 0, cs = 0;
+    for (int Tc = t_max; Tc >= 1 && !T; Tc--)
+      if (tc_need(J, NQ, Tc, J.b1, sh.stages) <= sh.budget) { T = Tc; cs = J.b1; }
+    for (int c = J.b1 - 1; c >= 1 && !T; c--)
+      if (tc_need(J, NQ, 1, c, sh.stages) <= sh.budget) { T = 1; cs = c; }
+    if (!T) return false;
+    // the CTAs that share an SM (by shared memory) fit their accumulators in its
+    // 512 TMEM columns together, or one's allocation waits for another to end
+    auto per_sm = [&](int Tc) { return std::max<size_t>(1, (228u * 1024u) / (tc_need(J, NQ, Tc, cs, sh.stages) + 1024)); };
+    while (T > 1 && (size_t)tmem_cols(T * J.n) * per_sm(T) > (size_t)kTcTmemCols) T--;
+    const long long reach = (long long)(J.b1 - 1) * J.fs0 + (J.b0 - 1);
+    for (int t0 = 0; t0 < J.ntiles; t0 += T) {
+      const int nt = std::min(T, J.ntiles - t0);
+      const long long last = (long long)(NQ - 1) * J.plane_cells + (long long)t0 * kTcM + (long long)nt * kTcM + reach;
+      if ((long long)J.plane_off * 2 / 16 + last > cells_total) return false;
+      if (J.lo_off >= 0 && (long long)J.lo_off * 2 / 16 + last > cells_total) return false;
+      chunks.push_back(make_int4((int)j, t0, nt, cs));
+      max_smem = std::max(max_smem, tc_need(J, NQ, nt, cs, sh.stages));
+    }
   }
-  const int P_valid = (J.c1 - 1) * J.fs0 + J.c0;
-  J.ntiles = (P_valid + kTcM - 1) / kTcM;
-  // tiles per CTA (T) and filter columns per phase (cs): one phase when the whole
-  // bank and slab fit, else fewer columns per phase; every phase needs
-  // head + bank columns + NQ planes of (T*128 + (cs-1)*fs0 + b0-1) cells x 16 B
-  const size_t col_bytes = (size_t)g.b0 * NQ * g.n_pad * 16;
-  auto need = [&](int Tc, int cs) {
-    return (size_t)kTcHead + ((cs * col_bytes + 127) & ~(size_t)127) +
-           ((size_t)Tc * kTcM + (size_t)(cs - 1) * fs0 + (g.b0 - 1)) * 16 * NQ;
+  // heaviest first (tiles x taps x N), so the long ones start in the first wave
+  auto cost = [&](const int4 &c) {
+    const TcJob &J = jobs[c.x];
+    return (long long)c.z * J.b0 * J.b1 * (J.n + 2 * J.n_lo);
   };
-  int T_cta = 0, cs = 0;
-  const int t_max = std::max(1, std::min(t_cap, kTcTmemCols / g.n_pad));   // accumulators fit TMEM
-  for (int Tc = t_max; Tc >= std::min(4, t_max) && !T_cta; Tc /= 2)
-    if (need(Tc, g.b1) <= budget) { T_cta = Tc; cs = g.b1; }
-  for (int Tc = std::min(8, t_max); Tc >= 1 && !T_cta; Tc /= 2)
-    for (int c = g.b1; c >= 1; c--)
-      if (need(Tc, c) <= budget) { T_cta = Tc; cs = c; break; }
-  if (!T_cta) return false;
-  // the CTAs that share an SM (by shared memory) must fit their accumulators in
-  // its 512 TMEM columns together, or one's allocation waits for another to end
-  auto tmem_cols = [&](int Tc) {
-    uint32_t c = 32;
-    while (c < (uint32_t)(Tc * g.n_pad)) c <<= 1;
-    return (int)c;
-  };
-  auto per_sm = [&](int Tc) { return std::max<size_t>(1, (size_t)(228 * 1024) / (need(Tc, cs) + 1024)); };
-  while (T_cta > 1 && (size_t)tmem_cols(T_cta) * per_sm(T_cta) > (size_t)kTcTmemCols) T_cta /= 2;
-  const int jid = (int)T.jobs.size();
-  T.jobs.push_back(J);
-  const long long reach = (long long)(g.b1 - 1) * fs0 + (g.b0 - 1);
-  for (int t0 = 0; t0 < J.ntiles; t0 += T_cta) {
-    const int nt = std::min(T_cta, J.ntiles - t0);
-    // the last plane's slab stays inside the buffer
-    if ((long long)(NQ - 1) * J.plane_cells + (long long)t0 * kTcM + nt * kTcM + reach > cells_avail) return false;
-    T.chunks.push_back(make_int4(jid, t0, nt, cs));
-    T.max_smem = std::max(T.max_smem, need(nt, cs));
-  }
+  std::stable_sort(chunks.begin(), chunks.end(), [&](const int4 &x, const int4 &y) { return cost(x) > cost(y); });
   return true;
 }
 
-static void launch_conv_tc(int NQ, const TcJob *jobs, const int4 *chunks, int n_chunks, const int *outs,
-                           const float *inv, const int2 *dims, const uint8_t *planes, const uint8_t *bank, float *out,
-                           int *err, size_t smem, cudaStream_t s) {
+static void launch_conv_tc(int NQ, const TcJob *jobs, const int4 *chunks, int n_chunks, const TcCol *cols,
+                           const uint8_t *planes, const uint8_t *bank, int bank_rows, int stages, float *out, int *err,
+                           size_t smem, cudaStream_t s) {
+  if (n_chunks <= 0) return;
   if (NQ == 4) {
     static SmemAttr a4;
     raise_smem(a4, k_conv_tc<4>, smem);
-    k_conv_tc<4><<<n_chunks, kTcThreads, smem, s>>>(jobs, chunks, outs, inv, dims, planes, bank, out, err);
+    k_conv_tc<4><<<n_chunks, kTcThreads, smem, s>>>(jobs, chunks, cols, planes, bank, bank_rows, stages, out, err);
   } else {
     static SmemAttr a2;
     raise_smem(a2, k_conv_tc<2>, smem);
-    k_conv_tc<2><<<n_chunks, kTcThreads, smem, s>>>(jobs, chunks, outs, inv, dims, planes, bank, out, err);
+    k_conv_tc<2><<<n_chunks, kTcThreads, smem, s>>>(jobs, chunks, cols, planes, bank, bank_rows, stages, out, err);
   }
 }
 
-// the model's banks for a precision (built once per model and mode; roots and
-// parts in separate groups)
-static geye_status ensure_bank(geye_ctx *ctx, geye_model *m, geye_conv_mode mode, std::vector<BankGroup> &groups) {
-  const HostModel &h = m->h;
-  std::vector<const float *> filt, d_filt;
-  std::vector<int> b0s, b1s, kinds;
-  for (int r = 0; r < h.NoR; r++) {
-    filt.push_back(h.rootfilter[r].data());
-    d_filt.push_back(m->d_filters + m->filt_off[r]);
-    b0s.push_back(h.root_size[3 * r]); b1s.push_back(h.root_size[3 * r + 1]); kinds.push_back(0);
+// ---------------------------------------------------------------------------
+// host: the plan's bank, jobs, column tables and root sums
+// ---------------------------------------------------------------------------
+// Before the arena is allocated: the rows (every model's part filters, then its
+// root filters cut into blocks of the part grid, then in BF16 mode the blocks'
+// remainders), one job per feature level over the rows it uses, the blocks'
+// position-indexed buffers (taken from the arena) and the root sums.
+geye_status plan_tc(geye_ctx *ctx, Plan &P, ArenaAlloc &A) {
+  TcPlan &T = P.tc;   // a fresh plan's (default-constructed)
+  const geye_conv_mode mode = ctx->conv_mode;
+  const bool split = mode == GEYE_CONV_BF16;
+  T.planes = tc_planes_of(mode);
+  int gb0 = 0, gb1 = 0;
+  for (auto &mp : P.models) {
+    const HostModel &h = mp->model->h;
+    for (int p = 0; p < h.NoP; p++) { gb0 = std::max(gb0, h.part_size[3 * p]); gb1 = std::max(gb1, h.part_size[3 * p + 1]); }
   }
-  for (int p = 0; p < h.NoP; p++) {
-    filt.push_back(h.partfilter[p].data());
-    d_filt.push_back(m->d_filters + m->filt_off[h.NoR + p]);
-    b0s.push_back(h.part_size[3 * p]); b1s.push_back(h.part_size[3 * p + 1]); kinds.push_back(1);
+  if (!gb0 || !gb1)   // no parts anywhere: one block per root
+    for (auto &mp : P.models) {
+      const HostModel &h = mp->model->h;
+      for (int r = 0; r < h.NoR; r++) { gb0 = std::max(gb0, h.root_size[3 * r]); gb1 = std::max(gb1, h.root_size[3 * r + 1]); }
+    }
+  T.grid_b0 = gb0;
+  T.grid_b1 = gb1;
+  // rows
+  struct PartRow { int mi, p; };
+  struct RootRow { int mi, c, y0, x0; };
+  std::vector<PartRow> parts;
+  std::vector<RootRow> roots;
+  for (int mi = 0; mi < (int)P.models.size(); mi++) {
+    const HostModel &h = P.models[mi]->model->h;
+    for (int p = 0; p < h.NoP; p++) parts.push_back({mi, p});
   }
-  std::vector<uint16_t> bank16;
-  std::vector<float> scale;
-  size_t total = 0;
-  build_banks(filt, b0s, b1s, kinds, mode, groups, bank16, scale, total);
-  void *&d_bank = mode == GEYE_CONV_FP8 ? m->d_bank8 : m->d_bank16;
-  if (d_bank) return GEYE_OK;
-  CUDA_TRY(cudaMalloc(&d_bank, std::max<size_t>(total, 16)));
-  const geye_status st = upload_bank(groups, mode, bank16, d_filt, scale, total, d_bank, ctx->stream);
-  CUDA_TRY(cudaStreamSynchronize(ctx->stream));
-  return st;
-}
-
-// chunks ordered by cost (tiles x taps x N), heaviest first, so that the long
-// ones start in the first wave
-static void sort_chunks(TcTables &T) {
-  auto cost = [&](const int4 &c) {
-    const TcJob &J = T.jobs[c.x];
-    return (long long)c.z * J.b0 * J.b1 * J.n_pad;
-  };
-  std::stable_sort(T.chunks.begin(), T.chunks.end(), [&](const int4 &x, const int4 &y) { return cost(x) > cost(y); });
-}
-
-// job tables of one model for a tile-shape candidate; chunks ordered by cost,
-// heaviest first, so that the long ones start in the first wave
-static geye_status build_tables(Plan &P, ModelPlan &mp, const std::vector<BankGroup> &groups, int NQ, int t_cap,
-                                size_t budget, TcTables &T) {
-  const HostModel &h = mp.model->h;
-  const long long total_cells = (long long)(P.arena16.bytes / 16);
-  const int NoC = h.numcomponent, NoP = h.NoP, interval = h.interval;
-  for (int level = interval; level < mp.LEN; level++) {
-    if (mp.skipped[level]) continue;
-    const int Lv = level - interval;
-    for (auto &g : groups) {
-      std::vector<int> map_off;
-      const bool root = g.kind == 0;
-      for (int f : g.filt) map_off.push_back(root ? mp.root_map_off[level * NoC + f] : mp.part_map_off[Lv * NoP + (f - h.NoR)]);
-      for (int v : map_off)
-        if (v < 0) { set_error("tensor-core conv: filter map missing from the plan"); return GEYE_ERR_UNSUPPORTED; }
-      const LevelInfo &L = root ? P.lv[level] : P.lv[Lv];
-      const long long avail = total_cells - (long long)L.feat16_off * 2 / 16;
-      if (!add_tc_job(T, NQ, L.feat16_off, L.fs0, L.fs1, g, map_off, avail, t_cap, budget)) {
-        set_error("tensor-core conv: a filter bank and its feature reach exceed shared memory");
+  for (int mi = 0; mi < (int)P.models.size(); mi++) {
+    const HostModel &h = P.models[mi]->model->h;
+    for (int c = 0; c < h.numcomponent; c++) {
+      const int rb0 = h.root_size[3 * c], rb1 = h.root_size[3 * c + 1];
+      const int na = (rb1 + gb1 - 1) / gb1, nb = (rb0 + gb0 - 1) / gb0;
+      if (na * nb > kMaxRootBlocks) {
+        set_error("tensor-core conv: a root filter needs more than 16 blocks of the part grid");
         return GEYE_ERR_UNSUPPORTED;
       }
+      for (int a = 0; a < na; a++)
+        for (int b = 0; b < nb; b++) roots.push_back({mi, c, b * gb0, a * gb1});
     }
   }
-  sort_chunks(T);
+  const int p16 = pad16((int)parts.size()), r16 = pad16((int)roots.size());
+  const int RS = r16 * (split ? 2 : 1);
+  if (p16 > kTcMaxN || RS > kTcMaxN) {
+    set_error("tensor-core conv: more than 256 filter rows in one section");
+    return GEYE_ERR_UNSUPPORTED;
+  }
+  T.rows = p16 + RS;
+  T.rows_p16 = p16;
+  T.rows_r16 = r16;
+  // host bank rows (filters and FP8 scales)
+  T.bank_rows.assign(T.rows, BankRowSpec{});
+  std::map<std::pair<int, int>, float> root_scale;
+  for (size_t j = 0; j < parts.size(); j++) {
+    geye_model *m = P.models[parts[j].mi]->model;
+    T.bank_rows[j] = BankRowSpec{parts[j].mi, m->h.NoR + parts[j].p, 0, 0, 0};
+  }
+  for (size_t j = 0; j < roots.size(); j++) {
+    T.bank_rows[p16 + j] = BankRowSpec{roots[j].mi, roots[j].c, roots[j].y0, roots[j].x0, 0};
+    if (split) T.bank_rows[p16 + r16 + j] = BankRowSpec{roots[j].mi, roots[j].c, roots[j].y0, roots[j].x0, 1};
+  }
+  auto filt_scale = [&](int mi, int f) {
+    if (mode != GEYE_CONV_FP8) return 1.f;
+    const HostModel &h = P.models[mi]->model->h;
+    const bool root = f < h.NoR;
+    const std::vector<float> &w = root ? h.rootfilter[f] : h.partfilter[f - h.NoR];
+    return e4m3_filter_scale(w.data(), w.size());
+  };
+  for (auto &b : T.bank_rows)
+    if (b.mi >= 0) b.scale = filt_scale(b.mi, b.filt);
+  // jobs per feature level
+  const int interval = P.interval;
+  for (int l = 0; l < P.LEN; l++) {
+    const LevelInfo &L = P.lv[l];
+    if (L.feat16_off < 0 || L.fs0 <= 0 || L.fs1 <= 0) continue;
+    std::vector<int> part_on(parts.size(), 0), root_on(roots.size(), 0);
+    bool any_p = false, any_r = false;
+    for (size_t j = 0; j < parts.size(); j++) {
+      const ModelPlan &mp = *P.models[parts[j].mi];
+      const int NoP = mp.model->h.NoP;
+      const size_t i = (size_t)l * NoP + parts[j].p;
+      if (i < mp.part_map_off.size() && mp.part_map_off[i] >= 0) { part_on[j] = 1; any_p = true; }
+    }
+    for (size_t j = 0; j < roots.size(); j++) {
+      const ModelPlan &mp = *P.models[roots[j].mi];
+      const size_t i = (size_t)l * mp.model->h.numcomponent + roots[j].c;
+      if (l >= interval && l < mp.LEN && i < mp.root_map_off.size() && mp.root_map_off[i] >= 0) {
+        root_on[j] = 1;
+        any_r = true;
+      }
+    }
+    if (!any_p && !any_r) continue;
+    const int ncell = L.fs0 * L.fs1;
+    std::vector<int> block_off(roots.size(), -1);
+    for (size_t j = 0; j < roots.size(); j++)
+      if (root_on[j]) block_off[j] = A.take((size_t)ncell);
+    // root sums: each root present at this level from its blocks
+    for (int mi = 0; mi < (int)P.models.size(); mi++) {
+      const ModelPlan &mp = *P.models[mi];
+      const int NoC = mp.model->h.numcomponent;
+      for (int c = 0; c < NoC; c++) {
+        RootSumJob S{};
+        for (size_t j = 0; j < roots.size(); j++) {
+          if (roots[j].mi != mi || roots[j].c != c || !root_on[j]) continue;
+          S.blk[S.nblk] = block_off[j];
+          S.shift[S.nblk] = roots[j].x0 * L.fs0 + roots[j].y0;
+          S.nblk++;
+        }
+        if (!S.nblk) continue;
+        S.out_off = mp.root_map_off[(size_t)l * NoC + c];
+        S.r0 = mp.root_r0[(size_t)l * NoC + c];
+        S.r1 = mp.root_r1[(size_t)l * NoC + c];
+        S.fs0 = L.fs0;
+        T.sums.push_back(S);
+        T.sum_max_r = std::max(T.sum_max_r, S.r0 * S.r1);
+      }
+    }
+    auto add_job = [&](int row0, int n, int lo_row, int n_lo, bool with_roots) {
+      TcJob J{};
+      J.plane_off = L.feat16_off;
+      J.lo_off = n_lo ? L.feat16lo_off : -1;
+      J.plane_cells = ncell + kTcPlanePad;
+      J.fs0 = L.fs0; J.fs1 = L.fs1;
+      J.b0 = gb0; J.b1 = gb1;
+      J.row0 = row0; J.n = n;
+      J.lo_row = lo_row; J.n_lo = n_lo;
+      J.col_tab = (int)T.cols.size();
+      int p_valid = 0;
+      for (int k = 0; k < n; k++) {
+        const int row = row0 + k;
+        TcCol C{};
+        C.inv = 1.f;
+        if (row < p16) {
+          if (row < (int)parts.size() && part_on[row]) {
+            const ModelPlan &mp = *P.models[parts[row].mi];
+            const size_t i = (size_t)l * mp.model->h.NoP + parts[row].p;
+            C.kind = 1;
+            C.off = mp.part_map_off[i];
+            C.rows = mp.part_d0[i];
+            C.cols = mp.part_d1[i];
+            C.inv = 1.f / (T.bank_rows[row].scale * (mode == GEYE_CONV_FP8 ? kFp8FeatScale : 1.f));
+            p_valid = std::max(p_valid, (C.cols - 1) * L.fs0 + C.rows);
+          }
+        } else if (row < p16 + r16) {
+          const int j = row - p16;
+          if (j < (int)roots.size() && root_on[j]) {
+            C.kind = 2;
+            C.off = block_off[j];
+            C.pair = split ? r16 : 0;
+            C.inv = 1.f / (T.bank_rows[row].scale * (mode == GEYE_CONV_FP8 ? kFp8FeatScale : 1.f));
+          }
+        }
+        T.cols.push_back(C);
+      }
+      J.ntiles = ((with_roots ? ncell : p_valid) + kTcM - 1) / kTcM;
+      if (J.ntiles > 0) T.jobs.push_back(J);
+    };
+    const int n_lo = split ? r16 : 0;
+    if (any_p && any_r && p16 + RS <= kTcMaxN) {
+      add_job(0, p16 + RS, p16, n_lo, true);
+    } else {
+      if (any_p) add_job(0, p16, 0, 0, false);
+      if (any_r) add_job(p16, RS, 0, n_lo, true);
+    }
+  }
   return GEYE_OK;
 }
 
-// Tile-shape autotuner: every candidate (largest tile run per CTA, shared
-// memory per CTA -- fewer tiles and less memory let more CTAs share an SM and
-// overlap one's copies with another's MMAs) is built for this plan's levels,
-// timed on the device (CUDA events, after one untimed launch) and the fastest
-// kept.  Runs once per plan, before the plan's first frame.
-struct TcShape {
-  int t_cap;
-  size_t budget;
-};
-static const TcShape kTcShapes[] = {{16, 220 * 1024}, {8, 220 * 1024}, {4, 220 * 1024},
-                                    {8, 110 * 1024},  {4, 110 * 1024}, {4, 72 * 1024}, {2, 72 * 1024}};
-
-geye_status build_tc_jobs(geye_ctx *ctx, Plan &P, ModelPlan &mp) {
-  geye_model *m = mp.model;
-  const geye_conv_mode mode = ctx->conv_mode;
-  std::vector<BankGroup> groups;
-  GEYE_TRY(ensure_bank(ctx, m, mode, groups));
-  const int NQ = tc_planes_of(mode);
-  const void *bank = NQ == 2 ? m->d_bank8 : m->d_bank16;
-  mp.tc_planes = NQ;
-  if (!P.arena16.p) {   // a plan built from features has no planes: run_conv_tc reports it
-    mp.tc_chunks = 0;
-    return GEYE_OK;
+// After the arena exists: the bank, then the tile-shape autotuner (every candidate
+// is chunked, timed on the plan's own arena with CUDA events after one untimed
+// launch, and the fastest kept; the choice is cached per models and geometry),
+// then the tables.
+geye_status build_tc_plan(geye_ctx *ctx, Plan &P) {
+  TcPlan &T = P.tc;
+  if (!P.arena16.p || T.jobs.empty()) return GEYE_OK;
+  const int NQ = T.planes;
+  // the bank
+  std::vector<BankRow> rows(T.rows);
+  for (int r = 0; r < T.rows; r++) {
+    const BankRowSpec &b = T.bank_rows[r];
+    if (b.mi < 0) continue;
+    geye_model *m = P.models[b.mi]->model;
+    const HostModel &h = m->h;
+    const bool root = b.filt < h.NoR;
+    BankRow R;
+    R.h = root ? h.rootfilter[b.filt].data() : h.partfilter[b.filt - h.NoR].data();
+    R.d = m->d_filters + m->filt_off[b.filt];
+    R.fb0 = root ? h.root_size[3 * b.filt] : h.part_size[3 * (b.filt - h.NoR)];
+    R.fb1 = root ? h.root_size[3 * b.filt + 1] : h.part_size[3 * (b.filt - h.NoR) + 1];
+    R.y0 = b.y0;
+    R.x0 = b.x0;
+    R.lo = b.lo;
+    R.scale = b.scale;
+    rows[r] = R;
   }
-  TcTables best;
-  int best_shape = -1;
+  GEYE_TRY(upload_bank(ctx, rows, NQ, T.grid_b0, T.grid_b1, T.rows, T.d_bank));
+  GEYE_TRY(upload_bytes(ctx, T.d_jobs, T.jobs.data(), sizeof(TcJob) * T.jobs.size()));
+  GEYE_TRY(upload_bytes(ctx, T.d_cols, T.cols.data(), sizeof(TcCol) * std::max<size_t>(T.cols.size(), 1)));
+  GEYE_TRY(upload_bytes(ctx, T.d_sums, T.sums.data(), sizeof(RootSumJob) * std::max<size_t>(T.sums.size(), 1)));
+  const long long cells_total = (long long)(P.arena16.bytes / 16);
+  int *err = P.d_small.as<int>() + 130;
+  // a geometry these models were tuned at before reuses that choice
+  std::string key = std::to_string(P.width) + "x" + std::to_string(P.height) + "/" + std::to_string(P.LEN) + "/" +
+                    std::to_string((int)ctx->conv_mode);
+  for (auto &mp : P.models) key += ":" + std::to_string(mp->model->id);
+  geye_model *m0 = P.models[0]->model;
+  int first = 0, last = kTcNumShapes;
   float best_ms = 0.f;
-  const bool tunable = P.arena16.p && P.arena.p && P.d_small.p;
-  int n_shapes = tunable ? (int)(sizeof(kTcShapes) / sizeof(kTcShapes[0])) : 1;
-  int first = 0;
-  // a geometry this model was tuned at before reuses that choice
-  const std::string key = std::to_string(P.width) + "x" + std::to_string(P.height) + "/" + std::to_string(mp.LEN) +
-                          "/" + std::to_string((int)mode);
   {
-    std::lock_guard<std::mutex> lk(m->tc_mu);
-    auto it = m->tc_tuned.find(key);
-    if (tunable && it != m->tc_tuned.end()) {
-      first = it->second.first;
-      n_shapes = first + 1;
-      best_ms = 3.0f * it->second.second;
-    }
+    std::lock_guard<std::mutex> lk(m0->tc_mu);
+    auto it = m0->tc_tuned.find(key);
+    if (it != m0->tc_tuned.end()) { first = it->second.first; last = first + 1; best_ms = 3.0f * it->second.second; }
   }
   // GEYE_TC_SHAPE=<i> pins candidate i (reproducible shapes; no timing)
   if (const char *e = getenv("GEYE_TC_SHAPE")) {
     const int i = atoi(e);
-    if (i >= 0 && i < (int)(sizeof(kTcShapes) / sizeof(kTcShapes[0]))) { first = i; n_shapes = i + 1; }
+    if (i >= 0 && i < kTcNumShapes) { first = i; last = i + 1; }
   }
-  const bool timed = tunable && n_shapes - first > 1;
+  const bool timed = last - first > 1;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   if (timed) {
     CUDA_TRY(cudaEventCreate(&e0));
     CUDA_TRY(cudaEventCreate(&e1));
   }
-  for (int si = first; si < n_shapes; si++) {
-    TcTables T;
-    if (build_tables(P, mp, groups, NQ, kTcShapes[si].t_cap, kTcShapes[si].budget, T) != GEYE_OK) continue;
-    if (!timed || T.chunks.empty()) {
-      best = std::move(T);
+  std::vector<int4> best;
+  size_t best_smem = 0;
+  int best_shape = -1;
+  for (int si = first; si < last; si++) {
+    std::vector<int4> chunks;
+    size_t smem = 0;
+    if (!chunk_jobs(T.jobs, NQ, kTcShapes[si], cells_total, chunks, smem)) continue;
+    if (!timed) {
+      best = std::move(chunks);
+      best_smem = smem;
       best_shape = si;
       break;
     }
-    DevBuf jobs, chunks, outs, inv, dims;
-    GEYE_TRY(upload_bytes(ctx, jobs, T.jobs.data(), sizeof(TcJob) * T.jobs.size()));
-    GEYE_TRY(upload_bytes(ctx, chunks, T.chunks.data(), sizeof(int4) * T.chunks.size()));
-    GEYE_TRY(upload_bytes(ctx, outs, T.outs.data(), sizeof(int) * T.outs.size()));
-    GEYE_TRY(upload_bytes(ctx, inv, T.inv.data(), sizeof(float) * T.inv.size()));
-    GEYE_TRY(upload_bytes(ctx, dims, T.dims.data(), sizeof(int2) * T.dims.size()));
+    DevBuf d_chunks;
+    GEYE_TRY(upload_bytes(ctx, d_chunks, chunks.data(), sizeof(int4) * chunks.size()));
     auto launch = [&]() {
-      launch_conv_tc(NQ, jobs.as<TcJob>(), chunks.as<int4>(), (int)T.chunks.size(), outs.as<int>(), inv.as<float>(),
-                     dims.as<int2>(), P.arena16.as<uint8_t>(), static_cast<const uint8_t *>(bank), P.arena.as<float>(),
-                     P.d_small.as<int>() + 130, T.max_smem, ctx->stream);
+      launch_conv_tc(NQ, T.d_jobs.as<TcJob>(), d_chunks.as<int4>(), (int)chunks.size(), T.d_cols.as<TcCol>(),
+                     P.arena16.as<uint8_t>(), T.d_bank.as<uint8_t>(), T.rows, kTcShapes[si].stages,
+                     P.arena.as<float>(), err, smem, ctx->stream);
     };
     launch();
     CUDA_TRY(cudaEventRecord(e0, ctx->stream));
@@ -714,65 +809,50 @@ geye_status build_tc_jobs(geye_ctx *ctx, Plan &P, ModelPlan &mp) {
     float ms = 0.f;
     CUDA_TRY(cudaEventElapsedTime(&ms, e0, e1));
     if (best_shape < 0 || ms < best_ms) {
-      best = std::move(T);
+      best = std::move(chunks);
+      best_smem = smem;
       best_shape = si;
       best_ms = ms;
     }
   }
   if (e0) cudaEventDestroy(e0);
   if (e1) cudaEventDestroy(e1);
-  if (timed) CUDA_TRY(cudaMemsetAsync(P.d_small.as<int>() + 130, 0, sizeof(int), ctx->stream));
-  if (best_shape < 0) return GEYE_ERR_UNSUPPORTED;   // the error of the last candidate stands
-  if (timed) {
-    std::lock_guard<std::mutex> lk(m->tc_mu);
-    m->tc_tuned[key] = {best_shape, best_ms / 3.0f};
+  if (timed) CUDA_TRY(cudaMemsetAsync(err, 0, sizeof(int), ctx->stream));
+  if (best_shape < 0) {
+    set_error("tensor-core conv: a level's slab and bank stages exceed shared memory or the planes' buffer");
+    return GEYE_ERR_UNSUPPORTED;
   }
-  mp.tc_smem = best.max_smem;
-  mp.tc_chunks = (int)best.chunks.size();
-  mp.tc_planes = NQ;
-  mp.tc_shape = best_shape;
-  mp.tc_tuned_ms = best_ms / 3.0f;
-  GEYE_TRY(upload_bytes(ctx, mp.d_tc_jobs, best.jobs.data(), sizeof(TcJob) * best.jobs.size()));
-  GEYE_TRY(upload_bytes(ctx, mp.d_tc_chunks, best.chunks.data(), sizeof(int4) * best.chunks.size()));
-  GEYE_TRY(upload_bytes(ctx, mp.d_tc_outs, best.outs.data(), sizeof(int) * best.outs.size()));
-  GEYE_TRY(upload_bytes(ctx, mp.d_tc_inv, best.inv.data(), sizeof(float) * best.inv.size()));
-  GEYE_TRY(upload_bytes(ctx, mp.d_tc_dims, best.dims.data(), sizeof(int2) * best.dims.size()));
+  if (timed) {
+    std::lock_guard<std::mutex> lk(m0->tc_mu);
+    m0->tc_tuned[key] = {best_shape, best_ms / 3.0f};
+  }
+  T.smem = best_smem;
+  T.n_chunks = (int)best.size();
+  T.stages = kTcShapes[best_shape].stages;
+  T.shape = best_shape;
+  T.tuned_ms = best_ms / 3.0f;
+  GEYE_TRY(upload_bytes(ctx, T.d_chunks, best.data(), sizeof(int4) * std::max<size_t>(best.size(), 1)));
   return GEYE_OK;
 }
 
-}  // namespace geye
-
-geye_status geye_conv_tuning(geye_ctx *ctx, const geye_model *m, int shape[3], float *ms) {
-  ARG_CHECK(ctx && m && shape && ms, "null argument");
-  ARG_CHECK(ctx->last_plan, "no run yet");
-  for (auto &mp : ctx->last_plan->models) {
-    if (mp->model != m) continue;
-    ARG_CHECK(mp->tc_shape >= 0, "the last run's plan has no tensor-core convolution");
-    shape[0] = geye::kTcShapes[mp->tc_shape].t_cap;
-    shape[1] = (int)(geye::kTcShapes[mp->tc_shape].budget / 1024);
-    shape[2] = mp->tc_chunks;
-    *ms = mp->tc_tuned_ms;
-    return GEYE_OK;
-  }
-  ARG_CHECK(false, "the last run has no such model");
-  return GEYE_ERR_ARG;
-}
-
-namespace geye {
-
-geye_status run_conv_tc(geye_ctx *ctx, Plan &P, ModelPlan &mp) {
+geye_status run_conv_tc(geye_ctx *ctx, Plan &P) {
+  const TcPlan &T = P.tc;
   if (!P.arena16.p) {
     set_error("tensor-core conv: the plan has no feature planes");
     return GEYE_ERR_UNSUPPORTED;
   }
-  if (mp.tc_chunks == 0) return GEYE_OK;
-  const void *bank = mp.tc_planes == 2 ? mp.model->d_bank8 : mp.model->d_bank16;
-  launch_conv_tc(mp.tc_planes, mp.d_tc_jobs.as<TcJob>(), mp.d_tc_chunks.as<int4>(), mp.tc_chunks,
-                 mp.d_tc_outs.as<int>(), mp.d_tc_inv.as<float>(), mp.d_tc_dims.as<int2>(), P.arena16.as<uint8_t>(),
-                 static_cast<const uint8_t *>(bank), P.arena.as<float>(), P.d_small.as<int>() + 130, mp.tc_smem,
-                 ctx->stream);
+  if (T.n_chunks == 0) return GEYE_OK;
+  launch_conv_tc(T.planes, T.d_jobs.as<TcJob>(), T.d_chunks.as<int4>(), T.n_chunks, T.d_cols.as<TcCol>(),
+                 P.arena16.as<uint8_t>(), T.d_bank.as<uint8_t>(), T.rows, T.stages, P.arena.as<float>(),
+                 P.d_small.as<int>() + 130, T.smem, ctx->stream);
   ctx->launches++;
-  const cudaError_t e = cudaGetLastError();
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess && !T.sums.empty()) {
+    dim3 g((T.sum_max_r + 255) / 256, (unsigned)T.sums.size());
+    k_root_sum<<<g, 256, 0, ctx->stream>>>(T.d_sums.as<RootSumJob>(), P.arena.as<float>());
+    ctx->launches++;
+    e = cudaGetLastError();
+  }
   if (e != cudaSuccess) {
     set_error(std::string("tensor-core conv: ") + cudaGetErrorString(e));
     return GEYE_ERR_CUDA;
@@ -782,61 +862,82 @@ geye_status run_conv_tc(geye_ctx *ctx, Plan &P, ModelPlan &mp) {
 
 // fconvsMT on the tensor cores for the stage entry point (the context's conv
 // mode): d_feat is [pos][32] float on the device (a0 x a1 cells), filters on
-// the host; maps go to d_out + out_off[i].  Temporary device buffers live in tmp.
+// the host; maps go to d_out + out_off[i].  One job: every filter a row of one
+// bank over the largest filter's grid.  Temporary device buffers live in tmp.
 geye_status conv_tc_maps(geye_ctx *ctx, const float *d_feat, int a0, int a1, const float *const *filters,
                          const int *b_dims, int n_filters, float *d_out, const std::vector<int> &out_off,
                          std::vector<std::unique_ptr<DevBuf>> &tmp) {
   const geye_conv_mode mode = ctx->conv_mode;
   const int NQ = tc_planes_of(mode);
   auto buf = [&]() { tmp.push_back(std::make_unique<DevBuf>()); return tmp.back().get(); };
-  std::vector<const float *> filt(filters, filters + n_filters), d_filt;
-  std::vector<int> b0s, b1s, kinds(n_filters, 0);
-  for (int i = 0; i < n_filters; i++) { b0s.push_back(b_dims[2 * i]); b1s.push_back(b_dims[2 * i + 1]); }
-  std::vector<BankGroup> groups;
-  std::vector<uint16_t> bank16;
-  std::vector<float> scale;
-  size_t total = 0;
-  build_banks(filt, b0s, b1s, kinds, mode, groups, bank16, scale, total, kTcMaxN);
-  for (int i = 0; i < n_filters; i++) {   // the FP8 bank is converted on the device from FP32 copies
+  int gb0 = 1, gb1 = 1;
+  for (int i = 0; i < n_filters; i++) { gb0 = std::max(gb0, b_dims[2 * i]); gb1 = std::max(gb1, b_dims[2 * i + 1]); }
+  const int R = pad16(n_filters);
+  if (R > kTcMaxN) {
+    set_error("tensor-core conv: more than 256 filters in one call");
+    return GEYE_ERR_UNSUPPORTED;
+  }
+  std::vector<BankRow> rows(R);
+  std::vector<TcCol> cols(R);
+  int p_valid = 0;
+  for (int i = 0; i < n_filters; i++) {
+    const int fb0 = b_dims[2 * i], fb1 = b_dims[2 * i + 1];
+    const size_t n = (size_t)fb0 * fb1 * kFeat;
     DevBuf *f = buf();
-    const size_t n = (size_t)b0s[i] * b1s[i] * kFeat;
     GEYE_TRY(upload_bytes(ctx, *f, filters[i], sizeof(float) * n));
-    d_filt.push_back(f->as<float>());
+    BankRow &B = rows[i];
+    B.h = filters[i];
+    B.d = f->as<float>();
+    B.fb0 = fb0;
+    B.fb1 = fb1;
+    B.scale = mode == GEYE_CONV_FP8 ? e4m3_filter_scale(filters[i], n) : 1.f;
+    TcCol &C = cols[i];
+    C.rows = a0 - fb0 + 1;
+    C.cols = a1 - fb1 + 1;
+    if (C.rows < 1 || C.cols < 1) continue;   // no map for a filter larger than the level
+    C.kind = 1;
+    C.off = out_off[i];
+    C.inv = 1.f / (B.scale * (mode == GEYE_CONV_FP8 ? kFp8FeatScale : 1.f));
+    p_valid = std::max(p_valid, (C.cols - 1) * a0 + C.rows);
   }
-  // planes, then a zeroed tail that slabs of filters smaller than their group's grid may read
+  if (p_valid == 0) return GEYE_OK;
+  TcJob J{};
+  J.plane_off = 0;
+  J.lo_off = -1;
+  J.plane_cells = a0 * a1 + kTcPlanePad;
+  J.fs0 = a0; J.fs1 = a1;
+  J.b0 = gb0; J.b1 = gb1;
+  J.row0 = 0; J.n = R;
+  J.ntiles = (p_valid + kTcM - 1) / kTcM;
+  // planes, then a zeroed tail that slabs near the end may read (their outputs are discarded)
   const int ncell = a0 * a1;
-  int mb0 = 1, mb1 = 1;
-  for (auto &g : groups) { mb0 = std::max(mb0, g.b0); mb1 = std::max(mb1, g.b1); }
-  const size_t tail_cells = (size_t)mb1 * a0 + mb0 + (size_t)kTcMaxTiles * kTcM;
+  const size_t tail_cells = (size_t)gb1 * a0 + gb0 + (size_t)kTcMaxTiles * kTcM;
   const size_t plane_total = (size_t)NQ * (ncell + kTcPlanePad);
-  TcTables T;
-  for (auto &g : groups) {
-    std::vector<int> map_off;
-    for (int f : g.filt) map_off.push_back(out_off[f]);
-    if (!add_tc_job(T, NQ, 0, a0, a1, g, map_off, (long long)(plane_total + tail_cells))) {
-      set_error("tensor-core conv: a filter bank and its feature reach exceed shared memory");
-      return GEYE_ERR_UNSUPPORTED;
-    }
+  std::vector<int4> chunks;
+  size_t smem = 0;
+  const std::vector<TcJob> jobs{J};
+  int stages = 0;
+  for (int si = 0; si < kTcNumShapes && !stages; si++)
+    if (chunk_jobs(jobs, NQ, kTcShapes[si], (long long)(plane_total + tail_cells), chunks, smem))
+      stages = kTcShapes[si].stages;
+  if (!stages) {
+    set_error("tensor-core conv: the filters' slab and bank stages exceed shared memory");
+    return GEYE_ERR_UNSUPPORTED;
   }
-  DevBuf *planes = buf(), *d_bank = buf(), *d_jobs = buf(), *d_chunks = buf(), *d_outs = buf(), *d_inv = buf(),
-         *d_dims = buf(), *d_err = buf();
+  DevBuf *planes = buf(), *d_bank = buf(), *d_jobs = buf(), *d_chunks = buf(), *d_cols = buf(), *d_err = buf();
   GEYE_TRY(planes->alloc(ctx, (plane_total + tail_cells) * 16));
   CUDA_TRY(cudaMemsetAsync(planes->as<uint8_t>() + plane_total * 16, 0, tail_cells * 16, ctx->stream));
-  GEYE_TRY(d_bank->alloc(ctx, std::max<size_t>(total, 16)));
-  GEYE_TRY(upload_bank(groups, mode, bank16, d_filt, scale, total, d_bank->p, ctx->stream));
-  GEYE_TRY(upload_bytes(ctx, *d_jobs, T.jobs.data(), sizeof(TcJob) * T.jobs.size()));
-  GEYE_TRY(upload_bytes(ctx, *d_chunks, T.chunks.data(), sizeof(int4) * T.chunks.size()));
-  GEYE_TRY(upload_bytes(ctx, *d_outs, T.outs.data(), sizeof(int) * T.outs.size()));
-  GEYE_TRY(upload_bytes(ctx, *d_inv, T.inv.data(), sizeof(float) * T.inv.size()));
-  GEYE_TRY(upload_bytes(ctx, *d_dims, T.dims.data(), sizeof(int2) * T.dims.size()));
+  GEYE_TRY(upload_bank(ctx, rows, NQ, gb0, gb1, R, *d_bank));
+  GEYE_TRY(upload_bytes(ctx, *d_jobs, &J, sizeof(TcJob)));
+  GEYE_TRY(upload_bytes(ctx, *d_chunks, chunks.data(), sizeof(int4) * chunks.size()));
+  GEYE_TRY(upload_bytes(ctx, *d_cols, cols.data(), sizeof(TcCol) * cols.size()));
   GEYE_TRY(d_err->alloc(ctx, 16));
   CUDA_TRY(cudaMemsetAsync(d_err->p, 0, 16, ctx->stream));
   const int grid = std::max(1, std::min((ncell + kTcPlanePad + 255) / 256, 1024));
   if (NQ == 4) k_feat_planes<4><<<grid, 256, 0, ctx->stream>>>(d_feat, ncell, planes->as<uint8_t>());
   else k_feat_planes<2><<<grid, 256, 0, ctx->stream>>>(d_feat, ncell, planes->as<uint8_t>());
-  launch_conv_tc(NQ, d_jobs->as<TcJob>(), d_chunks->as<int4>(), (int)T.chunks.size(), d_outs->as<int>(),
-                 d_inv->as<float>(), d_dims->as<int2>(), planes->as<uint8_t>(), d_bank->as<uint8_t>(), d_out,
-                 d_err->as<int>(), T.max_smem, ctx->stream);
+  launch_conv_tc(NQ, d_jobs->as<TcJob>(), d_chunks->as<int4>(), (int)chunks.size(), d_cols->as<TcCol>(),
+                 planes->as<uint8_t>(), d_bank->as<uint8_t>(), R, stages, d_out, d_err->as<int>(), smem, ctx->stream);
   CUDA_TRY(cudaGetLastError());
   int errw = 0;
   CUDA_TRY(cudaMemcpyAsync(&errw, d_err->p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
@@ -849,3 +950,18 @@ geye_status conv_tc_maps(geye_ctx *ctx, const float *d_feat, int a0, int a1, con
 }
 
 }  // namespace geye
+
+geye_status geye_conv_tuning(geye_ctx *ctx, const geye_model *m, int shape[3], float *ms) {
+  ARG_CHECK(ctx && m && shape && ms, "null argument");
+  ARG_CHECK(ctx->last_plan, "no run yet");
+  const geye::Plan &P = *ctx->last_plan;
+  bool in_plan = false;
+  for (auto &mp : P.models) in_plan |= mp->model == m;
+  ARG_CHECK(in_plan, "the last run has no such model");
+  ARG_CHECK(P.tc.shape >= 0, "the last run's plan has no tensor-core convolution");
+  shape[0] = geye::kTcShapes[P.tc.shape].t_cap;
+  shape[1] = (int)(geye::kTcShapes[P.tc.shape].budget / 1024);
+  shape[2] = P.tc.n_chunks;
+  *ms = P.tc.tuned_ms;
+  return GEYE_OK;
+}

@@ -27,21 +27,25 @@ constexpr int kTcPlanePad = 128;   // cells after each bf16 feature plane (reach
 // Raises a kernel's dynamic shared-memory limit to at least `smem` bytes on the
 // current device. The attribute belongs to the device, so the record of the largest
 // size set is kept per device; raises are serialised, so a concurrent smaller raise
-// never lowers a limit another thread's launch relies on.
+// never lowers a limit another thread's launch relies on.  Only a raise that
+// succeeded is recorded: a failed one is tried again by the next launch, and
+// its error comes back (the launch that needs the limit then fails and reports).
 constexpr int kSmemAttrDevices = 64;
 struct SmemAttr {
   size_t set[kSmemAttrDevices] = {};
   std::mutex mu;
 };
 template <typename K>
-inline void raise_smem(SmemAttr &A, K *kernel, size_t smem) {
-  if (smem <= 48 * 1024) return;
+inline cudaError_t raise_smem(SmemAttr &A, K *kernel, size_t smem) {
+  if (smem <= 48 * 1024) return cudaSuccess;
   int dev = 0;
-  cudaGetDevice(&dev);
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
   std::lock_guard<std::mutex> g(A.mu);
-  if (dev >= 0 && dev < kSmemAttrDevices && A.set[dev] >= smem) return;
-  cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (dev >= 0 && dev < kSmemAttrDevices) A.set[dev] = smem;
+  if (dev >= 0 && dev < kSmemAttrDevices && A.set[dev] >= smem) return cudaSuccess;
+  e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e == cudaSuccess && dev >= 0 && dev < kSmemAttrDevices) A.set[dev] = smem;
+  return e;
 }
 
 // ----------------------------------------------------------------------------
@@ -65,6 +69,7 @@ struct HogJob {
   int fs0, fs1;            // output cells
   int feat_off;            // [pos][32] float
   int feat16_off;          // tensor-core planes (offset in 2-byte units), -1 = not written
+  int feat16lo_off;        // BF16 remainder planes (root levels in BF16 mode), -1 = none
   int tc_planes;           // 4: bf16 planes [4][fs0*fs1 + kTcPlanePad][16 B]; 2: e4m3 planes; 0: none
   int mag_off, bin_off;    // the image's pixel magnitudes (float) and bins (u8), [x * pix_Y + y]
   int pix_Y;
@@ -87,6 +92,34 @@ struct ConvJob {           // a block of outputs of one (level, filter group)
   int c0, c1;              // output dims
   int out_off;             // output of filter g at out_off + g*c0*c1
   int tiles_y, tiles_x;    // output tiles of this job
+};
+
+// tensor-core convolution (conv_tc.cu)
+struct TcJob {             // one feature level's MMA chain over the rows of the filter bank it uses
+  int plane_off;           // the level's NQ feature planes, in 2-byte units of arena16
+  int lo_off;              // its BF16 remainder planes (split chain), -1: none
+  int plane_cells;         // cells per plane (fs0*fs1 + kTcPlanePad)
+  int fs0, fs1;            // feature rows, columns
+  int b0, b1;              // tap grid
+  int row0, n;             // bank rows row0 .. row0+n-1: the MMA's N columns (a multiple of 16)
+  int lo_row, n_lo;        // split chain: rows row0+lo_row .. +n_lo (0: none), accumulated into TMEM columns lo_row ..
+  int col_tab;             // first entry of the job's column table (n entries)
+  int ntiles;              // 128-position tiles the job covers
+};
+
+struct TcCol {             // what the epilogue does with one MMA column of a job
+  int kind;                // 0: nothing; 1: a map; 2: a root block
+  int off;                 // 1: the map's float offset; 2: the block buffer's (indexed by position)
+  int rows, cols;          // 1: the map's rows (c0) and columns (c1)
+  int pair;                // 2: the column of the block's hi*lo products, relative (0: none)
+  float inv;               // factor undoing the operand scaling (FP8), else 1
+};
+
+constexpr int kMaxRootBlocks = 16;
+struct RootSumJob {        // one (level, component) root map as the sum of its blocks
+  int out_off, r0, r1, fs0, nblk;
+  int blk[kMaxRootBlocks];     // block buffers (position-indexed)
+  int shift[kMaxRootBlocks];   // the block's position offset: x0*fs0 + y0
 };
 
 struct DtJob {             // one part map: DT of the negated map
@@ -174,11 +207,9 @@ struct geye_model {
   int *d_filt_off = nullptr;   // float offsets, NoR + NoP entries
   float *d_coef = nullptr;     // box regression [comp][x1, y1, x2, y2][ML]
   std::vector<int> filt_off;
-  // filter banks for the tensor-core convolution (built on first use): bf16, e4m3
-  void *d_bank16 = nullptr;
-  void *d_bank8 = nullptr;
-  // tile shape the autotuner chose per plan geometry (frame size, levels, mode),
-  // shared by every context that plans this model at that geometry
+  // tile shapes the autotuners chose per plan geometry (frame size, levels, mode,
+  // and for the tensor-core convolution the plan's other models), shared by every
+  // context that plans this model at that geometry
   std::mutex tc_mu;
   std::map<std::string, std::pair<int, float>> tc_tuned;   // candidate, ms per launch
   int gl() const { return (h.numpart[0] + 1) * 4 + 3; }

@@ -419,6 +419,7 @@ __global__ void k_hog_feat(const HogJob *__restrict__ jobs, float *__restrict__ 
       const size_t plane = ((size_t)ncell + kTcPlanePad) * 16;
       if (J.tc_planes == 4) tc_store_planes<4>(out, planes, plane, i);
       else if (J.tc_planes == 2) tc_store_planes<2>(out, planes, plane, i);
+      if (J.feat16lo_off >= 0) tc_store_planes_lo(out, arena16 + 2 * (size_t)J.feat16lo_off, plane, i);
     }
   }
 }

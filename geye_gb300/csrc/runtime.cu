@@ -249,15 +249,6 @@ static void feature_dims(int h, int w, int sbin, int &b0, int &b1, int &fs0, int
 // ----------------------------------------------------------------------------
 // plan construction
 // ----------------------------------------------------------------------------
-struct ArenaAlloc {
-  size_t words = 0;
-  int take(size_t n) {
-    size_t o = (words + 31) & ~size_t(31);   // 128-byte alignment
-    words = o + n;
-    return (int)o;
-  }
-};
-
 static geye_status build_model_plan(geye_ctx *ctx, Plan &P, geye_model *mdl, int LEN_m, ArenaAlloc &A) {
   const HostModel &m = mdl->h;
   auto mp = std::make_unique<ModelPlan>();
@@ -520,12 +511,19 @@ static geye_status build_pyramid_plan(geye_ctx *ctx, Plan &P, int width, int hei
       size_t o = (P.arena16_elems + 63) & ~size_t(63);
       L.feat16_off = (int)o;
       P.arena16_elems = o + (size_t)tc_planes * ((size_t)L.fs0 * L.fs1 + kTcPlanePad) * 8;
+      // root levels in BF16 mode: the BF16 remainder planes right after (root filters
+      // run on split operands, conv_tc.cu)
+      if (tc_planes == 4 && l >= interval) {
+        L.feat16lo_off = (int)P.arena16_elems;
+        P.arena16_elems += (size_t)4 * ((size_t)L.fs0 * L.fs1 + kTcPlanePad) * 8;
+      }
     }
     L.hist_off = A.take((size_t)19 * std::max(b0 * b1, 1));
     if (b0 > 0 && b1 > 0) {
       HogJob J{};
       J.img_off = L.img_off; J.h = L.img_h; J.w = L.img_w; J.sbin = L.sbin; J.b0 = b0; J.b1 = b1;
       J.hist_off = L.hist_off; J.fs0 = L.fs0; J.fs1 = L.fs1; J.feat_off = L.feat_off; J.feat16_off = L.feat16_off;
+      J.feat16lo_off = L.feat16lo_off;
       J.tc_planes = tc_planes;
       J.corner_off = A.take((size_t)(L.fs0 + 1) * (L.fs1 + 1));
       J.mag_off = L.img_level;   // resolved below, once the image's pixel buffer is placed
@@ -777,10 +775,11 @@ static geye_status get_frame_plan(geye_ctx *ctx, geye_model *const *models, int 
   ArenaAlloc A;
   GEYE_TRY(build_pyramid_plan(ctx, *P, width, height, LEN, interval, sbin, A, tc_planes));
   for (int i = 0; i < n_models; i++) GEYE_TRY(build_model_plan(ctx, *P, models[i], LENs[i], A));
+  if (ctx->conv_mode != GEYE_CONV_FP32) GEYE_TRY(plan_tc(ctx, *P, A));
   GEYE_TRY(finish_plan(ctx, *P, A));
   // after the arena exists: the tile shapes are tuned on it
   if (ctx->conv_mode != GEYE_CONV_FP32)
-    for (auto &mp : P->models) GEYE_TRY(build_tc_jobs(ctx, *P, *mp));
+    GEYE_TRY(build_tc_plan(ctx, *P));
   else
     for (auto &mp : P->models) GEYE_TRY(tune_conv_fp32(ctx, *P, *mp));
   GEYE_TRY(P->d_bgr.alloc(ctx, (size_t)width * height * 3 + 64));
@@ -850,12 +849,10 @@ geye_status run_hog(geye_ctx *ctx, Plan &P) {
   return check_launch(ctx, "hog");
 }
 
-geye_status run_conv_tc(geye_ctx *ctx, Plan &P, ModelPlan &mp);
-
+// FP32 conv of one model (the tensor-core modes convolve every model at once: run_conv_tc)
 geye_status run_conv(geye_ctx *ctx, Plan &P, ModelPlan &mp) {
   geye_model *m = mp.model;
   float *arena = P.arena.as<float>();
-  if (ctx->conv_mode != GEYE_CONV_FP32) return run_conv_tc(ctx, P, mp);
   if (!mp.root_jobs.empty()) {
     launch_conv_fp32(mp.d_root_jobs.as<ConvJob>(), (int)mp.root_jobs.size(), mp.root_tiles_y, mp.root_tiles_x,
                      m->d_filters, m->d_filt_off, arena, arena, mp.root_max_b0, mp.root_max_b1, mp.root_max_g,
@@ -991,8 +988,11 @@ static geye_status run_body(geye_ctx *ctx, Plan &P, float thresh, float overlap)
   T.mark(1);
   GEYE_TRY(run_hog(ctx, P));
   T.mark(2);
+  const bool tc = ctx->conv_mode != GEYE_CONV_FP32;
+  if (tc) GEYE_TRY(run_conv_tc(ctx, P));   // every model's filters in one launch
   if (ctx->timing || P.models.size() < 2) {   // stage by stage (per-stage times)
-    for (auto &mp : P.models) GEYE_TRY(run_conv(ctx, P, *mp));
+    if (!tc)
+      for (auto &mp : P.models) GEYE_TRY(run_conv(ctx, P, *mp));
     T.mark(3);
     for (auto &mp : P.models) GEYE_TRY(run_dt(ctx, P, *mp));
     T.mark(4);
@@ -1003,7 +1003,7 @@ static geye_status run_body(geye_ctx *ctx, Plan &P, float thresh, float overlap)
     // beside model 0 (their kernels take the context's stream, swapped while
     // they are issued), joined before NMS
     auto chain = [&](size_t mi) -> geye_status {
-      GEYE_TRY(run_conv(ctx, P, *P.models[mi]));
+      if (!tc) GEYE_TRY(run_conv(ctx, P, *P.models[mi]));
       GEYE_TRY(run_dt(ctx, P, *P.models[mi]));
       return run_score(ctx, P, *P.models[mi], (int)mi, thresh);
     };
@@ -1159,8 +1159,6 @@ geye_status features_plan(geye_ctx *ctx, geye_model *model, const int *ftsize, c
   }
   GEYE_TRY(build_model_plan(ctx, *P, model, n_levels, A));
   GEYE_TRY(finish_plan(ctx, *P, A));
-  if (ctx->conv_mode != GEYE_CONV_FP32)
-    for (auto &mp : P->models) GEYE_TRY(build_tc_jobs(ctx, *P, *mp));
   std::string key = "features:" + std::to_string((uintptr_t)P.get());
   *out = P.get();
   ctx->plans[key] = std::move(P);

@@ -50,8 +50,12 @@ struct Plan;
 struct ModelPlan;
 // copies n bytes from the host into buf (allocated to fit)
 geye_status upload_bytes(geye_ctx *ctx, DevBuf &buf, const void *src, size_t n);
-// tensor-core convolution job tables of one model of a plan (conv_tc.cu)
-geye_status build_tc_jobs(geye_ctx *ctx, Plan &P, ModelPlan &mp);
+struct ArenaAlloc;
+// tensor-core convolution of a plan's models together (conv_tc.cu): tables and
+// arena space before the arena exists, bank and tuned chunks after, the launch
+geye_status plan_tc(geye_ctx *ctx, Plan &P, ArenaAlloc &A);
+geye_status build_tc_plan(geye_ctx *ctx, Plan &P);
+geye_status run_conv_tc(geye_ctx *ctx, Plan &P);
 // d_small[kSortLevelsUsed]: the deepest NMS sort level with work in the frame;
 // d_small[kNmsRoundsUsed]: the greedy batches it took
 constexpr int kSortLevelsUsed = 48, kNmsRoundsUsed = 49;
@@ -60,6 +64,16 @@ void note_sort_levels(geye_ctx *ctx, Plan &P, int used, int rounds);
 geye_status conv_tc_maps(geye_ctx *ctx, const float *d_feat, int a0, int a1, const float *const *filters,
                          const int *b_dims, int n_filters, float *d_out, const std::vector<int> &out_off,
                          std::vector<std::unique_ptr<DevBuf>> &tmp);
+
+// Bump allocator of a plan's float arena (128-byte aligned offsets, in words).
+struct ArenaAlloc {
+  size_t words = 0;
+  int take(size_t n) {
+    size_t o = (words + 31) & ~size_t(31);   // 128-byte alignment
+    words = o + n;
+    return (int)o;
+  }
+};
 
 // Device buffer owned by a plan or context.
 struct DevBuf {
@@ -80,6 +94,7 @@ struct LevelInfo {
   float scale = 0.f;          // scales[] entry
   int feat_off = -1;          // [pos][32]
   int feat16_off = -1;        // tensor-core planes, 2-byte units
+  int feat16lo_off = -1;      // BF16 remainder planes (root levels, BF16 mode), 2-byte units
   int hist_off = -1;
 };
 
@@ -102,15 +117,34 @@ struct ModelPlan {
   std::vector<int> part_map_off, part_d0, part_d1;     // [L*NoP + p]
   std::vector<int> skipped;                            // per level
   double conv_flops = 0, conv_bytes = 0, dt_bytes = 0, score_bytes = 0;
-  // tensor-core convolution (conv_tc.cu): jobs, CTA chunks, map offsets and
-  // per-map factors undoing the operand scaling; planes per position (4 bf16, 2 e4m3)
-  DevBuf d_tc_jobs, d_tc_chunks, d_tc_outs, d_tc_inv, d_tc_dims;
   // A_SCORE lookups: [job][image column] score-map column base, [job][image row] score row
   DevBuf d_as_col, d_as_row;
-  int tc_chunks = 0, tc_planes = 0;
-  int tc_shape = -1;          // tile-shape candidate the autotuner chose
-  float tc_tuned_ms = 0.f;    // its measured time per launch
-  size_t tc_smem = 0;
+};
+
+// One row of the tensor-core convolution's filter bank (conv_tc.cu): filter
+// `filt` of model `mi` (its roots, then its parts), from filter row y0 and
+// column x0 on, or the BF16 remainder of those weights; mi < 0: a padding row.
+struct BankRowSpec {
+  int mi = -1, filt = 0, y0 = 0, x0 = 0, lo = 0;
+  float scale = 1.f;   // FP8: the filter's power-of-two scale
+};
+
+// The tensor-core convolution of all of a plan's models (conv_tc.cu): bank
+// rows, one job per feature level, the epilogue's column tables, the root sums.
+struct TcPlan {
+  int planes = 0;                       // 4: BF16 planes, 2: e4m3
+  int grid_b0 = 0, grid_b1 = 0;         // the bank's tap grid
+  int rows = 0, rows_p16 = 0, rows_r16 = 0;
+  std::vector<BankRowSpec> bank_rows;
+  std::vector<TcJob> jobs;
+  std::vector<TcCol> cols;
+  std::vector<RootSumJob> sums;
+  int sum_max_r = 0;
+  DevBuf d_bank, d_jobs, d_chunks, d_cols, d_sums;
+  int n_chunks = 0, stages = 0;
+  size_t smem = 0;
+  int shape = -1;                       // tile-shape candidate the autotuner chose
+  float tuned_ms = 0.f;                 // its measured time per launch
 };
 
 struct Plan {
@@ -130,6 +164,7 @@ struct Plan {
   DevBuf d_pix_jobs;
   int pix_max_xe = 0;
   std::vector<std::unique_ptr<ModelPlan>> models;
+  TcPlan tc;                             // BF16 / FP8 modes
   // memory
   size_t arena_words = 0, arena16_elems = 0;
   DevBuf arena, arena16;

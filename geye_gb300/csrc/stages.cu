@@ -176,7 +176,7 @@ geye_status geye_calc_feature(geye_ctx *ctx, const float *src, const int *isize,
   CUDA_TRY(cudaMemcpyAsync(arena, src, sizeof(float) * n_img, cudaMemcpyHostToDevice, ctx->stream));
   HogJob J{};
   J.img_off = 0; J.h = h; J.w = w; J.sbin = sbin; J.b0 = b0; J.b1 = b1; J.hist_off = (int)hist;
-  J.fs0 = fs0; J.fs1 = fs1; J.feat_off = (int)feat_off; J.feat16_off = -1;
+  J.fs0 = fs0; J.fs1 = fs1; J.feat_off = (int)feat_off; J.feat16_off = -1; J.feat16lo_off = -1;
   J.mag_off = X.mag_off; J.bin_off = X.bin_off; J.pix_Y = X.Y; J.corner_off = (int)corner_off;
   HogJob *d_j;
   GEYE_TRY(S.put(&J, 1, &d_j));

@@ -37,4 +37,21 @@ __device__ __forceinline__ void tc_store_planes(const float *f, uint8_t *planes,
   }
 }
 
+// the BF16 remainders of position i's channels, f - bf16(f), rounded to BF16
+// (four planes like tc_store_planes<4>): with the high planes, a split operand
+// whose two BF16 parts carry about 16 significant bits
+__device__ __forceinline__ void tc_store_planes_lo(const float *f, uint8_t *planes, size_t plane_bytes, size_t i) {
+#pragma unroll
+  for (int q = 0; q < 4; q++) {
+    __nv_bfloat162 v[4];
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      const float a = f[8 * q + 2 * k], b = f[8 * q + 2 * k + 1];
+      v[k] = __floats2bfloat162_rn(a - __bfloat162float(__float2bfloat16_rn(a)),
+                                   b - __bfloat162float(__float2bfloat16_rn(b)));
+    }
+    *reinterpret_cast<uint4 *>(planes + q * plane_bytes + i * 16) = *reinterpret_cast<uint4 *>(v);
+  }
+}
+
 }  // namespace geye

@@ -618,6 +618,71 @@ void orc_fconv_f64(const float *A, int a0, int a1, const float *B, int b0, int b
         }
 }
 
+/* Tensor-core operand emulation, for measuring what a reduced-precision      */
+/* convolution does to detections (not the reference's arithmetic): each      */
+/* operand is rounded to BF16 (round to nearest even), or split into a BF16   */
+/* high part and the BF16 rounding of the remainder, and the products are     */
+/* summed in double, then rounded to float.  mode 1: both operands BF16;      */
+/* 2: both split, hi*hi + hi*lo + lo*hi; 3: features BF16, filters FP32;      */
+/* 4: features split, filters BF16 (hi*b + lo*b); 5: TF32 operands (10-bit   */
+/* mantissa, round to nearest even); 6: mode 2 for root filters, mode 1 for   */
+/* part filters.                                                              */
+static float bf16_rne(float x)
+{
+    uint32_t u;
+    memcpy(&u, &x, 4);
+    if ((u & 0x7f800000u) == 0x7f800000u) return x;
+    u += 0x7fffu + ((u >> 16) & 1u);
+    u &= 0xffff0000u;
+    memcpy(&x, &u, 4);
+    return x;
+}
+
+static float tf32_rne(float x)
+{
+    uint32_t u;
+    memcpy(&u, &x, 4);
+    if ((u & 0x7f800000u) == 0x7f800000u) return x;
+    u += 0xfffu + ((u >> 13) & 1u);
+    u &= 0xffffe000u;
+    memcpy(&x, &u, 4);
+    return x;
+}
+
+static int g_conv_emulation = 0;
+void orc_set_conv_emulation(int mode) { g_conv_emulation = mode; }
+
+static void fconv_emul(const float *A, int a0, int a1, const float *B, int b0, int b1, float *C, int mode)
+{
+    const int c0 = a0 - b0 + 1, c1 = a1 - b1 + 1;
+    if (c0 < 1 || c1 < 1) return;
+    const size_t ASQ = (size_t)a0 * a1, BSQ = (size_t)b0 * b1;
+    float *Ah = (float *)malloc(sizeof(float) * 31 * ASQ), *Al = (float *)malloc(sizeof(float) * 31 * ASQ);
+    float *Bh = (float *)malloc(sizeof(float) * 31 * BSQ), *Bl = (float *)malloc(sizeof(float) * 31 * BSQ);
+    for (size_t i = 0; i < 31 * ASQ; i++) { Ah[i] = bf16_rne(A[i]); Al[i] = bf16_rne(A[i] - Ah[i]); }
+    for (size_t i = 0; i < 31 * BSQ; i++) { Bh[i] = bf16_rne(B[i]); Bl[i] = bf16_rne(B[i] - Bh[i]); }
+    for (int x = 0; x < c1; x++)
+        for (int y = 0; y < c0; y++) {
+            double acc = 0;
+            for (int f = 0; f < 31; f++)
+                for (int xp = 0; xp < b1; xp++)
+                    for (int yp = 0; yp < b0; yp++) {
+                        const size_t ia = f * ASQ + (size_t)(x + xp) * a0 + y + yp, ib = f * BSQ + xp * b0 + yp;
+                        double p;
+                        switch (mode) {
+                        case 1: p = (double)Ah[ia] * Bh[ib]; break;
+                        case 2: p = (double)Ah[ia] * Bh[ib] + (double)Ah[ia] * Bl[ib] + (double)Al[ia] * Bh[ib]; break;
+                        case 3: p = (double)Ah[ia] * B[ib]; break;
+                        case 5: p = (double)tf32_rne(A[ia]) * tf32_rne(B[ib]); break;
+                        default: p = (double)Ah[ia] * Bh[ib] + (double)Al[ia] * Bh[ib]; break;
+                        }
+                        acc += p;
+                    }
+            C[(size_t)x * c0 + y] = (float)acc;
+        }
+    free(Ah); free(Al); free(Bh); free(Bl);
+}
+
 /* max over positions of sum |A| |B| (the magnitude that bounds rounding errors) */
 static double fconv_abs_max(const float *A, int a0, int a1, const float *B, int b0, int b1)
 {
@@ -812,7 +877,11 @@ orc_scores *orc_compute_scores(const orc_model *m, const orc_pyramid *P, int nth
         int c0 = a0 - bs[0] + 1, c1 = a1 - bs[1] + 1;
         if (c0 < 1 || c1 < 1) { c0 = c1 = 0; }
         float *C = (float *)calloc((size_t)(c0 > 0 ? c0 : 1) * (c1 > 0 ? c1 : 1), sizeof(float));
-        if (c0 > 0) orc_fconv(P->feat[lv], a0, a1, kind == 0 ? m->rootfilter[j] : m->partfilter[j], bs[0], bs[1], C);
+        if (c0 > 0 && g_conv_emulation)
+            fconv_emul(P->feat[lv], a0, a1, kind == 0 ? m->rootfilter[j] : m->partfilter[j], bs[0], bs[1], C,
+                       g_conv_emulation == 6 ? (kind == 0 ? 2 : 1) : g_conv_emulation);
+        else if (c0 > 0)
+            orc_fconv(P->feat[lv], a0, a1, kind == 0 ? m->rootfilter[j] : m->partfilter[j], bs[0], bs[1], C);
         if (kind == 0) { S->root[lv * NoC + j] = C; S->rsz[2 * (lv * NoC + j)] = c0; S->rsz[2 * (lv * NoC + j) + 1] = c1; }
         else { S->part[lv * m->NoP + j] = C; S->psz[2 * (lv * m->NoP + j)] = c0; S->psz[2 * (lv * m->NoP + j) + 1] = c1; }
     }

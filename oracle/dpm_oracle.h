@@ -79,6 +79,9 @@ orc_pyramid *orc_build_pyramid(const orc_model *m, int max_scale, const uint8_t 
 void orc_free_pyramid(orc_pyramid *P);
 void orc_fconv(const float *A, int a0, int a1, const float *B, int b0, int b1, float *C);
 void orc_fconv_f64(const float *A, int a0, int a1, const float *B, int b0, int b1, double *C);
+/* 0 (default): the reference's FP32 convolution; 1-4: tensor-core operand
+ * emulation (BF16 / split BF16), see dpm_oracle.c; process-wide */
+void orc_set_conv_emulation(int mode);
 void orc_dt(const float *vals, float ax, float bx, float ay, float by, const int *dims, float *M, int *Ix, int *Iy);
 void orc_add_part(float *score, const float *M, const int *rootsize, const int *partsize, int ax, int ay);
 void orc_rootbox(int x, int y, float scale, int padx, int pady, const int *rsize, float *Out);

@@ -117,8 +117,9 @@ def test_conv_tile_shape_autotuner(tmp_path):
         tuned = [c.conv_tuning(m) for m in ms]
         for m in ms:
             m.close()
+    assert tuned[0] == tuned[1]   # one launch convolves both models
     for t in tuned:
-        assert t["tiles_per_cta"] in (2, 4, 8, 16)
+        assert t["tiles_per_cta"] in (1, 2, 4, 8)
         assert 64 <= t["smem_kb"] <= 220 and t["ctas"] > 0 and t["ms"] > 0
 
 
@@ -131,3 +132,36 @@ def test_bf16_wide_filter_groups_bit_identical(ctx16, n):
     got = ctx16.fconvsMT(feat, filters)
     for m, f in zip(got, filters):
         assert np.array_equal(m.view(np.int32), O.fconv(feat, f).view(np.int32))
+
+
+def test_bf16_root_blocks_on_split_operands(tmp_path):
+    """Root filters in the pipeline run as blocks of the part grid on split BF16
+    operands (hi*hi + hi*lo + lo*hi).  With every part filter zero (their maps and
+    DT outputs are then exactly equal in both modes), a score map differs from the
+    FP32 pipeline's only by its root: within 2**-14 * sum|a*b| of the FP32 root,
+    128 times tighter than plain BF16 operands allow, so a wrong block, tap,
+    shift or remainder plane shows at once."""
+    import geye_gb300 as g
+    from geye_gb300 import synth
+    spec = synth.ModelSpec("car_zp", roots=[(6, 16), (8, 13)], seed=31,
+                           parts=[[(6, 6)] * 4, [(6, 6)] * 4], root_std=0.01, part_std=0.0,
+                           offsets=[0.05, -0.03], def_ranges=((0.01, 0.1),) * 4)
+    paths = synth.write_model_csv(spec, str(tmp_path))
+    frame = synth.make_frame(640, 480, seed=5)
+    om = O.Model(*paths)
+    S = O.Scores(om, O.Pyramid(om, frame))
+    maps = {}
+    for mode in (g.CONV_FP32, g.CONV_BF16):
+        with g.Context(0, conv=mode) as c:
+            m = g.Model(c, *paths)
+            c.detect_multi(frame, [m], -0.5, 0.5, None)
+            maps[mode] = {(lv, k): c.score_map(m, lv, k) for lv in range(S.interval, S.LEN) if not S.skipped[lv]
+                          for k in range(S.NoC)}
+            m.close()
+    worst = 0.0
+    for key, s32 in maps[g.CONV_FP32].items():
+        s64, mag = S.score_f64(*key)
+        err = np.abs(maps[g.CONV_BF16][key].astype(np.float64) - s32.astype(np.float64)).max()
+        worst = max(worst, err / mag)
+        assert err <= 2.0 ** -14 * mag, (key, err, mag)
+    assert worst > 0   # the split path ran (plain FP32 would give exactly 0)

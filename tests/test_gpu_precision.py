@@ -12,7 +12,12 @@ subnormal range).  Agreement: the share of FP32 detections with a
 same-component detection of IoU >= 0.9 in the other precision.  The report
 holds the max and the mean absolute error per level.
 
-Set GEYE_PRECISION_REPORT=<file> to write the per-level table as JSON.
+Two workloads: the precision configuration itself, the car+person pair on
+1280x720 frames (four seeds), where BF16 must agree on at least 99.5% of the
+FP32 detections, and 640x480 frames (three seeds) beside it.
+
+Set GEYE_PRECISION_REPORT=<prefix> to write each workload's per-level table as
+JSON (<prefix>_<w>x<h>.json).
 """
 import json
 import os
@@ -24,8 +29,10 @@ from oracle import oracle as O
 
 pytestmark = pytest.mark.gpu
 
-FRAMES = (0, 1, 2)
-W, H = 640, 480
+# (width, height, frame seeds, lowest BF16 agreement, lowest FP8 agreement)
+# (measured on GB300: BF16 99.70% / 99.68%, FP8 84.6% / 80.3%; the FP8 floors sit
+# one point under the measurement)
+WORKLOADS = [(1280, 720, (0, 1, 2, 3), 0.995, 0.835), (640, 480, (0, 1, 2), 0.995, 0.79)]
 
 
 def _iou(a, b):
@@ -46,9 +53,10 @@ def _matched(ref, got):
     return hit
 
 
-@pytest.fixture(scope="module")
-def report(tmp_path_factory):
+@pytest.fixture(scope="module", params=WORKLOADS, ids=lambda w: f"{w[0]}x{w[1]}")
+def report(request, tmp_path_factory):
     import geye_gb300 as g
+    W, H, FRAMES, min_bf16, min_fp8 = request.param
     from geye_gb300 import synth
     d = str(tmp_path_factory.mktemp("models"))
     specs = (synth.CAR_SPEC, synth.PERSON_SPEC)
@@ -95,10 +103,10 @@ def report(tmp_path_factory):
            "levels": {name: [{"level": lv, "max_abs_err": v[0], "mean_abs_err": v[3] / max(v[4], 1),
                               "max_err_over_mag": v[1], "mag": v[2]}
                              for (n, lv), v in sorted(levels.items()) if n == name] for name in modes},
-           "agreement_vs_fp32": agree}
+           "agreement_vs_fp32": agree, "min_agreement": {"bf16": min_bf16, "fp8": min_fp8}}
     out = os.environ.get("GEYE_PRECISION_REPORT")
     if out:
-        with open(out, "w") as f:
+        with open(f"{out}_{W}x{H}.json", "w") as f:
             json.dump(rep, f, indent=1)
     return rep
 
@@ -119,6 +127,6 @@ def test_fp8_scores_within_operand_rounding(report):
 
 
 def test_detection_agreement(report):
-    a = report["agreement_vs_fp32"]
-    assert a["bf16"]["agreement"] >= 0.9, a["bf16"]
-    assert a["fp8"]["agreement"] >= 0.5, a["fp8"]
+    a, lo = report["agreement_vs_fp32"], report["min_agreement"]
+    assert a["bf16"]["agreement"] >= lo["bf16"], a["bf16"]
+    assert a["fp8"]["agreement"] >= lo["fp8"], a["fp8"]
