@@ -62,6 +62,7 @@ constexpr int kTcM = 128;                        // positions per tile (TMEM lan
 constexpr int kTcMaxTiles = 8;                   // tiles per CTA, at most
 constexpr int kTcMaxStages = 8;                  // bank stages in the ring, at most
 constexpr int kTcHead = 256;                     // mbarriers and the TMEM address
+constexpr int kTcColBytes = 256 * 24;            // the job's column table (N <= 256 entries)
 constexpr int kTcMaxN = 256;                     // N of an MMA, at most
 constexpr int kTcTmemCols = 512;                 // tiles per CTA x N, at most
 constexpr unsigned long long kWaitNs = 1000000000ull;   // a wait gives up after 1 s (then 4 s for the drain)
@@ -175,7 +176,7 @@ __host__ __device__ constexpr uint32_t idesc_e4m3(int M, int N) {
 template <int NQ>
 __global__ void __launch_bounds__(kTcThreads, 1)
     k_conv_tc(const TcJob *__restrict__ jobs, const int4 *__restrict__ chunks, const TcCol *__restrict__ cols,
-              const uint8_t *__restrict__ arena16, const uint8_t *__restrict__ bank, int bank_rows, int n_stages,
+              const uint8_t *__restrict__ arena16, const uint8_t *__restrict__ bank, int n_stages, int tps,
               float *__restrict__ arena, int *err) {
   extern __shared__ __align__(128) uint8_t sm[];
   uint64_t *bar = reinterpret_cast<uint64_t *>(sm);
@@ -185,17 +186,24 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   const int tile0 = ch.y, ntile = ch.z, cs = ch.w;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int NS = n_stages;
+  // taps a stage: tps > 0 that many, 0 a filter column, < 0 every tap of a phase (the bank
+  // of the phase resident at once: one copy with the slab, no refills while the MMAs run)
+  const bool whole = tps < 0;
+  tps = whole ? cs * J.b0 : (tps > 0 ? tps : J.b0);
   const int p_begin = tile0 * kTcM;
   const int S = ntile * kTcM + (cs - 1) * J.fs0 + (J.b0 - 1);   // slab cells per plane
   const uint32_t plane_bytes = (uint32_t)S * 16u;
   const bool split = J.n_lo > 0;
-  uint8_t *slab = sm + kTcHead;
+  TcCol *col_s = reinterpret_cast<TcCol *>(sm + kTcHead);          // the job's column table
+  uint8_t *slab = sm + kTcHead + kTcColBytes;
   uint8_t *slab_lo = slab + (size_t)NQ * plane_bytes;
-  const size_t slab_end = kTcHead + (size_t)NQ * plane_bytes * (split ? 2 : 1);
+  const size_t slab_end = kTcHead + kTcColBytes + (size_t)NQ * plane_bytes * (split ? 2 : 1);
   uint8_t *stages = sm + ((slab_end + 127) & ~(size_t)127);
-  const uint32_t stage_bytes = (uint32_t)NQ * (uint32_t)J.n * 16u;
+  const uint32_t tap_bytes = (uint32_t)NQ * (uint32_t)J.n * 16u;   // one tap of the job's bank
+  const uint32_t stage_bytes = (uint32_t)tps * tap_bytes;           // room of a stage
   uint32_t ncols = 32;
   while (ncols < (uint32_t)(ntile * J.n)) ncols <<= 1;
+  for (int k = threadIdx.x; k < J.n; k += kTcThreads) col_s[k] = cols[J.col_tab + k];
 
   if (threadIdx.x == 0) {
     for (int i = 0; i < 3 + 2 * kTcMaxStages; i++) mbar_init(&bar[i], 1);
@@ -227,21 +235,19 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                    arena16 + 2 * (size_t)J.lo_off + ((size_t)q * J.plane_cells + cell0) * 16, plane_bytes,
                    &bar[kBarSlabFull]);
       slabs++;
-      for (int xp = xp0; xp < xp0 + ncol && ok; xp++)
-        for (int yp = 0; yp < J.b0; yp++) {
-          const int s = issued % NS;
-          if (issued >= NS && !mbar_wait(&bar[kBarStageFree + s], (uint32_t)((issued / NS - 1) & 1), kWaitNs)) {
-            ok = false;
-            break;
-          }
-          const int t = xp * J.b0 + yp;
-          uint8_t *dst = stages + (size_t)s * stage_bytes;
-          mbar_expect_tx(&bar[kBarStageFull + s], stage_bytes);
-          for (int q = 0; q < NQ; q++)
-            bulk_g2s(dst + (size_t)q * J.n * 16, bank + ((size_t)(t * NQ + q) * bank_rows + J.row0) * 16,
-                     (uint32_t)J.n * 16u, &bar[kBarStageFull + s]);
-          issued++;
+      // the phase's taps t = xp*b0 + yp, step to a stage (tps divides b0: no stage crosses a phase)
+      const int step = whole ? ncol * J.b0 : tps;
+      for (int t = xp0 * J.b0; t < (xp0 + ncol) * J.b0 && ok; t += step) {
+        const int s = issued % NS;
+        if (issued >= NS && !mbar_wait(&bar[kBarStageFree + s], (uint32_t)((issued / NS - 1) & 1), kWaitNs)) {
+          ok = false;
+          break;
         }
+        mbar_expect_tx(&bar[kBarStageFull + s], (uint32_t)step * tap_bytes);
+        bulk_g2s(stages + (size_t)s * stage_bytes, bank + (size_t)J.bank_off + (size_t)t * tap_bytes,
+                 (uint32_t)step * tap_bytes, &bar[kBarStageFull + s]);
+        issued++;
+      }
     }
     if (!ok) {
       atomicOr(err, 1);
@@ -267,13 +273,16 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     for (int ph = 0; ph < phases && ok; ph++) {
       const int xp0 = ph * cs, ncol = min(cs, J.b1 - xp0);
       if (!mbar_wait(&bar[kBarSlabFull], (uint32_t)(ph & 1), kWaitNs)) { ok = false; break; }
-      for (int xp = xp0; xp < xp0 + ncol && ok; xp++)
-        for (int yp = 0; yp < J.b0; yp++) {
-          const int s = used % NS;
-          if (!mbar_wait(&bar[kBarStageFull + s], (uint32_t)((used / NS) & 1), kWaitNs)) { ok = false; break; }
-          tc_fence_after();
-          const uint64_t b_base = sdesc(smem_u32(stages + (size_t)s * stage_bytes), (uint32_t)J.n * 16u, 128u);
-          const uint32_t acc = (xp > 0 || yp > 0) ? 1u : 0u;
+      const int step = whole ? ncol * J.b0 : tps;
+      for (int t0 = xp0 * J.b0; t0 < (xp0 + ncol) * J.b0 && ok; t0 += step) {
+        const int s = used % NS;
+        if (!mbar_wait(&bar[kBarStageFull + s], (uint32_t)((used / NS) & 1), kWaitNs)) { ok = false; break; }
+        tc_fence_after();
+        const uint64_t stage_desc = sdesc(smem_u32(stages + (size_t)s * stage_bytes), (uint32_t)J.n * 16u, 128u);
+        for (int u = 0; u < step; u++) {
+          const int t = t0 + u, xp = t / J.b0, yp = t - (t / J.b0) * J.b0;
+          const uint64_t b_base = stage_desc + (uint32_t)(u * NQ * J.n);   // tap u of the stage: NQ*n rows of 16 B on
+          const uint32_t acc = t > 0 ? 1u : 0u;
           const uint32_t shift = (uint32_t)((xp - xp0) * J.fs0 + yp);
           for (int i = 0; i < ntile; i++) {
             const uint32_t d = tmem + (uint32_t)(i * J.n);
@@ -289,9 +298,10 @@ __global__ void __launch_bounds__(kTcThreads, 1)
               }
             }
           }
-          tc_commit(&bar[kBarStageFree + s]);   // the stage is free once these MMAs are done
-          used++;
         }
+        tc_commit(&bar[kBarStageFree + s]);   // the stage is free once these MMAs are done
+        used++;
+      }
       tc_commit(&bar[kBarSlabFree]);   // and the slab once the phase's MMAs are
     }
     if (!ok) atomicOr(err, 2);
@@ -312,7 +322,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     const int x = p / J.fs0, y = p - x * J.fs0;
     const uint32_t row_addr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(i * J.n);
     for (int c0 = 0; c0 < J.n; c0 += 16) {
-      const TcCol head = cols[J.col_tab + c0];   // a 16-column chunk lies inside one section
+      const TcCol head = col_s[c0];               // a 16-column chunk lies inside one section
       if (head.kind == 0) continue;               // (uniform across the warp: the loads below are collective)
       uint32_t r[16], r2[16];
       __syncwarp();
@@ -322,7 +332,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       if (ok && p < ncell) {
 #pragma unroll
         for (int k = 0; k < 16; k++) {
-          const TcCol c = cols[J.col_tab + c0 + k];
+          const TcCol c = col_s[c0 + k];
           float v;
           memcpy(&v, &r[k], 4);
           if (c.kind == 1) {
@@ -434,29 +444,37 @@ __global__ void k_bank_e4m3(const DevRow *__restrict__ rows, int n_rows, int R, 
   }
 }
 
-// uploads the bank of `rows` over the b0 x b1 grid into dst (sized by bank_bytes)
-static size_t bank_bytes(int NQ, int b0, int b1, int R) { return (size_t)b0 * b1 * NQ * R * 16; }
+// A job's bank holds its own rows (first, n) contiguously, [tap][q][n][16 B], so a
+// stage of consecutive taps is one bulk copy.  One buffer holds every layout.
+struct BankLayout {
+  int first, n;     // rows of the plan's row list
+  size_t off;       // byte offset in the buffer
+};
+static size_t layout_bytes(int NQ, int b0, int b1, int n) { return (size_t)b0 * b1 * NQ * n * 16; }
 
-static geye_status upload_bank(geye_ctx *ctx, const std::vector<BankRow> &rows, int NQ, int b0, int b1, int R,
-                               DevBuf &dst) {
-  GEYE_TRY(dst.alloc(ctx, std::max<size_t>(bank_bytes(NQ, b0, b1, R), 16)));
+static geye_status upload_bank(geye_ctx *ctx, const std::vector<BankRow> &rows, int NQ, int b0, int b1,
+                               const std::vector<BankLayout> &layouts, size_t total, DevBuf &dst) {
+  GEYE_TRY(dst.alloc(ctx, std::max<size_t>(total, 16)));
   if (NQ == 4) {
-    std::vector<uint16_t> bank((size_t)b0 * b1 * 4 * R * 8, 0);
-    for (int xp = 0; xp < b1; xp++)
-      for (int yp = 0; yp < b0; yp++) {
-        const size_t t = (size_t)xp * b0 + yp;
-        for (size_t r = 0; r < rows.size(); r++) {
-          const BankRow &B = rows[r];
-          const int x = B.x0 + xp, y = B.y0 + yp;
-          if (!B.h || x >= B.fb1 || y >= B.fb0) continue;
-          for (int c = 0; c < kFeat; c++) {
-            const float w = B.h[(size_t)c * B.fb0 * B.fb1 + (size_t)x * B.fb0 + y];
-            const uint16_t hi = to_bf16(w);
-            bank[((t * 4 + (c >> 3)) * R + r) * 8 + (c & 7)] = B.lo ? to_bf16(w - from_bf16(hi)) : hi;
+    std::vector<uint16_t> bank(total / 2, 0);
+    for (const BankLayout &L : layouts) {
+      uint16_t *out = bank.data() + L.off / 2;
+      for (int xp = 0; xp < b1; xp++)
+        for (int yp = 0; yp < b0; yp++) {
+          const size_t t = (size_t)xp * b0 + yp;
+          for (int r = 0; r < L.n; r++) {
+            const BankRow &B = rows[L.first + r];
+            const int x = B.x0 + xp, y = B.y0 + yp;
+            if (!B.h || x >= B.fb1 || y >= B.fb0) continue;
+            for (int c = 0; c < kFeat; c++) {
+              const float w = B.h[(size_t)c * B.fb0 * B.fb1 + (size_t)x * B.fb0 + y];
+              const uint16_t hi = to_bf16(w);
+              out[((t * 4 + (c >> 3)) * L.n + r) * 8 + (c & 7)] = B.lo ? to_bf16(w - from_bf16(hi)) : hi;
+            }
           }
         }
-      }
-    CUDA_TRY(cudaMemcpyAsync(dst.p, bank.data(), bank.size() * 2, cudaMemcpyHostToDevice, ctx->stream));
+    }
+    CUDA_TRY(cudaMemcpyAsync(dst.p, bank.data(), total, cudaMemcpyHostToDevice, ctx->stream));
     CUDA_TRY(cudaStreamSynchronize(ctx->stream));
     return GEYE_OK;
   }
@@ -465,12 +483,32 @@ static geye_status upload_bank(geye_ctx *ctx, const std::vector<BankRow> &rows, 
   DevBuf d_rows;
   GEYE_TRY(upload_bytes(ctx, d_rows, dr.data(), sizeof(DevRow) * std::max<size_t>(dr.size(), 1)));
   const int taps = b0 * b1;
-  const size_t elems = (size_t)taps * 2 * R * 16;
-  k_bank_e4m3<<<(int)std::max<size_t>(1, std::min<size_t>((elems + 255) / 256, 2048)), 256, 0, ctx->stream>>>(
-      d_rows.as<DevRow>(), (int)dr.size(), R, b0, taps, dst.as<uint8_t>());
-  CUDA_TRY(cudaGetLastError());
+  for (const BankLayout &L : layouts) {
+    const size_t elems = (size_t)taps * 2 * L.n * 16;
+    k_bank_e4m3<<<(int)std::max<size_t>(1, std::min<size_t>((elems + 255) / 256, 2048)), 256, 0, ctx->stream>>>(
+        d_rows.as<DevRow>() + L.first, std::max(0, std::min(L.n, (int)dr.size() - L.first)), L.n, b0, taps,
+        dst.as<uint8_t>() + L.off);
+    CUDA_TRY(cudaGetLastError());
+  }
   CUDA_TRY(cudaStreamSynchronize(ctx->stream));
   return GEYE_OK;
+}
+
+// one layout per distinct row range of the jobs; sets each job's bank_off
+static size_t assign_layouts(std::vector<TcJob> &jobs, int NQ, int b0, int b1, std::vector<BankLayout> &layouts) {
+  size_t total = 0;
+  for (TcJob &J : jobs) {
+    const BankLayout *hit = nullptr;
+    for (const BankLayout &L : layouts)
+      if (L.first == J.row0 && L.n == J.n) hit = &L;
+    if (!hit) {
+      layouts.push_back(BankLayout{J.row0, J.n, total});
+      total += layout_bytes(NQ, b0, b1, J.n);
+      hit = &layouts.back();
+    }
+    J.bank_off = (int)hit->off;
+  }
+  return total;
 }
 
 // ---------------------------------------------------------------------------
@@ -480,16 +518,23 @@ struct TcShape {
   int t_cap;        // tiles per CTA, at most
   size_t budget;    // dynamic shared memory per CTA, at most
   int stages;       // bank stages in the ring
+  int col;          // a stage holds -1: every tap of a phase (the bank resident), 1: a filter column, 0: one tap
 };
-static const TcShape kTcShapes[] = {{4, 220 * 1024, 6}, {8, 220 * 1024, 4}, {2, 110 * 1024, 4},
-                                    {4, 110 * 1024, 3}, {1, 72 * 1024, 4},  {2, 72 * 1024, 3},
-                                    {8, 220 * 1024, 8}};
+static const TcShape kTcShapes[] = {{4, 110 * 1024, 2, 1},  {2, 72 * 1024, 3, 0},  {4, 220 * 1024, 1, -1},
+                                    {2, 220 * 1024, 1, -1}, {8, 220 * 1024, 1, -1}, {2, 110 * 1024, 1, -1},
+                                    {1, 72 * 1024, 4, 0},   {4, 220 * 1024, 8, 0}};
 constexpr int kTcNumShapes = (int)(sizeof(kTcShapes) / sizeof(kTcShapes[0]));
 
-static size_t tc_need(const TcJob &J, int NQ, int T, int cs, int NS) {
+// taps a stage holds for a phase of cs columns: one, a column (b0), or the whole phase
+static int taps_per_stage(const TcJob &J, const TcShape &sh, int cs) {
+  return sh.col < 0 ? cs * J.b0 : sh.col ? J.b0 : 1;
+}
+static int tps_arg(const TcShape &sh) { return sh.col < 0 ? -1 : sh.col ? 0 : 1; }
+
+static size_t tc_need(const TcJob &J, int NQ, int T, int cs, const TcShape &sh) {
   const size_t S = (size_t)T * kTcM + (size_t)(cs - 1) * J.fs0 + (J.b0 - 1);
-  const size_t slab = kTcHead + (size_t)NQ * S * 16 * (J.n_lo > 0 ? 2 : 1);
-  return ((slab + 127) & ~(size_t)127) + (size_t)NS * NQ * J.n * 16;
+  const size_t slab = kTcHead + kTcColBytes + (size_t)NQ * S * 16 * (J.n_lo > 0 ? 2 : 1);
+  return ((slab + 127) & ~(size_t)127) + (size_t)sh.stages * taps_per_stage(J, sh, cs) * NQ * J.n * 16;
 }
 
 static int tmem_cols(int c) {
@@ -509,13 +554,13 @@ static bool chunk_jobs(const std::vector<TcJob> &jobs, int NQ, const TcShape &sh
     const int t_max = std::max(1, std::min(sh.t_cap, kTcTmemCols / J.n));
     int T = 0, cs = 0;
     for (int Tc = t_max; Tc >= 1 && !T; Tc--)
-      if (tc_need(J, NQ, Tc, J.b1, sh.stages) <= sh.budget) { T = Tc; cs = J.b1; }
+      if (tc_need(J, NQ, Tc, J.b1, sh) <= sh.budget) { T = Tc; cs = J.b1; }
     for (int c = J.b1 - 1; c >= 1 && !T; c--)
-      if (tc_need(J, NQ, 1, c, sh.stages) <= sh.budget) { T = 1; cs = c; }
+      if (tc_need(J, NQ, 1, c, sh) <= sh.budget) { T = 1; cs = c; }
     if (!T) return false;
     // the CTAs that share an SM (by shared memory) fit their accumulators in its
     // 512 TMEM columns together, or one's allocation waits for another to end
-    auto per_sm = [&](int Tc) { return std::max<size_t>(1, (228u * 1024u) / (tc_need(J, NQ, Tc, cs, sh.stages) + 1024)); };
+    auto per_sm = [&](int Tc) { return std::max<size_t>(1, (228u * 1024u) / (tc_need(J, NQ, Tc, cs, sh) + 1024)); };
     while (T > 1 && (size_t)tmem_cols(T * J.n) * per_sm(T) > (size_t)kTcTmemCols) T--;
     const long long reach = (long long)(J.b1 - 1) * J.fs0 + (J.b0 - 1);
     for (int t0 = 0; t0 < J.ntiles; t0 += T) {
@@ -524,7 +569,7 @@ static bool chunk_jobs(const std::vector<TcJob> &jobs, int NQ, const TcShape &sh
       if ((long long)J.plane_off * 2 / 16 + last > cells_total) return false;
       if (J.lo_off >= 0 && (long long)J.lo_off * 2 / 16 + last > cells_total) return false;
       chunks.push_back(make_int4((int)j, t0, nt, cs));
-      max_smem = std::max(max_smem, tc_need(J, NQ, nt, cs, sh.stages));
+      max_smem = std::max(max_smem, tc_need(J, NQ, nt, cs, sh));
     }
   }
   // heaviest first (tiles x taps x N), so the long ones start in the first wave
@@ -536,18 +581,19 @@ static bool chunk_jobs(const std::vector<TcJob> &jobs, int NQ, const TcShape &sh
   return true;
 }
 
+// tps: taps per stage for every job of the launch (> 0 that many, 0: a filter column, < 0: a whole phase)
 static void launch_conv_tc(int NQ, const TcJob *jobs, const int4 *chunks, int n_chunks, const TcCol *cols,
-                           const uint8_t *planes, const uint8_t *bank, int bank_rows, int stages, float *out, int *err,
+                           const uint8_t *planes, const uint8_t *bank, int stages, int tps, float *out, int *err,
                            size_t smem, cudaStream_t s) {
   if (n_chunks <= 0) return;
   if (NQ == 4) {
     static SmemAttr a4;
     raise_smem(a4, k_conv_tc<4>, smem);
-    k_conv_tc<4><<<n_chunks, kTcThreads, smem, s>>>(jobs, chunks, cols, planes, bank, bank_rows, stages, out, err);
+    k_conv_tc<4><<<n_chunks, kTcThreads, smem, s>>>(jobs, chunks, cols, planes, bank, stages, tps, out, err);
   } else {
     static SmemAttr a2;
     raise_smem(a2, k_conv_tc<2>, smem);
-    k_conv_tc<2><<<n_chunks, kTcThreads, smem, s>>>(jobs, chunks, cols, planes, bank, bank_rows, stages, out, err);
+    k_conv_tc<2><<<n_chunks, kTcThreads, smem, s>>>(jobs, chunks, cols, planes, bank, stages, tps, out, err);
   }
 }
 
@@ -713,13 +759,11 @@ geye_status plan_tc(geye_ctx *ctx, Plan &P, ArenaAlloc &A) {
       J.ntiles = ((with_roots ? ncell : p_valid) + kTcM - 1) / kTcM;
       if (J.ntiles > 0) T.jobs.push_back(J);
     };
+    // parts and root blocks as separate jobs, so each job's bank can stay resident in
+    // shared memory (the part filters' bank alone, the root blocks' with its remainders)
     const int n_lo = split ? r16 : 0;
-    if (any_p && any_r && p16 + RS <= kTcMaxN) {
-      add_job(0, p16 + RS, p16, n_lo, true);
-    } else {
-      if (any_p) add_job(0, p16, 0, 0, false);
-      if (any_r) add_job(p16, RS, 0, n_lo, true);
-    }
+    if (any_p) add_job(0, p16, 0, 0, false);
+    if (any_r) add_job(p16, RS, 0, n_lo, true);
   }
   return GEYE_OK;
 }
@@ -751,7 +795,9 @@ geye_status build_tc_plan(geye_ctx *ctx, Plan &P) {
     R.scale = b.scale;
     rows[r] = R;
   }
-  GEYE_TRY(upload_bank(ctx, rows, NQ, T.grid_b0, T.grid_b1, T.rows, T.d_bank));
+  std::vector<BankLayout> layouts;
+  const size_t bank_total = assign_layouts(T.jobs, NQ, T.grid_b0, T.grid_b1, layouts);
+  GEYE_TRY(upload_bank(ctx, rows, NQ, T.grid_b0, T.grid_b1, layouts, bank_total, T.d_bank));
   GEYE_TRY(upload_bytes(ctx, T.d_jobs, T.jobs.data(), sizeof(TcJob) * T.jobs.size()));
   GEYE_TRY(upload_bytes(ctx, T.d_cols, T.cols.data(), sizeof(TcCol) * std::max<size_t>(T.cols.size(), 1)));
   GEYE_TRY(upload_bytes(ctx, T.d_sums, T.sums.data(), sizeof(RootSumJob) * std::max<size_t>(T.sums.size(), 1)));
@@ -797,8 +843,8 @@ geye_status build_tc_plan(geye_ctx *ctx, Plan &P) {
     GEYE_TRY(upload_bytes(ctx, d_chunks, chunks.data(), sizeof(int4) * chunks.size()));
     auto launch = [&]() {
       launch_conv_tc(NQ, T.d_jobs.as<TcJob>(), d_chunks.as<int4>(), (int)chunks.size(), T.d_cols.as<TcCol>(),
-                     P.arena16.as<uint8_t>(), T.d_bank.as<uint8_t>(), T.rows, kTcShapes[si].stages,
-                     P.arena.as<float>(), err, smem, ctx->stream);
+                     P.arena16.as<uint8_t>(), T.d_bank.as<uint8_t>(), kTcShapes[si].stages,
+                     tps_arg(kTcShapes[si]), P.arena.as<float>(), err, smem, ctx->stream);
     };
     launch();
     CUDA_TRY(cudaEventRecord(e0, ctx->stream));
@@ -829,6 +875,7 @@ geye_status build_tc_plan(geye_ctx *ctx, Plan &P) {
   T.smem = best_smem;
   T.n_chunks = (int)best.size();
   T.stages = kTcShapes[best_shape].stages;
+  T.tps = tps_arg(kTcShapes[best_shape]);
   T.shape = best_shape;
   T.tuned_ms = best_ms / 3.0f;
   GEYE_TRY(upload_bytes(ctx, T.d_chunks, best.data(), sizeof(int4) * std::max<size_t>(best.size(), 1)));
@@ -843,7 +890,7 @@ geye_status run_conv_tc(geye_ctx *ctx, Plan &P) {
   }
   if (T.n_chunks == 0) return GEYE_OK;
   launch_conv_tc(T.planes, T.d_jobs.as<TcJob>(), T.d_chunks.as<int4>(), T.n_chunks, T.d_cols.as<TcCol>(),
-                 P.arena16.as<uint8_t>(), T.d_bank.as<uint8_t>(), T.rows, T.stages, P.arena.as<float>(),
+                 P.arena16.as<uint8_t>(), T.d_bank.as<uint8_t>(), T.stages, T.tps, P.arena.as<float>(),
                  P.d_small.as<int>() + 130, T.smem, ctx->stream);
   ctx->launches++;
   cudaError_t e = cudaGetLastError();
@@ -915,11 +962,15 @@ geye_status conv_tc_maps(geye_ctx *ctx, const float *d_feat, int a0, int a1, con
   const size_t plane_total = (size_t)NQ * (ncell + kTcPlanePad);
   std::vector<int4> chunks;
   size_t smem = 0;
-  const std::vector<TcJob> jobs{J};
-  int stages = 0;
+  std::vector<TcJob> jobs{J};
+  std::vector<BankLayout> layouts;
+  const size_t bank_total = assign_layouts(jobs, NQ, gb0, gb1, layouts);
+  int stages = 0, tps = 1;
   for (int si = 0; si < kTcNumShapes && !stages; si++)
-    if (chunk_jobs(jobs, NQ, kTcShapes[si], (long long)(plane_total + tail_cells), chunks, smem))
+    if (chunk_jobs(jobs, NQ, kTcShapes[si], (long long)(plane_total + tail_cells), chunks, smem)) {
       stages = kTcShapes[si].stages;
+      tps = tps_arg(kTcShapes[si]);
+    }
   if (!stages) {
     set_error("tensor-core conv: the filters' slab and bank stages exceed shared memory");
     return GEYE_ERR_UNSUPPORTED;
@@ -927,8 +978,8 @@ geye_status conv_tc_maps(geye_ctx *ctx, const float *d_feat, int a0, int a1, con
   DevBuf *planes = buf(), *d_bank = buf(), *d_jobs = buf(), *d_chunks = buf(), *d_cols = buf(), *d_err = buf();
   GEYE_TRY(planes->alloc(ctx, (plane_total + tail_cells) * 16));
   CUDA_TRY(cudaMemsetAsync(planes->as<uint8_t>() + plane_total * 16, 0, tail_cells * 16, ctx->stream));
-  GEYE_TRY(upload_bank(ctx, rows, NQ, gb0, gb1, R, *d_bank));
-  GEYE_TRY(upload_bytes(ctx, *d_jobs, &J, sizeof(TcJob)));
+  GEYE_TRY(upload_bank(ctx, rows, NQ, gb0, gb1, layouts, bank_total, *d_bank));
+  GEYE_TRY(upload_bytes(ctx, *d_jobs, jobs.data(), sizeof(TcJob)));
   GEYE_TRY(upload_bytes(ctx, *d_chunks, chunks.data(), sizeof(int4) * chunks.size()));
   GEYE_TRY(upload_bytes(ctx, *d_cols, cols.data(), sizeof(TcCol) * cols.size()));
   GEYE_TRY(d_err->alloc(ctx, 16));
@@ -937,7 +988,7 @@ geye_status conv_tc_maps(geye_ctx *ctx, const float *d_feat, int a0, int a1, con
   if (NQ == 4) k_feat_planes<4><<<grid, 256, 0, ctx->stream>>>(d_feat, ncell, planes->as<uint8_t>());
   else k_feat_planes<2><<<grid, 256, 0, ctx->stream>>>(d_feat, ncell, planes->as<uint8_t>());
   launch_conv_tc(NQ, d_jobs->as<TcJob>(), d_chunks->as<int4>(), (int)chunks.size(), d_cols->as<TcCol>(),
-                 planes->as<uint8_t>(), d_bank->as<uint8_t>(), R, stages, d_out, d_err->as<int>(), smem, ctx->stream);
+                 planes->as<uint8_t>(), d_bank->as<uint8_t>(), stages, tps, d_out, d_err->as<int>(), smem, ctx->stream);
   CUDA_TRY(cudaGetLastError());
   int errw = 0;
   CUDA_TRY(cudaMemcpyAsync(&errw, d_err->p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));

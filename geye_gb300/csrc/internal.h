@@ -101,10 +101,12 @@ struct TcJob {             // one feature level's MMA chain over the rows of the
   int plane_cells;         // cells per plane (fs0*fs1 + kTcPlanePad)
   int fs0, fs1;            // feature rows, columns
   int b0, b1;              // tap grid
-  int row0, n;             // bank rows row0 .. row0+n-1: the MMA's N columns (a multiple of 16)
-  int lo_row, n_lo;        // split chain: rows row0+lo_row .. +n_lo (0: none), accumulated into TMEM columns lo_row ..
+  int bank_off;            // byte offset of the job's bank [tap][q][n][16 B] (its rows, contiguous)
+  int n;                   // the job's bank rows: the MMA's N columns (a multiple of 16)
+  int lo_row, n_lo;        // split chain: rows lo_row .. lo_row+n_lo (0: none), accumulated into TMEM columns lo_row ..
   int col_tab;             // first entry of the job's column table (n entries)
   int ntiles;              // 128-position tiles the job covers
+  int row0;                // the job's first row in the plan's row list (host bookkeeping)
 };
 
 struct TcCol {             // what the epilogue does with one MMA column of a job

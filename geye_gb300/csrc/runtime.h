@@ -141,7 +141,7 @@ struct TcPlan {
   std::vector<RootSumJob> sums;
   int sum_max_r = 0;
   DevBuf d_bank, d_jobs, d_chunks, d_cols, d_sums;
-  int n_chunks = 0, stages = 0;
+  int n_chunks = 0, stages = 0, tps = 1;   // bank stages; taps a stage (0: a filter column, -1: a phase)
   size_t smem = 0;
   int shape = -1;                       // tile-shape candidate the autotuner chose
   float tuned_ms = 0.f;                 // its measured time per launch
