@@ -533,6 +533,36 @@ def ref_load_model(comp: str, root: str, part: str) -> np.ndarray:
     return out
 
 
+def get_new_rects(model: Model, boxes: np.ndarray, width: int, height: int) -> dict:
+    """The oracle's box regression (tracking.cpp:90-166) of kept records [K][GL]."""
+    b = _f32(boxes)
+    K = b.shape[0] if b.ndim == 2 else 0
+    n = max(K, 1)
+    point = np.zeros((n, 4), np.int32); or_point = np.zeros((n, 4), np.int32)
+    typ = np.zeros(n, np.int32); scale = np.zeros(n, np.float32); score = np.zeros(n, np.float32)
+    lib().orc_get_new_rects(model._p, _ptr(b) if K else None, K, width, height, _ptr(point), _ptr(or_point),
+                            _ptr(typ), _ptr(scale), _ptr(score))
+    return dict(num=K, point=point[:K], or_point=or_point[:K], type=typ[:K], scale=scale[:K], score=score[:K])
+
+
+def ref_get_new_rects(comp: str, root: str, part: str, ratio: float, boxes: np.ndarray, width: int,
+                      height: int) -> dict:
+    """The reference's own get_new_rects (tracking.cpp:90-166) on kept records [K][GL] of the
+    model its loader reads from the CSV triple."""
+    R = _R()
+    R.ref_get_new_rects.restype = C.c_int
+    R.ref_get_new_rects.argtypes = [C.c_char_p, C.c_char_p, C.c_char_p, C.c_float, C.c_void_p, C.c_int, C.c_int,
+                                    C.c_int] + [C.c_void_p] * 5
+    b = _f32(boxes).copy()
+    K = b.shape[0] if b.ndim == 2 else 0
+    n = max(K, 1)
+    point = np.zeros((n, 4), np.int32); or_point = np.zeros((n, 4), np.int32)
+    typ = np.zeros(n, np.int32); scale = np.zeros(n, np.float32); score = np.zeros(n, np.float32)
+    k = R.ref_get_new_rects(comp.encode(), root.encode(), part.encode(), ratio, _ptr(b), K, width, height,
+                            _ptr(point), _ptr(or_point), _ptr(typ), _ptr(scale), _ptr(score))
+    return dict(num=k, point=point[:k], or_point=or_point[:k], type=typ[:k], scale=scale[:k], score=score[:k])
+
+
 def ref_quicksort(vals: np.ndarray):
     a = _f32(vals).copy()
     order = np.arange(len(a), dtype=np.int32)

@@ -26,6 +26,10 @@ Model_info *load_modelinfo(char *filename);                                     
 Rootfilters *load_rootfilter(char *filename);                                      /* load_model.cpp:250 */
 Partfilters *load_partfilter(char *filename);                                      /* load_model.cpp:390 */
 extern int sum_size_def_array;                                                     /* load_model.cpp:25, set at :178 */
+RESULT *get_new_rects(IplImage *Image, MODEL *MO, FLOAT *boxes, int *NUM);         /* tracking.cpp:90 */
+
+/* get_new_rects logs every box to this file (main.cpp opens it) */
+FILE *resFP;
 
 extern "C" {
 
@@ -144,6 +148,33 @@ int ref_nms(float *boxes, int num, int numpart0, float overlap, int *keep)
 }
 
 void ref_quicksort(float *ary, int *order, int first, int last) { quickSort(ary, order, first, last); }
+
+/* get_new_rects (tracking.cpp:90-166) on kept boxes [num][GL] of a model loaded by
+ * the reference's loader; fills point/or_point (4 ints a box), type, scale, score. */
+int ref_get_new_rects(const char *comp, const char *root, const char *part, float ratio, float *boxes, int num,
+                      int img_w, int img_h, int *point, int *or_point, int *type, float *scale, float *score)
+{
+    if (!resFP) resFP = fopen("/dev/null", "w");
+    MODEL MO;
+    MO.MI = load_modelinfo((char *)comp);
+    MO.RF = NULL;
+    MO.PF = NULL;
+    MO.MI->ratio = ratio;
+    IplImage im;
+    memset(&im, 0, sizeof(im));
+    im.width = img_w;
+    im.height = img_h;
+    int n = num;
+    RESULT *R = get_new_rects(&im, &MO, boxes, &n);
+    for (int i = 0; i < R->num; i++) {
+        memcpy(point + 4 * i, R->point + 4 * i, sizeof(int) * 4);
+        memcpy(or_point + 4 * i, R->OR_point + 4 * i, sizeof(int) * 4);
+        type[i] = R->type[i];
+        scale[i] = R->scale[i];
+        score[i] = R->score[i];
+    }
+    return R->num;
+}
 
 /* Loads a model CSV triple with the reference's own loader functions and
  * writes every parsed field, in a fixed order, into out[] as floats (the

@@ -1,8 +1,8 @@
 /*
  * Link stubs for building the reference's CPU translation units
- * (resize.cc, dt.cpp, nms.cpp, get_boxes.cpp, featurepyramid.cpp) into a
- * shared library on a machine without the reference's GPU runtime.
- * TEST INFRASTRUCTURE ONLY.
+ * (resize.cc, dt.cpp, nms.cpp, get_boxes.cpp, featurepyramid.cpp,
+ * load_model.cpp, tracking.cpp) into a shared library on a machine without
+ * the reference's GPU runtime or OpenCV.  TEST INFRASTRUCTURE ONLY.
  *
  * cuMemHostAlloc / cuMemFreeHost are the only driver calls reached on the CPU
  * path (get_boxes.cpp:75-114 padarray); they map to calloc/free.  Every other
@@ -14,6 +14,7 @@
 #include <sys/time.h>
 #include <cuda.h>
 #include "cv.h"
+#include "legacy.hpp"
 #include "switch_float.h"
 
 static void die(const char *what) { fprintf(stderr, "reference GPU path reached on the CPU build: %s\n", what); abort(); }
@@ -61,3 +62,28 @@ CUdeviceptr *part_C_dev, *part_error_array_dev;
 size_t size_A_SCORE;
 struct timeval tv_memcpy_start, tv_memcpy_end, tv_kernel_start, tv_kernel_end;
 float time_memcpy, time_kernel;
+
+/* OpenCV image and tracker calls of tracking.cpp's tracker; get_new_rects and
+ * create_result (the only tracking.cpp functions the oracle calls) reach none */
+CvSize cvSize(int, int) { die("cvSize"); return CvSize{}; }
+CvRect cvRect(int, int, int, int) { die("cvRect"); return CvRect{}; }
+CvPoint cvPoint(int, int) { die("cvPoint"); return CvPoint{}; }
+CvScalar cvScalar(double, double, double, double) { die("cvScalar"); return CvScalar{}; }
+IplImage *cvCreateImage(CvSize, int, int) { die("cvCreateImage"); return 0; }
+IplImage *cvCloneImage(const IplImage *) { die("cvCloneImage"); return 0; }
+void cvReleaseImage(IplImage **) { die("cvReleaseImage"); }
+void cvSetImageROI(IplImage *, CvRect) { die("cvSetImageROI"); }
+void cvResetImageROI(IplImage *) { die("cvResetImageROI"); }
+void cvCopy(const void *, void *, const void *) { die("cvCopy"); }
+void cvCvtColor(const void *, void *, int) { die("cvCvtColor"); }
+void cvResize(const void *, void *, int) { die("cvResize"); }
+CvMat *cvCreateMat(int, int, int) { die("cvCreateMat"); return 0; }
+void cvReleaseMat(CvMat **) { die("cvReleaseMat"); }
+void cvmSet(CvMat *, int, int, double) { die("cvmSet"); }
+double cvmGet(const CvMat *, int, int) { die("cvmGet"); return 0; }
+void cvMatchTemplate(const void *, const void *, void *, int) { die("cvMatchTemplate"); }
+CvConDensation *cvCreateConDensation(int, int, int) { die("cvCreateConDensation"); return 0; }
+void cvReleaseConDensation(CvConDensation **) { die("cvReleaseConDensation"); }
+void cvConDensInitSampleSet(CvConDensation *, CvMat *, CvMat *) { die("cvConDensInitSampleSet"); }
+void cvConDensUpdateByTime(CvConDensation *) { die("cvConDensUpdateByTime"); }
+void cvRandInit(CvRandState *, double, double, int, int) { die("cvRandInit"); }

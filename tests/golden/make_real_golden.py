@@ -10,7 +10,10 @@ repository):
   - the oracle's detections (thresh -0.5, overlap 0.4, ratio 1: the
     reference's run parameters, CAR_TRACKING/main.cpp:86-88) for every frame
     and model, with the digests of the A_SCORE map and of every (level,
-    component) score map.
+    component) score map;
+  - the reference's own get_new_rects (tracking.cpp, compiled into
+    oracle/_ref) on every kept record and on those records moved past the
+    image borders, at two model ratios.
 
 Run from the repository root:  python tests/golden/make_real_golden.py
 """
@@ -68,6 +71,26 @@ def main() -> None:
                 E[k + "score_sha256"] = np.stack([np.frombuffer(RD.float_digest(S.score(lv, c)), np.uint8)
                                                   for lv, c in maps])
                 print(name, i, "D", r["D"], "kept", r["K"], "oob", r["probe_oob"])
+    # get_new_rects (tracking.cpp:90-166) by the reference's own function: every
+    # kept record of every frame, and those records moved past each image border
+    # (the clamps) and to negative coordinates, at ratios 1 and 0.75 (or_point)
+    for name in RD.MODEL_NAMES:
+        paths = [os.path.join(src, f"{name}_{k}.csv") for k in ("comp", "root", "part")]
+        kept = np.concatenate([E[f"{name}_{i}_kept"] for i in range(RD.N_FRAMES)])
+        moved = []
+        for dx, dy in ((-300.0, 0.0), (400.0, 0.0), (0.0, -250.0), (0.0, 300.0), (-500.0, -400.0)):
+            k2 = kept.copy()
+            k2[:, 0:kept.shape[1] - 3:4] += dy   # y1 of the root and every part box
+            k2[:, 2:kept.shape[1] - 3:4] += dy   # y2
+            k2[:, 1:kept.shape[1] - 3:4] += dx   # x1
+            k2[:, 3:kept.shape[1] - 3:4] += dx   # x2
+            moved.append(k2)
+        boxes = np.concatenate([kept] + moved).astype(np.float32)
+        E[f"gnr_{name}_boxes"] = boxes
+        for ratio in RD.GNR_RATIOS:
+            r = O.ref_get_new_rects(*paths, ratio, boxes, 640, 480)
+            for key in ("point", "or_point", "type", "scale", "score"):
+                E[f"gnr_{name}_{ratio}_{key}"] = r[key]
     np.savez_compressed(RD.EXPECTED, **E)
     for p in (RD.FRAMES, RD.MODELS, RD.EXPECTED):
         print(p, os.path.getsize(p), "bytes")

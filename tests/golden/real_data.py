@@ -15,7 +15,10 @@ Files:
   real_expected.npz  per model and frame: the oracle's kept records and
                      RESULT fields, the box count before NMS, the SHA-256
                      of the A_SCORE map's float bits and of every (level,
-                     component) score map's (score_maps lists the pairs)
+                     component) score map's (score_maps lists the pairs);
+                     gnr_<name>_boxes and gnr_<name>_<ratio>_<field>: the
+                     reference's own get_new_rects on kept records (and on
+                     those records moved past the image borders)
 """
 from __future__ import annotations
 
@@ -35,6 +38,8 @@ N_FRAMES = 21
 THRESH = -0.5
 OVERLAP = 0.4
 RATIO = 1.0
+# model ratios at which the reference's get_new_rects is recorded (or_point = point / ratio)
+GNR_RATIOS = (1.0, 0.75)
 
 
 def encode_frames(frames: np.ndarray) -> np.ndarray:
@@ -134,6 +139,14 @@ def write_model_csv(dump: np.ndarray, out_dir: str, name: str) -> tuple[str, str
 
 def model_dump(name: str) -> np.ndarray:
     return np.load(MODELS)[f"{name}_dump"]
+
+
+def get_new_rects_vectors(name: str) -> tuple:
+    """(boxes, {ratio: RESULT fields}) recorded from the reference's get_new_rects."""
+    E = np.load(EXPECTED)
+    out = {ratio: {k: E[f"gnr_{name}_{ratio}_{k}"] for k in ("point", "or_point", "type", "scale", "score")}
+           for ratio in GNR_RATIOS}
+    return E[f"gnr_{name}_boxes"], out
 
 
 def expected(name: str, frame: int) -> dict:

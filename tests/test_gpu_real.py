@@ -146,3 +146,16 @@ def test_tensor_core_modes_agree_on_real_frames(model_paths, frames):
             json.dump(report, f, indent=1)
     print(report)
     assert report["bf16"]["agreement"] >= 0.9, report
+
+
+@pytest.mark.parametrize("name", RD.MODEL_NAMES)
+def test_get_new_rects_against_the_reference_function(ctx, model_paths, name):
+    """geye_get_new_rects on the records the reference's own get_new_rects
+    (tracking.cpp:90-166) regressed: every kept record, and those records moved
+    past each image border, at two model ratios; bit for bit."""
+    import geye_gb300 as g
+    boxes, want = RD.get_new_rects_vectors(name)
+    for ratio in RD.GNR_RATIOS:
+        m = g.Model(ctx, *model_paths[name], ratio)
+        _check_result(ctx.get_new_rects((640, 480), m, boxes), want[ratio], (name, ratio))
+        m.close()

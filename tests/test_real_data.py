@@ -232,3 +232,34 @@ def test_oracle_stages_on_a_real_frame_match_reference_functions(real_models):
                 gM, gIx, gIy = S.dt(lv, c, k)
                 assert np.array_equal(gM.view(np.int32), M.view(np.int32)) and np.array_equal(gIx, Ix) \
                     and np.array_equal(gIy, Iy), (lv, c, k)
+
+
+# ---------------------------------------------------------------------------
+# get_new_rects against the reference's own function
+# ---------------------------------------------------------------------------
+def _same_rects(got, want, where):
+    assert got["num"] == len(want["score"]), where
+    for k in ("point", "or_point", "type"):
+        assert np.array_equal(got[k], want[k]), (where, k)
+    for k in ("scale", "score"):
+        assert np.array_equal(got[k].view(np.uint32), want[k].view(np.uint32)), (where, k)
+
+
+@pytest.mark.parametrize("name", RD.MODEL_NAMES)
+def test_oracle_get_new_rects_matches_the_reference_vectors(name, tmp_path):
+    """The oracle's box regression (tracking.cpp:90-166) against the outputs of the
+    reference's compiled get_new_rects, kept records and records past the borders."""
+    boxes, want = RD.get_new_rects_vectors(name)
+    paths = RD.write_model_csv(RD.model_dump(name), str(tmp_path), name)
+    for ratio in RD.GNR_RATIOS:
+        got = O.get_new_rects(O.Model(*paths, ratio), boxes, 640, 480)
+        _same_rects(got, want[ratio], (name, ratio))
+
+
+@needs_ref
+@pytest.mark.parametrize("name", RD.MODEL_NAMES)
+def test_reference_get_new_rects_reproduces_its_vectors(name):
+    boxes, want = RD.get_new_rects_vectors(name)
+    paths = [os.path.join(O.REF_SRC_DIR, f"{name}_{k}.csv") for k in ("comp", "root", "part")]
+    for ratio in RD.GNR_RATIOS:
+        _same_rects(O.ref_get_new_rects(*paths, ratio, boxes, 640, 480), want[ratio], (name, ratio))
