@@ -49,12 +49,16 @@ WORKLOADS = {
     # served: frames from many streams in flight at once through geye_server_* (BF16 tensor-core conv)
     "served_bf16_car+person_640x480": dict(w=640, h=480, models=("car", "person"), conv="bf16", served=True, slots=16),
     # 64 simulated cameras, Poisson arrivals at 30 fps each, mixed resolutions, trackers on, 40 GB budget
+    # (latency-aware admission: at most one frame of a camera waits for a slot, a newer one replaces it,
+    # and a frame that waited more than 40 ms is dropped rather than served late)
+    # (at most 16 slots: frames in flight share the GPU, so more slots lengthen every frame's latency)
     "serve64_mixed_bf16": dict(w=640, h=480, models=("car", "person"), conv="bf16", sim=True, streams=64, fps=30.0,
-                               sizes=((640, 480), (1280, 720), (1920, 1080)), seconds=6.0),
+                               sizes=((640, 480), (1280, 720), (1920, 1080)), seconds=6.0, slots=16,
+                               admission=(1, 40.0)),
     # 64 cameras at 640x480 only (the served BF16 pipeline's latency target at 64 streams)
     # (at most 16 slots: more frames in flight only lengthen each frame's share of the GPU)
     "serve64_640x480_bf16": dict(w=640, h=480, models=("car", "person"), conv="bf16", sim=True, streams=64, fps=30.0,
-                                 sizes=((640, 480),), seconds=6.0, slots=16),
+                                 sizes=((640, 480),), seconds=6.0, slots=16, admission=(1, 40.0)),
     # a batch of 32 frames of mixed sizes as one CUDA graph (geye_batch_run)
     "batch32_mixed_fp32": dict(w=640, h=480, models=("car", "person"), conv="fp32", batch=32,
                                sizes=((320, 240), (640, 480), (1280, 720), (1920, 1080))),
@@ -158,6 +162,19 @@ def _write_models(spec_names, d):
     from geye_gb300 import synth
     specs = {"car": synth.CAR_SPEC, "person": synth.PERSON_SPEC}
     return [synth.write_model_csv(specs[n], d) for n in spec_names]
+
+
+def cpu_baseline_line(wl, paths, frame):
+    """The CPU oracle on one frame of the workload with every host thread, and with one."""
+    from oracle import oracle as O
+    O.build()
+    nthreads = os.cpu_count() or 1
+    fps, dt = cpu_oracle_frames_per_sec(wl, paths, frame, nthreads, n_frames=1)
+    fps1, dt1 = cpu_oracle_frames_per_sec(wl, paths, frame, 1, n_frames=1)
+    return {"value": fps, "unit": "frames/s", "cores": nthreads, "kind": "port",
+            "sample": f"1 frame of the workload ({dt:.2f} s wall, both models, oracle with {nthreads} threads; "
+                      f"{dt1:.2f} s with one thread)",
+            "one_thread": {"value": fps1, "unit": "frames/s", "cores": 1}}
 
 
 def cpu_oracle_frames_per_sec(wl, paths, frame, nthreads, n_frames=1):
@@ -338,12 +355,7 @@ def run_gpu(args, wl):
     # ---- CPU baseline (rank 0, N=1 only)
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        from oracle import oracle as O
-        O.build()
-        nthreads = os.cpu_count() or 1
-        fps_cpu, dt = cpu_oracle_frames_per_sec(wl, paths, frame, nthreads, n_frames=1)
-        cpu = {"value": fps_cpu, "unit": "frames/s", "cores": nthreads, "kind": "port",
-               "sample": f"1 frame of the workload ({dt:.2f} s wall, both models, oracle with {nthreads} threads)"}
+        cpu = cpu_baseline_line(wl, paths, frame)
 
     clocks = clk.summary()
     tuning = [ctx.conv_tuning(m) for m in models] if wl["conv"] != "fp32" else None
@@ -554,6 +566,8 @@ def run_served(args, wl):
     plain = _plain_fp32(paths, frames[0], 30)
     agree = _agreement(paths, frames[:4], g.CONV_BF16)
     stages, last = _stage_breakdown(paths, frames[0], g.CONV_BF16)
+    stage_gbs = {k: (last["bytes"][k] / (stages[k] / 1000.0) / 1e9 if stages.get(k) and last["bytes"].get(k) else None)
+                 for k in ("pyramid", "hog", "dt", "score")}
     hbm, bf16, bf16s, peak_src = _peaks()
     conv_flops = last["conv_flops"]
     achieved = conv_flops / (stages["conv"] / 1000.0) / 1e12
@@ -563,13 +577,18 @@ def run_served(args, wl):
                 "flops_per_launch": conv_flops, "ms_per_launch": stages["conv"]}
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        from oracle import oracle as O
-        O.build()
-        nthreads = os.cpu_count() or 1
-        fps_cpu, dt = cpu_oracle_frames_per_sec(wl, paths, frames[0], nthreads, n_frames=1)
-        cpu = {"value": fps_cpu, "unit": "frames/s", "cores": nthreads, "kind": "port",
-               "sample": f"1 frame of the workload ({dt:.2f} s wall, both models, oracle with {nthreads} threads)"}
+        cpu = cpu_baseline_line(wl, paths, frames[0])
     clocks = clk.summary()
+    # the 64-camera serving workloads, a few seconds each (open loop, Poisson arrivals)
+    serving = None
+    if rank == 0 and world == 1:
+        serving = {}
+        for name in ("serve64_640x480_bf16", "serve64_mixed_bf16"):
+            sw = dict(WORKLOADS[name])
+            sw["seconds"] = 3.0
+            r = serve_sim(sw, models, sw.get("slots", 64))
+            serving[name] = {k: r[k] for k in ("offered_fps", "served_fps", "dropped_fps", "p50_ms", "p99_ms",
+                                               "slots", "admission", "sizes")}
     if rank == 0:
         line = {
             "metric": "frames_per_sec", "value": value, "unit": "frames/s", "n_gpus": world, "steps": args.steps,
@@ -590,9 +609,11 @@ def run_served(args, wl):
             "agreement_vs_fp32": agree,
             "gpu_launches": int(launches_per_frame * S * args.steps),
             "stage_ms": stages,
+            "stage_gbs": stage_gbs,
             "roofline": roofline,
             "cpu_baseline": cpu,
             "clocks": clocks,
+            "serving": serving,
         }
         print(json.dumps(line), flush=True)
     for m in models:
@@ -603,25 +624,19 @@ def run_served(args, wl):
     return 0
 
 
-def run_serve_sim(args, wl):
-    """64 simulated cameras: Poisson arrivals, mixed resolutions, trackers, HBM budget; open loop."""
+def serve_sim(wl, models, max_slots):
+    """Simulated cameras through one geye_server_*: Poisson arrivals at wl["fps"] per stream, each
+    stream's resolution drawn from wl["sizes"], trackers on, 40 GB budget; open loop for wl["seconds"].
+    Latency of a served frame: arrival to results on the host.  Dropped frames (the admission limits
+    of wl["admission"] = (frames a stream may hold waiting, longest wait in ms)) are counted apart."""
     import geye_gb300 as g
     from geye_gb300 import synth
-    rank, world, local = dist_info()
-    if world > 1 and rank != 0:
-        return 0
     rng = np.random.default_rng(7)
-    tmp = tempfile.TemporaryDirectory()
-    paths = _write_models(wl["models"], tmp.name)
-    owner = g.Context(0, conv=g.CONV_BF16)
-    models = [g.Model(owner, *p) for p in paths]
     n = wl["streams"]
     sizes = [wl["sizes"][i] for i in rng.integers(0, len(wl["sizes"]), size=n)]
-    frames = {}
-    for s in range(n):
-        for k in range(2):
-            frames[(s, k)] = synth.make_frame(*sizes[s], seed=1000 * s + k)
-    max_slots = args.slots or wl.get("slots", 64)
+    # four distinct frames per resolution, shared by the streams (stream s alternates two of them)
+    base = {(sz, k): synth.make_frame(*sz, seed=1000 * j + k) for j, sz in enumerate(sorted(set(sizes))) for k in range(4)}
+    frames = {(s, k): base[(sizes[s], (s + k) % 4)] for s in range(n) for k in range(2)}
     srv = g.Server(models, conv=g.CONV_BF16, hbm_budget=40 << 30, max_slots=max_slots, track=True)
     for sz in sorted(set(sizes)):   # slots, plans and graphs for every resolution before the clock starts
         s0 = sizes.index(sz)
@@ -630,6 +645,8 @@ def run_serve_sim(args, wl):
                 srv.submit(s0, frames[(s0, 0)])
             srv.drain()
             srv.poll(1024)
+    adm = wl.get("admission", (0, 0.0))
+    srv.set_admission(adm[0], adm[1])
     T = wl["seconds"]
     arrivals = []
     for s in range(n):
@@ -639,7 +656,7 @@ def run_serve_sim(args, wl):
             t += rng.exponential(1.0 / wl["fps"])
     arrivals.sort()
     lat, sub_at, k_of = [], {}, {}
-    i = done = 0
+    i = done = dropped = 0
     t0 = time.perf_counter()
     with ClockSampler(0) as clk:
         while done < len(arrivals):
@@ -653,7 +670,10 @@ def run_serve_sim(args, wl):
             out = srv.poll(256, with_results=False)
             for d in out:
                 ta, ts = sub_at.pop(d["ticket"])
-                lat.append(1000.0 * (ts - ta) + d["latency_ns"] / 1e6)
+                if d["dropped"]:
+                    dropped += 1
+                else:
+                    lat.append(1000.0 * (ts - ta) + d["latency_ns"] / 1e6)
                 done += 1
             if not out:
                 time.sleep(0.0002)
@@ -661,24 +681,47 @@ def run_serve_sim(args, wl):
     st = srv.stats()
     tracks = sum(len(srv.tracks(s)) for s in range(n))
     srv.close()
+    return {"arrivals": len(arrivals), "wall": wall, "offered_fps": len(arrivals) / T,
+            "served_fps": len(lat) / wall, "dropped_fps": dropped / wall,
+            "p50_ms": float(np.percentile(lat, 50)) if lat else None,
+            "p99_ms": float(np.percentile(lat, 99)) if lat else None,
+            "slots": st["slots"], "max_slots": max_slots, "bytes_held": st["bytes_held"], "live_tracks_end": tracks,
+            "admission": {"max_waiting_per_stream": adm[0], "max_wait_ms": adm[1]},
+            "sizes": {f"{a}x{b}": sizes.count((a, b)) for a, b in sorted(set(sizes))},
+            "h2d_bytes_per_frame": int(np.mean([a * b * 3 for a, b in sizes])), "clocks": clk.summary()}
+
+
+def run_serve_sim(args, wl):
+    """64 simulated cameras: Poisson arrivals, mixed resolutions, trackers, HBM budget; open loop."""
+    import geye_gb300 as g
+    rank, world, local = dist_info()
+    if world > 1 and rank != 0:
+        return 0
+    tmp = tempfile.TemporaryDirectory()
+    paths = _write_models(wl["models"], tmp.name)
+    owner = g.Context(0, conv=g.CONV_BF16)
+    models = [g.Model(owner, *p) for p in paths]
+    r = serve_sim(wl, models, args.slots or wl.get("slots", 64))
     for m in models:
         m.close()
     owner.close()
+    n = r["arrivals"]
     line = {
-        "metric": "frames_per_sec", "value": len(arrivals) / wall, "unit": "frames/s", "n_gpus": 1,
-        "steps": len(arrivals), "warmup": len(set(sizes)), "ms_per_step": 1000.0 * wall / len(arrivals),
+        "metric": "frames_per_sec", "value": r["served_fps"], "unit": "frames/s", "n_gpus": 1,
+        "steps": n, "warmup": len(r["sizes"]), "ms_per_step": 1000.0 * r["wall"] / max(n, 1),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "bf16", "data": "synthetic",
-        "config": {"workload": args.workload, "streams": n, "arrivals": f"Poisson {wl['fps']} fps per stream",
-                   "offered_fps": len(arrivals) / T, "sizes": {f"{a}x{b}": sizes.count((a, b)) for a, b in set(sizes)},
-                   "seconds": T, "tracker": "500 particles/track, Philox, sigma 4 px", "hbm_budget_gb": 40,
-                   "models": list(wl["models"]), "conv": "bf16"},
-        "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
-        "e2e": {"value": len(arrivals) / wall, "unit": "frames/s", "api": "geye_server_submit/poll",
-                "h2d_bytes_per_step": int(np.mean([a * b * 3 for a, b in sizes])), "d2h_bytes_per_step": 4 * (64 + 2 * 11 * 4096),
-                "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99))},
-        "server": {"slots": st["slots"], "max_slots": max_slots, "bytes_held": st["bytes_held"],
-                   "live_tracks_end": tracks},
-        "clocks": clk.summary(),
+        "config": {"workload": args.workload, "streams": wl["streams"], "arrivals": f"Poisson {wl['fps']} fps per stream",
+                   "offered_fps": r["offered_fps"], "sizes": r["sizes"], "seconds": wl["seconds"],
+                   "tracker": "500 particles/track, Philox, sigma 4 px", "hbm_budget_gb": 40,
+                   "models": list(wl["models"]), "conv": "bf16", "admission": r["admission"]},
+        "p50_ms": r["p50_ms"], "p99_ms": r["p99_ms"],
+        "e2e": {"value": r["served_fps"], "unit": "frames/s", "api": "geye_server_submit/poll",
+                "h2d_bytes_per_step": r["h2d_bytes_per_frame"], "d2h_bytes_per_step": 4 * (64 + 2 * 11 * 4096),
+                "p50_ms": r["p50_ms"], "p99_ms": r["p99_ms"]},
+        "offered_fps": r["offered_fps"], "dropped_fps": r["dropped_fps"],
+        "server": {"slots": r["slots"], "max_slots": r["max_slots"], "bytes_held": r["bytes_held"],
+                   "live_tracks_end": r["live_tracks_end"]},
+        "clocks": r["clocks"],
     }
     print(json.dumps(line), flush=True)
     return 0

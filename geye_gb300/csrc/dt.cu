@@ -196,18 +196,21 @@ __device__ __forceinline__ bool dt_monotone(float vabs, float a, float b, int K)
 // PASS 1: along y (dim 0) of each column x of the negated part map -> tmpM, tmpI.
 // PASS 2: along x (dim 1) of each row y of tmpM -> M, Ix, Iy = tmpIy[Ix*d0 + y]
 // (dt.cpp:123-133).
+// One block per entry of `blocks` (job, first line of its tile): the launch covers
+// exactly the tiles of every map, however their sizes differ across levels.
 template <int PASS>
-__global__ void __launch_bounds__(kDtThreads) k_dt(const DtJob *__restrict__ jobs, float *__restrict__ arena,
-                                                    int *__restrict__ arena_i, int *fallback_count) {
+__global__ void __launch_bounds__(kDtThreads) k_dt(const DtJob *__restrict__ jobs, const int2 *__restrict__ blocks,
+                                                    float *__restrict__ arena, int *__restrict__ arena_i,
+                                                    int *fallback_count) {
   extern __shared__ float dsm[];
-  const DtJob J = jobs[blockIdx.y];
+  const int2 blk = blocks[blockIdx.x];
+  const DtJob J = jobs[blk.x];
   const int d0 = J.d0;
   const int n = PASS == 1 ? J.d0 : J.d1;           // line length
   const int nlines = PASS == 1 ? J.d1 : J.d0;
   const int lgL = PASS == 1 ? 0 : dt_lg_lines2(n);
   const int L = PASS == 1 ? dt_lines1(n) : (1 << lgL);
-  const int line0 = blockIdx.x * L;
-  if (line0 >= nlines) return;
+  const int line0 = blk.y;
   const int nl = min(L, nlines - line0);
   const int stride = n + kDtPad;
   float *v_s = dsm + kDtPad;                       // line l at v_s[l * stride], +inf pads between
@@ -333,19 +336,34 @@ __global__ void __launch_bounds__(kDtThreads) k_dt(const DtJob *__restrict__ job
   }
 }
 
-void launch_dt(const DtJob *d_jobs, int n_jobs, int max_d0, int max_d1, float *arena, int *arena_i,
-               int *fallback_count, cudaStream_t s) {
-  if (n_jobs <= 0) return;
-  // the longest lines get the fewest lines per block, so these grids cover every job
-  const int L1 = dt_lines1(max_d0), L2 = 1 << dt_lg_lines2(max_d1);
+void dt_block_lists(const std::vector<DtJob> &jobs, std::vector<int2> &b1, std::vector<int2> &b2) {
+  b1.clear();
+  b2.clear();
+  for (size_t j = 0; j < jobs.size(); j++) {
+    const DtJob &J = jobs[j];
+    const int L1 = dt_lines1(J.d0), L2 = 1 << dt_lg_lines2(J.d1);
+    for (int l = 0; l < J.d1; l += L1) b1.push_back(make_int2((int)j, l));
+    for (int l = 0; l < J.d0; l += L2) b2.push_back(make_int2((int)j, l));
+  }
+  // the largest maps' tiles first, so the long blocks start in the first wave
+  auto by_size = [&](const int2 &x, const int2 &y) {
+    return (long long)jobs[x.x].d0 * jobs[x.x].d1 > (long long)jobs[y.x].d0 * jobs[y.x].d1;
+  };
+  std::stable_sort(b1.begin(), b1.end(), by_size);
+  std::stable_sort(b2.begin(), b2.end(), by_size);
+}
+
+void launch_dt(const DtJob *d_jobs, const int2 *d_b1, int n_b1, const int2 *d_b2, int n_b2, int max_d0, int max_d1,
+               float *arena, int *arena_i, int *fallback_count, cudaStream_t s) {
+  if (n_b1 <= 0) return;
   size_t smem1 = 0, smem2 = 0;
   for (int n = 1; n <= max_d0; n++) smem1 = std::max(smem1, dt_smem_bytes(dt_lines1(n), n));
   for (int n = 1; n <= max_d1; n++) smem2 = std::max(smem2, dt_smem_bytes(1 << dt_lg_lines2(n), n));
   static SmemAttr a1, a2;
   raise_smem(a1, k_dt<1>, smem1);
   raise_smem(a2, k_dt<2>, smem2);
-  k_dt<1><<<dim3((max_d1 + L1 - 1) / L1, n_jobs), kDtThreads, smem1, s>>>(d_jobs, arena, arena_i, fallback_count);
-  k_dt<2><<<dim3((max_d0 + L2 - 1) / L2, n_jobs), kDtThreads, smem2, s>>>(d_jobs, arena, arena_i, fallback_count);
+  k_dt<1><<<n_b1, kDtThreads, smem1, s>>>(d_jobs, d_b1, arena, arena_i, fallback_count);
+  k_dt<2><<<n_b2, kDtThreads, smem2, s>>>(d_jobs, d_b2, arena, arena_i, fallback_count);
 }
 
 }  // namespace geye

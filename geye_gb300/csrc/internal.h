@@ -234,13 +234,16 @@ void launch_from_ref_layout(const float *ref, int fs0, int fs1, float *feat, cud
 void launch_conv_fp32(const ConvJob *d_jobs, int n_jobs, int max_tiles_y, int max_tiles_x, const float *filters,
                       const int *filt_off, const float *arena_in, float *arena_out, int max_b0, int max_b1,
                       int max_group, cudaStream_t s, int cr = 4);
-void launch_dt(const DtJob *d_jobs, int n_jobs, int max_d0, int max_d1, float *arena, int *arena_i,
-               int *fallback_count, cudaStream_t s);
-void launch_score(const ScoreJob *d_jobs, int n_jobs, int max_r, float thresh, float *arena, int *block_counts,
-                  int blocks_per_job_stride, cudaStream_t s);
-void launch_boxes(const ScoreJob *d_jobs, int n_jobs, int max_r, float thresh, const float *arena,
-                  const int *arena_i, const int *block_offsets, int blocks_per_job_stride, int GL, float *boxes,
-                  cudaStream_t s);
+// (job, first line) of every DT block, pass 1 (columns) and pass 2 (rows), largest maps first
+void dt_block_lists(const std::vector<DtJob> &jobs, std::vector<int2> &b1, std::vector<int2> &b2);
+void launch_dt(const DtJob *d_jobs, const int2 *d_b1, int n_b1, const int2 *d_b2, int n_b2, int max_d0, int max_d1,
+               float *arena, int *arena_i, int *fallback_count, cudaStream_t s);
+// (job, block of 256 positions) of every score map, in job order
+void score_block_list(const std::vector<ScoreJob> &jobs, std::vector<int2> &blocks);
+void launch_score(const ScoreJob *d_jobs, const int2 *d_blocks, int n_blocks, float thresh, float *arena,
+                  int *block_counts, cudaStream_t s);
+void launch_boxes(const ScoreJob *d_jobs, const int2 *d_blocks, int n_blocks, float thresh, const float *arena,
+                  const int *arena_i, const int *block_offsets, int GL, float *boxes, cudaStream_t s);
 void launch_scan_counts(int *counts, int n, int *total, cudaStream_t s);
 void launch_ascore(const int *col, const int *row, int n_jobs, const float *arena, float *a_score, int im_w,
                   int im_h, float thresh, unsigned *max_bits, cudaStream_t s);

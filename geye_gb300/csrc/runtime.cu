@@ -402,12 +402,25 @@ static geye_status build_model_plan(geye_ctx *ctx, Plan &P, geye_model *mdl, int
     }
   }
   if (mp->dt_max_d0 > 1100 || mp->dt_max_d1 > 1100) { set_error("frame too large for the DT kernels"); return GEYE_ERR_UNSUPPORTED; }
-  mp->score_stride = (mp->score_max_r + 255) / 256;
   GEYE_TRY(upload(ctx, mp->d_root_jobs, mp->root_jobs));
   GEYE_TRY(upload(ctx, mp->d_part_jobs, mp->part_jobs));
   GEYE_TRY(upload(ctx, mp->d_dt_jobs, mp->dt_jobs));
+  {
+    std::vector<int2> b1, b2;
+    dt_block_lists(mp->dt_jobs, b1, b2);
+    mp->dt_nblocks1 = (int)b1.size();
+    mp->dt_nblocks2 = (int)b2.size();
+    GEYE_TRY(upload(ctx, mp->d_dt_blocks1, b1));
+    GEYE_TRY(upload(ctx, mp->d_dt_blocks2, b2));
+  }
   GEYE_TRY(upload(ctx, mp->d_score_jobs, mp->score_jobs));
-  GEYE_TRY(mp->d_counts.alloc(ctx, sizeof(int) * ((size_t)std::max<size_t>(mp->score_jobs.size(), 1) * std::max(mp->score_stride, 1) + 8)));
+  {
+    std::vector<int2> sb;
+    score_block_list(mp->score_jobs, sb);
+    mp->score_nblocks = (int)sb.size();
+    GEYE_TRY(upload(ctx, mp->d_score_blocks, sb));
+  }
+  GEYE_TRY(mp->d_counts.alloc(ctx, sizeof(int) * ((size_t)std::max(mp->score_nblocks, 1) + 8)));
   P.models.push_back(std::move(mp));
   return GEYE_OK;
 }
@@ -870,7 +883,8 @@ geye_status run_conv(geye_ctx *ctx, Plan &P, ModelPlan &mp) {
 
 geye_status run_dt(geye_ctx *ctx, Plan &P, ModelPlan &mp) {
   if (mp.dt_jobs.empty()) return GEYE_OK;
-  launch_dt(mp.d_dt_jobs.as<DtJob>(), (int)mp.dt_jobs.size(), mp.dt_max_d0, mp.dt_max_d1, P.arena.as<float>(),
+  launch_dt(mp.d_dt_jobs.as<DtJob>(), mp.d_dt_blocks1.as<int2>(), mp.dt_nblocks1, mp.d_dt_blocks2.as<int2>(),
+            mp.dt_nblocks2, mp.dt_max_d0, mp.dt_max_d1, P.arena.as<float>(),
             P.arena.as<int>(), ctx->d_diag.as<int>(), ctx->stream);
   ctx->launches++;
   return check_launch(ctx, "dt");
@@ -885,14 +899,14 @@ geye_status run_score(geye_ctx *ctx, Plan &P, ModelPlan &mp, int mi, float thres
     CUDA_TRY(cudaMemsetAsync(d_num, 0, sizeof(int), ctx->stream));
     return GEYE_OK;
   }
-  launch_score(mp.d_score_jobs.as<ScoreJob>(), nj, mp.score_max_r, thresh, P.arena.as<float>(), counts,
-               mp.score_stride, ctx->stream);
+  launch_score(mp.d_score_jobs.as<ScoreJob>(), mp.d_score_blocks.as<int2>(), mp.score_nblocks, thresh,
+               P.arena.as<float>(), counts, ctx->stream);
   GEYE_TRY(check_launch(ctx, "score"));
-  launch_scan_counts(counts, nj * mp.score_stride, d_num, ctx->stream);
+  launch_scan_counts(counts, mp.score_nblocks, d_num, ctx->stream);
   GEYE_TRY(check_launch(ctx, "scan"));
   float *boxes = P.d_boxes.as<float>() + (size_t)mi * P.max_cap * P.gl;
-  launch_boxes(mp.d_score_jobs.as<ScoreJob>(), nj, mp.score_max_r, thresh, P.arena.as<float>(), P.arena.as<int>(),
-               counts, mp.score_stride, mp.model->gl(), boxes, ctx->stream);
+  launch_boxes(mp.d_score_jobs.as<ScoreJob>(), mp.d_score_blocks.as<int2>(), mp.score_nblocks, thresh,
+               P.arena.as<float>(), P.arena.as<int>(), counts, mp.model->gl(), boxes, ctx->stream);
   return check_launch(ctx, "boxes");
 }
 

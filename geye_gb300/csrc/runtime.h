@@ -108,10 +108,14 @@ struct ModelPlan {
   std::vector<DtJob> dt_jobs;
   int dt_max_d0 = 0, dt_max_d1 = 0;
   std::vector<ScoreJob> score_jobs;
-  int score_max_r = 0, score_stride = 0;
+  int score_max_r = 0;
   int cap = 0;                          // max detections (sum of root map sizes)
   // device copies
   DevBuf d_root_jobs, d_part_jobs, d_dt_jobs, d_score_jobs, d_counts;
+  DevBuf d_dt_blocks1, d_dt_blocks2;    // DT tiles of every map (dt_block_lists)
+  int dt_nblocks1 = 0, dt_nblocks2 = 0;
+  DevBuf d_score_blocks;                // score / box blocks of every map (score_block_list)
+  int score_nblocks = 0;
   // per-(level, comp) and per-(L, part) map offsets for stage readback
   std::vector<int> root_map_off, root_r0, root_r1;     // [level*NoC + c], -1 if none
   std::vector<int> part_map_off, part_d0, part_d1;     // [L*NoP + p]

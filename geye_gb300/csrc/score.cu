@@ -41,11 +41,17 @@ __device__ __forceinline__ float assemble(const ScoreJob &J, const float *__rest
   return s;
 }
 
-__global__ void k_score(const ScoreJob *__restrict__ jobs, float thresh, float *__restrict__ arena,
-                        int *__restrict__ block_counts, int stride) {
-  const ScoreJob &J = jobs[blockIdx.y];
+// One block per entry of `blocks` (job, block of 256 positions): exactly the
+// blocks the maps need, whatever their sizes across levels.  Its count of
+// positions above the threshold goes to block_counts[blockIdx.x]; the list is
+// in job order, so the exclusive scan of the counts places every block's
+// records in the reference's order.
+__global__ void k_score(const ScoreJob *__restrict__ jobs, const int2 *__restrict__ blocks, float thresh,
+                        float *__restrict__ arena, int *__restrict__ block_counts) {
+  const int2 blk = blocks[blockIdx.x];
+  const ScoreJob &J = jobs[blk.x];
   const int n = J.r0 * J.r1;
-  const int i = blockIdx.x * kScoreThreads + threadIdx.x;
+  const int i = blk.y * kScoreThreads + threadIdx.x;
   int flag = 0;
   if (i < n) {
     const int y = i % J.r0, x = i / J.r0;
@@ -54,14 +60,19 @@ __global__ void k_score(const ScoreJob *__restrict__ jobs, float thresh, float *
     flag = s > thresh;
   }
   const int c = __syncthreads_count(flag);
-  if (threadIdx.x == 0) block_counts[blockIdx.y * stride + blockIdx.x] = c;
+  if (threadIdx.x == 0) block_counts[blockIdx.x] = c;   // block-list order: job, then position
 }
 
-void launch_score(const ScoreJob *d_jobs, int n_jobs, int max_r, float thresh, float *arena, int *block_counts,
-                  int stride, cudaStream_t s) {
-  if (n_jobs <= 0) return;
-  dim3 grid((max_r + kScoreThreads - 1) / kScoreThreads, n_jobs);
-  k_score<<<grid, kScoreThreads, 0, s>>>(d_jobs, thresh, arena, block_counts, stride);
+void score_block_list(const std::vector<ScoreJob> &jobs, std::vector<int2> &blocks) {
+  blocks.clear();
+  for (size_t j = 0; j < jobs.size(); j++)
+    for (int b = 0; b * kScoreThreads < jobs[j].r0 * jobs[j].r1; b++) blocks.push_back(make_int2((int)j, b));
+}
+
+void launch_score(const ScoreJob *d_jobs, const int2 *d_blocks, int n_blocks, float thresh, float *arena,
+                  int *block_counts, cudaStream_t s) {
+  if (n_blocks <= 0) return;
+  k_score<<<n_blocks, kScoreThreads, 0, s>>>(d_jobs, d_blocks, thresh, arena, block_counts);
 }
 
 // exclusive scan of n ints in place (one block); *total gets the sum
@@ -131,17 +142,18 @@ __device__ __forceinline__ float sum_minus_one(float q, float h) {
   return (float)((double)q + (double)h - 1.0);
 }
 
-__global__ void __launch_bounds__(kScoreThreads) k_boxes(const ScoreJob *__restrict__ jobs, float thresh,
+__global__ void __launch_bounds__(kScoreThreads) k_boxes(const ScoreJob *__restrict__ jobs,
+                                                         const int2 *__restrict__ blocks, float thresh,
                                                          const float *__restrict__ arena,
                                                          const int *__restrict__ arena_i,
-                                                         const int *__restrict__ block_offsets, int stride, int GL,
+                                                         const int *__restrict__ block_offsets, int GL,
                                                          float *__restrict__ boxes) {
   extern __shared__ float rec_s[];   // [count][GL]
   __shared__ int warp_cnt[kScoreThreads / 32];
-  const ScoreJob &J = jobs[blockIdx.y];
+  const int2 blk = blocks[blockIdx.x];
+  const ScoreJob &J = jobs[blk.x];
   const int n = J.r0 * J.r1;
-  if ((int)blockIdx.x * kScoreThreads >= n) return;
-  const int i = blockIdx.x * kScoreThreads + threadIdx.x;
+  const int i = blk.y * kScoreThreads + threadIdx.x;
   float s = 0.f;
   int flag = 0;
   if (i < n) {
@@ -190,18 +202,17 @@ __global__ void __launch_bounds__(kScoreThreads) k_boxes(const ScoreJob *__restr
     Q[2] = scale;
   }
   __syncthreads();
-  float *out = boxes + (size_t)block_offsets[blockIdx.y * stride + blockIdx.x] * GL;
+  float *out = boxes + (size_t)block_offsets[blockIdx.x] * GL;
   for (int t = threadIdx.x; t < count * GL; t += kScoreThreads) out[t] = rec_s[t];
 }
 
-void launch_boxes(const ScoreJob *d_jobs, int n_jobs, int max_r, float thresh, const float *arena,
-                  const int *arena_i, const int *block_offsets, int stride, int GL, float *boxes, cudaStream_t s) {
-  if (n_jobs <= 0) return;
-  dim3 grid((max_r + kScoreThreads - 1) / kScoreThreads, n_jobs);
+void launch_boxes(const ScoreJob *d_jobs, const int2 *d_blocks, int n_blocks, float thresh, const float *arena,
+                  const int *arena_i, const int *block_offsets, int GL, float *boxes, cudaStream_t s) {
+  if (n_blocks <= 0) return;
   const size_t smem = sizeof(float) * kScoreThreads * GL;
   static SmemAttr attr;
   raise_smem(attr, k_boxes, smem);
-  k_boxes<<<grid, kScoreThreads, smem, s>>>(d_jobs, thresh, arena, arena_i, block_offsets, stride, GL, boxes);
+  k_boxes<<<n_blocks, kScoreThreads, smem, s>>>(d_jobs, d_blocks, thresh, arena, arena_i, block_offsets, GL, boxes);
 }
 
 // A_SCORE in gather form: target pixel (X, Y) takes the max over every

@@ -355,6 +355,7 @@ size_t plan_device_bytes(const Plan &P) {
   b += P.tc.d_bank.bytes + P.tc.d_jobs.bytes + P.tc.d_chunks.bytes + P.tc.d_cols.bytes + P.tc.d_sums.bytes;
   for (auto &mp : P.models)
     b += mp->d_root_jobs.bytes + mp->d_part_jobs.bytes + mp->d_dt_jobs.bytes + mp->d_score_jobs.bytes +
+         mp->d_dt_blocks1.bytes + mp->d_dt_blocks2.bytes + mp->d_score_blocks.bytes +
          mp->d_counts.bytes + mp->d_as_col.bytes + mp->d_as_row.bytes;
   return b;
 }
