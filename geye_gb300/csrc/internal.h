@@ -70,6 +70,8 @@ struct HogJob {
   int feat_off;            // [pos][32] float
   int feat16_off;          // tensor-core planes (offset in 2-byte units), -1 = not written
   int feat16lo_off;        // BF16 remainder planes (root levels in BF16 mode), -1 = none
+  int fast;                // 1 (tensor-core modes): float normalisation factors computed per cell,
+                           // no corner pass; 0: the reference's double form, bit for bit
   int tc_planes;           // 4: bf16 planes [4][fs0*fs1 + kTcPlanePad][16 B]; 2: e4m3 planes; 0: none
   int mag_off, bin_off;    // the image's pixel magnitudes (float) and bins (u8), [x * pix_Y + y]
   int pix_Y;
@@ -226,8 +228,12 @@ void launch_fill(float *p, size_t n, float v, cudaStream_t s);
 void launch_ingest(const uint8_t *bgr, int width, int height, int width_step, float *planes, cudaStream_t s);
 void launch_resize_pass(const ResizeJob *d_jobs, int n_jobs, int max_cols, int vertical, const int *d_tap_start,
                         const int *d_tap_si, const float *d_tap_alpha, float *arena, cudaStream_t s);
-void launch_hog(const HogJob *d_jobs, int n_jobs, int max_b0, int max_b1, const HogPixJob *d_pix, int n_pix,
-                int max_xe, float *arena, void *arena16, cudaStream_t s);   // arena16: base of the tensor-core planes (bytes)
+// (job, block of histogram blocks) of every level's vote kernel
+void hog_vote_blocks(const std::vector<HogJob> &jobs, std::vector<int2> &blocks);
+// corners: run the corner-factor pass (jobs with fast = 0 read its factors)
+void launch_hog(const HogJob *d_jobs, int n_jobs, const int2 *d_vote_blocks, int n_vote_blocks, int max_b0,
+                int max_b1, const HogPixJob *d_pix, int n_pix, int max_xe, float *arena, void *arena16,
+                bool corners, cudaStream_t s);   // arena16: base of the tensor-core planes (bytes)
 void launch_to_ref_layout(const float *feat, int fs0, int fs1, float *out, cudaStream_t s);
 void launch_flip_feat(const float *feat, int n0, int n1, float *out, cudaStream_t s);
 void launch_from_ref_layout(const float *ref, int fs0, int fs1, float *feat, cudaStream_t s);

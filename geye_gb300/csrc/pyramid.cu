@@ -278,12 +278,16 @@ __device__ __forceinline__ void hog_vote_pow2(float *myh, const float *__restric
   }
 }
 
-__global__ void __launch_bounds__(kVoteThreads, 4) k_hog_vote(const HogJob *__restrict__ jobs, float *__restrict__ arena) {
+// One CUDA block per entry of `blocks` (job, block of kVoteThreads histogram
+// blocks): exactly the blocks every level needs.
+__global__ void __launch_bounds__(kVoteThreads, 4) k_hog_vote(const HogJob *__restrict__ jobs,
+                                                             const int2 *__restrict__ blocks,
+                                                             float *__restrict__ arena) {
   __shared__ float hist_s[18 * kVoteThreads];
-  const HogJob J = jobs[blockIdx.y];
+  const int2 blk = blocks[blockIdx.x];
+  const HogJob J = jobs[blk.x];
   const int nb = J.b0 * J.b1;
-  const int pos = blockIdx.x * kVoteThreads + threadIdx.x;
-  if ((int)blockIdx.x * kVoteThreads >= nb) return;
+  const int pos = blk.y * kVoteThreads + threadIdx.x;
   float *myh = hist_s + threadIdx.x;   // bin o at myh[o * kVoteThreads]
 #pragma unroll
   for (int o = 0; o < 18; o++) myh[o * kVoteThreads] = 0.f;
@@ -377,10 +381,24 @@ __global__ void k_hog_feat(const HogJob *__restrict__ jobs, float *__restrict__ 
   float *feat = arena + J.feat_off;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < ncell; i += gridDim.x * blockDim.x) {
     const int y = i % J.fs0, x = i / J.fs0;
-    const float n1 = N[(x + 1) * C0 + y + 1];
-    const float n2 = N[(x + 1) * C0 + y];
-    const float n3 = N[x * C0 + y + 1];
-    const float n4 = N[x * C0 + y];
+    float n1, n2, n3, n4;
+    if (J.fast) {
+      // the tensor-core modes: the four corner factors in float here (no FP64, no corner pass)
+      const float *e = hist + (size_t)18 * nb;
+      auto corner = [&](int cx, int cy) {
+        const float *p = e + cx * b0 + cy;
+        return 1.0f / sqrtf(p[0] + p[1] + p[b0] + p[b0 + 1] + 0.0001f);
+      };
+      n1 = corner(x + 1, y + 1);
+      n2 = corner(x + 1, y);
+      n3 = corner(x, y + 1);
+      n4 = corner(x, y);
+    } else {
+      n1 = N[(x + 1) * C0 + y + 1];
+      n2 = N[(x + 1) * C0 + y];
+      n3 = N[x * C0 + y + 1];
+      n4 = N[x * C0 + y];
+    }
     const float *src = hist + (x + 1) * b0 + (y + 1);
     float out[32];
     float t1 = 0, t2 = 0, t3 = 0, t4 = 0;
@@ -406,10 +424,17 @@ __global__ void k_hog_feat(const HogJob *__restrict__ jobs, float *__restrict__ 
       float h4 = d < 0.2f ? d : 0.2f;
       out[18 + o] = 0.5f * (h1 + h2 + h3 + h4);
     }
-    out[27] = (float)(0.2357 * (double)t1);
-    out[28] = (float)(0.2357 * (double)t2);
-    out[29] = (float)(0.2357 * (double)t3);
-    out[30] = (float)(0.2357 * (double)t4);
+    if (J.fast) {
+      out[27] = 0.2357f * t1;
+      out[28] = 0.2357f * t2;
+      out[29] = 0.2357f * t3;
+      out[30] = 0.2357f * t4;
+    } else {   // the reference's double product, rounded once
+      out[27] = (float)(0.2357 * (double)t1);
+      out[28] = (float)(0.2357 * (double)t2);
+      out[29] = (float)(0.2357 * (double)t3);
+      out[30] = (float)(0.2357 * (double)t4);
+    }
     out[31] = 0.f;
     float4 *dst = reinterpret_cast<float4 *>(feat + (size_t)i * kFeatPad);
 #pragma unroll
@@ -424,18 +449,24 @@ __global__ void k_hog_feat(const HogJob *__restrict__ jobs, float *__restrict__ 
   }
 }
 
-void launch_hog(const HogJob *d_jobs, int n_jobs, int max_b0, int max_b1, const HogPixJob *d_pix, int n_pix,
-                int max_xe, float *arena, void *arena16, cudaStream_t s) {
+void hog_vote_blocks(const std::vector<HogJob> &jobs, std::vector<int2> &blocks) {
+  blocks.clear();
+  for (size_t j = 0; j < jobs.size(); j++)
+    for (int b = 0; b * kVoteThreads < jobs[j].b0 * jobs[j].b1; b++) blocks.push_back(make_int2((int)j, b));
+}
+
+void launch_hog(const HogJob *d_jobs, int n_jobs, const int2 *d_vote_blocks, int n_vote_blocks, int max_b0,
+                int max_b1, const HogPixJob *d_pix, int n_pix, int max_xe, float *arena, void *arena16,
+                bool corners, cudaStream_t s) {
   if (n_jobs <= 0) return;
   dim3 g0((max_xe + kPixWarps - 1) / kPixWarps, n_pix);
   k_hog_pix<<<g0, kPixWarps * 32, 0, s>>>(d_pix, arena);
+  k_hog_vote<<<n_vote_blocks, kVoteThreads, 0, s>>>(d_jobs, d_vote_blocks, arena);
   const int max_cells = max_b0 * max_b1;
-  dim3 g1((max_cells + kVoteThreads - 1) / kVoteThreads, n_jobs);
-  k_hog_vote<<<g1, kVoteThreads, 0, s>>>(d_jobs, arena);
   int bx = (max_cells + 255) / 256;
   if (bx > 512) bx = 512;
   dim3 g2(bx, n_jobs);
-  k_hog_norm<<<g2, 256, 0, s>>>(d_jobs, arena);
+  if (corners) k_hog_norm<<<g2, 256, 0, s>>>(d_jobs, arena);
   k_hog_feat<<<g2, 256, 0, s>>>(d_jobs, arena, reinterpret_cast<uint8_t *>(arena16));
 }
 

@@ -538,6 +538,7 @@ static geye_status build_pyramid_plan(geye_ctx *ctx, Plan &P, int width, int hei
       J.hist_off = L.hist_off; J.fs0 = L.fs0; J.fs1 = L.fs1; J.feat_off = L.feat_off; J.feat16_off = L.feat16_off;
       J.feat16lo_off = L.feat16lo_off;
       J.tc_planes = tc_planes;
+      J.fast = tc_planes ? 1 : 0;
       J.corner_off = A.take((size_t)(L.fs0 + 1) * (L.fs1 + 1));
       J.mag_off = L.img_level;   // resolved below, once the image's pixel buffer is placed
       P.hog_jobs.push_back(J);
@@ -585,6 +586,12 @@ static geye_status build_pyramid_plan(geye_ctx *ctx, Plan &P, int width, int hei
     GEYE_TRY(upload(ctx, P.d_hjobs[i], P.hjobs[i]));
   }
   GEYE_TRY(upload(ctx, P.d_hog_jobs, P.hog_jobs));
+  {
+    std::vector<int2> vb;
+    hog_vote_blocks(P.hog_jobs, vb);
+    P.hog_vote_nblocks = (int)vb.size();
+    GEYE_TRY(upload(ctx, P.d_hog_vote_blocks, vb));
+  }
   GEYE_TRY(upload(ctx, P.d_pix_jobs, P.pix_jobs));
   return GEYE_OK;
 }
@@ -855,9 +862,10 @@ geye_status run_pyramid(geye_ctx *ctx, Plan &P, const uint8_t *d_bgr, int width_
 }
 
 geye_status run_hog(geye_ctx *ctx, Plan &P) {
-  launch_hog(P.d_hog_jobs.as<HogJob>(), (int)P.hog_jobs.size(), P.hog_max_b0, P.hog_max_b1,
-             P.d_pix_jobs.as<HogPixJob>(), (int)P.pix_jobs.size(), P.pix_max_xe, P.arena.as<float>(), P.arena16.p,
-             ctx->stream);
+  const bool fast = !P.hog_jobs.empty() && P.hog_jobs[0].fast;
+  launch_hog(P.d_hog_jobs.as<HogJob>(), (int)P.hog_jobs.size(), P.d_hog_vote_blocks.as<int2>(), P.hog_vote_nblocks,
+             P.hog_max_b0, P.hog_max_b1, P.d_pix_jobs.as<HogPixJob>(), (int)P.pix_jobs.size(), P.pix_max_xe,
+             P.arena.as<float>(), P.arena16.p, !fast, ctx->stream);
   ctx->launches += 3;   // pixels, votes, corner norms, features
   return check_launch(ctx, "hog");
 }

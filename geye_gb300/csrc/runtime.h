@@ -163,6 +163,8 @@ struct Plan {
   DevBuf d_tap_start, d_tap_si, d_tap_alpha;
   std::vector<HogJob> hog_jobs;
   DevBuf d_hog_jobs;
+  DevBuf d_hog_vote_blocks;             // vote kernel blocks of every level (hog_vote_blocks)
+  int hog_vote_nblocks = 0;
   int hog_max_b0 = 0, hog_max_b1 = 0;
   std::vector<HogPixJob> pix_jobs;   // one per image
   DevBuf d_pix_jobs;

@@ -176,13 +176,17 @@ geye_status geye_calc_feature(geye_ctx *ctx, const float *src, const int *isize,
   CUDA_TRY(cudaMemcpyAsync(arena, src, sizeof(float) * n_img, cudaMemcpyHostToDevice, ctx->stream));
   HogJob J{};
   J.img_off = 0; J.h = h; J.w = w; J.sbin = sbin; J.b0 = b0; J.b1 = b1; J.hist_off = (int)hist;
-  J.fs0 = fs0; J.fs1 = fs1; J.feat_off = (int)feat_off; J.feat16_off = -1; J.feat16lo_off = -1;
+  J.fs0 = fs0; J.fs1 = fs1; J.feat_off = (int)feat_off; J.feat16_off = -1; J.feat16lo_off = -1; J.fast = 0;
   J.mag_off = X.mag_off; J.bin_off = X.bin_off; J.pix_Y = X.Y; J.corner_off = (int)corner_off;
   HogJob *d_j;
   GEYE_TRY(S.put(&J, 1, &d_j));
   HogPixJob *d_x;
   GEYE_TRY(S.put(&X, 1, &d_x));
-  launch_hog(d_j, 1, b0, b1, d_x, 1, X.xe, arena, nullptr, ctx->stream);
+  std::vector<int2> vb;
+  hog_vote_blocks(std::vector<HogJob>{J}, vb);
+  int2 *d_vb;
+  GEYE_TRY(S.put(vb.data(), vb.size(), &d_vb));
+  launch_hog(d_j, 1, d_vb, (int)vb.size(), b0, b1, d_x, 1, X.xe, arena, nullptr, true, ctx->stream);
   launch_to_ref_layout(arena + feat_off, fs0, fs1, out, ctx->stream);
   CUDA_TRY(cudaGetLastError());
   CUDA_TRY(cudaMemcpyAsync(feat, out, sizeof(float) * (size_t)fs0 * fs1 * kFeat, cudaMemcpyDeviceToHost, ctx->stream));
