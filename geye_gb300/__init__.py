@@ -6,4 +6,5 @@ C++ host runtime under geye_gb300/csrc).  This package builds it
 seeded synthetic frames and models (geye_gb300.synth).
 """
 from . import build, synth  # noqa: F401
-from .dpm import CONV_BF16, CONV_FP8, CONV_FP32, Batch, Context, GeyeError, Model, Server, lib  # noqa: F401
+from .dpm import (CONV_BF16, CONV_FP8, CONV_FP32, NMS_ORDER_KEY, NMS_ORDER_QUICKSORT, Batch, Context,  # noqa: F401
+                  GeyeError, Model, Server, lib)

@@ -71,10 +71,12 @@ geye_status geye_ctx_create(int device, void *cuda_stream, geye_ctx **out) {
   }
   {
     cudaError_t e = cudaStreamCreateWithFlags(&ctx->side, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->aux, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming);
     if (e != cudaSuccess) {
       if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
+      if (ctx->aux) cudaStreamDestroy(ctx->aux);
       if (ctx->side) cudaStreamDestroy(ctx->side);
       if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
       delete ctx;
@@ -115,6 +117,7 @@ geye_status geye_ctx_destroy(geye_ctx *ctx) {
     cudaStreamSynchronize(ctx->side);
     cudaStreamDestroy(ctx->side);
   }
+  if (ctx->aux) cudaStreamDestroy(ctx->aux);
   if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
   return GEYE_OK;
@@ -124,6 +127,13 @@ geye_status geye_ctx_set_conv_mode(geye_ctx *ctx, geye_conv_mode mode) {
   ARG_CHECK(ctx, "ctx is null");
   ARG_CHECK(mode == GEYE_CONV_FP32 || mode == GEYE_CONV_BF16 || mode == GEYE_CONV_FP8, "unknown conv mode");
   ctx->conv_mode = mode;
+  return GEYE_OK;
+}
+
+geye_status geye_ctx_set_nms_order(geye_ctx *ctx, int order) {
+  ARG_CHECK(ctx, "ctx is null");
+  ARG_CHECK(order == GEYE_NMS_ORDER_KEY || order == GEYE_NMS_ORDER_QUICKSORT, "unknown NMS order");
+  ctx->nms_order = order == GEYE_NMS_ORDER_KEY ? kNmsOrderKey : kNmsOrderQuicksort;
   return GEYE_OK;
 }
 

@@ -262,21 +262,32 @@ void launch_nms(const float *boxes, const int *d_num, int n_models, int GL, floa
 constexpr int kNmsBatch = 256;     // boxes resolved per round
 constexpr int kNmsSegS = 16384;    // sort segments finished in shared memory (one block, ~203 KB)
 constexpr int kNmsTile = 4096;     // elements per block in the sort's grid-wide partitions
+constexpr int kRsT = 2048;         // elements per block in the key-order radix sort
 __host__ __device__ inline int nms_big_cap(int cap) { return cap / kNmsSegS + 2; }
 __host__ __device__ inline int nms_tile_cap(int cap) { return cap / kNmsTile + nms_big_cap(cap) + 1; }
+__host__ __device__ inline int nms_rs_tiles(int cap) { return (cap + kRsT - 1) / kRsT; }
 __host__ __device__ inline size_t nms_model_words(int cap) {
-  const size_t w = 8 * (size_t)cap + 64 + 5 * kNmsBatch + 4 * (size_t)nms_big_cap(cap) + 2 * (size_t)nms_tile_cap(cap);
+  const size_t w = 8 * (size_t)cap + 64 + 5 * kNmsBatch + 4 * (size_t)nms_big_cap(cap) +
+                   2 * (size_t)nms_tile_cap(cap) + 256 * (size_t)nms_rs_tiles(cap);
   return (w + 31) & ~(size_t)31;
 }
-// diag (optional): per model m, diag[8m+1..8m+4] = sort segments left to the fallback, batches, picks,
-// whether the finish kernel ran rounds itself
+// diag (optional): per model m, diag[8m+1..8m+5] = sort segments left to the fallback, batches, picks,
+// whether the finish kernel ran rounds itself, whether the quicksort order was needed
 // levels, lv_used: as for launch_nms_sort (nms_common.h); rounds: resolve/pass
 // rounds launched before the finish kernel (<= 0: kNmsRounds), *rounds_used
 // (optional) gets the batches the frame took, the finish kernel's included
-constexpr int kNmsRounds = 8;
-void launch_nms_batch(const float *boxes, const int *d_num, int n_models, int GL, float overlap, int cap, int *si,
-                      float *sf, float *out, int *d_kept, int *err, long long *diag, int levels, int *lv_used,
-                      int rounds, int *rounds_used, cudaStream_t s);
+// need: n_models ints, zero on entry; order: kNmsOrderKey (the scores in
+// key order, the quicksort's order only for the models that need it: need[m]
+// raised) or kNmsOrderQuicksort (the quicksort's order for every model)
+constexpr int kNmsRounds = 8, kNmsMaxRounds = 64;
+constexpr int kNmsOrderKey = 0, kNmsOrderQuicksort = 1;
+// aux: null for plain launches on s; when s is capturing a graph, a second
+// stream that captures the bodies of the conditional nodes (the greedy rounds
+// as a while node, the quicksort-order pass as an if node)
+cudaError_t launch_nms_batch(const float *boxes, const int *d_num, int n_models, int GL, float overlap, int cap,
+                             int *si, float *sf, float *out, int *d_kept, int *err, long long *diag, int levels,
+                             int *lv_used, int rounds, int *rounds_used, int *need, int order, cudaStream_t s,
+                             cudaStream_t aux);
 int nms_sort_levels(int cap);   // the default number of grid-wide sort levels for cap boxes
 void launch_new_rects(const float *kept, const int *d_kept, int GL, int np, const float *coef, int img_w,
                       int img_h, float ratio, int *point, int *or_point, int *type, float *scale, float *score,

@@ -57,7 +57,8 @@ __global__ void __launch_bounds__(kPassNT) k_nms_gather(const float *__restrict_
 // 3a. resolve the next batch (whole block)
 // ---------------------------------------------------------------------------
 struct ResolveSmem {
-  int mem_pos[kBatch];
+  int mem_pos[kBatch + 1];
+  int run_end[kBatch];   // key order: last member with the same score
   float my[5][kBatch];
   unsigned rows[kBatch][kBW];
   int pick_mem[kBatch];
@@ -66,10 +67,21 @@ struct ResolveSmem {
   int nb, np, last_word, done;
 };
 
+__device__ __forceinline__ unsigned sorted_key(const Slots &S, int pos) {
+  return reinterpret_cast<const unsigned *>(S.val)[pos];
+}
+
 // Returns with R.np picks in R.pick_mem, the batch's picks appended to S.picks
 // and written to S.bp, the members cleared from the bitmap and the state
 // advanced; R.done set when no alive box was left.
-__device__ void resolve_batch(Slots &S, float overlap, ResolveSmem &R) {
+// KEY_ORDER (positions in nms_radix.cu's order): a run of equal scores never
+// straddles two batches (the batch ends before a run that the next alive box
+// continues), and *need is raised where the order inside a run could matter:
+// a pick that suppresses an alive member of its own run, or a run longer than
+// a batch.
+template <bool KEY_ORDER>
+__device__ void resolve_batch(Slots &S, float overlap, ResolveSmem &R, int *need) {
+  constexpr int want = kBatch + (KEY_ORDER ? 1 : 0);   // key order: one more, to see the run at the boundary
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   BatchState &st = *S.st;
   const int nwords = st.nwords;
@@ -78,7 +90,7 @@ __device__ void resolve_batch(Slots &S, float overlap, ResolveSmem &R) {
   // members: the first kBatch alive sorted positions from scan_word on
   for (int base = st.scan_word; base < nwords; base += kSortNT) {
     const int have = R.nb;   // uniform: written before the last barrier
-    if (have >= kBatch) break;
+    if (have >= want) break;
     const int w = base + threadIdx.x;
     const unsigned word = w < nwords ? S.bits[w] : 0u;
     const int c = __popc(word);
@@ -98,7 +110,7 @@ __device__ void resolve_batch(Slots &S, float overlap, ResolveSmem &R) {
     }
     int rank = have + before;
     unsigned rem = word;
-    while (rem && rank < kBatch) {
+    while (rem && rank < want) {
       const int b = __ffs(rem) - 1;
       rem &= rem - 1;
       R.mem_pos[rank] = (w << 5) + b;
@@ -107,9 +119,23 @@ __device__ void resolve_batch(Slots &S, float overlap, ResolveSmem &R) {
     }
     __syncthreads();   // everyone has read wtot and R.nb
     if (threadIdx.x == 0) {
-      const int nb = min(kBatch, have + tot);
-      if (have + tot <= kBatch) R.last_word = min(base + kSortNT, nwords);   // took every alive box up to here
+      const int nb = min(want, have + tot);
+      if (have + tot <= want) R.last_word = min(base + kSortNT, nwords);   // took every alive box up to here
       R.nb = nb;
+    }
+    __syncthreads();
+  }
+  if (KEY_ORDER) {
+    if (threadIdx.x == 0 && R.nb == want) {   // an alive box follows the batch
+      const unsigned kb = sorted_key(S, R.mem_pos[kBatch]);
+      int nb = kBatch;
+      while (nb > 0 && sorted_key(S, R.mem_pos[nb - 1]) == kb) nb--;
+      if (nb == 0) {   // a run longer than a batch
+        *need = 1;
+        nb = kBatch;
+      }
+      R.nb = nb;
+      R.last_word = R.mem_pos[nb - 1] >> 5;
     }
     __syncthreads();
   }
@@ -122,6 +148,12 @@ __device__ void resolve_batch(Slots &S, float overlap, ResolveSmem &R) {
     R.my[2][threadIdx.x] = S.y2[r];
     R.my[3][threadIdx.x] = S.x2[r];
     R.my[4][threadIdx.x] = S.ar[r];
+    if (KEY_ORDER) {
+      const unsigned k = sorted_key(S, r);
+      int e = threadIdx.x;
+      while (e + 1 < nb && sorted_key(S, R.mem_pos[e + 1]) == k) e++;
+      R.run_end[threadIdx.x] = e;
+    }
   }
   __syncthreads();
   // suppression rows: bit j of row i = member i (kept) suppresses member j > i
@@ -155,6 +187,15 @@ __device__ void resolve_batch(Slots &S, float overlap, ResolveSmem &R) {
       if (lane == fl) alive &= ~(1u << (i & 31));
       const unsigned row = lane < nwm ? R.rows[i][lane] : 0u;
       const bool any = __ballot_sync(0xffffffffu, (alive & row) != 0u) != 0u;
+      if (KEY_ORDER) {
+        const int e = R.run_end[i];
+        if (e > i) {   // does the pick suppress an alive member of its own run (i, e]?
+          const int lo = max(i + 1, 32 * lane), hi = min(e, 32 * lane + 31);
+          unsigned span = 0u;
+          if (lo <= hi) span = (hi - lo == 31 ? ~0u : ((1u << (hi - lo + 1)) - 1u)) << (lo - 32 * lane);
+          if (__any_sync(0xffffffffu, (alive & row & span) != 0u) && lane == 0) *need = 1;
+        }
+      }
       alive &= ~row;
       if (lane == 0) {
         R.pick_mem[np] = i;
@@ -190,11 +231,12 @@ __device__ void resolve_batch(Slots &S, float overlap, ResolveSmem &R) {
   __syncthreads();
 }
 
-__global__ void __launch_bounds__(kSortNT) k_nms_resolve(int cap, int *si, float *sf, float overlap) {
+template <bool KEY_ORDER>
+__global__ void __launch_bounds__(kSortNT) k_nms_resolve(int cap, int *si, float *sf, float overlap, int *need) {
   __shared__ ResolveSmem R;
   Slots S = slots(si, sf, blockIdx.x, cap);
   if (S.st->done) return;
-  resolve_batch(S, overlap, R);
+  resolve_batch<KEY_ORDER>(S, overlap, R, need ? need + blockIdx.x : nullptr);
 }
 
 // ---------------------------------------------------------------------------
@@ -251,8 +293,21 @@ __device__ void pass_words(Slots &S, const float (*pk)[kBatch], int np, int pick
   }
 }
 
-__global__ void __launch_bounds__(kPassNT) k_nms_pass(int cap, int *si, float *sf, float overlap) {
+// loop: inside a frame graph's while node, block (0, 0) sets the node's
+// condition for the next round: a model is not done and has taken fewer than
+// max_batches batches (the finish kernel takes any rest)
+__global__ void __launch_bounds__(kPassNT) k_nms_pass(int cap, int *si, float *sf, float overlap,
+                                                      cudaGraphConditionalHandle loop, int use_loop,
+                                                      int max_batches) {
   __shared__ float pk[5][kBatch];
+  if (use_loop && blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) {
+    unsigned more = 0;
+    for (int m = 0; m < (int)gridDim.y; m++) {
+      const BatchState &b = *slots(si, sf, m, cap).st;
+      more |= (!b.done && b.batches < max_batches) ? 1u : 0u;
+    }
+    cudaGraphSetConditional(loop, more);
+  }
   Slots S = slots(si, sf, blockIdx.y, cap);
   if (S.st->done) return;
   const int np = S.st->npb;
@@ -267,13 +322,20 @@ __global__ void __launch_bounds__(kPassNT) k_nms_pass(int cap, int *si, float *s
 // ---------------------------------------------------------------------------
 // 4. remaining rounds, final-pick rule, kept records in input order
 // ---------------------------------------------------------------------------
+// KEY_ORDER: the key-order pass (writes every model's result; raises need[m]
+// where the quicksort order could differ).  Otherwise the quicksort-order pass:
+// with need given, only the models that raised it (their result replaces the
+// key-order one); without, every model.
+template <bool KEY_ORDER>
 __global__ void __launch_bounds__(kSortNT) k_nms_finish(const float *__restrict__ boxes_all, int GL, int cap,
                                                         int *si, float *sf, float overlap, float *out_all,
-                                                        int *d_kept, int *err, long long *diag, int *rounds_used) {
+                                                        int *d_kept, int *err, long long *diag, int *rounds_used,
+                                                        int *need) {
   __shared__ ResolveSmem R;
   __shared__ float pk[5][kBatch];
   __shared__ int wcnt[kSortNT / 32];
   const int m = blockIdx.x;
+  if (!KEY_ORDER && need && !need[m]) return;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   Slots S = slots(si, sf, m, cap);
   BatchState &st = *S.st;
@@ -287,7 +349,7 @@ __global__ void __launch_bounds__(kSortNT) k_nms_finish(const float *__restrict_
         if (threadIdx.x == 0) atomicOr(err, 2);
         break;
       }
-      resolve_batch(S, overlap, R);
+      resolve_batch<KEY_ORDER>(S, overlap, R, need ? need + m : nullptr);
       if (R.done) break;
       const int np = R.np;
       for (int k = threadIdx.x; k < np; k += kSortNT)
@@ -298,6 +360,9 @@ __global__ void __launch_bounds__(kSortNT) k_nms_finish(const float *__restrict_
     }
   }
   const int npk = st.npicks;
+  // the last pick shares its score with another pick: which of them is last is the quicksort's call
+  if (KEY_ORDER && threadIdx.x == 0 && npk >= 2 && sorted_key(S, S.picks[npk - 1]) == sorted_key(S, S.picks[npk - 2]))
+    need[m] = 1;
   const int K = npk - ((npk > 0 && S.flag[npk - 1] == 0) ? 1 : 0);
   int written = 0;
   if (K <= kRankSortMax) {
@@ -349,24 +414,126 @@ __global__ void __launch_bounds__(kSortNT) k_nms_finish(const float *__restrict_
       diag[8 * m + 2] = st.batches;
       diag[8 * m + 3] = npk;
       diag[8 * m + 4] = st.fallback;
+      diag[8 * m + 5] = need ? need[m] : 1;
     }
   }
 }
 
-void launch_nms_batch(const float *boxes, const int *d_num, int n_models, int GL, float overlap, int cap, int *si,
-                      float *sf, float *out, int *d_kept, int *err, long long *diag, int levels, int *lv_used,
-                      int rounds, int *rounds_used, cudaStream_t s) {
-  if (n_models <= 0) return;
-  launch_nms_sort(boxes, d_num, n_models, GL, cap, si, sf, err, diag, levels, lv_used, s);
+// sets an if node's condition: some model raised need
+__global__ void k_nms_need(cudaGraphConditionalHandle h, const int *need, int n_models) {
+  unsigned any = 0;
+  for (int m = 0; m < n_models; m++) any |= need[m] ? 1u : 0u;
+  cudaGraphSetConditional(h, any);
+}
+
+// Inside a stream capture: a handle for a conditional node of the graph s is
+// capturing (its condition reset to init at every launch of the graph)
+static cudaError_t cond_handle(cudaStream_t s, unsigned init, cudaGraphConditionalHandle *h) {
+  cudaStreamCaptureStatus cs;
+  cudaGraph_t g = nullptr;
+  cudaError_t e = cudaStreamGetCaptureInfo(s, &cs, nullptr, &g, nullptr, nullptr, nullptr);
+  if (e != cudaSuccess) return e;
+  if (cs != cudaStreamCaptureStatusActive) return cudaErrorStreamCaptureUnsupported;
+  return cudaGraphConditionalHandleCreate(h, g, init, cudaGraphCondAssignDefault);
+}
+
+// the conditional node on s's current dependencies, which become the node;
+// aux then captures its body (the capture is begun here, end_conditional ends it)
+static cudaError_t begin_conditional(cudaStream_t s, cudaStream_t aux, cudaGraphConditionalNodeType type,
+                                     cudaGraphConditionalHandle h) {
+  cudaStreamCaptureStatus cs;
+  cudaGraph_t g = nullptr;
+  const cudaGraphNode_t *deps = nullptr;
+  const cudaGraphEdgeData *ed = nullptr;
+  size_t nd = 0;
+  cudaError_t e = cudaStreamGetCaptureInfo(s, &cs, nullptr, &g, &deps, &ed, &nd);
+  if (e != cudaSuccess) return e;
+  cudaGraphNodeParams p = {};
+  p.type = cudaGraphNodeTypeConditional;
+  p.conditional.handle = h;
+  p.conditional.type = type;
+  p.conditional.size = 1;
+  cudaGraphNode_t node;
+  if ((e = cudaGraphAddNode(&node, g, deps, ed, nd, &p)) != cudaSuccess) return e;
+  if ((e = cudaStreamUpdateCaptureDependencies(s, &node, nullptr, 1, cudaStreamSetCaptureDependencies)) != cudaSuccess)
+    return e;
+  return cudaStreamBeginCaptureToGraph(aux, p.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                       cudaStreamCaptureModeRelaxed);
+}
+
+static cudaError_t end_conditional(cudaStream_t aux) {
+  cudaGraph_t body = nullptr;
+  cudaError_t e = cudaStreamEndCapture(aux, &body);
+  if (e != cudaSuccess) return e;
+  return cudaGetLastError();   // a launch inside the body
+}
+
+constexpr int kNmsLoopBatches = 512;   // while-node rounds before the finish kernel takes the rest
+
+// gather, the greedy rounds and the finish, in the order the sort left in (val, ord).
+// aux non-null: s is capturing a graph, and the rounds are a while node (as many
+// as the frame needs) instead of `rounds` launches
+template <bool KEY_ORDER>
+static cudaError_t launch_greedy(const float *boxes, int n_models, int GL, float overlap, int cap, int *si, float *sf,
+                                 float *out, int *d_kept, int *err, long long *diag, int rounds, int *rounds_used,
+                                 int *need, cudaStream_t s, cudaStream_t aux) {
   k_nms_gather<<<dim3((cap + kPassNT - 1) / kPassNT, n_models), kPassNT, 0, s>>>(boxes, GL, cap, si, sf);
   const int words = (cap + 31) / 32;
   const int pass_blocks = std::max(1, std::min((words + kPassNT / 32 - 1) / (kPassNT / 32), 512));
-  if (rounds <= 0) rounds = kNmsRounds;
-  for (int r = 0; r < rounds; r++) {
-    k_nms_resolve<<<n_models, kSortNT, 0, s>>>(cap, si, sf, overlap);
-    k_nms_pass<<<dim3(pass_blocks, n_models), kPassNT, 0, s>>>(cap, si, sf, overlap);
+  if (aux) {
+    cudaGraphConditionalHandle loop;
+    cudaError_t e = cond_handle(s, 1u, &loop);
+    if (e == cudaSuccess) e = begin_conditional(s, aux, cudaGraphCondTypeWhile, loop);
+    if (e != cudaSuccess) return e;
+    k_nms_resolve<KEY_ORDER><<<n_models, kSortNT, 0, aux>>>(cap, si, sf, overlap, need);
+    k_nms_pass<<<dim3(pass_blocks, n_models), kPassNT, 0, aux>>>(cap, si, sf, overlap, loop, 1, kNmsLoopBatches);
+    if ((e = end_conditional(aux)) != cudaSuccess) return e;
+  } else {
+    for (int r = 0; r < rounds; r++) {
+      k_nms_resolve<KEY_ORDER><<<n_models, kSortNT, 0, s>>>(cap, si, sf, overlap, need);
+      k_nms_pass<<<dim3(pass_blocks, n_models), kPassNT, 0, s>>>(cap, si, sf, overlap, 0, 0, 0);
+    }
   }
-  k_nms_finish<<<n_models, kSortNT, 0, s>>>(boxes, GL, cap, si, sf, overlap, out, d_kept, err, diag, rounds_used);
+  k_nms_finish<KEY_ORDER><<<n_models, kSortNT, 0, s>>>(boxes, GL, cap, si, sf, overlap, out, d_kept, err, diag,
+                                                       rounds_used, need);
+  return cudaSuccess;
+}
+
+cudaError_t launch_nms_batch(const float *boxes, const int *d_num, int n_models, int GL, float overlap, int cap,
+                             int *si, float *sf, float *out, int *d_kept, int *err, long long *diag, int levels,
+                             int *lv_used, int rounds, int *rounds_used, int *need, int order, cudaStream_t s,
+                             cudaStream_t aux) {
+  if (n_models <= 0) return cudaSuccess;
+  if (rounds <= 0) rounds = kNmsRounds;
+  cudaError_t e;
+  if (order == kNmsOrderQuicksort) {
+    launch_nms_sort(boxes, d_num, n_models, GL, cap, si, sf, err, diag, levels, lv_used, nullptr, s);
+    return launch_greedy<false>(boxes, n_models, GL, overlap, cap, si, sf, out, d_kept, err, diag, rounds,
+                                rounds_used, nullptr, s, aux);
+  }
+  launch_nms_radix(boxes, d_num, n_models, GL, cap, si, sf, need, s);
+  e = launch_greedy<true>(boxes, n_models, GL, overlap, cap, si, sf, out, d_kept, err, diag, rounds, rounds_used,
+                          need, s, aux);
+  if (e != cudaSuccess) return e;
+  // the models whose kept set could depend on the order inside a run of equal
+  // scores, again in the quicksort's order: in a graph, an if node that runs
+  // only when some model needs it; otherwise launches that do nothing for the others
+  cudaStream_t q = s;
+  if (aux) {
+    cudaGraphConditionalHandle h;
+    if ((e = cond_handle(s, 0u, &h)) != cudaSuccess) return e;
+    k_nms_need<<<1, 1, 0, s>>>(h, need, n_models);
+    if ((e = begin_conditional(s, aux, cudaGraphCondTypeIf, h)) != cudaSuccess) return e;
+    q = aux;
+  }
+  launch_nms_sort(boxes, d_num, n_models, GL, cap, si, sf, err, diag, levels, lv_used, need, q);
+  e = launch_greedy<false>(boxes, n_models, GL, overlap, cap, si, sf, out, d_kept, err, diag, rounds, rounds_used,
+                           need, q, nullptr);
+  if (aux) {
+    const cudaError_t e2 = end_conditional(aux);
+    if (e == cudaSuccess) e = e2;
+  }
+  return e;
 }
 
 }  // namespace geye

@@ -36,6 +36,7 @@ struct Slots {
   float *bp;         // current round's picks: y1, x1, y2, x2, area (kNmsBatch each)
   int2 *big[2];      // nms_big_cap(cap) segments each
   int2 *tiles;       // nms_tile_cap(cap) per-tile (<= key, >= key) counts
+  int *hist;         // 256 * nms_rs_tiles(cap) radix-sort digit counts (nms_radix.cu)
   float *y1, *x1, *y2, *x2, *ar;   // boxes in sorted order
 };
 
@@ -60,6 +61,7 @@ __device__ __forceinline__ Slots slots(int *si, float *sf, int m, int cap) {
   S.big[0] = reinterpret_cast<int2 *>(l);
   S.big[1] = reinterpret_cast<int2 *>(l + 2 * bc);
   S.tiles = reinterpret_cast<int2 *>(l + 4 * bc);
+  S.hist = l + 4 * bc + 2 * nms_tile_cap(cap);
   S.y1 = f;
   S.x1 = f + cap;
   S.y2 = f + 2 * (size_t)cap;
@@ -262,8 +264,14 @@ __device__ __forceinline__ bool supp(float Ay1, float Ax1, float Ay2, float Ax2,
 // sort stage (nms_sort.cu): leaves val/ord sorted for every model and the
 // BatchState initialised; diag[8m + 1] gets the segments left to k_qs_rest.
 // levels: grid-wide partition levels to launch (<= 0: nms_sort_levels(cap));
-// *lv_used (optional) gets the deepest level that had a segment to partition
+// *lv_used (optional) gets the deepest level that had a segment to partition.
+// need (optional): only the models with need[m] set are sorted; the others
+// are left with an empty, finished state
 void launch_nms_sort(const float *boxes, const int *d_num, int n_models, int GL, int cap, int *si, float *sf,
-                     int *err, long long *diag, int levels, int *lv_used, cudaStream_t s);
+                     int *err, long long *diag, int levels, int *lv_used, const int *need, cudaStream_t s);
+// key-order sort (nms_radix.cu): val = transformed keys, ord = input index,
+// BatchState initialised; need[m] set for a NaN score
+void launch_nms_radix(const float *boxes, const int *d_num, int n_models, int GL, int cap, int *si, float *sf,
+                      int *need, cudaStream_t s);
 
 }  // namespace geye

@@ -36,11 +36,12 @@ constexpr int kQ = 1024;         // k_qs_rest's block-tier queue
 // load
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256) k_qs_load(const float *__restrict__ boxes_all, const int *__restrict__ d_num,
-                                                 int GL, int cap, int *si, float *sf) {
+                                                 int GL, int cap, int *si, float *sf, const int *need) {
   const int m = blockIdx.y;
   Slots S = slots(si, sf, m, cap);
   const float *boxes = boxes_all + (size_t)m * cap * GL;
-  const int D = max(0, min(d_num[m], cap));
+  // a model that does not need the quicksort order: nothing to sort or resolve
+  const int D = (need && !need[m]) ? 0 : max(0, min(d_num[m], cap));
   const int i = blockIdx.x * 256 + threadIdx.x;
   if (i < D) {
     S.val[i] = boxes[(size_t)i * GL + GL - 2];
@@ -500,9 +501,9 @@ int nms_sort_levels(int cap) {
 }
 
 void launch_nms_sort(const float *boxes, const int *d_num, int n_models, int GL, int cap, int *si, float *sf,
-                     int *err, long long *diag, int levels, int *lv_used, cudaStream_t s) {
+                     int *err, long long *diag, int levels, int *lv_used, const int *need, cudaStream_t s) {
   if (levels <= 0) levels = nms_sort_levels(cap);
-  k_qs_load<<<dim3((cap + 255) / 256, n_models), 256, 0, s>>>(boxes, d_num, GL, cap, si, sf);
+  k_qs_load<<<dim3((cap + 255) / 256, n_models), 256, 0, s>>>(boxes, d_num, GL, cap, si, sf, need);
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);

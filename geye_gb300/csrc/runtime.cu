@@ -948,27 +948,36 @@ geye_status run_ascore(geye_ctx *ctx, Plan &P, ModelPlan &mp, int mi, float thre
   return ascore_compute(ctx, P, mp, mi, thresh, ctx->stream);
 }
 
-// After a frame of the plan has completed: `used` is the deepest grid-wide sort
-// level that had a segment to partition, `rounds` the greedy batches the frame
-// took.  The first frame launches the default counts (nms_sort_levels,
-// kNmsRounds); if it needed fewer, the plan launches three levels and one
-// round more than it needed from then on (each empty level costs three
-// launches on the frame's path, each empty round two).  A frame whose last
-// launched level still had work left its remaining segments to the
-// single-block sort fallback, and one that took more batches than the rounds
-// launched ran them in the finish kernel (both exact, slower): the plan goes
-// back to the default counts for good.  A change drops the plan's frame
-// graphs after its stream has drained; the next frame captures them again.
+// After a frame of the plan has completed: `used` is the deepest grid-wide
+// quicksort level that had a segment to partition (0 when no model needed the
+// quicksort's order), `rounds` the greedy batches the frame took.
+// Sort levels: the first frame that sorts launches the default count
+// (nms_sort_levels); if it needed fewer, the plan launches three levels more
+// than it needed from then on (each empty level costs three launches).  A
+// frame whose last launched level still had work left its remaining segments
+// to the single-block fallback (exact, slower): the plan goes back to the
+// default count for good.
+// Rounds: the first frame launches kNmsRounds; one that needed fewer makes the
+// plan launch one more than it needed; one that took more batches than were
+// launched (the rest ran in the finish kernel's single block) makes it launch
+// two more than that frame took, and the count only grows from then on.
+// A change drops the plan's frame graphs after its stream has drained; the
+// next frame captures them again.
 void note_sort_levels(geye_ctx *ctx, Plan &P, int used, int rounds) {
   const int full = nms_sort_levels(P.max_cap);
   const int launched = P.sort_levels > 0 ? P.sort_levels : full;
   const int r_launched = P.nms_rounds > 0 ? P.nms_rounds : kNmsRounds;
   int next = P.sort_levels, r_next = P.nms_rounds;
-  if (used >= launched || rounds > r_launched) {
-    if (P.sort_levels > 0 || P.nms_rounds > 0) { next = 0; r_next = 0; P.sort_levels_fixed = true; }
-  } else if (!P.sort_levels_fixed && P.sort_levels == 0 && P.nms_rounds == 0) {
-    if (used + 3 < full) next = std::max(4, used + 3);
-    if (rounds + 1 < kNmsRounds) r_next = std::max(2, rounds + 1);
+  if (used >= launched) {
+    if (P.sort_levels > 0) { next = 0; P.sort_levels_fixed = true; }
+  } else if (!P.sort_levels_fixed && P.sort_levels == 0 && used > 0 && used + 3 < full) {
+    next = std::max(4, used + 3);
+  }
+  if (rounds > r_launched) {
+    r_next = std::min(kNmsMaxRounds, rounds + 2);
+    P.nms_rounds_fixed = true;
+  } else if (!P.nms_rounds_fixed && P.nms_rounds == 0 && rounds + 1 < kNmsRounds) {
+    r_next = std::max(2, rounds + 1);
   }
   if (next == P.sort_levels && r_next == P.nms_rounds) return;
   P.sort_levels = next;
@@ -983,10 +992,16 @@ geye_status run_nms(geye_ctx *ctx, Plan &P, int n_models, float overlap) {
   int *d_num = P.d_small.as<int>();
   int *d_kept = d_num + 32;
   int *err = d_num + 128;
-  launch_nms_batch(P.d_boxes.as<float>(), d_num, n_models, P.gl, overlap, P.max_cap, P.d_nms_i.as<int>(),
-                   P.d_nms_f.as<float>(), P.d_kept_boxes.as<float>(), d_kept, err,
-                   reinterpret_cast<long long *>(d_num + 512), P.sort_levels, d_num + kSortLevelsUsed, P.nms_rounds,
-                   d_num + kNmsRoundsUsed, ctx->stream);
+  const cudaError_t ge =
+      launch_nms_batch(P.d_boxes.as<float>(), d_num, n_models, P.gl, overlap, P.max_cap, P.d_nms_i.as<int>(),
+                       P.d_nms_f.as<float>(), P.d_kept_boxes.as<float>(), d_kept, err,
+                       reinterpret_cast<long long *>(d_num + 512), P.sort_levels, d_num + kSortLevelsUsed,
+                       P.nms_rounds, d_num + kNmsRoundsUsed, d_num + kNmsNeed, ctx->nms_order, ctx->stream,
+                       ctx->capturing ? ctx->aux : nullptr);
+  if (ge != cudaSuccess) {
+    set_error(std::string("nms graph nodes: ") + cudaGetErrorString(ge));
+    return GEYE_ERR_CUDA;
+  }
   GEYE_TRY(check_launch(ctx, "nms"));
   for (int mi = 0; mi < n_models; mi++) {
     ModelPlan &mp = *P.models[mi];
@@ -1061,7 +1076,7 @@ static geye_status run_body_graph(geye_ctx *ctx, Plan &P, float thresh, float ov
   unsigned tb, ob;
   memcpy(&tb, &thresh, 4);
   memcpy(&ob, &overlap, 4);
-  snprintf(key, sizeof key, "%08x:%08x:%d", tb, ob, ctx->timing ? 1 : 0);
+  snprintf(key, sizeof key, "%08x:%08x:%d:%d", tb, ob, ctx->timing ? 1 : 0, ctx->nms_order);
   Plan::FrameGraph &g = P.graphs[key];
   if (!g.exec) {
     const int before = ctx->launches;

@@ -59,6 +59,8 @@ geye_status run_conv_tc(geye_ctx *ctx, Plan &P);
 // d_small[kSortLevelsUsed]: the deepest NMS sort level with work in the frame;
 // d_small[kNmsRoundsUsed]: the greedy batches it took
 constexpr int kSortLevelsUsed = 48, kNmsRoundsUsed = 49;
+// d_small[kNmsNeed + m]: model m's kept set was resolved again in the quicksort's order
+constexpr int kNmsNeed = 160;
 void note_sort_levels(geye_ctx *ctx, Plan &P, int used, int rounds);
 // tensor-core fconvsMT of one feature map ([pos][32] float on the device) for the stage entry point
 geye_status conv_tc_maps(geye_ctx *ctx, const float *d_feat, int a0, int a1, const float *const *filters,
@@ -190,8 +192,8 @@ struct Plan {
   // grid-wide NMS sort levels launched per frame (0: the default for max_cap),
   // adapted once to the depth the plan's frames need (note_sort_levels)
   int sort_levels = 0;
-  int nms_rounds = 0;   // greedy resolve/pass rounds per frame (0: kNmsRounds), adapted with the levels
-  bool sort_levels_fixed = false;
+  int nms_rounds = 0;   // greedy resolve/pass rounds per frame (0: kNmsRounds), adapted to the frames
+  bool sort_levels_fixed = false, nms_rounds_fixed = false;
   // asynchronous submission (serve.cu): pinned frame staging, pinned result
   // block (counts, then per model kHostRes records) and the completion event
   void *h_bgr = nullptr, *h_res = nullptr;
@@ -214,6 +216,8 @@ struct geye_ctx {
   // A_SCORE runs beside NMS on this stream (forked after the score stage,
   // joined before the frame ends)
   cudaStream_t side = nullptr;
+  // captures the bodies of the frame graph's conditional nodes (NMS rounds, quicksort pass)
+  cudaStream_t aux = nullptr;
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   geye_conv_mode conv_mode = GEYE_CONV_FP32;
   std::map<std::string, std::unique_ptr<geye::Plan>> plans;
@@ -226,6 +230,7 @@ struct geye_ctx {
   double conv_flops = 0;
   int launches = 0;
   bool use_graphs = true;   // replay the frame as a CUDA graph (GEYE_NO_GRAPHS=1 at creation: plain launches)
+  int nms_order = geye::kNmsOrderKey;   // geye_ctx_set_nms_order
   bool capturing = false;
   // fault injection (host side)
   std::string inject_op;

@@ -50,6 +50,7 @@ def lib(build_if_missing: bool = True):
             "geye_ctx_create": [i32, vp, C.POINTER(vp)],
             "geye_ctx_destroy": [vp],
             "geye_ctx_set_conv_mode": [vp, i32],
+            "geye_ctx_set_nms_order": [vp, i32],
             "geye_ctx_synchronize": [vp],
             "geye_model_load_csv": [vp, C.c_char_p, C.c_char_p, C.c_char_p, C.c_float, C.POINTER(vp)],
             "geye_model_free": [vp],
@@ -145,6 +146,8 @@ def _result_to_dict(r: _Result) -> dict:
 
 
 CONV_FP32, CONV_BF16, CONV_FP8 = 0, 1, 2
+# whole-path NMS order (geye_ctx_set_nms_order)
+NMS_ORDER_KEY, NMS_ORDER_QUICKSORT = 0, 1
 
 
 class Context:
@@ -176,6 +179,11 @@ class Context:
 
     def set_conv_mode(self, mode: int):
         _check(lib().geye_ctx_set_conv_mode(self.h, mode), "set_conv_mode")
+
+    def set_nms_order(self, order: int):
+        """NMS_ORDER_KEY (default: score order, the quicksort's order only for a model
+        that needs it) or NMS_ORDER_QUICKSORT (the quicksort's order always)."""
+        _check(lib().geye_ctx_set_nms_order(self.h, order), "set_nms_order")
 
     def synchronize(self):
         _check(lib().geye_ctx_synchronize(self.h), "synchronize")

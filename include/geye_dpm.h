@@ -275,9 +275,21 @@ geye_status geye_ctx_enable_timing(geye_ctx *ctx, int enable);
 geye_status geye_ctx_stage_times(geye_ctx *ctx, float ms[GEYE_N_STAGES], double bytes[GEYE_N_STAGES],
                                  double *conv_flops, int *kernel_launches);
 
-/* Diagnostic counters of the last whole-path run (per model, 8 values each:
- * NMS sort cycles, NMS greedy cycles, greedy batches, picks, ...). */
+/* Diagnostic counters of the last whole-path run (per model m, 8 values each:
+ * [8m+1] sort segments left to the one-block quicksort tier, [8m+2] greedy
+ * batches, [8m+3] picks, [8m+4] whether the finish kernel ran batches itself,
+ * [8m+5] whether the model's kept set was resolved in the quicksort's order). */
 geye_status geye_ctx_debug_counters(geye_ctx *ctx, long long *out, int n);
+
+/* Order in which the whole-path NMS resolves the detections (the kept set is
+ * nms.cpp's in both):
+ *   GEYE_NMS_ORDER_KEY (default): score order, equal scores by input index;
+ *     a model whose kept set could depend on the order among equal scores is
+ *     resolved again in the order of the reference's quicksort (nms.cpp:70-84);
+ *   GEYE_NMS_ORDER_QUICKSORT: the quicksort's order for every model. */
+#define GEYE_NMS_ORDER_KEY 0
+#define GEYE_NMS_ORDER_QUICKSORT 1
+geye_status geye_ctx_set_nms_order(geye_ctx *ctx, int order);
 
 /* Score map (root + offset - parts, before the threshold) of pyramid level
  * `level` and component `comp` of model m, from the last whole-path run on this

@@ -275,18 +275,21 @@ def test_pipeline_odd_and_large_frames(ctx, car, w, h):
 
 
 def test_nms_sort_levels_adapt_and_fall_back(tmp_path):
-    """A plan fits its NMS sort levels to the depth its frames need (a shallow
-    frame first: few boxes) and returns to the default when a later frame
-    needs more (the leftover segments take the exact single-block fallback):
-    every result equals a fresh context's, which launches the default levels."""
+    """A plan fits its NMS quicksort levels to the depth its frames need (a
+    shallow frame first: few boxes) and returns to the default when a later
+    frame needs more (the leftover segments take the exact single-block
+    fallback): every result equals a fresh context's, which launches the
+    default levels.  (Quicksort order for every model, so that every frame sorts.)"""
     import geye_gb300 as g
     paths = [synth.write_model_csv(s, str(tmp_path)) for s in (synth.CAR_SPEC, synth.PERSON_SPEC)]
     fr = synth.make_frame(640, 480, seed=6)
     c1 = g.Context(0)
+    c1.set_nms_order(g.NMS_ORDER_QUICKSORT)
     m1 = [g.Model(c1, *p) for p in paths]
     for thresh in (0.9, 0.9, -0.5, -0.5):
         got = c1.detect_multi(fr, m1, thresh, 0.5)
         c2 = g.Context(0)
+        c2.set_nms_order(g.NMS_ORDER_QUICKSORT)
         m2 = [g.Model(c2, *p) for p in paths]
         want = c2.detect_multi(fr, m2, thresh, 0.5)
         for m in m2:
