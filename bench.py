@@ -52,8 +52,9 @@ WORKLOADS = {
     # (latency-aware admission: at most one frame of a camera waits for a slot, a newer one replaces it,
     # and a frame that waited more than 40 ms is dropped rather than served late)
     # (at most 16 slots: frames in flight share the GPU, so more slots lengthen every frame's latency)
+    # (12 slots: each keeps a plan per resolution, about 2.8 GB for the three, within the budget)
     "serve64_mixed_bf16": dict(w=640, h=480, models=("car", "person"), conv="bf16", sim=True, streams=64, fps=30.0,
-                               sizes=((640, 480), (1280, 720), (1920, 1080)), seconds=6.0, slots=16,
+                               sizes=((640, 480), (1280, 720), (1920, 1080)), seconds=6.0, slots=12,
                                admission=(1, 40.0)),
     # 64 cameras at 640x480 only (the served BF16 pipeline's latency target at 64 streams)
     # (at most 16 slots: more frames in flight only lengthen each frame's share of the GPU)

@@ -262,13 +262,18 @@ void launch_nms(const float *boxes, const int *d_num, int n_models, int GL, floa
 constexpr int kNmsBatch = 256;     // boxes resolved per round
 constexpr int kNmsSegS = 16384;    // sort segments finished in shared memory (one block, ~203 KB)
 constexpr int kNmsTile = 4096;     // elements per block in the sort's grid-wide partitions
-constexpr int kRsT = 2048;         // elements per block in the key-order radix sort
+constexpr int kRsT = 4096;         // elements per block in the key-order radix sort
 __host__ __device__ inline int nms_big_cap(int cap) { return cap / kNmsSegS + 2; }
 __host__ __device__ inline int nms_tile_cap(int cap) { return cap / kNmsTile + nms_big_cap(cap) + 1; }
+constexpr int kNmsCells = 64;      // cells per image axis of the greedy's pick masks
+constexpr int kNmsLevels = 7;      // their sparse-table levels (spans of 1..64 cells)
 __host__ __device__ inline int nms_rs_tiles(int cap) { return (cap + kRsT - 1) / kRsT; }
+// summary bitmap: one bit per word of the alive bitmap
+__host__ __device__ inline int nms_summary_words(int cap) { return ((cap + 31) / 32 + 31) / 32 + 1; }
 __host__ __device__ inline size_t nms_model_words(int cap) {
   const size_t w = 8 * (size_t)cap + 64 + 5 * kNmsBatch + 4 * (size_t)nms_big_cap(cap) +
-                   2 * (size_t)nms_tile_cap(cap) + 256 * (size_t)nms_rs_tiles(cap);
+                   2 * (size_t)nms_tile_cap(cap) + 256 * (size_t)nms_rs_tiles(cap) + nms_summary_words(cap) +
+                   2 * kNmsLevels * kNmsCells * (kNmsBatch / 32);
   return (w + 31) & ~(size_t)31;
 }
 // diag (optional): per model m, diag[8m+1..8m+5] = sort segments left to the fallback, batches, picks,
@@ -284,10 +289,12 @@ constexpr int kNmsOrderKey = 0, kNmsOrderQuicksort = 1;
 // aux: null for plain launches on s; when s is capturing a graph, a second
 // stream that captures the bodies of the conditional nodes (the greedy rounds
 // as a while node, the quicksort-order pass as an if node)
-cudaError_t launch_nms_batch(const float *boxes, const int *d_num, int n_models, int GL, float overlap, int cap,
-                             int *si, float *sf, float *out, int *d_kept, int *err, long long *diag, int levels,
-                             int *lv_used, int rounds, int *rounds_used, int *need, int order, cudaStream_t s,
-                             cudaStream_t aux);
+// extent: box coordinates in [0, extent) spread over the pick masks' cells
+// (any value is exact; boxes outside share the edge cells)
+cudaError_t launch_nms_batch(const float *boxes, const int *d_num, int n_models, int GL, float overlap,
+                             float extent, int cap, int *si, float *sf, float *out, int *d_kept, int *err,
+                             long long *diag, int levels, int *lv_used, int rounds, int *rounds_used, int *need,
+                             int order, cudaStream_t s, cudaStream_t aux);
 int nms_sort_levels(int cap);   // the default number of grid-wide sort levels for cap boxes
 void launch_new_rects(const float *kept, const int *d_kept, int GL, int np, const float *coef, int img_w,
                       int img_h, float ratio, int *point, int *or_point, int *type, float *scale, float *score,

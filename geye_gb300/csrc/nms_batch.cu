@@ -50,7 +50,25 @@ __global__ void __launch_bounds__(kPassNT) k_nms_gather(const float *__restrict_
     S.ar[r] = (P[3] - P[1] + 1.0) * (P[2] - P[0] + 1.0);   // nms.cpp's area expression
   }
   const unsigned bal = __ballot_sync(0xffffffffu, r < D);
-  if ((threadIdx.x & 31) == 0 && (r >> 5) < ((D + 31) >> 5)) S.bits[r >> 5] = bal;
+  const int nwords = (D + 31) >> 5;
+  if ((threadIdx.x & 31) == 0 && (r >> 5) < nwords) S.bits[r >> 5] = bal;
+  // summary: every word below nwords starts with an alive box
+  if (r < (nwords + 31) >> 5) {
+    const int n = min(32, nwords - 32 * r);
+    S.sbits[r] = n == 32 ? ~0u : (1u << n) - 1u;
+  }
+}
+
+// clears the alive bits `clear` of word w (more than one thread may clear bits
+// of the same word); the last clear of a word clears its summary bit
+__device__ __forceinline__ void clear_alive(const Slots &S, int w, unsigned clear) {
+  const unsigned old = atomicAnd(&S.bits[w], ~clear);
+  if (old != 0u && (old & ~clear) == 0u) atomicAnd(&S.sbits[w >> 5], ~(1u << (w & 31)));
+}
+
+// cell of a coordinate on one axis of the pick masks (monotone; NaN to cell 0)
+__device__ __forceinline__ int nms_cell(float v, float inv) {
+  return (int)fminf(fmaxf(v * inv, 0.0f), (float)(kNmsCells - 1));
 }
 
 // ---------------------------------------------------------------------------
@@ -58,14 +76,41 @@ __global__ void __launch_bounds__(kPassNT) k_nms_gather(const float *__restrict_
 // ---------------------------------------------------------------------------
 struct ResolveSmem {
   int mem_pos[kBatch + 1];
+  int wl[kBatch + 1];    // non-empty words of the alive bitmap holding the members
   int run_end[kBatch];   // key order: last member with the same score
+  unsigned key[kBatch + 1];   // key order: the candidates' keys
   float my[5][kBatch];
-  unsigned rows[kBatch][kBW];
+  unsigned cm[2][kNmsCells][kBW];   // the picks by cell, built for the pass
+  unsigned und[kBW], pk_bits[kBW];  // undecided and picked members
+  int killed_any[kBatch];           // member (a pick) removed a member alive at its turn
+  unsigned span[kBatch];            // member's cell span (bytes y0, y1, x0, x1)
   int pick_mem[kBatch];
   int pick_any[kBatch];
   int wtot[kSortNT / 32];
-  int nb, np, last_word, done;
+  int nb, nw, np, last_word, done;
 };
+
+// exclusive block scan of c (kSortNT threads); *tot gets the sum
+__device__ __forceinline__ int block_excl_scan(int c, int *tot, int *wtot) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  int inc = c;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int t = __shfl_up_sync(0xffffffffu, inc, o);
+    if (lane >= o) inc += t;
+  }
+  __syncthreads();   // wtot free
+  if (lane == 31) wtot[warp] = inc;
+  __syncthreads();
+  int before = inc - c, t = 0;
+  for (int k = 0; k < kSortNT / 32; k++) {
+    const int v = wtot[k];
+    if (k < warp) before += v;
+    t += v;
+  }
+  *tot = t;
+  return before;
+}
 
 __device__ __forceinline__ unsigned sorted_key(const Slots &S, int pos) {
   return reinterpret_cast<const unsigned *>(S.val)[pos];
@@ -80,62 +125,68 @@ __device__ __forceinline__ unsigned sorted_key(const Slots &S, int pos) {
 // a pick that suppresses an alive member of its own run, or a run longer than
 // a batch.
 template <bool KEY_ORDER>
-__device__ void resolve_batch(Slots &S, float overlap, ResolveSmem &R, int *need) {
+__device__ void resolve_batch(Slots &S, float overlap, float cell_inv, ResolveSmem &R, int *need) {
   constexpr int want = kBatch + (KEY_ORDER ? 1 : 0);   // key order: one more, to see the run at the boundary
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   BatchState &st = *S.st;
   const int nwords = st.nwords;
-  if (threadIdx.x == 0) { R.nb = 0; R.last_word = st.scan_word; }
+  if (threadIdx.x == 0) R.nw = 0;
   __syncthreads();
-  // members: the first kBatch alive sorted positions from scan_word on
-  for (int base = st.scan_word; base < nwords; base += kSortNT) {
-    const int have = R.nb;   // uniform: written before the last barrier
+  // members: the first `want` alive sorted positions from scan_word on, found
+  // through the summary (words before scan_word hold no alive box): the first
+  // `want` non-empty words, then the first `want` alive bits of those
+  const int nsw = (nwords + 31) >> 5;
+  for (int sb = st.scan_word >> 5; sb < nsw; sb += kSortNT) {
+    const int have = R.nw;   // uniform: written before the last barrier
     if (have >= want) break;
-    const int w = base + threadIdx.x;
-    const unsigned word = w < nwords ? S.bits[w] : 0u;
-    const int c = __popc(word);
-    int inc = c;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const int t = __shfl_up_sync(0xffffffffu, inc, o);
-      if (lane >= o) inc += t;
-    }
-    if (lane == 31) R.wtot[warp] = inc;
-    __syncthreads();
-    int before = inc - c, tot = 0;
-    for (int k = 0; k < kSortNT / 32; k++) {
-      const int v = R.wtot[k];
-      if (k < warp) before += v;
-      tot += v;
-    }
-    int rank = have + before;
-    unsigned rem = word;
+    const int j = sb + threadIdx.x;
+    const unsigned sw = j < nsw ? S.sbits[j] : 0u;
+    int tot;
+    int rank = have + block_excl_scan(__popc(sw), &tot, R.wtot);
+    unsigned rem = sw;
     while (rem && rank < want) {
-      const int b = __ffs(rem) - 1;
+      R.wl[rank++] = (j << 5) + __ffs(rem) - 1;
       rem &= rem - 1;
-      R.mem_pos[rank] = (w << 5) + b;
-      if (rank == kBatch - 1) R.last_word = w;
-      rank++;
     }
-    __syncthreads();   // everyone has read wtot and R.nb
-    if (threadIdx.x == 0) {
-      const int nb = min(want, have + tot);
-      if (have + tot <= want) R.last_word = min(base + kSortNT, nwords);   // took every alive box up to here
-      R.nb = nb;
-    }
+    __syncthreads();   // everyone has read R.nw
+    if (threadIdx.x == 0) R.nw = min(want, have + tot);
     __syncthreads();
   }
-  if (KEY_ORDER) {
-    if (threadIdx.x == 0 && R.nb == want) {   // an alive box follows the batch
-      const unsigned kb = sorted_key(S, R.mem_pos[kBatch]);
-      int nb = kBatch;
-      while (nb > 0 && sorted_key(S, R.mem_pos[nb - 1]) == kb) nb--;
-      if (nb == 0) {   // a run longer than a batch
-        *need = 1;
-        nb = kBatch;
+  const int nw = R.nw;
+  {
+    const int w = threadIdx.x < nw ? R.wl[threadIdx.x] : 0;
+    const unsigned word = threadIdx.x < nw ? S.bits[w] : 0u;
+    int tot;
+    int rank = block_excl_scan(__popc(word), &tot, R.wtot);
+    unsigned rem = word;
+    while (rem && rank < want) {
+      const int r = (w << 5) + __ffs(rem) - 1;
+      R.mem_pos[rank] = r;
+      if (KEY_ORDER) R.key[rank] = sorted_key(S, r);
+      rank++;
+      rem &= rem - 1;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      int nb = min(want, tot);
+      // every alive box is a member: the summary was exhausted and held no more than a batch
+      const bool all_taken = nw < want && tot <= kBatch;
+      if (KEY_ORDER && nb == want) {   // an alive box follows the batch: end before its run
+        const unsigned kb = R.key[kBatch];
+        int lo = 0, hi = kBatch;   // first candidate with key kb (keys ascend): in [lo, hi]
+        while (lo < hi) {
+          const int mid = (lo + hi) >> 1;
+          if (R.key[mid] < kb) lo = mid + 1;
+          else hi = mid;
+        }
+        nb = lo;
+        if (nb == 0) {   // a run longer than a batch
+          *need = 1;
+          nb = kBatch;
+        }
       }
       R.nb = nb;
-      R.last_word = R.mem_pos[nb - 1] >> 5;
+      R.last_word = (all_taken || nb == 0) ? nwords : (R.mem_pos[nb - 1] >> 5);
     }
     __syncthreads();
   }
@@ -148,62 +199,114 @@ __device__ void resolve_batch(Slots &S, float overlap, ResolveSmem &R, int *need
     R.my[2][threadIdx.x] = S.y2[r];
     R.my[3][threadIdx.x] = S.x2[r];
     R.my[4][threadIdx.x] = S.ar[r];
-    if (KEY_ORDER) {
-      const unsigned k = sorted_key(S, r);
-      int e = threadIdx.x;
-      while (e + 1 < nb && sorted_key(S, R.mem_pos[e + 1]) == k) e++;
-      R.run_end[threadIdx.x] = e;
+    if (KEY_ORDER) {   // last member with this key (keys ascend)
+      const unsigned k = R.key[threadIdx.x];
+      int lo = threadIdx.x, hi = nb - 1;
+      while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (R.key[mid] == k) lo = mid;
+        else hi = mid - 1;
+      }
+      R.run_end[threadIdx.x] = lo;
     }
   }
   __syncthreads();
-  // suppression rows: bit j of row i = member i (kept) suppresses member j > i
+  // The batch's decisions, in parallel rounds.  Four threads per member j
+  // hold its column (bit i of word w: member i < j suppresses j; thread q of
+  // the group: words q and q + 4).  A round decides every undecided member
+  // that an earlier pick suppresses (removed) or whose earlier suppressors
+  // are all decided and none picked (picked): the sequential walk's decision
+  // for it, since the members before it are decided as the walk would.  The
+  // first undecided member is always decided, so the rounds end.
   const int nwm = (nb + 31) >> 5;
-  for (int item = threadIdx.x; item < nb * nwm; item += kSortNT) {
-    const int i = item / nwm, w = item % nwm;
-    unsigned word = 0u;
-    if (32 * w + 31 > i) {
-      const float a0 = R.my[0][i], a1 = R.my[1][i], a2 = R.my[2][i], a3 = R.my[3][i], a4 = R.my[4][i];
-      for (int b = 0; b < 32; b++) {
-        const int j = 32 * w + b;
-        if (j > i && j < nb &&
-            supp(a0, a1, a2, a3, a4, R.my[0][j], R.my[1][j], R.my[2][j], R.my[3][j], R.my[4][j], overlap))
-          word |= 1u << b;
-      }
-    }
-    R.rows[i][w] = word;
+  const int gj = threadIdx.x >> 2, gq = threadIdx.x & 3;
+  // each member's cell span, widened by two pixels (bytes y0, y1, x0, x1): two
+  // boxes that can suppress each other have overlapping spans on both axes
+  if (threadIdx.x < nb) {
+    const int i = threadIdx.x;
+    const int y0 = nms_cell(fminf(R.my[0][i], R.my[2][i]) - 2.0f, cell_inv);
+    const int y1 = nms_cell(fmaxf(R.my[0][i], R.my[2][i]) + 2.0f, cell_inv);
+    const int x0 = nms_cell(fminf(R.my[1][i], R.my[3][i]) - 2.0f, cell_inv);
+    const int x1 = nms_cell(fmaxf(R.my[1][i], R.my[3][i]) + 2.0f, cell_inv);
+    R.span[i] = (unsigned)y0 | ((unsigned)y1 << 8) | ((unsigned)x0 << 16) | ((unsigned)x1 << 24);
   }
   __syncthreads();
-  // warp 0 walks the batch in order
-  if (warp == 0) {
-    unsigned alive = 0u;
-    if (lane < nwm) alive = (lane == nwm - 1 && (nb & 31)) ? (1u << (nb & 31)) - 1u : ~0u;
-    int np = 0;
-    for (int guard = 0; guard < kBatch; guard++) {
-      const unsigned nz = __ballot_sync(0xffffffffu, alive != 0u);
-      if (!nz) break;
-      const int fl = __ffs(nz) - 1;
-      const unsigned fw = __shfl_sync(0xffffffffu, alive, fl);
-      const int i = (fl << 5) + __ffs(fw) - 1;
-      if (lane == fl) alive &= ~(1u << (i & 31));
-      const unsigned row = lane < nwm ? R.rows[i][lane] : 0u;
-      const bool any = __ballot_sync(0xffffffffu, (alive & row) != 0u) != 0u;
-      if (KEY_ORDER) {
-        const int e = R.run_end[i];
-        if (e > i) {   // does the pick suppress an alive member of its own run (i, e]?
-          const int lo = max(i + 1, 32 * lane), hi = min(e, 32 * lane + 31);
-          unsigned span = 0u;
-          if (lo <= hi) span = (hi - lo == 31 ? ~0u : ((1u << (hi - lo + 1)) - 1u)) << (lo - 32 * lane);
-          if (__any_sync(0xffffffffu, (alive & row & span) != 0u) && lane == 0) *need = 1;
-        }
+  unsigned col[2] = {0u, 0u};
+  if (gj < nb) {
+    const float b0 = R.my[0][gj], b1 = R.my[1][gj], b2 = R.my[2][gj], b3 = R.my[3][gj], b4 = R.my[4][gj];
+    const unsigned sj = R.span[gj];
+    const int jy0 = sj & 255, jy1 = (sj >> 8) & 255, jx0 = (sj >> 16) & 255, jx1 = sj >> 24;
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+      const int w = gq + 4 * h;
+      const int i0 = 32 * w, i1 = min(i0 + 32, gj);
+      unsigned word = 0u;
+      for (int i = i0; i < i1; i++) {
+        const unsigned si_ = R.span[i];
+        if ((int)(si_ & 255) > jy1 || (int)((si_ >> 8) & 255) < jy0 || (int)((si_ >> 16) & 255) > jx1 ||
+            (int)(si_ >> 24) < jx0)
+          continue;
+        if (supp(R.my[0][i], R.my[1][i], R.my[2][i], R.my[3][i], R.my[4][i], b0, b1, b2, b3, b4, overlap))
+          word |= 1u << (i - i0);
       }
-      alive &= ~row;
-      if (lane == 0) {
-        R.pick_mem[np] = i;
-        R.pick_any[np] = any ? 1 : 0;
-      }
-      np++;
+      col[h] = word;
     }
-    if (lane == 0) R.np = np;
+  }
+  if (threadIdx.x < kBW) {
+    const int w = threadIdx.x;
+    R.und[w] = w < nwm ? ((w == nwm - 1 && (nb & 31)) ? (1u << (nb & 31)) - 1u : ~0u) : 0u;
+    R.pk_bits[w] = 0u;
+  }
+  if (threadIdx.x < kBatch) R.killed_any[threadIdx.x] = 0;
+  __syncthreads();
+  for (int round = 0; round <= kBatch; round++) {
+    const bool mine_und = gj < nb && ((R.und[gj >> 5] >> (gj & 31)) & 1u);
+    int hp = ((col[0] & R.pk_bits[gq]) | (col[1] & R.pk_bits[gq + 4])) != 0u;
+    int hu = ((col[0] & R.und[gq]) | (col[1] & R.und[gq + 4])) != 0u;
+    hp |= __shfl_xor_sync(0xffffffffu, hp, 1);
+    hp |= __shfl_xor_sync(0xffffffffu, hp, 2);
+    hu |= __shfl_xor_sync(0xffffffffu, hu, 1);
+    hu |= __shfl_xor_sync(0xffffffffu, hu, 2);
+    const bool decide = mine_und && (hp || !hu), pick = decide && !hp;
+    __syncthreads();   // every group has read the round's state
+    if (gq == 0 && decide) {
+      atomicAnd(&R.und[gj >> 5], ~(1u << (gj & 31)));
+      if (pick) atomicOr(&R.pk_bits[gj >> 5], 1u << (gj & 31));
+    }
+    __syncthreads();
+    unsigned left = 0u;
+#pragma unroll
+    for (int w = 0; w < kBW; w++) left |= R.und[w];
+    if (!left) break;
+  }
+  // a removed member's first suppressor among the picks removed it in the
+  // walk: that pick suppressed a box alive at its turn (its flag); in key
+  // order, a pick that removes a member of its own run of equal scores needs
+  // the quicksort's order
+  {
+    const bool removed = gj < nb && !((R.pk_bits[gj >> 5] >> (gj & 31)) & 1u);
+    const unsigned h0 = removed ? col[0] & R.pk_bits[gq] : 0u, h1 = removed ? col[1] & R.pk_bits[gq + 4] : 0u;
+    int wfirst = h0 ? gq : (h1 ? gq + 4 : 64);   // smallest word with a suppressing pick
+    wfirst = min(wfirst, __shfl_xor_sync(0xffffffffu, wfirst, 1));
+    wfirst = min(wfirst, __shfl_xor_sync(0xffffffffu, wfirst, 2));
+    const unsigned hw = wfirst == gq ? h0 : (wfirst == gq + 4 ? h1 : 0u);
+    if (hw) {
+      const int killer = 32 * wfirst + __ffs(hw) - 1;
+      R.killed_any[killer] = 1;
+      if (KEY_ORDER && R.key[killer] == R.key[gj]) *need = 1;
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x < nb && ((R.pk_bits[threadIdx.x >> 5] >> (threadIdx.x & 31)) & 1u)) {
+    int rank = __popc(R.pk_bits[threadIdx.x >> 5] & ((1u << (threadIdx.x & 31)) - 1u));
+    for (int w = 0; w < (threadIdx.x >> 5); w++) rank += __popc(R.pk_bits[w]);
+    R.pick_mem[rank] = threadIdx.x;
+    R.pick_any[rank] = R.killed_any[threadIdx.x];
+  }
+  if (threadIdx.x == 0) {
+    int np = 0;
+    for (int w = 0; w < kBW; w++) np += __popc(R.pk_bits[w]);
+    R.np = np;
   }
   __syncthreads();
   const int np = R.np, base = st.npicks;
@@ -213,9 +316,27 @@ __device__ void resolve_batch(Slots &S, float overlap, ResolveSmem &R, int *need
     S.flag[base + k] = R.pick_any[k];
     for (int c = 0; c < 5; c++) S.bp[c * kBatch + k] = R.my[c][i];
   }
+  // the picks by cell for the pass (the suppression rows are free now): a
+  // pick is listed on every cell of its span widened by two pixels, so a box
+  // that it can suppress (positive overlap, or containment) shares a row and a
+  // column cell with it
+  unsigned *cm = &R.cm[0][0][0];   // [axis][cell][kBW]
+  for (int k = threadIdx.x; k < 2 * kNmsCells * kBW; k += kSortNT) cm[k] = 0u;
+  __syncthreads();
+  for (int k = threadIdx.x; k < np; k += kSortNT) {
+    const int i = R.pick_mem[k];
+    const unsigned bit = 1u << (k & 31);
+    for (int a = 0; a < 2; a++) {   // a = 0: y (my[0], my[2]); 1: x (my[1], my[3])
+      const float lo = fminf(R.my[a][i], R.my[a + 2][i]) - 2.0f, hi = fmaxf(R.my[a][i], R.my[a + 2][i]) + 2.0f;
+      const int c1 = nms_cell(hi, cell_inv);
+      for (int c = nms_cell(lo, cell_inv); c <= c1; c++) atomicOr(&cm[(a * kNmsCells + c) * kBW + (k >> 5)], bit);
+    }
+  }
+  __syncthreads();
+  for (int k = threadIdx.x; k < 2 * kNmsCells * kBW; k += kSortNT) S.cmask[k] = cm[k];
   for (int k = threadIdx.x; k < nb; k += kSortNT) {
     const int r = R.mem_pos[k];
-    atomicAnd(&S.bits[r >> 5], ~(1u << (r & 31)));   // every member is resolved
+    clear_alive(S, r >> 5, 1u << (r & 31));   // every member is resolved
   }
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -232,11 +353,12 @@ __device__ void resolve_batch(Slots &S, float overlap, ResolveSmem &R, int *need
 }
 
 template <bool KEY_ORDER>
-__global__ void __launch_bounds__(kSortNT) k_nms_resolve(int cap, int *si, float *sf, float overlap, int *need) {
+__global__ void __launch_bounds__(kSortNT) k_nms_resolve(int cap, int *si, float *sf, float overlap, float cell_inv,
+                                                         int *need) {
   __shared__ ResolveSmem R;
   Slots S = slots(si, sf, blockIdx.x, cap);
   if (S.st->done) return;
-  resolve_batch<KEY_ORDER>(S, overlap, R, need ? need + blockIdx.x : nullptr);
+  resolve_batch<KEY_ORDER>(S, overlap, cell_inv, R, need ? need + blockIdx.x : nullptr);
 }
 
 // ---------------------------------------------------------------------------
@@ -268,7 +390,7 @@ __device__ void pass_words(Slots &S, const float (*pk)[kBatch], int np, int pick
           }
       const unsigned gone = __ballot_sync(0xffffffffu, first >= 0);
       if (first >= 0) S.flag[pick_base + first] = 1;
-      if (lane == 0 && gone) S.bits[w] = word & ~gone;
+      if (lane == 0 && gone) clear_alive(S, w, gone);
       continue;
     }
     unsigned out = word, rem = word;
@@ -289,17 +411,26 @@ __device__ void pass_words(Slots &S, const float (*pk)[kBatch], int np, int pick
         }
       }
     }
-    if (lane == 0 && out != word) S.bits[w] = out;
+    if (lane == 0 && out != word) clear_alive(S, w, word & ~out);
   }
 }
 
-// loop: inside a frame graph's while node, block (0, 0) sets the node's
-// condition for the next round: a model is not done and has taken fewer than
-// max_batches batches (the finish kernel takes any rest)
-__global__ void __launch_bounds__(kPassNT) k_nms_pass(int cap, int *si, float *sf, float overlap,
+// The round's pass: a lane per alive box of a word, testing only the picks
+// that share a row cell and a column cell with it (the union of the picks
+// listed on its cell span, per axis, from a sparse table of spans of 2^l
+// cells), in pick order; the first that suppresses it removes it and is
+// flagged.  loop: inside a frame graph's while node, block (0, 0) sets the
+// node's condition for the next round: a model is not done and has taken
+// fewer than max_batches batches (the finish kernel takes any rest).
+struct PassSmem {
+  float pk[5][kBatch];
+  unsigned tab[2][kNmsLevels][kNmsCells][kBW];
+};
+
+__global__ void __launch_bounds__(kPassNT) k_nms_pass(int cap, int *si, float *sf, float overlap, float cell_inv,
                                                       cudaGraphConditionalHandle loop, int use_loop,
                                                       int max_batches) {
-  __shared__ float pk[5][kBatch];
+  __shared__ PassSmem Z;
   if (use_loop && blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) {
     unsigned more = 0;
     for (int m = 0; m < (int)gridDim.y; m++) {
@@ -309,14 +440,60 @@ __global__ void __launch_bounds__(kPassNT) k_nms_pass(int cap, int *si, float *s
     cudaGraphSetConditional(loop, more);
   }
   Slots S = slots(si, sf, blockIdx.y, cap);
-  if (S.st->done) return;
-  const int np = S.st->npb;
+  const BatchState &st = *S.st;
+  if (st.done) return;
+  const int np = st.npb;
   if (np <= 0) return;
+  const int nwm = (np + 31) >> 5;
   for (int k = threadIdx.x; k < np; k += kPassNT)
-    for (int c = 0; c < 5; c++) pk[c][k] = S.bp[c * kBatch + k];
+    for (int c = 0; c < 5; c++) Z.pk[c][k] = S.bp[c * kBatch + k];
+  for (int e = threadIdx.x; e < 2 * kNmsCells * nwm; e += kPassNT) {
+    const int a = e / (kNmsCells * nwm), rem = e - a * kNmsCells * nwm, c = rem / nwm, k = rem - c * nwm;
+    Z.tab[a][0][c][k] = S.cmask[(a * kNmsCells + c) * kBW + k];
+  }
   __syncthreads();
-  pass_words(S, pk, np, S.st->npicks - np, overlap, blockIdx.x * (kPassNT / 32) + (threadIdx.x >> 5),
-             gridDim.x * (kPassNT / 32));
+  for (int l = 1; l < kNmsLevels; l++) {
+    for (int e = threadIdx.x; e < 2 * kNmsCells * nwm; e += kPassNT) {
+      const int a = e / (kNmsCells * nwm), rem = e - a * kNmsCells * nwm, c = rem / nwm, k = rem - c * nwm;
+      Z.tab[a][l][c][k] = Z.tab[a][l - 1][c][k] | Z.tab[a][l - 1][min(c + (1 << (l - 1)), kNmsCells - 1)][k];
+    }
+    __syncthreads();
+  }
+  const int lane = threadIdx.x & 31;
+  const int pick_base = st.npicks - np;
+  const int nwords = st.nwords;
+  const int nwarps = gridDim.x * (kPassNT / 32);
+  for (int w = st.scan_word + blockIdx.x * (kPassNT / 32) + (threadIdx.x >> 5); w < nwords; w += nwarps) {
+    const unsigned word = S.bits[w];
+    if (!word) continue;
+    const int r = (w << 5) + lane;
+    int first = -1;
+    if ((word >> lane) & 1u) {
+      const float e0 = S.y1[r], e1 = S.x1[r], e2 = S.y2[r], e3 = S.x2[r], e4 = S.ar[r];
+      const int cy0 = nms_cell(fminf(e0, e2), cell_inv), cy1 = nms_cell(fmaxf(e0, e2), cell_inv);
+      const int cx0 = nms_cell(fminf(e1, e3), cell_inv), cx1 = nms_cell(fmaxf(e1, e3), cell_inv);
+      const int ly = 31 - __clz(cy1 - cy0 + 1), lx = 31 - __clz(cx1 - cx0 + 1);
+      const int cy2 = cy1 - (1 << ly) + 1, cx2 = cx1 - (1 << lx) + 1;
+      for (int k = 0; k < nwm && first < 0; k++) {
+        unsigned cand = (Z.tab[0][ly][cy0][k] | Z.tab[0][ly][cy2][k]) & (Z.tab[1][lx][cx0][k] | Z.tab[1][lx][cx2][k]);
+        while (cand) {
+          const int t = (k << 5) + __ffs(cand) - 1;
+          cand &= cand - 1;
+          if (supp(Z.pk[0][t], Z.pk[1][t], Z.pk[2][t], Z.pk[3][t], Z.pk[4][t], e0, e1, e2, e3, e4, overlap)) {
+            first = t;
+            break;
+          }
+        }
+      }
+    }
+    const unsigned gone = __ballot_sync(0xffffffffu, first >= 0);
+    if (first >= 0) S.flag[pick_base + first] = 1;
+    if (lane == 0 && gone) {   // this warp owns word w in this kernel
+      const unsigned left = word & ~gone;
+      S.bits[w] = left;
+      if (!left) atomicAnd(&S.sbits[w >> 5], ~(1u << (w & 31)));
+    }
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -330,7 +507,7 @@ template <bool KEY_ORDER>
 __global__ void __launch_bounds__(kSortNT) k_nms_finish(const float *__restrict__ boxes_all, int GL, int cap,
                                                         int *si, float *sf, float overlap, float *out_all,
                                                         int *d_kept, int *err, long long *diag, int *rounds_used,
-                                                        int *need) {
+                                                        int *need, float cell_inv) {
   __shared__ ResolveSmem R;
   __shared__ float pk[5][kBatch];
   __shared__ int wcnt[kSortNT / 32];
@@ -349,7 +526,7 @@ __global__ void __launch_bounds__(kSortNT) k_nms_finish(const float *__restrict_
         if (threadIdx.x == 0) atomicOr(err, 2);
         break;
       }
-      resolve_batch<KEY_ORDER>(S, overlap, R, need ? need + m : nullptr);
+      resolve_batch<KEY_ORDER>(S, overlap, cell_inv, R, need ? need + m : nullptr);
       if (R.done) break;
       const int np = R.np;
       for (int k = threadIdx.x; k < np; k += kSortNT)
@@ -474,9 +651,9 @@ constexpr int kNmsLoopBatches = 512;   // while-node rounds before the finish ke
 // aux non-null: s is capturing a graph, and the rounds are a while node (as many
 // as the frame needs) instead of `rounds` launches
 template <bool KEY_ORDER>
-static cudaError_t launch_greedy(const float *boxes, int n_models, int GL, float overlap, int cap, int *si, float *sf,
-                                 float *out, int *d_kept, int *err, long long *diag, int rounds, int *rounds_used,
-                                 int *need, cudaStream_t s, cudaStream_t aux) {
+static cudaError_t launch_greedy(const float *boxes, int n_models, int GL, float overlap, float cell_inv, int cap,
+                                 int *si, float *sf, float *out, int *d_kept, int *err, long long *diag, int rounds,
+                                 int *rounds_used, int *need, cudaStream_t s, cudaStream_t aux) {
   k_nms_gather<<<dim3((cap + kPassNT - 1) / kPassNT, n_models), kPassNT, 0, s>>>(boxes, GL, cap, si, sf);
   const int words = (cap + 31) / 32;
   const int pass_blocks = std::max(1, std::min((words + kPassNT / 32 - 1) / (kPassNT / 32), 512));
@@ -485,35 +662,37 @@ static cudaError_t launch_greedy(const float *boxes, int n_models, int GL, float
     cudaError_t e = cond_handle(s, 1u, &loop);
     if (e == cudaSuccess) e = begin_conditional(s, aux, cudaGraphCondTypeWhile, loop);
     if (e != cudaSuccess) return e;
-    k_nms_resolve<KEY_ORDER><<<n_models, kSortNT, 0, aux>>>(cap, si, sf, overlap, need);
-    k_nms_pass<<<dim3(pass_blocks, n_models), kPassNT, 0, aux>>>(cap, si, sf, overlap, loop, 1, kNmsLoopBatches);
+    k_nms_resolve<KEY_ORDER><<<n_models, kSortNT, 0, aux>>>(cap, si, sf, overlap, cell_inv, need);
+    k_nms_pass<<<dim3(pass_blocks, n_models), kPassNT, 0, aux>>>(cap, si, sf, overlap, cell_inv, loop, 1,
+                                                                 kNmsLoopBatches);
     if ((e = end_conditional(aux)) != cudaSuccess) return e;
   } else {
     for (int r = 0; r < rounds; r++) {
-      k_nms_resolve<KEY_ORDER><<<n_models, kSortNT, 0, s>>>(cap, si, sf, overlap, need);
-      k_nms_pass<<<dim3(pass_blocks, n_models), kPassNT, 0, s>>>(cap, si, sf, overlap, 0, 0, 0);
+      k_nms_resolve<KEY_ORDER><<<n_models, kSortNT, 0, s>>>(cap, si, sf, overlap, cell_inv, need);
+      k_nms_pass<<<dim3(pass_blocks, n_models), kPassNT, 0, s>>>(cap, si, sf, overlap, cell_inv, 0, 0, 0);
     }
   }
   k_nms_finish<KEY_ORDER><<<n_models, kSortNT, 0, s>>>(boxes, GL, cap, si, sf, overlap, out, d_kept, err, diag,
-                                                       rounds_used, need);
+                                                       rounds_used, need, cell_inv);
   return cudaSuccess;
 }
 
-cudaError_t launch_nms_batch(const float *boxes, const int *d_num, int n_models, int GL, float overlap, int cap,
-                             int *si, float *sf, float *out, int *d_kept, int *err, long long *diag, int levels,
-                             int *lv_used, int rounds, int *rounds_used, int *need, int order, cudaStream_t s,
-                             cudaStream_t aux) {
+cudaError_t launch_nms_batch(const float *boxes, const int *d_num, int n_models, int GL, float overlap,
+                             float extent, int cap, int *si, float *sf, float *out, int *d_kept, int *err,
+                             long long *diag, int levels, int *lv_used, int rounds, int *rounds_used, int *need,
+                             int order, cudaStream_t s, cudaStream_t aux) {
+  const float cell_inv = (float)kNmsCells / std::max(extent, 1.0f);
   if (n_models <= 0) return cudaSuccess;
   if (rounds <= 0) rounds = kNmsRounds;
   cudaError_t e;
   if (order == kNmsOrderQuicksort) {
     launch_nms_sort(boxes, d_num, n_models, GL, cap, si, sf, err, diag, levels, lv_used, nullptr, s);
-    return launch_greedy<false>(boxes, n_models, GL, overlap, cap, si, sf, out, d_kept, err, diag, rounds,
+    return launch_greedy<false>(boxes, n_models, GL, overlap, cell_inv, cap, si, sf, out, d_kept, err, diag, rounds,
                                 rounds_used, nullptr, s, aux);
   }
   launch_nms_radix(boxes, d_num, n_models, GL, cap, si, sf, need, s);
-  e = launch_greedy<true>(boxes, n_models, GL, overlap, cap, si, sf, out, d_kept, err, diag, rounds, rounds_used,
-                          need, s, aux);
+  e = launch_greedy<true>(boxes, n_models, GL, overlap, cell_inv, cap, si, sf, out, d_kept, err, diag, rounds,
+                          rounds_used, need, s, aux);
   if (e != cudaSuccess) return e;
   // the models whose kept set could depend on the order inside a run of equal
   // scores, again in the quicksort's order: in a graph, an if node that runs
@@ -527,8 +706,8 @@ cudaError_t launch_nms_batch(const float *boxes, const int *d_num, int n_models,
     q = aux;
   }
   launch_nms_sort(boxes, d_num, n_models, GL, cap, si, sf, err, diag, levels, lv_used, need, q);
-  e = launch_greedy<false>(boxes, n_models, GL, overlap, cap, si, sf, out, d_kept, err, diag, rounds, rounds_used,
-                           need, q, nullptr);
+  e = launch_greedy<false>(boxes, n_models, GL, overlap, cell_inv, cap, si, sf, out, d_kept, err, diag, rounds,
+                           rounds_used, need, q, nullptr);
   if (aux) {
     const cudaError_t e2 = end_conditional(aux);
     if (e == cudaSuccess) e = e2;

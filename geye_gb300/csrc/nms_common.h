@@ -37,6 +37,8 @@ struct Slots {
   int2 *big[2];      // nms_big_cap(cap) segments each
   int2 *tiles;       // nms_tile_cap(cap) per-tile (<= key, >= key) counts
   int *hist;         // 256 * nms_rs_tiles(cap) radix-sort digit counts (nms_radix.cu)
+  unsigned *sbits;   // summary of bits: bit w set while word w has an alive box
+  unsigned *cmask;   // the round's picks by cell: [axis y, x][level][cell][pick word] (nms_batch.cu)
   float *y1, *x1, *y2, *x2, *ar;   // boxes in sorted order
 };
 
@@ -62,6 +64,8 @@ __device__ __forceinline__ Slots slots(int *si, float *sf, int m, int cap) {
   S.big[1] = reinterpret_cast<int2 *>(l + 2 * bc);
   S.tiles = reinterpret_cast<int2 *>(l + 4 * bc);
   S.hist = l + 4 * bc + 2 * nms_tile_cap(cap);
+  S.sbits = reinterpret_cast<unsigned *>(S.hist + 256 * (size_t)nms_rs_tiles(cap));
+  S.cmask = S.sbits + nms_summary_words(cap);
   S.y1 = f;
   S.x1 = f + cap;
   S.y2 = f + 2 * (size_t)cap;

@@ -105,9 +105,12 @@ __global__ void __launch_bounds__(kRsNT) k_rs_count(int pass, int cap, int *si, 
   for (int d = threadIdx.x; d < 256; d += kRsNT) S.hist[(size_t)d * nt + t] = h[d];
 }
 
-// exclusive scan of H (digit-major) in place, one block per model
-constexpr int kRsScanNT = 1024;
+// exclusive scan of H (digit-major) in place, one block per model: chunks of
+// kRsScanNT * kRsScanItems counts staged in shared memory with coalesced
+// loads and stores, each thread scanning kRsScanItems consecutive ones
+constexpr int kRsScanNT = 1024, kRsScanItems = 8, kRsScanPad = kRsScanItems + 1;
 __global__ void __launch_bounds__(kRsScanNT) k_rs_scan(int cap, int *si, float *sf) {
+  __shared__ int buf[kRsScanNT * kRsScanPad];   // thread t's items at t * kRsScanPad (no bank conflicts)
   __shared__ int wsum[kRsScanNT / 32];
   __shared__ int carry_s;
   Slots S = slots(si, sf, blockIdx.x, cap);
@@ -116,14 +119,17 @@ __global__ void __launch_bounds__(kRsScanNT) k_rs_scan(int cap, int *si, float *
   const int n = 256 * ((D + kRsT - 1) / kRsT);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   int carry = 0;
-  for (int base = 0; base < n; base += 4 * kRsScanNT) {
-    const int i0 = base + 4 * threadIdx.x;
-    int v[4], s = 0;
+  for (int base = 0; base < n; base += kRsScanItems * kRsScanNT) {
 #pragma unroll
-    for (int k = 0; k < 4; k++) {
-      v[k] = i0 + k < n ? S.hist[i0 + k] : 0;
-      s += v[k];
+    for (int k = 0; k < kRsScanItems; k++) {
+      const int e = k * kRsScanNT + threadIdx.x;   // chunk element, coalesced
+      buf[(e / kRsScanItems) * kRsScanPad + e % kRsScanItems] = base + e < n ? S.hist[base + e] : 0;
     }
+    __syncthreads();
+    int *mine = buf + threadIdx.x * kRsScanPad;
+    int s = 0;
+#pragma unroll
+    for (int k = 0; k < kRsScanItems; k++) s += mine[k];
     int inc = s;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
@@ -145,12 +151,19 @@ __global__ void __launch_bounds__(kRsScanNT) k_rs_scan(int cap, int *si, float *
     __syncthreads();
     int run = carry + (warp ? wsum[warp - 1] : 0) + inc - s;
 #pragma unroll
-    for (int k = 0; k < 4; k++) {
-      if (i0 + k < n) S.hist[i0 + k] = run;
-      run += v[k];
+    for (int k = 0; k < kRsScanItems; k++) {
+      const int v = mine[k];
+      mine[k] = run;
+      run += v;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < kRsScanItems; k++) {
+      const int e = k * kRsScanNT + threadIdx.x;
+      if (base + e < n) S.hist[base + e] = buf[(e / kRsScanItems) * kRsScanPad + e % kRsScanItems];
     }
     carry += carry_s;
-    __syncthreads();   // wsum and carry_s reused by the next chunk
+    __syncthreads();   // buf, wsum and carry_s reused by the next chunk
   }
 }
 

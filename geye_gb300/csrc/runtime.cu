@@ -957,10 +957,11 @@ geye_status run_ascore(geye_ctx *ctx, Plan &P, ModelPlan &mp, int mi, float thre
 // frame whose last launched level still had work left its remaining segments
 // to the single-block fallback (exact, slower): the plan goes back to the
 // default count for good.
-// Rounds: the first frame launches kNmsRounds; one that needed fewer makes the
-// plan launch one more than it needed; one that took more batches than were
-// launched (the rest ran in the finish kernel's single block) makes it launch
-// two more than that frame took, and the count only grows from then on.
+// Rounds (plain launches only; a frame graph loops them in a while node): the
+// first frame launches kNmsRounds; one that needed fewer makes the plan launch
+// one more than it needed; one that took more batches than were launched (the
+// rest ran in the finish kernel's single block) makes it launch two more than
+// that frame took, and the count only grows from then on.
 // A change drops the plan's frame graphs after its stream has drained; the
 // next frame captures them again.
 void note_sort_levels(geye_ctx *ctx, Plan &P, int used, int rounds) {
@@ -973,7 +974,9 @@ void note_sort_levels(geye_ctx *ctx, Plan &P, int used, int rounds) {
   } else if (!P.sort_levels_fixed && P.sort_levels == 0 && used > 0 && used + 3 < full) {
     next = std::max(4, used + 3);
   }
-  if (rounds > r_launched) {
+  if (ctx->use_graphs) {
+    // frame graphs loop the rounds in a while node, as many as the frame needs
+  } else if (rounds > r_launched) {
     r_next = std::min(kNmsMaxRounds, rounds + 2);
     P.nms_rounds_fixed = true;
   } else if (!P.nms_rounds_fixed && P.nms_rounds == 0 && rounds + 1 < kNmsRounds) {
@@ -993,7 +996,8 @@ geye_status run_nms(geye_ctx *ctx, Plan &P, int n_models, float overlap) {
   int *d_kept = d_num + 32;
   int *err = d_num + 128;
   const cudaError_t ge =
-      launch_nms_batch(P.d_boxes.as<float>(), d_num, n_models, P.gl, overlap, P.max_cap, P.d_nms_i.as<int>(),
+      launch_nms_batch(P.d_boxes.as<float>(), d_num, n_models, P.gl, overlap,
+                       1.25f * (float)std::max(P.width, P.height), P.max_cap, P.d_nms_i.as<int>(),
                        P.d_nms_f.as<float>(), P.d_kept_boxes.as<float>(), d_kept, err,
                        reinterpret_cast<long long *>(d_num + 512), P.sort_levels, d_num + kSortLevelsUsed,
                        P.nms_rounds, d_num + kNmsRoundsUsed, d_num + kNmsNeed, ctx->nms_order, ctx->stream,
@@ -1160,6 +1164,19 @@ geye_status collect_stage_times(geye_ctx *ctx) {
 
 geye_status frame_plan(geye_ctx *ctx, geye_model *const *models, int n, int w, int h, Plan **out) {
   return get_frame_plan(ctx, models, n, w, h, out);
+}
+
+void drop_frame_plans(geye_ctx *ctx, int w, int h) {
+  for (auto it = ctx->plans.begin(); it != ctx->plans.end();) {
+    Plan *P = it->second.get();
+    if (!P->from_features && P->width == w && P->height == h) {
+      if (ctx->last_plan == P) ctx->last_plan = nullptr;
+      if (ctx->pending == P) ctx->pending = nullptr;
+      it = ctx->plans.erase(it);
+    } else {
+      ++it;
+    }
+  }
 }
 
 geye_status parse_model_files(const char *c, const char *r, const char *p, HostModel &m) { return parse_model(c, r, p, m); }

@@ -6,9 +6,11 @@
 // memory, replays the frame graph on the context's stream and queues the
 // result copies; a completion event tells when it is done.  The server keeps a
 // pool of slots and a FIFO of submitted frames.  A frame goes to a free slot
-// that already holds a plan for its size, else to a free slot that gets one,
-// else to a new slot while the device memory held by slots stays within the
-// budget.  Frames in different slots overlap on the GPU; a stream's frames are
+// that already holds a plan for its size, else to a new slot while the device
+// memory held by slots stays within the budget, else to any free slot, which
+// builds a plan for the size beside the ones it holds (or in their place once
+// the memory held reaches the budget).  Frames in different slots overlap on
+// the GPU; a stream's frames are
 // dispatched in submission order and its tracker updates are chained with
 // events so they run in that order too.
 #include <stdlib.h>
@@ -28,6 +30,7 @@ namespace geye {
 geye_status run_frame(geye_ctx *ctx, Plan &P, const uint8_t *d_bgr, int width_step, float thresh, float overlap,
                       const float *const *h_ascore_init);
 geye_status frame_plan(geye_ctx *ctx, geye_model *const *models, int n, int w, int h, Plan **out);
+void drop_frame_plans(geye_ctx *ctx, int w, int h);   // the context's whole-path plans for frames of w x h
 size_t plan_device_bytes(const Plan &P);
 
 constexpr int kHostRes = 4096;   // records per model returned through pinned memory
@@ -42,10 +45,13 @@ static long long now_ns() {
 }
 
 // queue everything of one frame on the context's stream (the frame already in P.h_bgr)
+// (from h_src, pinned and kept until the frame completes, when given)
 static geye_status enqueue_frame(geye_ctx *ctx, Plan &P, float thresh, float overlap, TrackerSet *trk, int stream,
-                                 cudaEvent_t after, cudaEvent_t tracked, bool record_done = true) {
+                                 cudaEvent_t after, cudaEvent_t tracked, bool record_done = true,
+                                 const void *h_src = nullptr) {
   const int n_models = (int)P.models.size();
-  CUDA_TRY(cudaMemcpyAsync(P.d_bgr.p, P.h_bgr, (size_t)3 * P.width * P.height, cudaMemcpyHostToDevice, ctx->stream));
+  CUDA_TRY(cudaMemcpyAsync(P.d_bgr.p, h_src ? h_src : P.h_bgr, (size_t)3 * P.width * P.height,
+                           cudaMemcpyHostToDevice, ctx->stream));
   GEYE_TRY(run_frame(ctx, P, P.d_bgr.as<uint8_t>(), 3 * P.width, thresh, overlap, nullptr));
   if (trk) {
     if (after) CUDA_TRY(cudaStreamWaitEvent(ctx->stream, after, 0));
@@ -182,18 +188,29 @@ struct geye_server {
   struct Slot {
     geye_ctx *ctx = nullptr;
     bool busy = false;
-    int w = 0, h = 0;               // size of the plan the slot holds
-    size_t bytes = 0;
+    struct Held {
+      size_t bytes;        // device bytes of the plan
+      long long used;      // last dispatch to it
+    };
+    std::map<long long, Held> sizes;   // (w << 32 | h) of each plan the slot holds
+    size_t bytes = 0;                  // their sum
     long long ticket = 0, t_submit = 0, t_dispatch = 0;
     int stream = 0;
     cudaEvent_t tracked = nullptr;  // this frame's tracker update
+    uint8_t *frame = nullptr;       // the frame's pinned buffer, held until it completes
+    size_t frame_bytes = 0;
   };
   std::vector<Slot> slots;
   struct Req {
     long long ticket, t_submit;
     int stream, w, h;
-    std::vector<uint8_t> bgr;
+    uint8_t *bgr;   // pinned (pool below), the H2D copy's source
+    size_t bytes;
   };
+  // pinned frame buffers by size: a submitted frame is copied once, into one of
+  // these, and goes to the device from there
+  std::map<size_t, std::vector<uint8_t *>> pinned_free;
+  std::vector<uint8_t *> pinned_all;
   std::deque<Req> queue;
   struct Done {
     geye_served info;
@@ -230,8 +247,27 @@ geye_status new_slot(geye_server *s, int *idx) {
   return GEYE_OK;
 }
 
+geye_status get_pinned(geye_server *s, size_t n, uint8_t **out) {
+  auto &v = s->pinned_free[n];
+  if (!v.empty()) {
+    *out = v.back();
+    v.pop_back();
+    return GEYE_OK;
+  }
+  void *p = nullptr;
+  CUDA_TRY(cudaMallocHost(&p, n));
+  s->pinned_all.push_back(static_cast<uint8_t *>(p));
+  *out = static_cast<uint8_t *>(p);
+  return GEYE_OK;
+}
+
+void put_pinned(geye_server *s, size_t n, uint8_t *p) {
+  if (p) s->pinned_free[n].push_back(p);
+}
+
 // a queued frame that will not run: reported by poll with dropped = 1 and empty results
 void drop_request(geye_server *s, const geye_server::Req &r) {
+  put_pinned(s, r.bytes, r.bgr);
   geye_server::Done d;
   d.info = geye_served{};
   d.info.ticket = r.ticket;
@@ -254,38 +290,53 @@ geye_status dispatch_one(geye_server *s, bool *dispatched) {
   }
   if (s->queue.empty()) return GEYE_OK;
   geye_server::Req &r = s->queue.front();
+  const long long key = ((long long)r.w << 32) | (unsigned)r.h;
   int pick = -1;
+  // a free slot that holds a plan (and its frame graph) for this size
   for (size_t i = 0; i < s->slots.size() && pick < 0; i++)
-    if (!s->slots[i].busy && s->slots[i].w == r.w && s->slots[i].h == r.h) pick = (int)i;
-  // else a new slot while slots and memory last: keeping every slot's plan (and its
-  // frame graph) for the size it holds avoids rebuilding plans when sizes mix
+    if (!s->slots[i].busy && s->slots[i].sizes.count(key)) pick = (int)i;
+  // else a new slot while slots and memory last
   if (pick < 0 && (int)s->slots.size() < s->max_slots && s->held < s->budget) GEYE_TRY(new_slot(s, &pick));
-  if (pick < 0)   // else a free slot whose plan is dropped for this size
-    for (size_t i = 0; i < s->slots.size() && pick < 0; i++)
-      if (!s->slots[i].busy && s->held < s->budget) pick = (int)i;
+  // else any free slot: it keeps its plans for other sizes (so that mixed sizes do
+  // not rebuild plans) while the memory held stays within the budget, else drops them
+  for (size_t i = 0; i < s->slots.size() && pick < 0; i++)
+    if (!s->slots[i].busy) pick = (int)i;
   if (pick < 0) return GEYE_OK;
   geye_server::Slot &sl = s->slots[pick];
-  if (sl.w != r.w || sl.h != r.h) {   // rebuild for the new size: the old plan's memory goes back
-    sl.ctx->plans.clear();
-    sl.ctx->last_plan = nullptr;
-    s->held -= sl.bytes;
-    sl.bytes = 0;
+  const bool fresh = !sl.sizes.count(key);
+  // room for a new plan: the least recently used plans of free slots go while
+  // the memory held is at the budget
+  while (fresh && (s->held >= s->budget || sl.sizes.size() >= 16)) {
+    geye_server::Slot *vs = nullptr;
+    long long vk = 0, vt = 0;
+    for (auto &o : s->slots) {
+      if (o.busy) continue;
+      for (auto &kv : o.sizes)
+        if (!vs || kv.second.used < vt) { vs = &o; vk = kv.first; vt = kv.second.used; }
+    }
+    if (!vs) break;
+    drop_frame_plans(vs->ctx, (int)(vk >> 32), (int)(vk & 0xffffffff));
+    s->held -= vs->sizes[vk].bytes;
+    vs->bytes -= vs->sizes[vk].bytes;
+    vs->sizes.erase(vk);
   }
   Plan *P = nullptr;
   GEYE_TRY(frame_plan(sl.ctx, s->models.data(), (int)s->models.size(), r.w, r.h, &P));
   GEYE_TRY(ensure_staging(*P));
-  if (sl.w != r.w || sl.h != r.h) {
-    sl.w = r.w;
-    sl.h = r.h;
-    sl.bytes = plan_device_bytes(*P);
-    s->held += sl.bytes;
+  if (fresh) {
+    const size_t b = plan_device_bytes(*P);
+    sl.sizes[key] = geye_server::Slot::Held{b, 0};
+    sl.bytes += b;
+    s->held += b;
   }
-  memcpy(P->h_bgr, r.bgr.data(), r.bgr.size());
+  sl.sizes[key].used = now_ns();
   cudaEvent_t after = nullptr;
   auto it = s->last_tracked.find(r.stream);
   if (it != s->last_tracked.end() && s->stream_busy[r.stream] > 0) after = it->second;
   GEYE_TRY(enqueue_frame(sl.ctx, *P, s->thresh, s->overlap, s->track ? &s->trk : nullptr, r.stream, after,
-                         sl.tracked));
+                         sl.tracked, true, r.bgr));
+  sl.frame = r.bgr;
+  sl.frame_bytes = r.bytes;
   s->last_tracked[r.stream] = sl.tracked;
   s->stream_busy[r.stream]++;
   sl.busy = true;
@@ -327,6 +378,8 @@ geye_status complete(geye_server *s, geye_server::Slot &sl) {
   d.info.n_tracks = s->track ? tracker_count(s->trk, sl.stream) : 0;
   s->done.push_back(std::move(d));
   s->stream_busy[sl.stream]--;
+  put_pinned(s, sl.frame_bytes, sl.frame);
+  sl.frame = nullptr;
   sl.busy = false;
   s->completed++;
   return GEYE_OK;
@@ -398,6 +451,7 @@ geye_status geye_server_destroy(geye_server *s) {
     if (sl.tracked) cudaEventDestroy(sl.tracked);
     geye_ctx_destroy(sl.ctx);
   }
+  for (uint8_t *p : s->pinned_all) cudaFreeHost(p);
   tracker_free(s->trk);
   delete s;
   return GEYE_OK;
@@ -416,9 +470,14 @@ geye_status geye_server_submit(geye_server *s, int stream, const uint8_t *bgr, i
   r.stream = stream;
   r.w = width;
   r.h = height;
-  r.bgr.resize((size_t)3 * width * height);
-  for (int y = 0; y < height; y++)
-    memcpy(r.bgr.data() + (size_t)y * 3 * width, bgr + (size_t)y * width_step, (size_t)3 * width);
+  r.bytes = (size_t)3 * width * height;
+  GEYE_TRY(get_pinned(s, r.bytes, &r.bgr));
+  if (width_step == 3 * width) {
+    memcpy(r.bgr, bgr, r.bytes);
+  } else {
+    for (int y = 0; y < height; y++)
+      memcpy(r.bgr + (size_t)y * 3 * width, bgr + (size_t)y * width_step, (size_t)3 * width);
+  }
   *ticket = r.ticket;
   s->queue.push_back(std::move(r));
   if (s->max_queued > 0) {   // the stream's oldest queued frames make way for its newest
