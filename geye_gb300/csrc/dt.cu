@@ -22,11 +22,14 @@
 // (an inf candidate never wins a strict comparison), using per-offset terms
 // (a*t)*t and b*t tabulated once per block -- the same roundings as dt_f.
 //
-// g(d) is searched in a window |d - s| < K.  K is chosen per line so that
-// every s outside the window has f_d(s) > max(v) >= f_d(d): with u = 2^-24,
+// g(d) is searched in a window |d - s| < K.  K is chosen so that every s
+// outside the window has f_d(s) > max(v) >= f_d(d): with u = 2^-24,
 // f_d(s) >= v_min + (1-8u) a t^2 - (1+8u)|b t| - 8u max|v| for a > 0, and K
 // is the first integer past the positive root of that bound minus v_max.
-// For a <= 0 the window is the whole line.
+// For a <= 0 the window is the whole line.  Pass 1 (columns: many short
+// lines per tile) takes one K from the whole tile's value range and, when the
+// order is proven and K <= 8, scans with the per-offset terms in registers;
+// pass 2 (rows: a few long lines) takes a K per line.
 #include <math.h>
 
 #include <algorithm>
@@ -98,7 +101,7 @@ __host__ __device__ __forceinline__ int dt_lg_lines2(int n) {
 }
 __host__ __device__ __forceinline__ size_t dt_smem_bytes(int L, int n) {
   return sizeof(float) * ((size_t)kDtPad + (size_t)L * (n + kDtPad) + 2 * (size_t)L * n + 2 * (2 * kDtPad - 1)) +
-         sizeof(int) * (2 * (size_t)L + 1);
+         sizeof(int) * (2 * (size_t)L + 1) + sizeof(float) * 3 * (kDtThreads / 32);
 }
 
 // Leftmost minimum of output d over the window |t| < KM of a padded line,
@@ -177,6 +180,44 @@ __device__ __forceinline__ void dt_scan_tile(const float *__restrict__ v_s, int 
   }
 }
 
+// Outputs of the tile when the argmin order is proven (every value finite,
+// one window K <= KM for the whole tile): the outputs d = c + q * i of every
+// line spread over the threads as in dt_scan_tile (consecutive outputs to
+// consecutive lanes: conflict-free shared-memory reads), with the per-offset
+// terms (a*t)*t and b*t (the same roundings as dt_f) held in registers; each
+// output is the leftmost minimum over its window, candidates in ascending order.
+template <int KM, int Q>
+__device__ __forceinline__ void dt_mono_tile(const float *__restrict__ v_s, int stride, int n, int nl, float a,
+                                             float b, float *__restrict__ o_s, int *__restrict__ g_s, int y0,
+                                             int par_y, int par_x) {
+  constexpr int W = 2 * KM - 1;
+  float At[W], Bt[W];
+#pragma unroll
+  for (int j = 0; j < W; j++) {
+    const float ft = (float)(KM - 1 - j);   // t = d - p for candidate j of a window
+    At[j] = a * ft * ft;
+    Bt[j] = b * ft;
+  }
+  const int m = (n + Q - 1) / Q;
+  const unsigned mg = 0xFFFFFFFFu / (unsigned)m + 1u;   // e / m for e < 2^32 / m
+  for (int e = threadIdx.x; e < nl * m; e += blockDim.x) {
+    const int l = __umulhi((unsigned)e, mg), i = e - l * m;
+    const int c = Q == 1 ? 0 : (((y0 + l) & 1) == par_y ? par_x : 1 - par_x);
+    const int d = c + Q * i;
+    if (d >= n) continue;
+    const float *v = v_s + l * stride + d - (KM - 1);   // padded: reads past the line see +inf
+    float best = INFINITY;
+    int s = 0;
+#pragma unroll
+    for (int j = 0; j < W; j++) {
+      const float f = (v[j] + At[j]) + Bt[j];
+      if (f < best) { best = f; s = j; }
+    }
+    o_s[l * n + d] = best;
+    g_s[l * n + d] = d - (KM - 1) + s;
+  }
+}
+
 // True when the computed leftmost argmin g(d) of a line is certainly
 // non-decreasing in d.  For s < p, the exact terms give
 //   [f_d(s) - f_d(p)] - [f_{d-1}(s) - f_{d-1}(p)] = 2a(p - s) >= 2a,
@@ -226,18 +267,24 @@ __global__ void __launch_bounds__(kDtThreads) k_dt(const DtJob *__restrict__ job
   const int cnt = nl * n;
   const unsigned magic = 0xFFFFFFFFu / (unsigned)n + 1u;   // e / n for e < 2^32 / n
 
-  // stage the tile, the pads and the per-offset terms
+  // stage the tile (pass 1: with each thread's value range), the pads and the per-offset terms
+  float vmin = INFINITY, vmax = -INFINITY, vabs = 0.f;
+  bool nan = false;   // fminf/fmaxf skip NaN
   if (PASS == 1) {
     const float *src = arena + J.in_off + (size_t)line0 * n;
     for (int e = tid; e < cnt; e += nth) {
       const int l = __umulhi((unsigned)e, magic), d = e - l * n;
-      v_s[l * stride + d] = J.negate ? -src[e] : src[e];   // inverse_Q (GPU_function.cu:695-794)
+      const float x = J.negate ? -src[e] : src[e];   // inverse_Q (GPU_function.cu:695-794)
+      v_s[l * stride + d] = x;
+      vmin = fminf(vmin, x); vmax = fmaxf(vmax, x); vabs = fmaxf(vabs, fabsf(x)); nan |= x != x;
     }
   } else {
     const float *tm = arena + J.tmpM_off;
     for (int e = tid; e < (n << lgL); e += nth) {
       const int l = e & (L - 1), x = e >> lgL;
-      if (l < nl) v_s[l * stride + x] = tm[(size_t)x * d0 + line0 + l];
+      if (l < nl) {
+        v_s[l * stride + x] = tm[(size_t)x * d0 + line0 + l];
+      }
     }
   }
   for (int i = tid; i < (nl + 1) * kDtPad; i += nth) {
@@ -252,19 +299,14 @@ __global__ void __launch_bounds__(kDtThreads) k_dt(const DtJob *__restrict__ job
   }
   __syncthreads();
 
-  // per-line window bound
+  // window bounds.  Pass 1 (many short lines per tile): one bound for the
+  // whole tile, from the tile's value range (a wider window than a line's own
+  // returns the same leftmost minimum, and the order proof only gets more
+  // conservative).  Pass 2 (a few long lines): a bound per line, each line's
+  // range reduced by a warp.
   const int lane = tid & 31, warp = tid >> 5;
-  for (int l = warp; l < nl; l += nth >> 5) {
-    const float *v = v_s + l * stride;
-    float vmin = INFINITY, vmax = -INFINITY, vabs = 0.f;
-    bool nan = false;   // fminf/fmaxf skip NaN
-    for (int i = lane; i < n; i += 32) {
-      const float x = v[i];
-      vmin = fminf(vmin, x);
-      vmax = fmaxf(vmax, x);
-      vabs = fmaxf(vabs, fabsf(x));
-      nan |= x != x;
-    }
+  int K = 0;
+  if (PASS == 1) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
       vmin = fminf(vmin, __shfl_xor_sync(0xffffffffu, vmin, o));
@@ -272,11 +314,53 @@ __global__ void __launch_bounds__(kDtThreads) k_dt(const DtJob *__restrict__ job
       vabs = fmaxf(vabs, __shfl_xor_sync(0xffffffffu, vabs, o));
     }
     nan = __any_sync(0xffffffffu, nan);
+    float *red = reinterpret_cast<float *>(mono_s + 1);   // [3][warps]: the warps' min, max, max |x| (-1: NaN)
     if (lane == 0) {
-      const int K = dt_window(vmin, vmax, vabs, a, b, n);
+      red[warp] = vmin;
+      red[kDtThreads / 32 + warp] = vmax;
+      red[2 * (kDtThreads / 32) + warp] = nan ? -1.0f : vabs;
+    }
+    __syncthreads();
+    float mn = INFINITY, mx = -INFINITY, ab = 0.f;
+    bool tile_nan = false;
+    for (int w = 0; w < (nth >> 5); w++) {
+      mn = fminf(mn, red[w]);
+      mx = fmaxf(mx, red[kDtThreads / 32 + w]);
+      const float aw = red[2 * (kDtThreads / 32) + w];
+      tile_nan |= aw < 0.f;
+      ab = fmaxf(ab, aw);
+    }
+    K = dt_window(mn, mx, ab, a, b, n);
+    if (tid == 0 && (tile_nan || !dt_monotone(ab, a, b, K))) *mono_s = 0;
+    for (int l = tid; l < nl; l += nth) {
       K_s[l] = K;
       bad_s[l] = 0;
-      if (nan || !dt_monotone(vabs, a, b, K)) *mono_s = 0;
+    }
+  } else {
+    for (int l = warp; l < nl; l += nth >> 5) {
+      const float *v = v_s + l * stride;
+      float lmin = INFINITY, lmax = -INFINITY, labs = 0.f;
+      bool lnan = false;
+      for (int i = lane; i < n; i += 32) {
+        const float x = v[i];
+        lmin = fminf(lmin, x);
+        lmax = fmaxf(lmax, x);
+        labs = fmaxf(labs, fabsf(x));
+        lnan |= x != x;
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        lmin = fminf(lmin, __shfl_xor_sync(0xffffffffu, lmin, o));
+        lmax = fmaxf(lmax, __shfl_xor_sync(0xffffffffu, lmax, o));
+        labs = fmaxf(labs, __shfl_xor_sync(0xffffffffu, labs, o));
+      }
+      lnan = __any_sync(0xffffffffu, lnan);
+      if (lane == 0) {
+        const int Kl = dt_window(lmin, lmax, labs, a, b, n);
+        K_s[l] = Kl;
+        bad_s[l] = 0;
+        if (lnan || !dt_monotone(labs, a, b, Kl)) *mono_s = 0;
+      }
     }
   }
   __syncthreads();
@@ -286,7 +370,21 @@ __global__ void __launch_bounds__(kDtThreads) k_dt(const DtJob *__restrict__ job
   const int q = (PASS == 2 && J.samp_m && J.samp_i) ? 2 : 1;
   if (*mono_s) {
     // the order holds: no check, no replay
-    dt_scan_tile(v_s, stride, n, nl, a, b, K_s, At, Bt, o_s, g_s, q, line0, J.par_y, J.par_x);
+    if (PASS == 1 && K <= 8) {   // (pass 2's long lines measured faster with a window per line)
+#define DT_MONO(KM)                                                                                       \
+  do {                                                                                                    \
+    if (q == 1) dt_mono_tile<KM, 1>(v_s, stride, n, nl, a, b, o_s, g_s, line0, J.par_y, J.par_x);          \
+    else dt_mono_tile<KM, 2>(v_s, stride, n, nl, a, b, o_s, g_s, line0, J.par_y, J.par_x);                 \
+  } while (0)
+      if (K <= 3) DT_MONO(3);
+      else if (K <= 4) DT_MONO(4);
+      else if (K <= 5) DT_MONO(5);
+      else if (K <= 6) DT_MONO(6);
+      else DT_MONO(8);
+#undef DT_MONO
+    } else {
+      dt_scan_tile(v_s, stride, n, nl, a, b, K_s, At, Bt, o_s, g_s, q, line0, J.par_y, J.par_x);
+    }
     __syncthreads();   // every output of the tile written before the stores read them
   } else {
     // every output's window, then the order check and the exact replay
