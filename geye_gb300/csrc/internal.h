@@ -230,6 +230,35 @@ void launch_resize_pass(const ResizeJob *d_jobs, int n_jobs, int max_cols, int v
                         const int *d_tap_si, const float *d_tap_alpha, float *arena, cudaStream_t s);
 // (job, block of histogram blocks) of every level's vote kernel
 void hog_vote_blocks(const std::vector<HogJob> &jobs, std::vector<int2> &blocks);
+
+// Batched front end (a batch of frames of any sizes): ingest, resize and HOG
+// of every level of every frame, each stage one persistent launch over a
+// ragged work list of (frame, job, chunk) items.  A frame's jobs are its own
+// plan's (the same device functions as the single-frame kernels).
+constexpr int kBatchMaxPhases = 16;
+struct BatchFrame {
+  const uint8_t *bgr;      // the frame on the device
+  int width, height, width_step;
+  float *arena;            // the frame's plan
+  uint8_t *arena16;
+  int img0_off;            // level-0 image planes (ingest output)
+  int n_phases;
+  const ResizeJob *vjobs[kBatchMaxPhases], *hjobs[kBatchMaxPhases];
+  const int *tap_start, *tap_si;
+  const float *tap_alpha;
+  const HogPixJob *pix;
+  const HogJob *hog;
+  const int2 *vote_blocks;
+};
+struct BatchItem {
+  int frame, job, chunk, pad;
+};
+enum BatchStage { kBatchIngest = 0, kBatchResizeV, kBatchResizeH, kBatchPix, kBatchVote, kBatchNorm, kBatchFeat };
+constexpr int kBatchColumns = 8;   // resize / pixel columns per item (a warp each)
+constexpr int kBatchCells = 256;   // corners / cells per item (a thread each)
+// one stage (phase: the resize phase) over n items
+void launch_batch_front(int stage, const BatchFrame *d_frames, const BatchItem *d_items, int n, int phase,
+                        cudaStream_t s);
 // corners: run the corner-factor pass (jobs with fast = 0 read its factors)
 void launch_hog(const HogJob *d_jobs, int n_jobs, const int2 *d_vote_blocks, int n_vote_blocks, int max_b0,
                 int max_b1, const HogPixJob *d_pix, int n_pix, int max_xe, float *arena, void *arena16,

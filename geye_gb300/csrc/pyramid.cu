@@ -12,6 +12,8 @@
 // atomics.
 #include <cuda_bf16.h>
 
+#include <algorithm>
+
 #include "internal.h"
 #include "tc_planes.h"
 
@@ -21,35 +23,43 @@ namespace geye {
 // ingest: u8 BGR rows -> float planes R,G,B column-major [c][w][h]
 // 32x32 pixel tile: rows read along x (coalesced bytes), planes written along y.
 // ----------------------------------------------------------------------------
-__global__ void k_ingest(const uint8_t *__restrict__ bgr, int width, int height, int width_step,
-                         float *__restrict__ planes) {
-  __shared__ float tile[3][32][33];
-  const int x0 = blockIdx.x * 32, y0 = blockIdx.y * 32;
-  for (int r = threadIdx.y; r < 32; r += blockDim.y) {
-    int y = y0 + r, x = x0 + threadIdx.x;
+// one 32x32 tile (x0, y0) by 256 threads (tx = lane, ty = warp)
+__device__ __forceinline__ void ingest_tile(const uint8_t *__restrict__ bgr, int width, int height, int width_step,
+                                            float *__restrict__ planes, int x0, int y0, int tx, int ty,
+                                            float (*tile)[32][33]) {
+  for (int r = ty; r < 32; r += 8) {
+    int y = y0 + r, x = x0 + tx;
     if (y < height && x < width) {
       const uint8_t *p = bgr + (size_t)y * width_step + 3 * x;
-      tile[0][threadIdx.x][r] = (float)p[2];   // R
-      tile[1][threadIdx.x][r] = (float)p[1];   // G
-      tile[2][threadIdx.x][r] = (float)p[0];   // B
+      tile[0][tx][r] = (float)p[2];   // R
+      tile[1][tx][r] = (float)p[1];   // G
+      tile[2][tx][r] = (float)p[0];   // B
     }
   }
   __syncthreads();
   const size_t SQ = (size_t)width * height;
-  for (int c = threadIdx.y; c < 32; c += blockDim.y) {
-    int x = x0 + c, y = y0 + threadIdx.x;
+  for (int c = ty; c < 32; c += 8) {
+    int x = x0 + c, y = y0 + tx;
     if (x < width && y < height) {
       size_t o = (size_t)x * height + y;
-      planes[o] = tile[0][c][threadIdx.x];
-      planes[SQ + o] = tile[1][c][threadIdx.x];
-      planes[2 * SQ + o] = tile[2][c][threadIdx.x];
+      planes[o] = tile[0][c][tx];
+      planes[SQ + o] = tile[1][c][tx];
+      planes[2 * SQ + o] = tile[2][c][tx];
     }
   }
+  __syncthreads();   // the tile is free for the next one
+}
+
+__global__ void __launch_bounds__(256) k_ingest(const uint8_t *__restrict__ bgr, int width, int height,
+                                                int width_step, float *__restrict__ planes) {
+  __shared__ float tile[3][32][33];
+  ingest_tile(bgr, width, height, width_step, planes, blockIdx.x * 32, blockIdx.y * 32, threadIdx.x & 31,
+              threadIdx.x >> 5, tile);
 }
 
 void launch_ingest(const uint8_t *bgr, int width, int height, int width_step, float *planes, cudaStream_t s) {
-  dim3 grid((width + 31) / 32, (height + 31) / 32), block(32, 8);
-  k_ingest<<<grid, block, 0, s>>>(bgr, width, height, width_step, planes);
+  dim3 grid((width + 31) / 32, (height + 31) / 32);
+  k_ingest<<<grid, 256, 0, s>>>(bgr, width, height, width_step, planes);
 }
 
 // ----------------------------------------------------------------------------
@@ -63,12 +73,10 @@ void launch_ingest(const uint8_t *bgr, int width, int height, int width_step, fl
 // ----------------------------------------------------------------------------
 constexpr int kResizeWarps = 4;
 
-__global__ void __launch_bounds__(kResizeWarps * 32) k_resize_pass(const ResizeJob *__restrict__ jobs, int vertical,
-                                                                   const int *__restrict__ tap_start,
-                                                                   const int *__restrict__ tap_si,
-                                                                   const float *__restrict__ tap_alpha,
-                                                                   float *__restrict__ arena) {
-  const ResizeJob J = jobs[blockIdx.y];
+// output column x of one pass (all three channels) by one warp
+__device__ __forceinline__ void resize_column(const ResizeJob &J, int vertical, const int *__restrict__ tap_start,
+                                              const int *__restrict__ tap_si, const float *__restrict__ tap_alpha,
+                                              float *__restrict__ arena, int x) {
   const float *src = arena + J.src_off;
   float *dst = arena + J.dst_off;
   const int *ts = tap_start + J.tap_start_off;
@@ -76,7 +84,7 @@ __global__ void __launch_bounds__(kResizeWarps * 32) k_resize_pass(const ResizeJ
   const float *al = tap_alpha + J.tap_off;
   const int lane = threadIdx.x & 31;
   const size_t src_plane = (size_t)J.src_w * J.src_h, dst_plane = (size_t)J.dst_w * J.dst_h;
-  for (int x = blockIdx.x * kResizeWarps + (threadIdx.x >> 5); x < J.dst_w; x += gridDim.x * kResizeWarps) {
+  {
     float *out = dst + (size_t)x * J.dst_h;
     if (vertical) {
       const float *col = src + (size_t)x * J.src_h;
@@ -139,6 +147,16 @@ __global__ void __launch_bounds__(kResizeWarps * 32) k_resize_pass(const ResizeJ
       }
     }
   }
+}
+
+__global__ void __launch_bounds__(kResizeWarps * 32) k_resize_pass(const ResizeJob *__restrict__ jobs, int vertical,
+                                                                   const int *__restrict__ tap_start,
+                                                                   const int *__restrict__ tap_si,
+                                                                   const float *__restrict__ tap_alpha,
+                                                                   float *__restrict__ arena) {
+  const ResizeJob J = jobs[blockIdx.y];
+  for (int x = blockIdx.x * kResizeWarps + (threadIdx.x >> 5); x < J.dst_w; x += gridDim.x * kResizeWarps)
+    resize_column(J, vertical, tap_start, tap_si, tap_alpha, arena, x);
 }
 
 // max_cols: the largest output column count (dst_w) of the phase's jobs
@@ -210,14 +228,12 @@ __device__ __forceinline__ void hog_interp_pow2(int p, float inv_sbin, int &ip, 
 // run along y; out [x * Y + y] for 1 <= x < xe, 1 <= y < ye.
 constexpr int kPixWarps = 8;
 
-__global__ void __launch_bounds__(kPixWarps * 32) k_hog_pix(const HogPixJob *__restrict__ jobs,
-                                                           float *__restrict__ arena) {
-  const HogPixJob J = jobs[blockIdx.y];
+__device__ __forceinline__ void hog_pix_column(const HogPixJob &J, float *__restrict__ arena, int x) {
   const float *img = arena + J.img_off;
   float *mag = arena + J.mag_off;
   uint8_t *bin = reinterpret_cast<uint8_t *>(arena + J.bin_off);
   const int lane = threadIdx.x & 31;
-  for (int x = 1 + blockIdx.x * kPixWarps + (threadIdx.x >> 5); x < J.xe; x += gridDim.x * kPixWarps) {
+  {
     for (int y = 1 + lane; y < J.ye; y += 64) {   // two pixels per lane in flight
       const int y2 = y + 32;
       int b, b2 = 0;
@@ -232,6 +248,13 @@ __global__ void __launch_bounds__(kPixWarps * 32) k_hog_pix(const HogPixJob *__r
       }
     }
   }
+}
+
+__global__ void __launch_bounds__(kPixWarps * 32) k_hog_pix(const HogPixJob *__restrict__ jobs,
+                                                           float *__restrict__ arena) {
+  const HogPixJob J = jobs[blockIdx.y];
+  for (int x = 1 + blockIdx.x * kPixWarps + (threadIdx.x >> 5); x < J.xe; x += gridDim.x * kPixWarps)
+    hog_pix_column(J, arena, x);
 }
 
 // Pass 2: one thread per histogram block sums its votes in the reference's
@@ -280,14 +303,9 @@ __device__ __forceinline__ void hog_vote_pow2(float *myh, const float *__restric
 
 // One CUDA block per entry of `blocks` (job, block of kVoteThreads histogram
 // blocks): exactly the blocks every level needs.
-__global__ void __launch_bounds__(kVoteThreads, 4) k_hog_vote(const HogJob *__restrict__ jobs,
-                                                             const int2 *__restrict__ blocks,
-                                                             float *__restrict__ arena) {
-  __shared__ float hist_s[18 * kVoteThreads];
-  const int2 blk = blocks[blockIdx.x];
-  const HogJob J = jobs[blk.x];
+// histogram block pos of one level by one thread (hist_s: the block's [18][kVoteThreads] bins)
+__device__ __forceinline__ void hog_vote_one(const HogJob &J, float *__restrict__ arena, int pos, float *hist_s) {
   const int nb = J.b0 * J.b1;
-  const int pos = blk.y * kVoteThreads + threadIdx.x;
   float *myh = hist_s + threadIdx.x;   // bin o at myh[o * kVoteThreads]
 #pragma unroll
   for (int o = 0; o < 18; o++) myh[o * kVoteThreads] = 0.f;
@@ -351,6 +369,14 @@ __global__ void __launch_bounds__(kVoteThreads, 4) k_hog_vote(const HogJob *__re
   hist[(size_t)18 * nb + pos] = norm;
 }
 
+__global__ void __launch_bounds__(kVoteThreads, 4) k_hog_vote(const HogJob *__restrict__ jobs,
+                                                             const int2 *__restrict__ blocks,
+                                                             float *__restrict__ arena) {
+  __shared__ float hist_s[18 * kVoteThreads];
+  const int2 blk = blocks[blockIdx.x];
+  hog_vote_one(jobs[blk.x], arena, blk.y * kVoteThreads + threadIdx.x, hist_s);
+}
+
 // 31 features per output cell (featurepyramid.cpp:421-487), written as 32
 // floats [pos][32] (channel 31 = 0), plus an optional copy as the tensor-core
 // convolution's channel planes (tc_planes.h).
@@ -358,28 +384,34 @@ __global__ void __launch_bounds__(kVoteThreads, 4) k_hog_vote(const HogJob *__re
 // 1 / sqrt(e(x,y) + e(x,y+1) + e(x+1,y) + e(x+1,y+1) + 0.0001) in the reference's
 // expression (float sum, double root and division, rounded to float), once per
 // corner: each is shared by the four output cells around it.
-__global__ void k_hog_norm(const HogJob *__restrict__ jobs, float *__restrict__ arena) {
-  const HogJob J = jobs[blockIdx.y];
-  const int C0 = J.fs0 + 1, nc = C0 * (J.fs1 + 1);
+__device__ __forceinline__ int hog_corners(const HogJob &J) { return (J.fs0 + 1) * (J.fs1 + 1); }
+
+__device__ __forceinline__ void hog_norm_one(const HogJob &J, float *__restrict__ arena, int i) {
+  const int C0 = J.fs0 + 1;
   const int b0 = J.b0, nb = J.b0 * J.b1;
   const float *norm = arena + J.hist_off + (size_t)18 * nb;
   float *N = arena + J.corner_off;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nc; i += gridDim.x * blockDim.x) {
-    const int y = i % C0, x = i / C0;
-    const float *p = norm + x * b0 + y;
-    N[i] = 1.0 / sqrt(p[0] + p[1] + p[b0] + p[b0 + 1] + 0.0001);
-  }
+  const int y = i % C0, x = i / C0;
+  const float *p = norm + x * b0 + y;
+  N[i] = 1.0 / sqrt(p[0] + p[1] + p[b0] + p[b0 + 1] + 0.0001);
 }
 
-__global__ void k_hog_feat(const HogJob *__restrict__ jobs, float *__restrict__ arena, uint8_t *__restrict__ arena16) {
+__global__ void k_hog_norm(const HogJob *__restrict__ jobs, float *__restrict__ arena) {
   const HogJob J = jobs[blockIdx.y];
+  const int nc = hog_corners(J);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nc; i += gridDim.x * blockDim.x) hog_norm_one(J, arena, i);
+}
+
+// output cell i of one level
+__device__ __forceinline__ void hog_feat_one(const HogJob &J, float *__restrict__ arena,
+                                             uint8_t *__restrict__ arena16, int i) {
   const int ncell = J.fs0 * J.fs1;
   const int b0 = J.b0, nb = J.b0 * J.b1;
   const float *hist = arena + J.hist_off;
   const float *N = arena + J.corner_off;
   const int C0 = J.fs0 + 1;
   float *feat = arena + J.feat_off;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < ncell; i += gridDim.x * blockDim.x) {
+  {
     const int y = i % J.fs0, x = i / J.fs0;
     float n1, n2, n3, n4;
     if (J.fast) {
@@ -446,6 +478,68 @@ __global__ void k_hog_feat(const HogJob *__restrict__ jobs, float *__restrict__ 
       else if (J.tc_planes == 2) tc_store_planes<2>(out, planes, plane, i);
       if (J.feat16lo_off >= 0) tc_store_planes_lo(out, arena16 + 2 * (size_t)J.feat16lo_off, plane, i);
     }
+  }
+}
+
+__global__ void k_hog_feat(const HogJob *__restrict__ jobs, float *__restrict__ arena, uint8_t *__restrict__ arena16) {
+  const HogJob J = jobs[blockIdx.y];
+  const int ncell = J.fs0 * J.fs1;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < ncell; i += gridDim.x * blockDim.x)
+    hog_feat_one(J, arena, arena16, i);
+}
+
+// ----------------------------------------------------------------------------
+// batched front end: persistent CTAs over a stage's (frame, job, chunk) items
+// ----------------------------------------------------------------------------
+template <int STAGE>
+__global__ void __launch_bounds__(256) k_batch_front(const BatchFrame *__restrict__ frames,
+                                                     const BatchItem *__restrict__ items, int n, int phase) {
+  __shared__ float sm[18 * kVoteThreads];   // a vote block's bins, or an ingest tile ([3][32][33] floats)
+  const int tid = threadIdx.x, warp = tid >> 5;
+  for (int it = blockIdx.x; it < n; it += gridDim.x) {
+    const BatchItem I = items[it];
+    const BatchFrame &F = frames[I.frame];
+    if (STAGE == kBatchIngest) {
+      ingest_tile(F.bgr, F.width, F.height, F.width_step, F.arena + F.img0_off, 32 * I.job, 32 * I.chunk, tid & 31,
+                  warp, reinterpret_cast<float (*)[32][33]>(sm));
+    } else if (STAGE == kBatchResizeV || STAGE == kBatchResizeH) {
+      const ResizeJob J = (STAGE == kBatchResizeV ? F.vjobs[phase] : F.hjobs[phase])[I.job];
+      const int x = I.chunk * kBatchColumns + warp;
+      if (x < J.dst_w) resize_column(J, STAGE == kBatchResizeV, F.tap_start, F.tap_si, F.tap_alpha, F.arena, x);
+    } else if (STAGE == kBatchPix) {
+      const HogPixJob J = F.pix[I.job];
+      const int x = 1 + I.chunk * kBatchColumns + warp;
+      if (x < J.xe) hog_pix_column(J, F.arena, x);
+    } else if (STAGE == kBatchVote) {
+      const int2 blk = F.vote_blocks[I.job];
+      hog_vote_one(F.hog[blk.x], F.arena, blk.y * kVoteThreads + tid, sm);
+    } else if (STAGE == kBatchNorm) {
+      const HogJob J = F.hog[I.job];
+      const int i = I.chunk * kBatchCells + tid;
+      if (i < hog_corners(J)) hog_norm_one(J, F.arena, i);
+    } else {
+      const HogJob J = F.hog[I.job];
+      const int i = I.chunk * kBatchCells + tid;
+      if (i < J.fs0 * J.fs1) hog_feat_one(J, F.arena, F.arena16, i);
+    }
+  }
+}
+
+void launch_batch_front(int stage, const BatchFrame *d_frames, const BatchItem *d_items, int n, int phase,
+                        cudaStream_t s) {
+  if (n <= 0) return;
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int grid = std::max(1, std::min(n, 4 * std::max(sms, 1)));   // persistent: a few CTAs per SM
+  switch (stage) {
+    case kBatchIngest: k_batch_front<kBatchIngest><<<grid, 256, 0, s>>>(d_frames, d_items, n, phase); break;
+    case kBatchResizeV: k_batch_front<kBatchResizeV><<<grid, 256, 0, s>>>(d_frames, d_items, n, phase); break;
+    case kBatchResizeH: k_batch_front<kBatchResizeH><<<grid, 256, 0, s>>>(d_frames, d_items, n, phase); break;
+    case kBatchPix: k_batch_front<kBatchPix><<<grid, 256, 0, s>>>(d_frames, d_items, n, phase); break;
+    case kBatchVote: k_batch_front<kBatchVote><<<grid, 256, 0, s>>>(d_frames, d_items, n, phase); break;
+    case kBatchNorm: k_batch_front<kBatchNorm><<<grid, 256, 0, s>>>(d_frames, d_items, n, phase); break;
+    default: k_batch_front<kBatchFeat><<<grid, 256, 0, s>>>(d_frames, d_items, n, phase); break;
   }
 }
 

@@ -1025,9 +1025,9 @@ geye_status run_nms(geye_ctx *ctx, Plan &P, int n_models, float overlap) {
 // it is captured once per (plan, threshold, overlap, timing) as a CUDA graph.
 static geye_status run_body(geye_ctx *ctx, Plan &P, float thresh, float overlap) {
   StageTimer T(ctx);
-  GEYE_TRY(run_resize(ctx, P));
+  if (!ctx->front_external) GEYE_TRY(run_resize(ctx, P));
   T.mark(1);
-  GEYE_TRY(run_hog(ctx, P));
+  if (!ctx->front_external) GEYE_TRY(run_hog(ctx, P));
   T.mark(2);
   const bool tc = ctx->conv_mode != GEYE_CONV_FP32;
   if (tc) GEYE_TRY(run_conv_tc(ctx, P));   // every model's filters in one launch
@@ -1132,7 +1132,7 @@ geye_status run_frame(geye_ctx *ctx, Plan &P, const uint8_t *d_bgr, int width_st
   ctx->launches = 0;
   CUDA_TRY(cudaMemsetAsync(P.d_small.p, 0, 4096, ctx->stream));
   T.mark(0);
-  GEYE_TRY(run_ingest(ctx, P, d_bgr, width_step));
+  if (!ctx->front_external) GEYE_TRY(run_ingest(ctx, P, d_bgr, width_step));
   for (size_t mi = 0; mi < P.models.size(); mi++)
     GEYE_TRY(ascore_init(ctx, P, (int)mi, h_ascore_init ? h_ascore_init[mi] : nullptr));
   if (ctx->use_graphs) GEYE_TRY(run_body_graph(ctx, P, thresh, overlap));

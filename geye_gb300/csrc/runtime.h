@@ -231,6 +231,7 @@ struct geye_ctx {
   int launches = 0;
   bool use_graphs = true;   // replay the frame as a CUDA graph (GEYE_NO_GRAPHS=1 at creation: plain launches)
   int nms_order = geye::kNmsOrderKey;   // geye_ctx_set_nms_order
+  bool front_external = false;   // a batch's front end ran ingest, resize and HOG of the frame already
   bool capturing = false;
   // fault injection (host side)
   std::string inject_op;

@@ -46,12 +46,14 @@ static long long now_ns() {
 
 // queue everything of one frame on the context's stream (the frame already in P.h_bgr)
 // (from h_src, pinned and kept until the frame completes, when given)
+// (copy_in false: the frame is on the device already)
 static geye_status enqueue_frame(geye_ctx *ctx, Plan &P, float thresh, float overlap, TrackerSet *trk, int stream,
                                  cudaEvent_t after, cudaEvent_t tracked, bool record_done = true,
-                                 const void *h_src = nullptr) {
+                                 const void *h_src = nullptr, bool copy_in = true) {
   const int n_models = (int)P.models.size();
-  CUDA_TRY(cudaMemcpyAsync(P.d_bgr.p, h_src ? h_src : P.h_bgr, (size_t)3 * P.width * P.height,
-                           cudaMemcpyHostToDevice, ctx->stream));
+  if (copy_in)
+    CUDA_TRY(cudaMemcpyAsync(P.d_bgr.p, h_src ? h_src : P.h_bgr, (size_t)3 * P.width * P.height,
+                             cudaMemcpyHostToDevice, ctx->stream));
   GEYE_TRY(run_frame(ctx, P, P.d_bgr.as<uint8_t>(), 3 * P.width, thresh, overlap, nullptr));
   if (trk) {
     if (after) CUDA_TRY(cudaStreamWaitEvent(ctx->stream, after, 0));
@@ -578,16 +580,132 @@ struct geye_batch {
   int max_frames = 0;
   std::vector<geye_ctx *> lanes;
   cudaStream_t stream = nullptr;
-  cudaEvent_t fork = nullptr;
+  cudaEvent_t fork = nullptr, front_done = nullptr;
   std::vector<cudaEvent_t> joins;
   struct Graph {
     cudaGraphExec_t exec = nullptr;
     int kernels = 0;
+    void *d_tables = nullptr;   // the batched front end's frame table and work items (read by the graph)
+    size_t frames_bytes = 0;    // the frame table's share of d_tables, items after it
+    int n_phases = 0;           // resize phases of the batch's deepest pyramid
+    std::vector<int> count, offset;   // items per list (front_list) and their offsets
   };
   std::map<std::string, Graph> graphs;   // by lane sizes, thresh, overlap
   int last_kernels = 0;
   cudaEvent_t t0 = nullptr, t1 = nullptr;   // around the last graph launch
 };
+
+namespace {
+
+// The batched front end's tables for one batch key: every frame's plan
+// pointers and, per stage, the ragged list of (frame, job, chunk) items,
+// in one device buffer that the batch graph reads.  Lists: ingest, vertical
+// and horizontal resize per phase, pixels, votes, corner norms, features.
+int front_list(int stage, int phase) {   // list index of a stage (resize: per phase)
+  if (stage == kBatchIngest) return 0;
+  if (stage == kBatchResizeV) return 1 + 2 * phase;
+  if (stage == kBatchResizeH) return 2 + 2 * phase;
+  return 1 + 2 * kBatchMaxPhases + (stage - kBatchPix);
+}
+
+geye_status batch_front_tables(geye_batch *b, const std::vector<Plan *> &plans, geye_batch::Graph &g) {
+  const int nf = (int)plans.size();
+  const int n_lists = 1 + 2 * kBatchMaxPhases + 4;
+  std::vector<std::vector<BatchItem>> L(n_lists);
+  std::vector<BatchFrame> fr(nf);
+  int max_ph = 0;
+  for (int f = 0; f < nf; f++) {
+    const Plan &P = *plans[f];
+    ARG_CHECK((int)P.vjobs.size() <= kBatchMaxPhases, "batch: too many resize phases");
+    BatchFrame &F = fr[f];
+    F = BatchFrame{};
+    F.bgr = P.d_bgr.as<uint8_t>();
+    F.width = P.width;
+    F.height = P.height;
+    F.width_step = 3 * P.width;
+    F.arena = P.arena.as<float>();
+    F.arena16 = static_cast<uint8_t *>(P.arena16.p);
+    F.img0_off = P.lv[0].img_off;
+    F.n_phases = (int)P.vjobs.size();
+    for (int ph = 0; ph < F.n_phases; ph++) {
+      F.vjobs[ph] = P.d_vjobs[ph].as<ResizeJob>();
+      F.hjobs[ph] = P.d_hjobs[ph].as<ResizeJob>();
+    }
+    F.tap_start = P.d_tap_start.as<int>();
+    F.tap_si = P.d_tap_si.as<int>();
+    F.tap_alpha = P.d_tap_alpha.as<float>();
+    F.pix = P.d_pix_jobs.as<HogPixJob>();
+    F.hog = P.d_hog_jobs.as<HogJob>();
+    F.vote_blocks = P.d_hog_vote_blocks.as<int2>();
+    max_ph = std::max(max_ph, F.n_phases);
+    for (int ty = 0; ty < (P.height + 31) / 32; ty++)
+      for (int tx = 0; tx < (P.width + 31) / 32; tx++) L[0].push_back(BatchItem{f, tx, ty, 0});
+    for (int ph = 0; ph < F.n_phases; ph++)
+      for (size_t j = 0; j < P.vjobs[ph].size(); j++) {
+        for (int c = 0; c * kBatchColumns < P.vjobs[ph][j].dst_w; c++)
+          L[front_list(kBatchResizeV, ph)].push_back(BatchItem{f, (int)j, c, 0});
+        for (int c = 0; c * kBatchColumns < P.hjobs[ph][j].dst_w; c++)
+          L[front_list(kBatchResizeH, ph)].push_back(BatchItem{f, (int)j, c, 0});
+      }
+    for (size_t j = 0; j < P.pix_jobs.size(); j++)
+      for (int c = 0; 1 + c * kBatchColumns < P.pix_jobs[j].xe; c++)
+        L[front_list(kBatchPix, 0)].push_back(BatchItem{f, (int)j, c, 0});
+    for (int k = 0; k < P.hog_vote_nblocks; k++) L[front_list(kBatchVote, 0)].push_back(BatchItem{f, k, 0, 0});
+    const bool fast = !P.hog_jobs.empty() && P.hog_jobs[0].fast;
+    for (size_t j = 0; j < P.hog_jobs.size(); j++) {
+      const HogJob &J = P.hog_jobs[j];
+      if (!fast)
+        for (int c = 0; c * kBatchCells < (J.fs0 + 1) * (J.fs1 + 1); c++)
+          L[front_list(kBatchNorm, 0)].push_back(BatchItem{f, (int)j, c, 0});
+      for (int c = 0; c * kBatchCells < J.fs0 * J.fs1; c++)
+        L[front_list(kBatchFeat, 0)].push_back(BatchItem{f, (int)j, c, 0});
+    }
+  }
+  g.n_phases = max_ph;
+  g.frames_bytes = ((sizeof(BatchFrame) * nf + 255) / 256) * 256;
+  g.count.clear();
+  g.offset.clear();
+  size_t items = 0;
+  for (auto &l : L) {
+    g.offset.push_back((int)items);
+    g.count.push_back((int)l.size());
+    items += l.size();
+  }
+  std::vector<uint8_t> host(g.frames_bytes + sizeof(BatchItem) * std::max<size_t>(items, 1));
+  memcpy(host.data(), fr.data(), sizeof(BatchFrame) * nf);
+  BatchItem *it = reinterpret_cast<BatchItem *>(host.data() + g.frames_bytes);
+  for (auto &l : L) {
+    if (!l.empty()) memcpy(it, l.data(), sizeof(BatchItem) * l.size());
+    it += l.size();
+  }
+  if (g.d_tables) cudaFree(g.d_tables);
+  g.d_tables = nullptr;
+  CUDA_TRY(cudaMalloc(&g.d_tables, host.size()));
+  CUDA_TRY(cudaMemcpy(g.d_tables, host.data(), host.size(), cudaMemcpyHostToDevice));
+  (void)b;
+  return GEYE_OK;
+}
+
+// the stages in order on the batch stream (inside its capture)
+void launch_batch_tables(geye_batch *b, geye_batch::Graph &g) {
+  const BatchFrame *frames = static_cast<const BatchFrame *>(g.d_tables);
+  const BatchItem *items = reinterpret_cast<const BatchItem *>(static_cast<uint8_t *>(g.d_tables) + g.frames_bytes);
+  auto run = [&](int stage, int phase) {
+    const int l = front_list(stage, phase);
+    launch_batch_front(stage, frames, items + g.offset[l], g.count[l], phase, b->stream);
+  };
+  run(kBatchIngest, 0);
+  for (int ph = 0; ph < g.n_phases; ph++) {
+    run(kBatchResizeV, ph);
+    run(kBatchResizeH, ph);
+  }
+  run(kBatchPix, 0);
+  run(kBatchVote, 0);
+  run(kBatchNorm, 0);
+  run(kBatchFeat, 0);
+}
+
+}  // namespace
 
 extern "C" {
 
@@ -605,10 +723,12 @@ geye_status geye_batch_create(int device, geye_model *const *models, int n_model
   b->max_frames = max_frames;
   cudaError_t e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->front_done, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaEventCreate(&b->t0);
   if (e == cudaSuccess) e = cudaEventCreate(&b->t1);
   if (e != cudaSuccess) {
     if (b->t0) cudaEventDestroy(b->t0);
+    if (b->front_done) cudaEventDestroy(b->front_done);
     if (b->fork) cudaEventDestroy(b->fork);
     if (b->stream) cudaStreamDestroy(b->stream);
     delete b;
@@ -623,9 +743,12 @@ geye_status geye_batch_destroy(geye_batch *b) {
   if (!b) return GEYE_OK;
   cudaSetDevice(b->device);
   cudaStreamSynchronize(b->stream);
-  for (auto &g : b->graphs)
+  for (auto &g : b->graphs) {
     if (g.second.exec) cudaGraphExecDestroy(g.second.exec);
+    if (g.second.d_tables) cudaFree(g.second.d_tables);
+  }
   for (auto e : b->joins) cudaEventDestroy(e);
+  if (b->front_done) cudaEventDestroy(b->front_done);
   for (auto *c : b->lanes) geye_ctx_destroy(c);
   cudaEventDestroy(b->fork);
   cudaEventDestroy(b->t0);
@@ -672,18 +795,30 @@ geye_status geye_batch_run(geye_batch *b, int n_frames, const uint8_t *const *bg
   }
   geye_batch::Graph &g = b->graphs[key];
   if (!g.exec) {
+    GEYE_TRY(batch_front_tables(b, plans, g));
     cudaGraph_t graph = nullptr;
     CUDA_TRY(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeRelaxed));
     geye_status st = GEYE_OK;
-    cudaError_t e = cudaEventRecord(b->fork, b->stream);
+    cudaError_t e = cudaSuccess;
+    // every frame in, then the batched front end: one persistent launch per stage for all frames
+    for (int i = 0; i < n_frames && e == cudaSuccess; i++)
+      e = cudaMemcpyAsync(plans[i]->d_bgr.p, plans[i]->h_bgr, (size_t)3 * widths[i] * heights[i],
+                          cudaMemcpyHostToDevice, b->stream);
+    if (e == cudaSuccess) {
+      launch_batch_tables(b, g);
+      e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaEventRecord(b->front_done, b->stream);
     for (int i = 0; i < n_frames && st == GEYE_OK && e == cudaSuccess; i++) {
       geye_ctx *c = b->lanes[i];
-      e = cudaStreamWaitEvent(c->stream, b->fork, 0);
+      e = cudaStreamWaitEvent(c->stream, b->front_done, 0);
       if (e != cudaSuccess) break;
       const bool graphs = c->use_graphs;
       c->use_graphs = false;   // the lane's kernels go straight into the batch graph
       c->capturing = true;
-      st = enqueue_frame(c, *plans[i], thresh, overlap, nullptr, 0, nullptr, nullptr, false);
+      c->front_external = true;
+      st = enqueue_frame(c, *plans[i], thresh, overlap, nullptr, 0, nullptr, nullptr, false, nullptr, false);
+      c->front_external = false;
       c->capturing = false;
       c->use_graphs = graphs;
       c->pending = nullptr;
@@ -693,6 +828,7 @@ geye_status geye_batch_run(geye_batch *b, int n_frames, const uint8_t *const *bg
     const cudaError_t ec = cudaStreamEndCapture(b->stream, &graph);
     if (st != GEYE_OK || e != cudaSuccess || ec != cudaSuccess) {
       if (graph) cudaGraphDestroy(graph);
+      if (g.d_tables) cudaFree(g.d_tables);
       b->graphs.erase(key);
       if (st != GEYE_OK) return st;
       set_error(std::string("batch graph capture: ") + cudaGetErrorString(e != cudaSuccess ? e : ec));
@@ -711,6 +847,7 @@ geye_status geye_batch_run(geye_batch *b, int n_frames, const uint8_t *const *bg
     cudaGraphDestroy(graph);
     if (ie != cudaSuccess) {
       g.exec = nullptr;
+      if (g.d_tables) cudaFree(g.d_tables);
       b->graphs.erase(key);
       set_error(std::string("batch graph instantiate: ") + cudaGetErrorString(ie));
       return GEYE_ERR_CUDA;
