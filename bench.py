@@ -582,7 +582,7 @@ def run_served(args, wl):
     clocks = clk.summary()
     # the 64-camera serving workloads, a few seconds each (open loop, Poisson arrivals)
     serving = None
-    if rank == 0 and world == 1:
+    if rank == 0 and world == 1 and not args.no_serving:
         serving = {}
         for name in ("serve64_640x480_bf16", "serve64_mixed_bf16"):
             sw = dict(WORKLOADS[name])
@@ -804,6 +804,7 @@ def main():
     ap.add_argument("--impl", default="geye", choices=["geye", "reference"])
     ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-serving", action="store_true", help="served workload: skip the 64-camera simulations")
     ap.add_argument("--slots", type=int, default=0, help="frames in flight for the served workload (0: workload default)")
     args = ap.parse_args()
     wl = WORKLOADS[args.workload]

@@ -316,8 +316,7 @@ __host__ __device__ inline size_t nms_model_words(int cap) {
 constexpr int kNmsRounds = 8, kNmsMaxRounds = 64;
 constexpr int kNmsOrderKey = 0, kNmsOrderQuicksort = 1;
 // aux: null for plain launches on s; when s is capturing a graph, a second
-// stream that captures the bodies of the conditional nodes (the greedy rounds
-// as a while node, the quicksort-order pass as an if node)
+// stream that captures the body of the quicksort-order pass's if node
 // extent: box coordinates in [0, extent) spread over the pick masks' cells
 // (any value is exact; boxes outside share the edge cells)
 cudaError_t launch_nms_batch(const float *boxes, const int *d_num, int n_models, int GL, float overlap,

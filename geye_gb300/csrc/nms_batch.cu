@@ -419,26 +419,14 @@ __device__ void pass_words(Slots &S, const float (*pk)[kBatch], int np, int pick
 // that share a row cell and a column cell with it (the union of the picks
 // listed on its cell span, per axis, from a sparse table of spans of 2^l
 // cells), in pick order; the first that suppresses it removes it and is
-// flagged.  loop: inside a frame graph's while node, block (0, 0) sets the
-// node's condition for the next round: a model is not done and has taken
-// fewer than max_batches batches (the finish kernel takes any rest).
+// flagged.
 struct PassSmem {
   float pk[5][kBatch];
   unsigned tab[2][kNmsLevels][kNmsCells][kBW];
 };
 
-__global__ void __launch_bounds__(kPassNT) k_nms_pass(int cap, int *si, float *sf, float overlap, float cell_inv,
-                                                      cudaGraphConditionalHandle loop, int use_loop,
-                                                      int max_batches) {
+__global__ void __launch_bounds__(kPassNT) k_nms_pass(int cap, int *si, float *sf, float overlap, float cell_inv) {
   __shared__ PassSmem Z;
-  if (use_loop && blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) {
-    unsigned more = 0;
-    for (int m = 0; m < (int)gridDim.y; m++) {
-      const BatchState &b = *slots(si, sf, m, cap).st;
-      more |= (!b.done && b.batches < max_batches) ? 1u : 0u;
-    }
-    cudaGraphSetConditional(loop, more);
-  }
   Slots S = slots(si, sf, blockIdx.y, cap);
   const BatchState &st = *S.st;
   if (st.done) return;
@@ -645,36 +633,20 @@ static cudaError_t end_conditional(cudaStream_t aux) {
   return cudaGetLastError();   // a launch inside the body
 }
 
-constexpr int kNmsLoopBatches = 512;   // while-node rounds before the finish kernel takes the rest
-
-// gather, the greedy rounds and the finish, in the order the sort left in (val, ord).
-// aux non-null: s is capturing a graph, and the rounds are a while node (as many
-// as the frame needs) instead of `rounds` launches
+// gather, the greedy rounds and the finish, in the order the sort left in (val, ord)
 template <bool KEY_ORDER>
-static cudaError_t launch_greedy(const float *boxes, int n_models, int GL, float overlap, float cell_inv, int cap,
-                                 int *si, float *sf, float *out, int *d_kept, int *err, long long *diag, int rounds,
-                                 int *rounds_used, int *need, cudaStream_t s, cudaStream_t aux) {
+static void launch_greedy(const float *boxes, int n_models, int GL, float overlap, float cell_inv, int cap, int *si,
+                          float *sf, float *out, int *d_kept, int *err, long long *diag, int rounds,
+                          int *rounds_used, int *need, cudaStream_t s) {
   k_nms_gather<<<dim3((cap + kPassNT - 1) / kPassNT, n_models), kPassNT, 0, s>>>(boxes, GL, cap, si, sf);
   const int words = (cap + 31) / 32;
   const int pass_blocks = std::max(1, std::min((words + kPassNT / 32 - 1) / (kPassNT / 32), 512));
-  if (aux) {
-    cudaGraphConditionalHandle loop;
-    cudaError_t e = cond_handle(s, 1u, &loop);
-    if (e == cudaSuccess) e = begin_conditional(s, aux, cudaGraphCondTypeWhile, loop);
-    if (e != cudaSuccess) return e;
-    k_nms_resolve<KEY_ORDER><<<n_models, kSortNT, 0, aux>>>(cap, si, sf, overlap, cell_inv, need);
-    k_nms_pass<<<dim3(pass_blocks, n_models), kPassNT, 0, aux>>>(cap, si, sf, overlap, cell_inv, loop, 1,
-                                                                 kNmsLoopBatches);
-    if ((e = end_conditional(aux)) != cudaSuccess) return e;
-  } else {
-    for (int r = 0; r < rounds; r++) {
-      k_nms_resolve<KEY_ORDER><<<n_models, kSortNT, 0, s>>>(cap, si, sf, overlap, cell_inv, need);
-      k_nms_pass<<<dim3(pass_blocks, n_models), kPassNT, 0, s>>>(cap, si, sf, overlap, cell_inv, 0, 0, 0);
-    }
+  for (int r = 0; r < rounds; r++) {
+    k_nms_resolve<KEY_ORDER><<<n_models, kSortNT, 0, s>>>(cap, si, sf, overlap, cell_inv, need);
+    k_nms_pass<<<dim3(pass_blocks, n_models), kPassNT, 0, s>>>(cap, si, sf, overlap, cell_inv);
   }
   k_nms_finish<KEY_ORDER><<<n_models, kSortNT, 0, s>>>(boxes, GL, cap, si, sf, overlap, out, d_kept, err, diag,
                                                        rounds_used, need, cell_inv);
-  return cudaSuccess;
 }
 
 cudaError_t launch_nms_batch(const float *boxes, const int *d_num, int n_models, int GL, float overlap,
@@ -684,20 +656,21 @@ cudaError_t launch_nms_batch(const float *boxes, const int *d_num, int n_models,
   const float cell_inv = (float)kNmsCells / std::max(extent, 1.0f);
   if (n_models <= 0) return cudaSuccess;
   if (rounds <= 0) rounds = kNmsRounds;
-  cudaError_t e;
   if (order == kNmsOrderQuicksort) {
     launch_nms_sort(boxes, d_num, n_models, GL, cap, si, sf, err, diag, levels, lv_used, nullptr, s);
-    return launch_greedy<false>(boxes, n_models, GL, overlap, cell_inv, cap, si, sf, out, d_kept, err, diag, rounds,
-                                rounds_used, nullptr, s, aux);
+    launch_greedy<false>(boxes, n_models, GL, overlap, cell_inv, cap, si, sf, out, d_kept, err, diag, rounds,
+                         rounds_used, nullptr, s);
+    return cudaGetLastError();
   }
   launch_nms_radix(boxes, d_num, n_models, GL, cap, si, sf, need, s);
-  e = launch_greedy<true>(boxes, n_models, GL, overlap, cell_inv, cap, si, sf, out, d_kept, err, diag, rounds,
-                          rounds_used, need, s, aux);
-  if (e != cudaSuccess) return e;
+  launch_greedy<true>(boxes, n_models, GL, overlap, cell_inv, cap, si, sf, out, d_kept, err, diag, rounds,
+                      rounds_used, need, s);
   // the models whose kept set could depend on the order inside a run of equal
-  // scores, again in the quicksort's order: in a graph, an if node that runs
-  // only when some model needs it; otherwise launches that do nothing for the others
+  // scores, again in the quicksort's order: in a graph captured with aux, an
+  // if node that runs only when some model needs it; otherwise launches that
+  // do nothing for the models that do not
   cudaStream_t q = s;
+  cudaError_t e = cudaSuccess;
   if (aux) {
     cudaGraphConditionalHandle h;
     if ((e = cond_handle(s, 0u, &h)) != cudaSuccess) return e;
@@ -706,13 +679,10 @@ cudaError_t launch_nms_batch(const float *boxes, const int *d_num, int n_models,
     q = aux;
   }
   launch_nms_sort(boxes, d_num, n_models, GL, cap, si, sf, err, diag, levels, lv_used, need, q);
-  e = launch_greedy<false>(boxes, n_models, GL, overlap, cell_inv, cap, si, sf, out, d_kept, err, diag, rounds,
-                           rounds_used, need, q, nullptr);
-  if (aux) {
-    const cudaError_t e2 = end_conditional(aux);
-    if (e == cudaSuccess) e = e2;
-  }
-  return e;
+  launch_greedy<false>(boxes, n_models, GL, overlap, cell_inv, cap, si, sf, out, d_kept, err, diag, rounds,
+                       rounds_used, need, q);
+  if (aux) e = end_conditional(aux);
+  return e == cudaSuccess ? cudaGetLastError() : e;
 }
 
 }  // namespace geye

@@ -957,11 +957,10 @@ geye_status run_ascore(geye_ctx *ctx, Plan &P, ModelPlan &mp, int mi, float thre
 // frame whose last launched level still had work left its remaining segments
 // to the single-block fallback (exact, slower): the plan goes back to the
 // default count for good.
-// Rounds (plain launches only; a frame graph loops them in a while node): the
-// first frame launches kNmsRounds; one that needed fewer makes the plan launch
-// one more than it needed; one that took more batches than were launched (the
-// rest ran in the finish kernel's single block) makes it launch two more than
-// that frame took, and the count only grows from then on.
+// Rounds: the first frame launches kNmsRounds; one that needed fewer makes the
+// plan launch one more than it needed; one that took more batches than were
+// launched (the rest ran in the finish kernel's single block) makes it launch
+// two more than that frame took, and the count only grows from then on.
 // A change drops the plan's frame graphs after its stream has drained; the
 // next frame captures them again.
 void note_sort_levels(geye_ctx *ctx, Plan &P, int used, int rounds) {
@@ -974,9 +973,7 @@ void note_sort_levels(geye_ctx *ctx, Plan &P, int used, int rounds) {
   } else if (!P.sort_levels_fixed && P.sort_levels == 0 && used > 0 && used + 3 < full) {
     next = std::max(4, used + 3);
   }
-  if (ctx->use_graphs) {
-    // frame graphs loop the rounds in a while node, as many as the frame needs
-  } else if (rounds > r_launched) {
+  if (rounds > r_launched) {
     r_next = std::min(kNmsMaxRounds, rounds + 2);
     P.nms_rounds_fixed = true;
   } else if (!P.nms_rounds_fixed && P.nms_rounds == 0 && rounds + 1 < kNmsRounds) {
@@ -1001,7 +998,7 @@ geye_status run_nms(geye_ctx *ctx, Plan &P, int n_models, float overlap) {
                        P.d_nms_f.as<float>(), P.d_kept_boxes.as<float>(), d_kept, err,
                        reinterpret_cast<long long *>(d_num + 512), P.sort_levels, d_num + kSortLevelsUsed,
                        P.nms_rounds, d_num + kNmsRoundsUsed, d_num + kNmsNeed, ctx->nms_order, ctx->stream,
-                       ctx->capturing ? ctx->aux : nullptr);
+                       (ctx->capturing && ctx->nms_if_node) ? ctx->aux : nullptr);
   if (ge != cudaSuccess) {
     set_error(std::string("nms graph nodes: ") + cudaGetErrorString(ge));
     return GEYE_ERR_CUDA;

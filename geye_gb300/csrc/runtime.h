@@ -231,6 +231,11 @@ struct geye_ctx {
   int launches = 0;
   bool use_graphs = true;   // replay the frame as a CUDA graph (GEYE_NO_GRAPHS=1 at creation: plain launches)
   int nms_order = geye::kNmsOrderKey;   // geye_ctx_set_nms_order
+  // the frame graph runs the NMS quicksort-order pass as an if node (a lone
+  // frame skips its launches when no model needs it); server slots and batch
+  // lanes launch it plainly (its kernels return at once there), which measured
+  // faster with frames of other contexts in flight
+  bool nms_if_node = true;
   bool front_external = false;   // a batch's front end ran ingest, resize and HOG of the frame already
   bool capturing = false;
   // fault injection (host side)

@@ -237,6 +237,7 @@ geye_status new_slot(geye_server *s, int *idx) {
   GEYE_TRY(geye_ctx_create(s->device, nullptr, &c));
   geye_status st = geye_ctx_set_conv_mode(c, s->mode);
   if (st != GEYE_OK) { geye_ctx_destroy(c); return st; }
+  c->nms_if_node = false;   // frames of other slots in flight
   geye_server::Slot sl;
   sl.ctx = c;
   if (cudaEventCreateWithFlags(&sl.tracked, cudaEventDisableTiming) != cudaSuccess) {
@@ -773,6 +774,7 @@ geye_status geye_batch_run(geye_batch *b, int n_frames, const uint8_t *const *bg
     while ((int)b->lanes.size() <= i) {
       geye_ctx *c = nullptr;
       GEYE_TRY(geye_ctx_create(b->device, nullptr, &c));
+      c->nms_if_node = false;   // the batch's other lanes in flight
       b->lanes.push_back(c);
       const geye_status st = geye_ctx_set_conv_mode(c, b->mode);
       if (st != GEYE_OK) return st;
