@@ -1016,3 +1016,16 @@ geye_status geye_conv_tuning(geye_ctx *ctx, const geye_model *m, int shape[3], f
   *ms = P.tc.tuned_ms;
   return GEYE_OK;
 }
+
+geye_status geye_dt_tuning(geye_ctx *ctx, const geye_model *m, int *elems, float ms[3]) {
+  ARG_CHECK(ctx && m && elems && ms, "null argument");
+  ARG_CHECK(ctx->last_plan, "no run yet");
+  for (auto &mp : ctx->last_plan->models)
+    if (mp->model == m) {
+      *elems = mp->dt_elems;
+      for (int c = 0; c < 3; c++) ms[c] = mp->dt_ms[c];
+      return GEYE_OK;
+    }
+  geye::set_error("the last run has no such model");
+  return GEYE_ERR_ARG;
+}

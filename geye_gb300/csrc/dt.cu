@@ -16,7 +16,8 @@
 // otherwise g is checked to be non-decreasing, and only if it is not does one
 // thread replay the recursion exactly (counted in *fallback_count).
 //
-// A block takes a tile of L consecutive lines (about kDtElems outputs) into
+// A block takes a tile of L consecutive lines (about `elems` outputs: the
+// plan's tuned tile size, kDtElems by default) into
 // shared memory, each line padded with +inf, and spreads the tile's outputs
 // over its threads: a thread scans its output's window with no bounds checks
 // (an inf candidate never wins a strict comparison), using per-offset terms
@@ -39,7 +40,7 @@
 namespace geye {
 
 constexpr int kDtThreads = 256;
-constexpr int kDtElems = 2048;      // outputs per block (about)
+// kDtElems (outputs per block, about) is in internal.h: plans tune it
 constexpr int kDtPad = 64;          // largest window half-width served by the fast loop
 
 __device__ __forceinline__ float dt_f(float v, float a, float b, int t) {
@@ -93,10 +94,10 @@ __device__ void dt_replay(const float *v, int n, float a, float b, float *out, i
 
 // lines per block: pass 1 (columns, contiguous) any count up to 64; pass 2
 // (rows, strided in memory) a power of two up to 16 so that staging is coalesced
-__host__ __device__ __forceinline__ int dt_lines1(int n) { return max(1, min(64, kDtElems / max(n, 1))); }
-__host__ __device__ __forceinline__ int dt_lg_lines2(int n) {
+__host__ __device__ __forceinline__ int dt_lines1(int n, int elems) { return max(1, min(64, elems / max(n, 1))); }
+__host__ __device__ __forceinline__ int dt_lg_lines2(int n, int elems) {
   int lg = 0;
-  while (lg < 4 && (2 << lg) * n <= kDtElems) lg++;
+  while (lg < 4 && (2 << lg) * n <= elems) lg++;
   return lg;
 }
 __host__ __device__ __forceinline__ size_t dt_smem_bytes(int L, int n) {
@@ -242,15 +243,15 @@ __device__ __forceinline__ bool dt_monotone(float vabs, float a, float b, int K)
 template <int PASS>
 __global__ void __launch_bounds__(kDtThreads) k_dt(const DtJob *__restrict__ jobs, const int2 *__restrict__ blocks,
                                                     float *__restrict__ arena, int *__restrict__ arena_i,
-                                                    int *fallback_count) {
+                                                    int *fallback_count, int elems) {
   extern __shared__ float dsm[];
   const int2 blk = blocks[blockIdx.x];
   const DtJob J = jobs[blk.x];
   const int d0 = J.d0;
   const int n = PASS == 1 ? J.d0 : J.d1;           // line length
   const int nlines = PASS == 1 ? J.d1 : J.d0;
-  const int lgL = PASS == 1 ? 0 : dt_lg_lines2(n);
-  const int L = PASS == 1 ? dt_lines1(n) : (1 << lgL);
+  const int lgL = PASS == 1 ? 0 : dt_lg_lines2(n, elems);
+  const int L = PASS == 1 ? dt_lines1(n, elems) : (1 << lgL);
   const int line0 = blk.y;
   const int nl = min(L, nlines - line0);
   const int stride = n + kDtPad;
@@ -434,12 +435,12 @@ __global__ void __launch_bounds__(kDtThreads) k_dt(const DtJob *__restrict__ job
   }
 }
 
-void dt_block_lists(const std::vector<DtJob> &jobs, std::vector<int2> &b1, std::vector<int2> &b2) {
+void dt_block_lists(const std::vector<DtJob> &jobs, std::vector<int2> &b1, std::vector<int2> &b2, int elems) {
   b1.clear();
   b2.clear();
   for (size_t j = 0; j < jobs.size(); j++) {
     const DtJob &J = jobs[j];
-    const int L1 = dt_lines1(J.d0), L2 = 1 << dt_lg_lines2(J.d1);
+    const int L1 = dt_lines1(J.d0, elems), L2 = 1 << dt_lg_lines2(J.d1, elems);
     for (int l = 0; l < J.d1; l += L1) b1.push_back(make_int2((int)j, l));
     for (int l = 0; l < J.d0; l += L2) b2.push_back(make_int2((int)j, l));
   }
@@ -452,16 +453,16 @@ void dt_block_lists(const std::vector<DtJob> &jobs, std::vector<int2> &b1, std::
 }
 
 void launch_dt(const DtJob *d_jobs, const int2 *d_b1, int n_b1, const int2 *d_b2, int n_b2, int max_d0, int max_d1,
-               float *arena, int *arena_i, int *fallback_count, cudaStream_t s) {
+               float *arena, int *arena_i, int *fallback_count, int elems, cudaStream_t s) {
   if (n_b1 <= 0) return;
   size_t smem1 = 0, smem2 = 0;
-  for (int n = 1; n <= max_d0; n++) smem1 = std::max(smem1, dt_smem_bytes(dt_lines1(n), n));
-  for (int n = 1; n <= max_d1; n++) smem2 = std::max(smem2, dt_smem_bytes(1 << dt_lg_lines2(n), n));
+  for (int n = 1; n <= max_d0; n++) smem1 = std::max(smem1, dt_smem_bytes(dt_lines1(n, elems), n));
+  for (int n = 1; n <= max_d1; n++) smem2 = std::max(smem2, dt_smem_bytes(1 << dt_lg_lines2(n, elems), n));
   static SmemAttr a1, a2;
   raise_smem(a1, k_dt<1>, smem1);
   raise_smem(a2, k_dt<2>, smem2);
-  k_dt<1><<<n_b1, kDtThreads, smem1, s>>>(d_jobs, d_b1, arena, arena_i, fallback_count);
-  k_dt<2><<<n_b2, kDtThreads, smem2, s>>>(d_jobs, d_b2, arena, arena_i, fallback_count);
+  k_dt<1><<<n_b1, kDtThreads, smem1, s>>>(d_jobs, d_b1, arena, arena_i, fallback_count, elems);
+  k_dt<2><<<n_b2, kDtThreads, smem2, s>>>(d_jobs, d_b2, arena, arena_i, fallback_count, elems);
 }
 
 }  // namespace geye

@@ -270,9 +270,13 @@ void launch_conv_fp32(const ConvJob *d_jobs, int n_jobs, int max_tiles_y, int ma
                       const int *filt_off, const float *arena_in, float *arena_out, int max_b0, int max_b1,
                       int max_group, cudaStream_t s, int cr = 4);
 // (job, first line) of every DT block, pass 1 (columns) and pass 2 (rows), largest maps first
-void dt_block_lists(const std::vector<DtJob> &jobs, std::vector<int2> &b1, std::vector<int2> &b2);
+// DT tiles of about `elems` outputs per block (kDtElems by default; a plan
+// tunes it on its first frame's maps among kDtElemsChoices)
+constexpr int kDtElems = 2048;
+constexpr int kDtElemsChoices[3] = {1024, 2048, 4096};
+void dt_block_lists(const std::vector<DtJob> &jobs, std::vector<int2> &b1, std::vector<int2> &b2, int elems);
 void launch_dt(const DtJob *d_jobs, const int2 *d_b1, int n_b1, const int2 *d_b2, int n_b2, int max_d0, int max_d1,
-               float *arena, int *arena_i, int *fallback_count, cudaStream_t s);
+               float *arena, int *arena_i, int *fallback_count, int elems, cudaStream_t s);
 // (job, block of 256 positions) of every score map, in job order
 void score_block_list(const std::vector<ScoreJob> &jobs, std::vector<int2> &blocks);
 void launch_score(const ScoreJob *d_jobs, const int2 *d_blocks, int n_blocks, float thresh, float *arena,

@@ -407,7 +407,7 @@ static geye_status build_model_plan(geye_ctx *ctx, Plan &P, geye_model *mdl, int
   GEYE_TRY(upload(ctx, mp->d_dt_jobs, mp->dt_jobs));
   {
     std::vector<int2> b1, b2;
-    dt_block_lists(mp->dt_jobs, b1, b2);
+    dt_block_lists(mp->dt_jobs, b1, b2, mp->dt_elems);
     mp->dt_nblocks1 = (int)b1.size();
     mp->dt_nblocks2 = (int)b2.size();
     GEYE_TRY(upload(ctx, mp->d_dt_blocks1, b1));
@@ -893,9 +893,74 @@ geye_status run_dt(geye_ctx *ctx, Plan &P, ModelPlan &mp) {
   if (mp.dt_jobs.empty()) return GEYE_OK;
   launch_dt(mp.d_dt_jobs.as<DtJob>(), mp.d_dt_blocks1.as<int2>(), mp.dt_nblocks1, mp.d_dt_blocks2.as<int2>(),
             mp.dt_nblocks2, mp.dt_max_d0, mp.dt_max_d1, P.arena.as<float>(),
-            P.arena.as<int>(), ctx->d_diag.as<int>(), ctx->stream);
+            P.arena.as<int>(), ctx->d_diag.as<int>(), mp.dt_elems, ctx->stream);
   ctx->launches++;
   return check_launch(ctx, "dt");
+}
+
+// DT tile size of each model of a plan, timed on the maps its last frame left
+// in the arena (the DT's cost depends on the values: they set the window
+// bounds and whether the argmin order is proven): each of kDtElemsChoices
+// runs once untimed and three times timed with CUDA events on the context's
+// stream, and the fastest is kept.  A DT run rewrites its outputs from its
+// inputs, so the frame's results are unchanged.  Returns true when a plan's
+// block lists changed (its frame graphs must be captured again).
+static bool tune_dt(geye_ctx *ctx, Plan &P) {
+  bool changed = false;
+  for (auto &mpp : P.models) {
+    ModelPlan &mp = *mpp;
+    if (mp.dt_tuned || mp.dt_jobs.empty()) continue;
+    mp.dt_tuned = true;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) {
+      if (e0) cudaEventDestroy(e0);
+      return changed;
+    }
+    int best = -1;
+    float best_ms = 0.f;
+    std::vector<int2> keep1, keep2;
+    for (int c = 0; c < 3; c++) {
+      const int elems = kDtElemsChoices[c];
+      std::vector<int2> b1, b2;
+      dt_block_lists(mp.dt_jobs, b1, b2, elems);
+      DevBuf t1, t2;
+      if (upload(ctx, t1, b1) != GEYE_OK || upload(ctx, t2, b2) != GEYE_OK) break;
+      float ms = 0.f;
+      for (int rep = 0; rep < 4; rep++) {
+        if (rep == 1) cudaEventRecord(e0, ctx->stream);
+        launch_dt(mp.d_dt_jobs.as<DtJob>(), t1.as<int2>(), (int)b1.size(), t2.as<int2>(), (int)b2.size(),
+                  mp.dt_max_d0, mp.dt_max_d1, P.arena.as<float>(), P.arena.as<int>(), ctx->d_diag.as<int>(), elems,
+                  ctx->stream);
+      }
+      cudaEventRecord(e1, ctx->stream);
+      if (cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) break;
+      mp.dt_ms[c] = ms / 3.0f;
+      if (best < 0 || mp.dt_ms[c] < best_ms) {
+        best = c;
+        best_ms = mp.dt_ms[c];
+        keep1 = b1;
+        keep2 = b2;
+      }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaGetLastError();
+    if (best >= 0 && kDtElemsChoices[best] != mp.dt_elems) {
+      if (upload(ctx, mp.d_dt_blocks1, keep1) != GEYE_OK || upload(ctx, mp.d_dt_blocks2, keep2) != GEYE_OK) {
+        // the old lists may be gone: rebuild them for the old size
+        std::vector<int2> b1, b2;
+        dt_block_lists(mp.dt_jobs, b1, b2, mp.dt_elems);
+        upload(ctx, mp.d_dt_blocks1, b1);
+        upload(ctx, mp.d_dt_blocks2, b2);
+        continue;
+      }
+      mp.dt_elems = kDtElemsChoices[best];
+      mp.dt_nblocks1 = (int)keep1.size();
+      mp.dt_nblocks2 = (int)keep2.size();
+      changed = true;
+    }
+  }
+  return changed;
 }
 
 // score maps, detection records; model index mi writes boxes at mi*cap*GL and its count at d_small[mi]
@@ -961,8 +1026,9 @@ geye_status run_ascore(geye_ctx *ctx, Plan &P, ModelPlan &mp, int mi, float thre
 // plan launch one more than it needed; one that took more batches than were
 // launched (the rest ran in the finish kernel's single block) makes it launch
 // two more than that frame took, and the count only grows from then on.
-// A change drops the plan's frame graphs after its stream has drained; the
-// next frame captures them again.
+// The plan's DT tile sizes are tuned here too, once, on this frame's maps
+// (tune_dt).  A change drops the plan's frame graphs after its stream has
+// drained; the next frame captures them again.
 void note_sort_levels(geye_ctx *ctx, Plan &P, int used, int rounds) {
   const int full = nms_sort_levels(P.max_cap);
   const int launched = P.sort_levels > 0 ? P.sort_levels : full;
@@ -979,7 +1045,8 @@ void note_sort_levels(geye_ctx *ctx, Plan &P, int used, int rounds) {
   } else if (!P.nms_rounds_fixed && P.nms_rounds == 0 && rounds + 1 < kNmsRounds) {
     r_next = std::max(2, rounds + 1);
   }
-  if (next == P.sort_levels && r_next == P.nms_rounds) return;
+  const bool dt_changed = P.from_features ? false : tune_dt(ctx, P);   // (behind the frame on its stream)
+  if (next == P.sort_levels && r_next == P.nms_rounds && !dt_changed) return;
   P.sort_levels = next;
   P.nms_rounds = r_next;
   cudaStreamSynchronize(ctx->stream);

@@ -116,6 +116,9 @@ struct ModelPlan {
   DevBuf d_root_jobs, d_part_jobs, d_dt_jobs, d_score_jobs, d_counts;
   DevBuf d_dt_blocks1, d_dt_blocks2;    // DT tiles of every map (dt_block_lists)
   int dt_nblocks1 = 0, dt_nblocks2 = 0;
+  int dt_elems = kDtElems;              // outputs per DT block: tuned on the plan's first frame (tune_dt)
+  bool dt_tuned = false;
+  float dt_ms[3] = {0, 0, 0};           // the timed launch per kDtElemsChoices entry
   DevBuf d_score_blocks;                // score / box blocks of every map (score_block_list)
   int score_nblocks = 0;
   // per-(level, comp) and per-(L, part) map offsets for stage readback

@@ -386,12 +386,12 @@ geye_status geye_dt(geye_ctx *ctx, const float *vals, float ax, float bx, float 
   DtJob *d_j;
   GEYE_TRY(S.put(&J, 1, &d_j));
   std::vector<int2> b1, b2;
-  dt_block_lists(std::vector<DtJob>{J}, b1, b2);
+  dt_block_lists(std::vector<DtJob>{J}, b1, b2, kDtElems);
   int2 *d_b1, *d_b2;
   GEYE_TRY(S.put(b1.data(), b1.size(), &d_b1));
   GEYE_TRY(S.put(b2.data(), b2.size(), &d_b2));
   launch_dt(d_j, d_b1, (int)b1.size(), d_b2, (int)b2.size(), d0, d1, arena, reinterpret_cast<int *>(arena),
-            ctx->d_diag.as<int>(), ctx->stream);
+            ctx->d_diag.as<int>(), kDtElems, ctx->stream);
   CUDA_TRY(cudaGetLastError());
   CUDA_TRY(cudaMemcpyAsync(M, arena + 3 * np, sizeof(float) * n, cudaMemcpyDeviceToHost, ctx->stream));
   CUDA_TRY(cudaMemcpyAsync(Ix, arena + 4 * np, sizeof(int) * n, cudaMemcpyDeviceToHost, ctx->stream));

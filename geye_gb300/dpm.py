@@ -51,6 +51,7 @@ def lib(build_if_missing: bool = True):
             "geye_ctx_destroy": [vp],
             "geye_ctx_set_conv_mode": [vp, i32],
             "geye_ctx_set_nms_order": [vp, i32],
+            "geye_dt_tuning": [vp, vp, ip, vp],
             "geye_ctx_synchronize": [vp],
             "geye_model_load_csv": [vp, C.c_char_p, C.c_char_p, C.c_char_p, C.c_float, C.POINTER(vp)],
             "geye_model_free": [vp],
@@ -408,6 +409,14 @@ class Context:
         ms = np.zeros(1, np.float32)
         _check(lib().geye_conv_tuning(self.h, model.h, _p(shape), _p(ms)), "conv_tuning")
         return {"tiles_per_cta": int(shape[0]), "smem_kb": int(shape[1]), "ctas": int(shape[2]), "ms": float(ms[0])}
+
+    def dt_tuning(self, model: "Model") -> dict:
+        """DT tile size (outputs per block) the plan of the last run chose for the model, and the
+        timed launch of each candidate (1024, 2048, 4096 outputs per block; zeros before tuning)."""
+        elems = C.c_int()
+        ms = np.zeros(3, np.float32)
+        _check(lib().geye_dt_tuning(self.h, model.h, C.byref(elems), _p(ms)), "dt_tuning")
+        return {"elems": elems.value, "ms": ms.tolist()}
 
     def inject_fault(self, op: str | None, nth: int):
         _check(lib().geye_debug_inject_fault(self.h, op.encode() if op else None, nth), "inject_fault")

@@ -305,6 +305,12 @@ geye_status geye_score_map(geye_ctx *ctx, const geye_model *m, int level, int co
  * per launch.  GEYE_ERR_ARG in FP32 mode or before a run. */
 geye_status geye_conv_tuning(geye_ctx *ctx, const geye_model *m, int shape[3], float *ms);
 
+/* DT tile size of model m in the last run's plan: elems = outputs per DT block,
+ * chosen after the plan's first completed frame by timing 1024, 2048 and 4096
+ * on that frame's part maps; ms = the timed DT launch of each (0 before the
+ * tuning has run).  GEYE_ERR_ARG before a run or for a model not in it. */
+geye_status geye_dt_tuning(geye_ctx *ctx, const geye_model *m, int *elems, float ms[3]);
+
 /* ---- fault injection (host side only) ------------------------------------ */
 /* The n-th subsequent call of the named operation ("alloc", "h2d", "launch")
  * fails with GEYE_ERR_INJECTED; n = 0 clears.  No device fault is ever raised. */

@@ -304,6 +304,26 @@ def test_nms_sort_levels_adapt_and_fall_back(tmp_path):
     c1.close()
 
 
+def test_dt_tile_tuning_keeps_results(car_paths, person_paths):
+    """After a plan's first frame its DT tile size is timed on that frame's maps
+    (1024, 2048 or 4096 outputs per block); later frames use the choice and
+    give the first frame's results, bit for bit."""
+    import geye_gb300 as g
+    fr = synth.make_frame(640, 480, seed=4)
+    with g.Context(0) as c:
+        ms = [g.Model(c, *p) for p in (car_paths, person_paths)]
+        runs = [c.detect_multi(fr, ms, -0.5, 0.5) for _ in range(3)]
+        for m in ms:
+            t = c.dt_tuning(m)
+            assert t["elems"] in (1024, 2048, 4096) and all(x > 0 for x in t["ms"]), t
+        for r in runs[1:]:
+            for x, y in zip(runs[0], r):
+                assert x["num"] == y["num"]
+                assert np.array_equal(x["point"], y["point"]) and np.array_equal(bits(x["score"]), bits(y["score"]))
+        for m in ms:
+            m.close()
+
+
 def test_model_of_destroyed_context_is_refused(car_paths):
     """A model's filters are freed with the context that loaded it: detecting with
     it afterwards is an argument error on the host, raised before any launch."""

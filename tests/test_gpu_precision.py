@@ -17,7 +17,7 @@ Two workloads: the precision configuration itself, the car+person pair on
 FP32 detections, and 640x480 frames (three seeds) beside it.
 
 Set GEYE_PRECISION_REPORT=<prefix> to write each workload's per-level table as
-JSON (<prefix>_<w>x<h>.json).
+JSON (<prefix>_<w>x<h>.json) and as a markdown table (<prefix>_<w>x<h>.md).
 """
 import json
 import os
@@ -108,7 +108,31 @@ def report(request, tmp_path_factory):
     if out:
         with open(f"{out}_{W}x{H}.json", "w") as f:
             json.dump(rep, f, indent=1)
+        with open(f"{out}_{W}x{H}.md", "w") as f:
+            f.write(_markdown(rep, W, H, FRAMES))
     return rep
+
+
+def _markdown(rep, W, H, frames):
+    lv = {n: {r["level"]: r for r in rows} for n, rows in rep["levels"].items()}
+    lines = [f"Workload: synthetic {W}x{H} frames (seeds {', '.join(map(str, frames))}), random-init car "
+             "(2 components) and person (3 components) models, thresh -0.5, overlap 0.5.  Per level: the largest "
+             "absolute error of the whole-path score maps (root + offset - DT parts) against the oracle's double-"
+             "precision score from the same FP32 features, over all frames, models and components; mag = max "
+             "sum|a||b| of the root plus each part.", "",
+             "| level | FP32 max err | BF16 max err | BF16 err/mag | FP8 max err | FP8 err/mag | mag |",
+             "|---|---|---|---|---|---|---|"]
+    for level in sorted(lv["fp32"]):
+        f, b, e = lv["fp32"][level], lv["bf16"].get(level), lv["fp8"].get(level)
+        lines.append(f"| {level} | {f['max_abs_err']:.1e} | {b['max_abs_err']:.2e} | {b['max_err_over_mag']:.2e} | "
+                     f"{e['max_abs_err']:.2e} | {e['max_err_over_mag']:.2e} | {f['mag']:.2f} |")
+    lines += ["", "Detection agreement with FP32 (same component, IoU >= 0.9):", ""]
+    for name in ("bf16", "fp8"):
+        a = rep["agreement_vs_fp32"][name]
+        per = ", ".join(f"{p['model']} {p['matched']}/{p['fp32_detections']}" for p in a["per_model"])
+        lines.append(f"- {name.upper()}: {100 * a['agreement']:.2f}% ({per}); the test asserts >= "
+                     f"{100 * rep['min_agreement'][name]:.1f}%")
+    return "\n".join(lines) + "\n"
 
 
 def test_fp32_scores_within_sum_rounding(report):
