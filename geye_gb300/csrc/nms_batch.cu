@@ -6,18 +6,25 @@
 // never emitted.  The greedy loop is restated so that most of it runs on every
 // SM:
 //
-//  1. the quicksort (nms_sort.cu).
-//  2. k_nms_gather: the boxes in sorted order (structure of arrays) and an
-//     alive bitmap over sorted positions.
+//  1. the order: score order from the radix sort (nms_radix.cu), checked for
+//     the cases where the quicksort's order among equal scores could change
+//     the kept set; the models that raise them go through steps 2-4 again in
+//     the quicksort's order (nms_sort.cu).
+//  2. k_nms_gather: the boxes in sorted order (structure of arrays), an alive
+//     bitmap over sorted positions and its summary (one bit per word).
 //  3. Rounds of two kernels, each a no-op for a model that is done:
 //     k_nms_resolve (one block per model) takes the first kBatch alive boxes
-//     in sorted order, computes their pairwise suppression bits and walks
-//     them in order: a member is picked unless an earlier pick of the batch
-//     suppresses it -- the sequential loop's decisions for these boxes, since
-//     every box before them is already resolved.
-//     k_nms_pass (grid) tests every other alive box against the batch's picks
-//     in pick order; the first pick that suppresses it is the one the
-//     sequential loop would have removed it with.
+//     in sorted order (found through the summary), computes for each member
+//     which earlier members suppress it (pairs whose cell spans overlap) and
+//     decides the members in parallel rounds: a member is picked when every
+//     earlier member that suppresses it is decided and none is picked, and
+//     removed when an earlier pick suppresses it -- the sequential loop's
+//     decisions, since every box before the batch is already resolved.  It
+//     then lists its picks by image cell on each axis.
+//     k_nms_pass (grid) tests every other alive box against the picks that
+//     share a row cell and a column cell with it, in pick order; the first
+//     pick that suppresses it is the one the sequential loop would have
+//     removed it with.
 //  4. k_nms_finish (one block per model) runs any remaining rounds itself,
 //     drops the final pick if it suppressed nothing (the reference's
 //     `while (cnum > 0)` with cnum = NUM-1 never takes a box that is alone at
