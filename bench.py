@@ -68,6 +68,7 @@ WORKLOADS = {
     # one frame at a time
     "car+person_1280x720_fp32": dict(w=1280, h=720, models=("car", "person"), conv="fp32"),
     "car+person_1280x720_bf16": dict(w=1280, h=720, models=("car", "person"), conv="bf16"),
+    "car+person_1920x1080_bf16": dict(w=1920, h=1080, models=("car", "person"), conv="bf16"),
     "car+person_640x480_fp32": dict(w=640, h=480, models=("car", "person"), conv="fp32"),
     "car+person_640x480_bf16": dict(w=640, h=480, models=("car", "person"), conv="bf16"),
     "car+person_640x480_fp8": dict(w=640, h=480, models=("car", "person"), conv="fp8"),
