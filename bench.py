@@ -642,9 +642,9 @@ def serve_sim(wl, models, max_slots):
     srv = g.Server(models, conv=g.CONV_BF16, hbm_budget=40 << 30, max_slots=max_slots, track=True)
     for sz in sorted(set(sizes)):   # slots, plans and graphs for every resolution before the clock starts
         s0 = sizes.index(sz)
-        for _ in range(2):          # the second round runs the graphs refitted to the frames' sort depth
-            for _ in range(max_slots):
-                srv.submit(s0, frames[(s0, 0)])
+        for rnd in range(3):        # later rounds run the graphs refitted to the frames' NMS depth
+            for k in range(max_slots):
+                srv.submit(s0, base[(sz, (rnd + k) % 4)])
             srv.drain()
             srv.poll(1024)
     adm = wl.get("admission", (0, 0.0))

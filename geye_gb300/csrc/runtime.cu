@@ -1025,7 +1025,8 @@ geye_status run_ascore(geye_ctx *ctx, Plan &P, ModelPlan &mp, int mi, float thre
 // Rounds: the first frame launches kNmsRounds; one that needed fewer makes the
 // plan launch one more than it needed; one that took more batches than were
 // launched (the rest ran in the finish kernel's single block) makes it launch
-// two more than that frame took, and the count only grows from then on.
+// half as many again plus two (so that a few frames settle it, each change
+// costing a graph capture), and the count only grows from then on.
 // The plan's DT tile sizes are tuned here too, once, on this frame's maps
 // (tune_dt).  A change drops the plan's frame graphs after its stream has
 // drained; the next frame captures them again.
@@ -1040,7 +1041,7 @@ void note_sort_levels(geye_ctx *ctx, Plan &P, int used, int rounds) {
     next = std::max(4, used + 3);
   }
   if (rounds > r_launched) {
-    r_next = std::min(kNmsMaxRounds, rounds + 2);
+    r_next = std::min(kNmsMaxRounds, rounds + rounds / 2 + 2);
     P.nms_rounds_fixed = true;
   } else if (!P.nms_rounds_fixed && P.nms_rounds == 0 && rounds + 1 < kNmsRounds) {
     r_next = std::max(2, rounds + 1);
