@@ -1022,11 +1022,11 @@ geye_status run_ascore(geye_ctx *ctx, Plan &P, ModelPlan &mp, int mi, float thre
 // frame whose last launched level still had work left its remaining segments
 // to the single-block fallback (exact, slower): the plan goes back to the
 // default count for good.
-// Rounds: the first frame launches kNmsRounds; one that needed fewer makes the
-// plan launch one more than it needed; one that took more batches than were
-// launched (the rest ran in the finish kernel's single block) makes it launch
-// half as many again plus two (so that a few frames settle it, each change
-// costing a graph capture), and the count only grows from then on.
+// Rounds: a plan launches kNmsRounds (a round with nothing left is two launches
+// that return at once); a frame that took more batches than were launched (the
+// rest ran in the finish kernel's single block) makes it launch half as many
+// again plus two, so that a few frames settle it (each change costs a graph
+// capture), and the count only grows.
 // The plan's DT tile sizes are tuned here too, once, on this frame's maps
 // (tune_dt).  A change drops the plan's frame graphs after its stream has
 // drained; the next frame captures them again.
@@ -1040,12 +1040,7 @@ void note_sort_levels(geye_ctx *ctx, Plan &P, int used, int rounds) {
   } else if (!P.sort_levels_fixed && P.sort_levels == 0 && used > 0 && used + 3 < full) {
     next = std::max(4, used + 3);
   }
-  if (rounds > r_launched) {
-    r_next = std::min(kNmsMaxRounds, rounds + rounds / 2 + 2);
-    P.nms_rounds_fixed = true;
-  } else if (!P.nms_rounds_fixed && P.nms_rounds == 0 && rounds + 1 < kNmsRounds) {
-    r_next = std::max(2, rounds + 1);
-  }
+  if (rounds > r_launched) r_next = std::min(kNmsMaxRounds, rounds + rounds / 2 + 2);
   const bool dt_changed = P.from_features ? false : tune_dt(ctx, P);   // (behind the frame on its stream)
   if (next == P.sort_levels && r_next == P.nms_rounds && !dt_changed) return;
   P.sort_levels = next;

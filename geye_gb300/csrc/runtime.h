@@ -196,7 +196,7 @@ struct Plan {
   // adapted once to the depth the plan's frames need (note_sort_levels)
   int sort_levels = 0;
   int nms_rounds = 0;   // greedy resolve/pass rounds per frame (0: kNmsRounds), adapted to the frames
-  bool sort_levels_fixed = false, nms_rounds_fixed = false;
+  bool sort_levels_fixed = false;
   // asynchronous submission (serve.cu): pinned frame staging, pinned result
   // block (counts, then per model kHostRes records) and the completion event
   void *h_bgr = nullptr, *h_res = nullptr;
