@@ -647,6 +647,12 @@ def serve_sim(wl, models, max_slots):
                 srv.submit(s0, base[(sz, (rnd + k) % 4)])
             srv.drain()
             srv.poll(1024)
+        # the pinned frame pool for as many frames of this size as can be queued and in flight at once
+        for k in range(max_slots + 2 * sizes.count(sz)):
+            srv.submit(s0, base[(sz, k % 4)])
+        srv.drain()
+        while srv.poll(1024):
+            pass
     adm = wl.get("admission", (0, 0.0))
     srv.set_admission(adm[0], adm[1])
     T = wl["seconds"]

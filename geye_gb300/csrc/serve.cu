@@ -210,9 +210,13 @@ struct geye_server {
     size_t bytes;
   };
   // pinned frame buffers by size: a submitted frame is copied once, into one of
-  // these, and goes to the device from there
+  // these, and goes to the device from there.  They are carved from slabs of
+  // kPinnedSlab bytes (cudaMallocHost is slow and synchronises the device, so
+  // it runs once per slab, not once per buffer) and reused, never returned.
   std::map<size_t, std::vector<uint8_t *>> pinned_free;
-  std::vector<uint8_t *> pinned_all;
+  std::vector<uint8_t *> pinned_all;   // the slabs
+  uint8_t *slab_next = nullptr;
+  size_t slab_left = 0;
   std::deque<Req> queue;
   struct Done {
     geye_served info;
@@ -250,6 +254,8 @@ geye_status new_slot(geye_server *s, int *idx) {
   return GEYE_OK;
 }
 
+constexpr size_t kPinnedSlab = 64ull << 20;
+
 geye_status get_pinned(geye_server *s, size_t n, uint8_t **out) {
   auto &v = s->pinned_free[n];
   if (!v.empty()) {
@@ -257,10 +263,18 @@ geye_status get_pinned(geye_server *s, size_t n, uint8_t **out) {
     v.pop_back();
     return GEYE_OK;
   }
-  void *p = nullptr;
-  CUDA_TRY(cudaMallocHost(&p, n));
-  s->pinned_all.push_back(static_cast<uint8_t *>(p));
-  *out = static_cast<uint8_t *>(p);
+  const size_t need = (n + 4095) & ~(size_t)4095;
+  if (s->slab_left < need) {
+    const size_t bytes = std::max(kPinnedSlab, need);
+    void *p = nullptr;
+    CUDA_TRY(cudaMallocHost(&p, bytes));
+    s->pinned_all.push_back(static_cast<uint8_t *>(p));
+    s->slab_next = static_cast<uint8_t *>(p);
+    s->slab_left = bytes;
+  }
+  *out = s->slab_next;
+  s->slab_next += need;
+  s->slab_left -= need;
   return GEYE_OK;
 }
 
