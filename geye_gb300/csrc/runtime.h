@@ -2,6 +2,7 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <map>
 #include <set>
 #include <memory>
@@ -157,6 +158,12 @@ struct TcPlan {
 };
 
 struct Plan {
+  // distinct for every plan a process builds (a rebuilt plan never reuses one)
+  const unsigned long long serial = next_plan_serial();
+  static unsigned long long next_plan_serial() {
+    static std::atomic<unsigned long long> n{0};
+    return ++n;
+  }
   int width = 0, height = 0;           // frame size (0 when built from features)
   int interval = 0, sbin = 0, LEN = 0;
   bool from_features = false;

@@ -604,6 +604,7 @@ struct geye_batch {
     size_t frames_bytes = 0;    // the frame table's share of d_tables, items after it
     int n_phases = 0;           // resize phases of the batch's deepest pyramid
     std::vector<int> count, offset;   // items per list (front_list) and their offsets
+    std::vector<unsigned long long> plans;   // serials of the lanes' plans the graph was captured with
   };
   std::map<std::string, Graph> graphs;   // by lane sizes, thresh, overlap
   int last_kernels = 0;
@@ -810,8 +811,18 @@ geye_status geye_batch_run(geye_batch *b, int n_frames, const uint8_t *const *bg
     key += std::to_string(tb) + ":" + std::to_string(ob);
   }
   geye_batch::Graph &g = b->graphs[key];
+  std::vector<unsigned long long> serials(n_frames);
+  for (int i = 0; i < n_frames; i++) serials[i] = plans[i]->serial;
+  if (g.exec && g.plans != serials) {
+    // a lane's plan was rebuilt since the capture (its context dropped its plans): the
+    // graph reads the old plan's buffers, so it is captured again
+    cudaStreamSynchronize(b->stream);
+    cudaGraphExecDestroy(g.exec);
+    g.exec = nullptr;
+  }
   if (!g.exec) {
     GEYE_TRY(batch_front_tables(b, plans, g));
+    g.plans = serials;
     cudaGraph_t graph = nullptr;
     CUDA_TRY(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeRelaxed));
     geye_status st = GEYE_OK;
