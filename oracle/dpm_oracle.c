@@ -1,7 +1,7 @@
 /*
  * dpm_oracle.c -- CPU restatement of CPFL/geye's DPM detection path.
  *
- * TEST INFRASTRUCTURE ONLY.  This file is the checker: the pytest suite, the
+ * TEST INFRASTRUCTURE ONLY.  This file is the oracle: the pytest suite, the
  * smoke check in __graft_entry__.py and the cpu_baseline leg of bench.py call it
  * to decide whether the CUDA path is right, and bench.py times it as the CPU
  * baseline.  The product (libgeye_dpm.so) never links, loads or calls it.

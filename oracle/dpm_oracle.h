@@ -1,6 +1,6 @@
 /*
  * dpm_oracle.h -- CPU restatement of CPFL/geye's DPM detection path.
- * TEST INFRASTRUCTURE ONLY (the checker); see dpm_oracle.c for the rules.
+ * TEST INFRASTRUCTURE ONLY (the oracle); see dpm_oracle.c for the rules.
  */
 #ifndef GEYE_DPM_ORACLE_H
 #define GEYE_DPM_ORACLE_H

@@ -2,8 +2,8 @@
 reference's own CPU functions built by oracle/ref/Makefile (oracle/_ref).
 
 TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and the
-cpu_baseline / reference legs of bench.py, always as the checker or as the
-timed CPU baseline, never as the thing measured or shipped.
+cpu_baseline / reference legs of bench.py, always as the oracle results are
+compared with or as the timed CPU baseline, never as the thing measured or shipped.
 
 Array conventions follow the reference's column-major storage: a map of
 d0 rows (y) by d1 columns (x) is a C-ordered numpy array of shape (d1, d0),

@@ -3,7 +3,7 @@ reference's own CPU functions (CAR_TRACKING sources compiled into oracle/_ref
 by oracle/ref/Makefile) for them.
 
 The reference ships no test vectors; these fixtures carry its results to
-machines without its sources (the GPU machine), where tests/test_golden.py checks
+machines without its sources, where tests/test_golden.py checks
 the oracle and tests/test_gpu_golden.py checks the CUDA stage entry points
 against them.  Run from the repository root:  python tests/golden/make_golden.py
 """
