@@ -65,6 +65,8 @@ WORKLOADS = {
                                sizes=((320, 240), (640, 480), (1280, 720), (1920, 1080))),
     "batch32_mixed_bf16": dict(w=640, h=480, models=("car", "person"), conv="bf16", batch=32,
                                sizes=((320, 240), (640, 480), (1280, 720), (1920, 1080))),
+    "batch16_640x480_bf16": dict(w=640, h=480, models=("car", "person"), conv="bf16", batch=16,
+                                 sizes=((640, 480),)),
     # one frame at a time
     "car+person_1280x720_fp32": dict(w=1280, h=720, models=("car", "person"), conv="fp32"),
     "car+person_1280x720_bf16": dict(w=1280, h=720, models=("car", "person"), conv="bf16"),

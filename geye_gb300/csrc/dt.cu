@@ -30,7 +30,9 @@
 // For a <= 0 the window is the whole line.  Pass 1 (columns: many short
 // lines per tile) takes one K from the whole tile's value range and, when the
 // order is proven and K <= 8, scans with the per-offset terms in registers;
-// pass 2 (rows: a few long lines) takes a K per line.
+// pass 2 (rows: a few long lines) takes a K per line and, when the order is
+// proven and every line's K <= 8, reads the terms of each line's window from
+// one register table.
 #include <math.h>
 
 #include <algorithm>
@@ -102,7 +104,7 @@ __host__ __device__ __forceinline__ int dt_lg_lines2(int n, int elems) {
 }
 __host__ __device__ __forceinline__ size_t dt_smem_bytes(int L, int n) {
   return sizeof(float) * ((size_t)kDtPad + (size_t)L * (n + kDtPad) + 2 * (size_t)L * n + 2 * (2 * kDtPad - 1)) +
-         sizeof(int) * (2 * (size_t)L + 1) + sizeof(float) * 3 * (kDtThreads / 32);
+         sizeof(int) * (2 * (size_t)L + 1) + sizeof(float) * 3 * (kDtThreads / 32) + sizeof(int);
 }
 
 // Leftmost minimum of output d over the window |t| < KM of a padded line,
@@ -219,6 +221,59 @@ __device__ __forceinline__ void dt_mono_tile(const float *__restrict__ v_s, int 
   }
 }
 
+// Leftmost minimum over the window |t| < KK of output d, the per-offset
+// terms taken from registers At8/Bt8 (offsets t = 7 - j, j = 0..14)
+template <int KK>
+__device__ __forceinline__ int dt_scan_slice(const float *__restrict__ line, int d, const float (&At8)[15],
+                                             const float (&Bt8)[15], float &best) {
+  const float *v = line + d - (KK - 1);
+  best = INFINITY;
+  int s = 0;
+#pragma unroll
+  for (int jj = 0; jj < 2 * KK - 1; jj++) {
+    const float f = (v[jj] + At8[jj + 8 - KK]) + Bt8[jj + 8 - KK];
+    if (f < best) { best = f; s = jj; }
+  }
+  return d - (KK - 1) + s;
+}
+
+// As dt_scan_tile for a proven order with every line's window at most 8: the
+// same outputs and candidates, a window per line, the per-offset terms in registers.
+template <int Q>
+__device__ __forceinline__ void dt_scan_tile_reg(const float *__restrict__ v_s, int stride, int n, int nl, float a,
+                                                 float b, const int *__restrict__ K_s, float *__restrict__ o_s,
+                                                 int *__restrict__ g_s, int y0, int par_y, int par_x) {
+  float At8[15], Bt8[15];
+#pragma unroll
+  for (int j = 0; j < 15; j++) {
+    const float ft = (float)(7 - j);
+    At8[j] = a * ft * ft;
+    Bt8[j] = b * ft;
+  }
+  const int m = (n + Q - 1) / Q;
+  const unsigned mg = 0xFFFFFFFFu / (unsigned)m + 1u;
+  for (int e = threadIdx.x; e < nl * m; e += blockDim.x) {
+    const int l = __umulhi((unsigned)e, mg), i = e - l * m;
+    const int c = Q == 1 ? 0 : (((y0 + l) & 1) == par_y ? par_x : 1 - par_x);
+    const int d = c + Q * i;
+    if (d >= n) continue;
+    const float *line = v_s + l * stride;
+    float best;
+    int p;
+    switch (K_s[l]) {
+      case 0: case 1: case 2: p = dt_scan_slice<2>(line, d, At8, Bt8, best); break;
+      case 3: p = dt_scan_slice<3>(line, d, At8, Bt8, best); break;
+      case 4: p = dt_scan_slice<4>(line, d, At8, Bt8, best); break;
+      case 5: p = dt_scan_slice<5>(line, d, At8, Bt8, best); break;
+      case 6: p = dt_scan_slice<6>(line, d, At8, Bt8, best); break;
+      case 7: p = dt_scan_slice<7>(line, d, At8, Bt8, best); break;
+      default: p = dt_scan_slice<8>(line, d, At8, Bt8, best); break;
+    }
+    o_s[l * n + d] = best;
+    g_s[l * n + d] = p;
+  }
+}
+
 // True when the computed leftmost argmin g(d) of a line is certainly
 // non-decreasing in d.  For s < p, the exact terms give
 //   [f_d(s) - f_d(p)] - [f_{d-1}(s) - f_{d-1}(p)] = 2a(p - s) >= 2a,
@@ -292,7 +347,11 @@ __global__ void __launch_bounds__(kDtThreads) k_dt(const DtJob *__restrict__ job
     const int l = i / kDtPad, k = i - l * kDtPad;
     v_s[l * stride - kDtPad + k] = INFINITY;   // pad before line l (l = nl: after the last line)
   }
-  if (tid == 0) *mono_s = 1;
+  int *kmax_s = mono_s + 1 + 3 * (kDtThreads / 32);   // pass 2: the widest line window of the tile
+  if (tid == 0) {
+    *mono_s = 1;
+    *kmax_s = 0;
+  }
   for (int t = tid - (kDtPad - 1); t < kDtPad; t += nth) {
     const float ft = (float)t;
     At[t] = a * ft * ft;
@@ -360,6 +419,7 @@ __global__ void __launch_bounds__(kDtThreads) k_dt(const DtJob *__restrict__ job
         const int Kl = dt_window(lmin, lmax, labs, a, b, n);
         K_s[l] = Kl;
         bad_s[l] = 0;
+        atomicMax(kmax_s, Kl);
         if (lnan || !dt_monotone(labs, a, b, Kl)) *mono_s = 0;
       }
     }
@@ -383,6 +443,9 @@ __global__ void __launch_bounds__(kDtThreads) k_dt(const DtJob *__restrict__ job
       else if (K <= 6) DT_MONO(6);
       else DT_MONO(8);
 #undef DT_MONO
+    } else if (PASS == 2 && *kmax_s <= 8) {   // a window per line, the terms in registers
+      if (q == 1) dt_scan_tile_reg<1>(v_s, stride, n, nl, a, b, K_s, o_s, g_s, line0, J.par_y, J.par_x);
+      else dt_scan_tile_reg<2>(v_s, stride, n, nl, a, b, K_s, o_s, g_s, line0, J.par_y, J.par_x);
     } else {
       dt_scan_tile(v_s, stride, n, nl, a, b, K_s, At, Bt, o_s, g_s, q, line0, J.par_y, J.par_x);
     }
