@@ -42,6 +42,10 @@ import time
 
 import numpy as np
 
+# 32 hardware work queues for the served slots' streams (CUDA reads this when the
+# first context is created, before torch or the library touch the GPU)
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
+
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
@@ -601,6 +605,7 @@ def run_served(args, wl):
             "config": {"workload": args.workload, "frame": f"{W}x{H}", "models": list(wl["models"]),
                        "conv": "bf16 (tcgen05, FP32 accumulation)", "thresh": -0.5, "overlap": 0.5,
                        "frames_in_flight": S, "step": f"{S} frames from {S} streams, one per slot",
+                       "hw_queues": int(os.environ.get("CUDA_DEVICE_MAX_CONNECTIONS", "8")),
                        "parallelism": f"replicas{world}",
                        "l2": "flushed between steps (256 MiB write, outside the timed events)"},
             "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),

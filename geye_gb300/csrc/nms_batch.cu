@@ -439,6 +439,20 @@ __global__ void __launch_bounds__(kPassNT) k_nms_pass(int cap, int *si, float *s
   if (st.done) return;
   const int np = st.npb;
   if (np <= 0) return;
+  const int nwarps = gridDim.x * (kPassNT / 32);
+  const int w_first = st.scan_word + blockIdx.x * (kPassNT / 32);
+  const int nwords = st.nwords;
+  {
+    // a block whose words hold no alive box leaves before it builds the tables
+    // (only this block's warps change its words, so the check stays true)
+    bool any = false;
+    for (int k = threadIdx.x; !any; k += kPassNT) {
+      const int w = w_first + (k & (kPassNT / 32 - 1)) + (k / (kPassNT / 32)) * nwarps;
+      if (w >= nwords) break;
+      any = S.bits[w] != 0u;
+    }
+    if (!__syncthreads_or(any)) return;
+  }
   const int nwm = (np + 31) >> 5;
   for (int k = threadIdx.x; k < np; k += kPassNT)
     for (int c = 0; c < 5; c++) Z.pk[c][k] = S.bp[c * kBatch + k];
@@ -456,9 +470,7 @@ __global__ void __launch_bounds__(kPassNT) k_nms_pass(int cap, int *si, float *s
   }
   const int lane = threadIdx.x & 31;
   const int pick_base = st.npicks - np;
-  const int nwords = st.nwords;
-  const int nwarps = gridDim.x * (kPassNT / 32);
-  for (int w = st.scan_word + blockIdx.x * (kPassNT / 32) + (threadIdx.x >> 5); w < nwords; w += nwarps) {
+  for (int w = w_first + (threadIdx.x >> 5); w < nwords; w += nwarps) {
     const unsigned word = S.bits[w];
     if (!word) continue;
     const int r = (w << 5) + lane;

@@ -204,7 +204,11 @@ geye_status geye_detect_collect(geye_ctx *ctx, geye_result *out);
  * slots stays within hbm_budget bytes and at most max_slots exist); frames of
  * different resolutions and streams overlap on the GPU.  Each stream's frames
  * are dispatched in submission order.  When track is nonzero every stream
- * keeps a device-resident particle-filter tracker fed with its detections. */
+ * keeps a device-resident particle-filter tracker fed with its detections.
+ * The slots' streams overlap only as far as the device's hardware work
+ * queues allow: a serving process should set CUDA_DEVICE_MAX_CONNECTIONS=32
+ * in its environment before its first CUDA call (with CUDA's default of 8,
+ * 16 slots at 640x480 run 2954 instead of 3384 frames/s end to end). */
 typedef struct geye_server geye_server;   /* the models must outlive the server */
 typedef struct {
     long long ticket;        /* from geye_server_submit                         */
