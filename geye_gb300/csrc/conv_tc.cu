@@ -30,15 +30,16 @@
 // significant bits per operand for the roots, whose rounding decides most
 // detections; part filters stay plain BF16.
 //
-// A CTA (4 warps) owns a run of up to 8 tiles of 128 positions of one job, each
+// A CTA (8 warps) owns a run of up to 8 tiles of 128 positions of one job, each
 // tile with its own TMEM accumulator.  The run's feature slab stays in shared
 // memory while the bank streams through a ring of stages, one tap per stage:
 // lane 0 of warp 0 bulk-copies (cp.async.bulk, mbarrier completion), lane 0
 // of warp 1 issues the tap's MMAs for every tile and commits them to the
 // stage's "free" mbarrier, so the copy of tap t+stages overlaps the MMAs of
 // tap t.  Grids wider than the slab allows are walked in column phases (the
-// slab reloaded per phase).  After the last MMA the four warps read the
-// accumulators with tcgen05.ld (warp w owns TMEM lanes 32w..32w+31) and write
+// slab reloaded per phase).  After the last MMA the eight warps read the
+// accumulators with tcgen05.ld (warp w reads TMEM lanes 32(w%4)..+31; the two
+// warps of a lane quarter take alternate tiles and column chunks) and write
 // part maps in the reference layout and root blocks by position.  Every
 // mbarrier wait is bounded; a timeout sets an error bit, and the CTA waits
 // (bounded) for its own copies and MMAs before it frees TMEM and leaves.
@@ -57,7 +58,7 @@
 
 namespace geye {
 
-constexpr int kTcThreads = 128;
+constexpr int kTcThreads = 256;                 // 8 warps: two per TMEM lane quarter in the epilogue
 constexpr int kTcM = 128;                        // positions per tile (TMEM lanes)
 constexpr int kTcMaxTiles = 8;                   // tiles per CTA, at most
 constexpr int kTcMaxStages = 8;                  // bank stages in the ring, at most
@@ -315,36 +316,37 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   }
   ok = __syncthreads_and(done && ok);
   tc_fence_after();
-  // ---- epilogue: row r of a tile is TMEM lane r; this thread owns row 32*warp + lane of every tile
+  // ---- epilogue: row r of a tile is TMEM lane r; warp w reads the rows 32*(w & 3) .. +31 of
+  // the tiles, and the two warps of a lane quarter take alternate (tile, 16-column chunk) items
   const int ncell = J.fs0 * J.fs1;
-  for (int i = 0; i < ntile; i++) {
-    const int p = p_begin + i * kTcM + warp * 32 + lane;
+  const int quarter = warp & 3, nch = J.n >> 4;
+  for (int item = warp >> 2; item < ntile * nch; item += kTcThreads / 128) {
+    const int i = item / nch, c0 = (item - i * nch) * 16;
+    const TcCol head = col_s[c0];               // a 16-column chunk lies inside one section
+    if (head.kind == 0) continue;               // (uniform across the warp: the loads below are collective)
+    const int p = p_begin + i * kTcM + quarter * 32 + lane;
     const int x = p / J.fs0, y = p - x * J.fs0;
-    const uint32_t row_addr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(i * J.n);
-    for (int c0 = 0; c0 < J.n; c0 += 16) {
-      const TcCol head = col_s[c0];               // a 16-column chunk lies inside one section
-      if (head.kind == 0) continue;               // (uniform across the warp: the loads below are collective)
-      uint32_t r[16], r2[16];
-      __syncwarp();
-      tc_ld16(row_addr + (uint32_t)c0, r);
-      if (head.kind == 2 && head.pair) tc_ld16(row_addr + (uint32_t)(c0 + head.pair), r2);
-      tc_wait_ld();
-      if (ok && p < ncell) {
+    const uint32_t row_addr = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(i * J.n);
+    uint32_t r[16], r2[16];
+    __syncwarp();
+    tc_ld16(row_addr + (uint32_t)c0, r);
+    if (head.kind == 2 && head.pair) tc_ld16(row_addr + (uint32_t)(c0 + head.pair), r2);
+    tc_wait_ld();
+    if (ok && p < ncell) {
 #pragma unroll
-        for (int k = 0; k < 16; k++) {
-          const TcCol c = col_s[c0 + k];
-          float v;
-          memcpy(&v, &r[k], 4);
-          if (c.kind == 1) {
-            if (x < c.cols && y < c.rows) arena[(size_t)c.off + (size_t)x * c.rows + y] = v * c.inv;
-          } else if (c.kind == 2) {
-            if (c.pair) {
-              float w;
-              memcpy(&w, &r2[k], 4);
-              v += w;
-            }
-            arena[(size_t)c.off + p] = v * c.inv;
+      for (int k = 0; k < 16; k++) {
+        const TcCol c = col_s[c0 + k];
+        float v;
+        memcpy(&v, &r[k], 4);
+        if (c.kind == 1) {
+          if (x < c.cols && y < c.rows) arena[(size_t)c.off + (size_t)x * c.rows + y] = v * c.inv;
+        } else if (c.kind == 2) {
+          if (c.pair) {
+            float w;
+            memcpy(&w, &r2[k], 4);
+            v += w;
           }
+          arena[(size_t)c.off + p] = v * c.inv;
         }
       }
     }
@@ -522,7 +524,8 @@ struct TcShape {
 };
 static const TcShape kTcShapes[] = {{4, 110 * 1024, 2, 1},  {2, 72 * 1024, 3, 0},  {4, 220 * 1024, 1, -1},
                                     {2, 220 * 1024, 1, -1}, {8, 220 * 1024, 1, -1}, {2, 110 * 1024, 1, -1},
-                                    {1, 72 * 1024, 4, 0},   {4, 220 * 1024, 8, 0}};
+                                    {1, 72 * 1024, 4, 0},   {4, 220 * 1024, 8, 0},  {4, 110 * 1024, 8, 0},
+                                    {4, 110 * 1024, 4, 0}};
 constexpr int kTcNumShapes = (int)(sizeof(kTcShapes) / sizeof(kTcShapes[0]));
 
 // taps a stage holds for a phase of cs columns: one, a column (b0), or the whole phase
