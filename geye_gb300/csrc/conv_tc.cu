@@ -34,9 +34,11 @@
 // tile with its own TMEM accumulator.  The run's feature slab stays in shared
 // memory while the bank streams through a ring of stages, one tap per stage:
 // lane 0 of warp 0 bulk-copies (cp.async.bulk, mbarrier completion), lane 0
-// of warp 1 issues the tap's MMAs for every tile and commits them to the
-// stage's "free" mbarrier, so the copy of tap t+stages overlaps the MMAs of
-// tap t.  Grids wider than the slab allows are walked in column phases (the
+// of warp 1+i issues the tap's MMAs for tile i (one issuing thread per tile:
+// one thread alone cannot issue MMAs of N = 48 as fast as the tensor pipe
+// retires them) and commits them to the stage's "free" mbarrier, which
+// completes when every issuer's MMAs are done, so the copy of tap t+stages
+// overlaps the MMAs of tap t.  Grids wider than the slab allows are walked in column phases (the
 // slab reloaded per phase).  After the last MMA the eight warps read the
 // accumulators with tcgen05.ld (warp w reads TMEM lanes 32(w%4)..+31; the two
 // warps of a lane quarter take alternate tiles and column chunks) and write
@@ -206,8 +208,12 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   while (ncols < (uint32_t)(ntile * J.n)) ncols <<= 1;
   for (int k = threadIdx.x; k < J.n; k += kTcThreads) col_s[k] = cols[J.col_tab + k];
 
+  // MMA issuers: warps 1 .. nis, one per tile (tiles i = w-1, w-1+nis, ...); each commits to the
+  // "free" and "done" barriers, so those complete once every issuer's MMAs are done
+  const int nis = min(ntile, kTcThreads / 32 - 1);
   if (threadIdx.x == 0) {
-    for (int i = 0; i < 3 + 2 * kTcMaxStages; i++) mbar_init(&bar[i], 1);
+    for (int i = 0; i < 3 + 2 * kTcMaxStages; i++)
+      mbar_init(&bar[i], (i == kBarSlabFree || i == kBarDone || i >= kBarStageFree) ? (uint32_t)nis : 1u);
     mbar_fence_init();
   }
   if (warp == 0) tmem_alloc(tslot, ncols);
@@ -259,8 +265,8 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         mbar_wait(&bar[kBarStageFull + s], (uint32_t)((last / NS) & 1), 4 * kWaitNs);
       }
     }
-  } else if (warp == 1 && lane == 0) {
-    // ---- MMA issue: per tap, every tile's chain (and the split chain of the root blocks)
+  } else if (warp >= 1 && warp <= nis && lane == 0) {
+    // ---- MMA issue: per tap, this warp's tiles' chains (and the split chain of the root blocks)
     // The start-address field of a descriptor is (address >> 4) in its low 14 bits and
     // every operand lies below 2^18 bytes, so moving an operand by a 16-byte multiple off
     // is adding off >> 4 to the descriptor: A moves by cells (16 B), B by rows (16 B).
@@ -285,7 +291,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
           const uint64_t b_base = stage_desc + (uint32_t)(u * NQ * J.n);   // tap u of the stage: NQ*n rows of 16 B on
           const uint32_t acc = t > 0 ? 1u : 0u;
           const uint32_t shift = (uint32_t)((xp - xp0) * J.fs0 + yp);
-          for (int i = 0; i < ntile; i++) {
+          for (int i = warp - 1; i < ntile; i += nis) {
             const uint32_t d = tmem + (uint32_t)(i * J.n);
             const uint64_t ad = a_base + ((uint32_t)(i * kTcM) + shift);
             tc_mma<NQ>(d, ad, b_base, idesc, acc);
@@ -354,6 +360,224 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   tc_fence_before();
   __syncthreads();
   if (warp == 0) tmem_dealloc(tmem, ncols);
+}
+
+// ---------------------------------------------------------------------------
+// persistent form: one CTA per SM walks a contiguous range of units (a unit: up
+// to two tiles of one job).  The bank of the units' jobs stays resident in
+// shared memory while consecutive units use it (reloaded where the range moves
+// to another bank), the slab of unit k+1 lands while the MMAs of unit k run
+// (two slab buffers; a slab too large for one buffer takes both, and its unit
+// waits for the one before), and two TMEM accumulator sets let the epilogue of
+// unit k overlap the MMAs of unit k+1.  Warp 0 copies, warps 1 and 2 issue the
+// MMAs (one per tile of a unit: a single thread cannot issue MMAs of N = 48
+// as fast as the tensor pipe retires them), warps 3..10 drain the accumulators
+// (two per TMEM lane quarter).  Every MMA of a tile runs in the same order as
+// in k_conv_tc, so the two forms give the same sums.
+// ---------------------------------------------------------------------------
+constexpr int kTcpIssuers = 2;                   // warps 1, 2: one per tile of a unit
+constexpr int kTcpWarps = 3 + 8;
+constexpr int kTcpThreads = 32 * kTcpWarps;
+constexpr int kTcpEpiWarps = 8;
+constexpr int kTcpHead = 256;
+constexpr int kTcpTiles = 2;                     // tiles per unit, at most
+constexpr uint32_t kTcpCopy = 32768;             // bytes per bulk copy of a bank
+// barriers: slab landed [2], unit's MMAs done [2], accumulators full [2] and
+// free [2] (one arrival per epilogue warp), bank landed, every MMA done
+constexpr int kPbSlabFull = 0, kPbMmaDone = 2, kPbAccFull = 4, kPbAccFree = 6, kPbBank = 8, kPbEnd = 9,
+              kPbCount = 10;
+
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+// units: (job, first tile, tiles, flags: bit 0 = the slab takes both buffers);
+// ctainfo[c]: CTA c's units (first, end), bank region and slab buffer bytes
+template <int NQ>
+__global__ void __launch_bounds__(kTcpThreads, 1)
+    k_conv_tcp(const TcJob *__restrict__ jobs, const int4 *__restrict__ units, const int4 *__restrict__ ctainfo,
+               const TcCol *__restrict__ cols, const uint8_t *__restrict__ arena16, const uint8_t *__restrict__ bank,
+               uint32_t colbuf, float *__restrict__ arena, int *err) {
+  extern __shared__ __align__(128) uint8_t sm[];
+  uint64_t *bar = reinterpret_cast<uint64_t *>(sm);
+  uint32_t *tslot = reinterpret_cast<uint32_t *>(sm + 8 * kPbCount);
+  // this CTA's units, and its shared memory: the bank region, then two slab buffers
+  const int4 R = ctainfo[blockIdx.x];
+  const int u0 = R.x, nu = R.y - R.x;
+  const uint32_t slab_half = (uint32_t)R.w;
+  uint8_t *bank_s = sm + kTcpHead;
+  uint8_t *slab_s = bank_s + (uint32_t)R.z;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < kPbCount; i++)
+      mbar_init(&bar[i], (i == kPbAccFree || i == kPbAccFree + 1)                      ? kTcpEpiWarps
+                         : (i == kPbSlabFull || i == kPbSlabFull + 1 || i == kPbBank) ? 1
+                                                                                       : kTcpIssuers);
+    mbar_fence_init();
+  }
+  if (warp == 0) tmem_alloc(tslot, 2 * colbuf);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tslot;
+  bool ok = true;
+
+  if (warp == 0 && lane == 0) {
+    // ---- copies: a bank where the range reaches a new one, then each unit's slab
+    int cur = -1, banks = 0, slabs = 0;
+    auto unit_done = [&](int j) { return mbar_wait(&bar[kPbMmaDone + (j & 1)], (uint32_t)((j >> 1) & 1), kWaitNs); };
+    for (int k = 0; k < nu && ok; k++) {
+      const int4 U = units[u0 + k];
+      const TcJob J = jobs[U.x];   // a copy: the MMA asm clobbers memory, a reference would reload every field
+      const bool big = U.w & 1, prev_big = k > 0 && (units[u0 + k - 1].w & 1);
+      const bool new_bank = J.bank_off != cur;
+      // the buffer's last user (unit k-2), and unit k-1 where its slab or bank is overwritten
+      if (k >= 2 && !unit_done(k - 2)) { ok = false; break; }
+      if (k >= 1 && (big || prev_big || new_bank) && !unit_done(k - 1)) { ok = false; break; }
+      if (new_bank) {
+        const uint32_t bytes = (uint32_t)J.b0 * J.b1 * NQ * J.n * 16u;
+        mbar_expect_tx(&bar[kPbBank], bytes);
+        for (uint32_t o = 0; o < bytes; o += kTcpCopy)
+          bulk_g2s(bank_s + o, bank + (size_t)J.bank_off + o, min(kTcpCopy, bytes - o), &bar[kPbBank]);
+        cur = J.bank_off;
+        banks++;
+      }
+      const int S = U.z * kTcM + (J.b1 - 1) * J.fs0 + (J.b0 - 1);
+      const uint32_t plane_bytes = (uint32_t)S * 16u;
+      const bool split = J.n_lo > 0;
+      uint8_t *slab = slab_s + (big ? 0u : (uint32_t)(k & 1) * slab_half);
+      const size_t cell0 = (size_t)U.y * kTcM;
+      mbar_expect_tx(&bar[kPbSlabFull + (k & 1)], (uint32_t)NQ * plane_bytes * (split ? 2u : 1u));
+      for (int q = 0; q < NQ; q++)
+        bulk_g2s(slab + (size_t)q * plane_bytes,
+                 arena16 + 2 * (size_t)J.plane_off + ((size_t)q * J.plane_cells + cell0) * 16, plane_bytes,
+                 &bar[kPbSlabFull + (k & 1)]);
+      if (split)
+        for (int q = 0; q < NQ; q++)
+          bulk_g2s(slab + (size_t)(NQ + q) * plane_bytes,
+                   arena16 + 2 * (size_t)J.lo_off + ((size_t)q * J.plane_cells + cell0) * 16, plane_bytes,
+                   &bar[kPbSlabFull + (k & 1)]);
+      slabs = k + 1;
+    }
+    if (!ok) {
+      atomicOr(err, 1);
+      // every copy issued lands before the CTA leaves
+      if (banks) mbar_wait(&bar[kPbBank], (uint32_t)((banks - 1) & 1), 4 * kWaitNs);
+      for (int j = max(0, slabs - 2); j < slabs; j++)
+        mbar_wait(&bar[kPbSlabFull + (j & 1)], (uint32_t)((j >> 1) & 1), 4 * kWaitNs);
+    }
+  } else if (warp >= 1 && warp <= kTcpIssuers && lane == 0) {
+    // ---- MMAs: every tap of this warp's tiles of the unit into accumulator set k & 1
+    int cur = -1, banks = 0;
+    for (int k = 0; k < nu && ok; k++) {
+      const int4 U = units[u0 + k];
+      const TcJob J = jobs[U.x];   // a copy: the MMA asm clobbers memory, a reference would reload every field
+      const bool big = U.w & 1, split = J.n_lo > 0;
+      if (J.bank_off != cur) {
+        if (!mbar_wait(&bar[kPbBank], (uint32_t)(banks & 1), kWaitNs)) { ok = false; break; }
+        cur = J.bank_off;
+        banks++;
+      }
+      if (!mbar_wait(&bar[kPbSlabFull + (k & 1)], (uint32_t)((k >> 1) & 1), kWaitNs)) { ok = false; break; }
+      if (k >= 2 && !mbar_wait(&bar[kPbAccFree + (k & 1)], (uint32_t)(((k - 2) >> 1) & 1), kWaitNs)) {
+        ok = false;
+        break;
+      }
+      tc_fence_after();
+      const int S = U.z * kTcM + (J.b1 - 1) * J.fs0 + (J.b0 - 1);
+      const uint32_t plane_bytes = (uint32_t)S * 16u;
+      const uint8_t *slab = slab_s + (big ? 0u : (uint32_t)(k & 1) * slab_half);
+      const uint32_t idesc = NQ == 4 ? idesc_bf16(kTcM, J.n) : idesc_e4m3(kTcM, J.n);
+      const uint32_t idesc_lo = idesc_bf16(kTcM, split ? J.n_lo : 16);
+      const uint64_t a_base = sdesc(smem_u32(slab), plane_bytes, 128u);
+      const uint64_t alo_base = sdesc(smem_u32(slab + (size_t)NQ * plane_bytes), plane_bytes, 128u);
+      const uint64_t b_desc = sdesc(smem_u32(bank_s), (uint32_t)J.n * 16u, 128u);
+      const uint32_t a_k1 = 2u * (uint32_t)S, b_k1 = 2u * (uint32_t)J.n;
+      const uint32_t dbase = tmem + (uint32_t)(k & 1) * colbuf;
+      const int taps = J.b0 * J.b1;
+      for (int t = 0, xp = 0, yp = 0; t < taps; t++) {
+        const uint64_t b_base = b_desc + (uint32_t)(t * NQ * J.n);
+        const uint32_t acc = t > 0 ? 1u : 0u;
+        const uint32_t shift = (uint32_t)(xp * J.fs0 + yp);
+        for (int i = warp - 1; i < U.z; i += kTcpIssuers) {
+          const uint32_t d = dbase + (uint32_t)(i * J.n);
+          const uint64_t ad = a_base + ((uint32_t)(i * kTcM) + shift);
+          tc_mma<NQ>(d, ad, b_base, idesc, acc);
+          if constexpr (NQ == 4) {
+            tc_mma<NQ>(d, ad + a_k1, b_base + b_k1, idesc, 1u);
+            if (split) {
+              const uint64_t al = alo_base + ((uint32_t)(i * kTcM) + shift);
+              const uint64_t bl = b_base + (uint32_t)J.lo_row;
+              tc_mma<NQ>(d + (uint32_t)J.lo_row, al, bl, idesc_lo, 1u);
+              tc_mma<NQ>(d + (uint32_t)J.lo_row, al + a_k1, bl + b_k1, idesc_lo, 1u);
+            }
+          }
+        }
+        if (++yp == J.b0) { yp = 0; xp++; }
+      }
+      tc_commit(&bar[kPbMmaDone + (k & 1)]);   // the slab (and bank) are free once these MMAs are done
+      tc_commit(&bar[kPbAccFull + (k & 1)]);   // and the accumulators full
+    }
+    if (!ok) atomicOr(err, 2);
+    if (nu > 0) tc_commit(&bar[kPbEnd]);   // tracks every MMA issued above
+  } else if (warp > kTcpIssuers) {
+    // ---- epilogue: warp w reads the rows 32*(w & 3) .. +31 of the unit's tiles; the
+    // two warps of a lane quarter take alternate (tile, 16-column chunk) items
+    const int quarter = warp & 3, half = (warp - kTcpIssuers - 1) >> 2;
+    for (int k = 0; k < nu && ok; k++) {
+      const int4 U = units[u0 + k];
+      const TcJob J = jobs[U.x];   // a copy: the MMA asm clobbers memory, a reference would reload every field
+      if (!mbar_wait(&bar[kPbAccFull + (k & 1)], (uint32_t)((k >> 1) & 1), kWaitNs)) { ok = false; break; }
+      tc_fence_after();
+      const int ncell = J.fs0 * J.fs1, nch = J.n >> 4, fs0 = J.fs0;
+      const TcCol *col = cols + J.col_tab;
+      const uint32_t abase = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(k & 1) * colbuf;
+      for (int item = half; item < U.z * nch; item += 2) {
+        const int i = item / nch, c0 = (item - i * nch) * 16;
+        const TcCol head = col[c0];                 // a 16-column chunk lies inside one section
+        if (head.kind == 0) continue;               // (uniform across the warp: the loads below are collective)
+        const int p = U.y * kTcM + i * kTcM + quarter * 32 + lane;
+        const int x = p / fs0, y = p - x * fs0;
+        const uint32_t row_addr = abase + (uint32_t)(i * J.n);
+        uint32_t r[16], r2[16];
+        __syncwarp();
+        tc_ld16(row_addr + (uint32_t)c0, r);
+        if (head.kind == 2 && head.pair) tc_ld16(row_addr + (uint32_t)(c0 + head.pair), r2);
+        tc_wait_ld();
+        if (p < ncell) {
+#pragma unroll
+          for (int kk = 0; kk < 16; kk++) {
+            const TcCol c = col[c0 + kk];
+            float v;
+            memcpy(&v, &r[kk], 4);
+            if (c.kind == 1) {
+              if (x < c.cols && y < c.rows) arena[(size_t)c.off + (size_t)x * c.rows + y] = v * c.inv;
+            } else if (c.kind == 2) {
+              if (c.pair) {
+                float w;
+                memcpy(&w, &r2[kk], 4);
+                v += w;
+              }
+              arena[(size_t)c.off + p] = v * c.inv;
+            }
+          }
+        }
+      }
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&bar[kPbAccFree + (k & 1)]);
+    }
+    if (!ok) atomicOr(err, 8);
+  }
+  __syncthreads();
+  // every MMA issued is done before TMEM is freed
+  if (nu > 0 && !mbar_wait(&bar[kPbEnd], 0u, kWaitNs)) {
+    atomicOr(err, 4);
+    mbar_wait(&bar[kPbEnd], 0u, 4 * kWaitNs);
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) tmem_dealloc(tmem, 2 * colbuf);
 }
 
 // Root maps from their blocks: root[x][y] = sum_k block_k[x*fs0 + y + shift_k],
@@ -601,6 +825,133 @@ static void launch_conv_tc(int NQ, const TcJob *jobs, const int4 *chunks, int n_
 }
 
 // ---------------------------------------------------------------------------
+// host: units and CTA ranges of the persistent form
+// ---------------------------------------------------------------------------
+struct TcpLayout {
+  std::vector<int4> units;   // (job, first tile, tiles, flags: 1 = the slab takes both buffers)
+  std::vector<int4> ctas;    // per CTA: first unit, end unit, bank region bytes, slab buffer bytes
+  uint32_t colbuf = 0;
+  size_t smem = 0;
+};
+constexpr size_t kTcpSmemMax = 227 * 1024;
+
+static size_t tcp_slab_bytes(const TcJob &J, int NQ, int T) {
+  const size_t S = (size_t)T * kTcM + (size_t)(J.b1 - 1) * J.fs0 + (J.b0 - 1);
+  return ((size_t)NQ * S * 16 * (J.n_lo > 0 ? 2 : 1) + 127) & ~(size_t)127;
+}
+
+// Units bank by bank; each bank's units get a share of the CTAs in proportion to
+// their cost (no CTA holds two banks), and each CTA's shared memory is carved for
+// its bank.  False when a job's bank and its slab do not fit one CTA, or a slab
+// would read past the planes' buffer (cells_total cells of 16 B).
+static bool tcp_layout(const std::vector<TcJob> &jobs, int NQ, int ctas, long long cells_total, TcpLayout &L) {
+  L = TcpLayout{};
+  if (jobs.empty() || ctas <= 0) return false;
+  std::vector<int> banks;   // distinct bank offsets, ascending
+  for (const TcJob &J : jobs) banks.push_back(J.bank_off);
+  std::sort(banks.begin(), banks.end());
+  banks.erase(std::unique(banks.begin(), banks.end()), banks.end());
+  struct Group {
+    int u0 = 0, u1 = 0;
+    size_t bank = 0, half = 0;
+    long long cost = 0;
+    int ctas = 0;
+  };
+  std::vector<Group> G(banks.size());
+  std::vector<long long> cost;
+  int cmax = 0;
+  for (size_t g = 0; g < banks.size(); g++) {
+    Group &gr = G[g];
+    std::vector<int> js;
+    for (size_t j = 0; j < jobs.size(); j++)
+      if (jobs[j].bank_off == banks[g]) js.push_back((int)j);
+    const TcJob &J0 = jobs[js[0]];
+    gr.bank = ((size_t)J0.b0 * J0.b1 * NQ * J0.n * 16 + 127) & ~(size_t)127;
+    if (kTcpHead + gr.bank >= kTcpSmemMax) return false;
+    const size_t half_cap = ((kTcpSmemMax - kTcpHead - gr.bank) / 2) & ~(size_t)127;
+    size_t whole = 0;
+    gr.u0 = (int)L.units.size();
+    for (int j : js) {
+      const TcJob &J = jobs[j];
+      int t = std::max(1, std::min(kTcpTiles, 128 / std::max(1, J.n)));   // a unit's accumulators: t*n <= 128 columns
+      while (t > 1 && tcp_slab_bytes(J, NQ, t) > half_cap) t--;
+      int big = 0;
+      if (tcp_slab_bytes(J, NQ, t) <= half_cap) {
+        gr.half = std::max(gr.half, tcp_slab_bytes(J, NQ, t));
+      } else if (tcp_slab_bytes(J, NQ, 1) <= 2 * half_cap) {
+        big = 1;
+        whole = std::max(whole, tcp_slab_bytes(J, NQ, 1));
+      } else {
+        return false;
+      }
+      cmax = std::max(cmax, t * J.n);
+      const long long reach = (long long)(J.b1 - 1) * J.fs0 + (J.b0 - 1);
+      const int taps = J.b0 * J.b1;
+      for (int t0 = 0; t0 < J.ntiles; t0 += t) {
+        const int nt = std::min(t, J.ntiles - t0);
+        const long long last = (long long)(NQ - 1) * J.plane_cells + (long long)(t0 + nt) * kTcM + reach;
+        if ((long long)J.plane_off * 2 / 16 + last > cells_total) return false;
+        if (J.lo_off >= 0 && (long long)J.lo_off * 2 / 16 + last > cells_total) return false;
+        L.units.push_back(make_int4(j, t0, nt, big));
+        // MMA columns of the unit, and a fixed share for its slab and epilogue
+        const long long c = (long long)nt * taps * (J.n + 2 * J.n_lo) + (long long)taps * 64;
+        cost.push_back(c);
+        gr.cost += c;
+      }
+    }
+    gr.u1 = (int)L.units.size();
+    gr.half = std::max(gr.half, (((whole + 1) / 2) + 127) & ~(size_t)127);
+    if (kTcpHead + gr.bank + 2 * gr.half > kTcpSmemMax) return false;
+    L.smem = std::max(L.smem, kTcpHead + gr.bank + 2 * gr.half);
+  }
+  uint32_t colbuf = 32;
+  while ((int)colbuf < cmax) colbuf <<= 1;
+  if (2 * colbuf > (uint32_t)kTcTmemCols) return false;
+  L.colbuf = colbuf;
+  // CTAs per bank in proportion to cost, at least one, at most its units
+  long long total = 0;
+  int free_ctas = ctas;
+  for (Group &gr : G) total += gr.cost, free_ctas -= 1, gr.ctas = 1;
+  if (free_ctas < 0) return false;
+  for (Group &gr : G) {
+    const int extra = (int)((double)free_ctas * (double)gr.cost / (double)std::max(1LL, total));
+    gr.ctas = std::min(gr.u1 - gr.u0, 1 + extra);
+  }
+  // units of a bank in ranges of about equal cost, none empty
+  for (const Group &gr : G) {
+    const int nu = gr.u1 - gr.u0, C = std::max(1, std::min(gr.ctas, nu));
+    std::vector<long long> prefix(nu + 1, 0);
+    for (int u = 0; u < nu; u++) prefix[u + 1] = prefix[u] + cost[gr.u0 + u];
+    int prev = 0;
+    for (int c = 1, u = 0; c <= C; c++) {
+      int end = nu;
+      if (c < C) {
+        while (u < nu && prefix[u] * C < prefix[nu] * c) u++;
+        end = std::min(std::max(u, prev + 1), nu - (C - c));
+      }
+      L.ctas.push_back(make_int4(gr.u0 + prev, gr.u0 + end, (int)gr.bank, (int)gr.half));
+      prev = end;
+    }
+  }
+  return !L.ctas.empty();
+}
+
+static void launch_conv_tcp(int NQ, const TcJob *jobs, const int4 *units, const int4 *ctainfo, int ctas,
+                            const TcCol *cols, const uint8_t *planes, const uint8_t *bank, uint32_t colbuf,
+                            float *out, int *err, size_t smem, cudaStream_t s) {
+  if (ctas <= 0) return;
+  if (NQ == 4) {
+    static SmemAttr a4;
+    raise_smem(a4, k_conv_tcp<4>, smem);
+    k_conv_tcp<4><<<ctas, kTcpThreads, smem, s>>>(jobs, units, ctainfo, cols, planes, bank, colbuf, out, err);
+  } else {
+    static SmemAttr a2;
+    raise_smem(a2, k_conv_tcp<2>, smem);
+    k_conv_tcp<2><<<ctas, kTcpThreads, smem, s>>>(jobs, units, ctainfo, cols, planes, bank, colbuf, out, err);
+  }
+}
+
+// ---------------------------------------------------------------------------
 // host: the plan's bank, jobs, column tables and root sums
 // ---------------------------------------------------------------------------
 // Before the arena is allocated: the rows (every model's part filters, then its
@@ -811,7 +1162,7 @@ geye_status build_tc_plan(geye_ctx *ctx, Plan &P) {
                     std::to_string((int)ctx->conv_mode);
   for (auto &mp : P.models) key += ":" + std::to_string(mp->model->id);
   geye_model *m0 = P.models[0]->model;
-  int first = 0, last = kTcNumShapes;
+  int first = 0, last = kTcNumShapes + 1;   // the tile shapes, then the persistent form
   float best_ms = 0.f;
   {
     std::lock_guard<std::mutex> lk(m0->tc_mu);
@@ -821,7 +1172,7 @@ geye_status build_tc_plan(geye_ctx *ctx, Plan &P) {
   // GEYE_TC_SHAPE=<i> pins candidate i (reproducible shapes; no timing)
   if (const char *e = getenv("GEYE_TC_SHAPE")) {
     const int i = atoi(e);
-    if (i >= 0 && i < kTcNumShapes) { first = i; last = i + 1; }
+    if (i >= 0 && i <= kTcNumShapes) { first = i; last = i + 1; }
   }
   const bool timed = last - first > 1;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
@@ -832,7 +1183,47 @@ geye_status build_tc_plan(geye_ctx *ctx, Plan &P) {
   std::vector<int4> best;
   size_t best_smem = 0;
   int best_shape = -1;
+  int sms = 0;
+  CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device));
   for (int si = first; si < last; si++) {
+    if (si == kTcNumShapes) {
+      TcpLayout L;
+      if (!tcp_layout(T.jobs, NQ, sms, cells_total, L)) continue;
+      DevBuf d_units, d_ranges;
+      GEYE_TRY(upload_bytes(ctx, d_units, L.units.data(), sizeof(int4) * L.units.size()));
+      GEYE_TRY(upload_bytes(ctx, d_ranges, L.ctas.data(), sizeof(int4) * L.ctas.size()));
+      const int ctas = (int)L.ctas.size();
+      auto launch = [&]() {
+        launch_conv_tcp(NQ, T.d_jobs.as<TcJob>(), d_units.as<int4>(), d_ranges.as<int4>(), ctas, T.d_cols.as<TcCol>(),
+                        P.arena16.as<uint8_t>(), T.d_bank.as<uint8_t>(), L.colbuf, P.arena.as<float>(), err, L.smem,
+                        ctx->stream);
+      };
+      float ms = 0.f;
+      if (timed) {
+        launch();
+        CUDA_TRY(cudaEventRecord(e0, ctx->stream));
+        for (int r = 0; r < 3; r++) launch();
+        CUDA_TRY(cudaEventRecord(e1, ctx->stream));
+        CUDA_TRY(cudaEventSynchronize(e1));
+        CUDA_TRY(cudaGetLastError());
+        CUDA_TRY(cudaEventElapsedTime(&ms, e0, e1));
+      }
+      if (!timed || best_shape < 0 || ms < best_ms) {
+        best.clear();
+        best_smem = L.smem;
+        best_shape = si;
+        best_ms = ms;
+        // the plan takes the candidate's buffers (its previous ones are freed with the candidate's)
+        std::swap(T.d_units.p, d_units.p);
+        std::swap(T.d_units.bytes, d_units.bytes);
+        std::swap(T.d_ranges.p, d_ranges.p);
+        std::swap(T.d_ranges.bytes, d_ranges.bytes);
+        T.tcp_ctas = ctas;
+        T.tcp_colbuf = L.colbuf;
+      }
+      if (!timed) break;
+      continue;
+    }
     std::vector<int4> chunks;
     size_t smem = 0;
     if (!chunk_jobs(T.jobs, NQ, kTcShapes[si], cells_total, chunks, smem)) continue;
@@ -877,11 +1268,16 @@ geye_status build_tc_plan(geye_ctx *ctx, Plan &P) {
   }
   T.smem = best_smem;
   T.n_chunks = (int)best.size();
-  T.stages = kTcShapes[best_shape].stages;
-  T.tps = tps_arg(kTcShapes[best_shape]);
   T.shape = best_shape;
+  if (best_shape < kTcNumShapes) {
+    T.stages = kTcShapes[best_shape].stages;
+    T.tps = tps_arg(kTcShapes[best_shape]);
+    T.d_units.release();
+    T.d_ranges.release();
+    T.tcp_ctas = 0;
+  }
   T.tuned_ms = best_ms / 3.0f;
-  GEYE_TRY(upload_bytes(ctx, T.d_chunks, best.data(), sizeof(int4) * std::max<size_t>(best.size(), 1)));
+  if (!best.empty()) GEYE_TRY(upload_bytes(ctx, T.d_chunks, best.data(), sizeof(int4) * best.size()));
   return GEYE_OK;
 }
 
@@ -891,10 +1287,16 @@ geye_status run_conv_tc(geye_ctx *ctx, Plan &P) {
     set_error("tensor-core conv: the plan has no feature planes");
     return GEYE_ERR_UNSUPPORTED;
   }
-  if (T.n_chunks == 0) return GEYE_OK;
-  launch_conv_tc(T.planes, T.d_jobs.as<TcJob>(), T.d_chunks.as<int4>(), T.n_chunks, T.d_cols.as<TcCol>(),
-                 P.arena16.as<uint8_t>(), T.d_bank.as<uint8_t>(), T.stages, T.tps, P.arena.as<float>(),
-                 P.d_small.as<int>() + 130, T.smem, ctx->stream);
+  if (T.shape == kTcNumShapes) {
+    launch_conv_tcp(T.planes, T.d_jobs.as<TcJob>(), T.d_units.as<int4>(), T.d_ranges.as<int4>(), T.tcp_ctas,
+                    T.d_cols.as<TcCol>(), P.arena16.as<uint8_t>(), T.d_bank.as<uint8_t>(), T.tcp_colbuf,
+                    P.arena.as<float>(), P.d_small.as<int>() + 130, T.smem, ctx->stream);
+  } else {
+    if (T.n_chunks == 0) return GEYE_OK;
+    launch_conv_tc(T.planes, T.d_jobs.as<TcJob>(), T.d_chunks.as<int4>(), T.n_chunks, T.d_cols.as<TcCol>(),
+                   P.arena16.as<uint8_t>(), T.d_bank.as<uint8_t>(), T.stages, T.tps, P.arena.as<float>(),
+                   P.d_small.as<int>() + 130, T.smem, ctx->stream);
+  }
   ctx->launches++;
   cudaError_t e = cudaGetLastError();
   if (e == cudaSuccess && !T.sums.empty()) {
@@ -1013,9 +1415,10 @@ geye_status geye_conv_tuning(geye_ctx *ctx, const geye_model *m, int shape[3], f
   for (auto &mp : P.models) in_plan |= mp->model == m;
   ARG_CHECK(in_plan, "the last run has no such model");
   ARG_CHECK(P.tc.shape >= 0, "the last run's plan has no tensor-core convolution");
-  shape[0] = geye::kTcShapes[P.tc.shape].t_cap;
-  shape[1] = (int)(geye::kTcShapes[P.tc.shape].budget / 1024);
-  shape[2] = P.tc.n_chunks;
+  const bool persistent = P.tc.shape == geye::kTcNumShapes;
+  shape[0] = persistent ? 0 : geye::kTcShapes[P.tc.shape].t_cap;
+  shape[1] = (int)((persistent ? P.tc.smem : geye::kTcShapes[P.tc.shape].budget) / 1024);
+  shape[2] = persistent ? P.tc.tcp_ctas : P.tc.n_chunks;
   *ms = P.tc.tuned_ms;
   return GEYE_OK;
 }

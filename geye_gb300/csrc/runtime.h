@@ -155,6 +155,11 @@ struct TcPlan {
   size_t smem = 0;
   int shape = -1;                       // tile-shape candidate the autotuner chose
   float tuned_ms = 0.f;                 // its measured time per launch
+  // the persistent form (shape == the candidate after the tile shapes): units, and per CTA
+  // its units, bank region and slab buffer bytes
+  DevBuf d_units, d_ranges;
+  int tcp_ctas = 0;
+  uint32_t tcp_colbuf = 0;
 };
 
 struct Plan {

@@ -404,7 +404,8 @@ class Context:
         return out
 
     def conv_tuning(self, model: "Model") -> dict:
-        """Tile shape the tensor-core convolution's autotuner chose for the model in the last run's plan."""
+        """Tile shape the tensor-core convolution's autotuner chose for the model in the last run's plan
+        (tiles_per_cta 0: the persistent form, one CTA per SM with the filter bank resident)."""
         shape = np.zeros(3, np.int32)
         ms = np.zeros(1, np.float32)
         _check(lib().geye_conv_tuning(self.h, model.h, _p(shape), _p(ms)), "conv_tuning")

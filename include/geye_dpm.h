@@ -304,7 +304,8 @@ geye_status geye_score_map(geye_ctx *ctx, const geye_model *m, int level, int co
                            int dims[2]);
 
 /* Tile shape the tensor-core convolution's autotuner chose for model m in the
- * last run's plan: shape = {largest tile run per CTA (128 positions a tile),
+ * last run's plan: shape = {largest tile run per CTA (128 positions a tile; 0:
+ * the persistent form, one CTA per SM with its filter bank resident),
  * shared-memory budget per CTA in KB, CTAs per launch}; ms = its measured time
  * per launch.  GEYE_ERR_ARG in FP32 mode or before a run. */
 geye_status geye_conv_tuning(geye_ctx *ctx, const geye_model *m, int shape[3], float *ms);

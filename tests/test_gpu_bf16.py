@@ -119,8 +119,36 @@ def test_conv_tile_shape_autotuner(tmp_path):
             m.close()
     assert tuned[0] == tuned[1]   # one launch convolves both models
     for t in tuned:
-        assert t["tiles_per_cta"] in (1, 2, 4, 8)
-        assert 64 <= t["smem_kb"] <= 220 and t["ctas"] > 0 and t["ms"] > 0
+        assert t["tiles_per_cta"] in (0, 1, 2, 4, 8)   # 0: the persistent form (one CTA per SM)
+        assert 64 <= t["smem_kb"] <= 227 and t["ctas"] > 0 and t["ms"] > 0
+
+
+@pytest.mark.parametrize("mode", ["bf16", "fp8"])
+@pytest.mark.parametrize("w,h", [(320, 240), (640, 480), (1280, 720)])
+def test_conv_persistent_form_matches_stage_ring(tmp_path, monkeypatch, mode, w, h):
+    """The persistent form (bank resident, one CTA per SM) runs every tile's MMAs in
+    the stage-ring form's order: same detections and scores, bit for bit."""
+    import geye_gb300 as g
+    from geye_gb300 import synth
+    conv = {"bf16": g.CONV_BF16, "fp8": g.CONV_FP8}[mode]
+    paths = [synth.write_model_csv(s, str(tmp_path)) for s in (synth.CAR_SPEC, synth.PERSON_SPEC)]
+    frame = synth.make_frame(w, h, seed=7)
+    out = {}
+    for shape in ("0", "10"):
+        monkeypatch.setenv("GEYE_TC_SHAPE", shape)
+        with g.Context(0, conv=conv) as c:
+            ms = [g.Model(c, *p) for p in paths]
+            out[shape] = (c.detect_multi(frame, ms, -0.5, 0.5), c.conv_tuning(ms[0]))
+            for m in ms:
+                m.close()
+    (ring, t_ring), (pers, t_pers) = out["0"], out["10"]
+    assert t_ring["tiles_per_cta"] == 4 and t_pers["tiles_per_cta"] == 0
+    for a, b in zip(ring, pers):
+        assert a["num"] == b["num"]
+        for k in ("point", "or_point", "type"):
+            assert np.array_equal(a[k], b[k])
+        for k in ("score", "scale"):
+            assert np.array_equal(np.asarray(a[k], np.float32).view(np.int32), np.asarray(b[k], np.float32).view(np.int32))
 
 
 @pytest.mark.parametrize("n", [40, 64])
