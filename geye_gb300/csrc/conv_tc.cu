@@ -30,7 +30,7 @@
 // significant bits per operand for the roots, whose rounding decides most
 // detections; part filters stay plain BF16.
 //
-// A CTA (8 warps) owns a run of up to 8 tiles of 128 positions of one job, each
+// A CTA (12 warps) owns a run of up to 8 tiles of 128 positions of one job, each
 // tile with its own TMEM accumulator.  The run's feature slab stays in shared
 // memory while the bank streams through a ring of stages, one tap per stage:
 // lane 0 of warp 0 bulk-copies (cp.async.bulk, mbarrier completion), lane 0
@@ -39,9 +39,9 @@
 // retires them) and commits them to the stage's "free" mbarrier, which
 // completes when every issuer's MMAs are done, so the copy of tap t+stages
 // overlaps the MMAs of tap t.  Grids wider than the slab allows are walked in column phases (the
-// slab reloaded per phase).  After the last MMA the eight warps read the
-// accumulators with tcgen05.ld (warp w reads TMEM lanes 32(w%4)..+31; the two
-// warps of a lane quarter take alternate tiles and column chunks) and write
+// slab reloaded per phase).  After the last MMA the twelve warps read the
+// accumulators with tcgen05.ld (warp w reads TMEM lanes 32(w%4)..+31; the three
+// warps of a lane quarter take turns at the tiles and column chunks) and write
 // part maps in the reference layout and root blocks by position.  Every
 // mbarrier wait is bounded; a timeout sets an error bit, and the CTA waits
 // (bounded) for its own copies and MMAs before it frees TMEM and leaves.
@@ -60,7 +60,7 @@
 
 namespace geye {
 
-constexpr int kTcThreads = 256;                 // 8 warps: two per TMEM lane quarter in the epilogue
+constexpr int kTcThreads = 384;                 // 12 warps: three per TMEM lane quarter in the epilogue
 constexpr int kTcM = 128;                        // positions per tile (TMEM lanes)
 constexpr int kTcMaxTiles = 8;                   // tiles per CTA, at most
 constexpr int kTcMaxStages = 8;                  // bank stages in the ring, at most
@@ -323,7 +323,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   ok = __syncthreads_and(done && ok);
   tc_fence_after();
   // ---- epilogue: row r of a tile is TMEM lane r; warp w reads the rows 32*(w & 3) .. +31 of
-  // the tiles, and the two warps of a lane quarter take alternate (tile, 16-column chunk) items
+  // the tiles, and the three warps of a lane quarter take turns at the (tile, 16-column chunk) items
   const int ncell = J.fs0 * J.fs1;
   const int quarter = warp & 3, nch = J.n >> 4;
   for (int item = warp >> 2; item < ntile * nch; item += kTcThreads / 128) {
