@@ -295,12 +295,15 @@ void launch_nms(const float *boxes, const int *d_num, int n_models, int GL, floa
 constexpr int kNmsBatch = 256;     // boxes resolved per round
 constexpr int kNmsSegS = 16384;    // sort segments finished in shared memory (one block, ~203 KB)
 constexpr int kNmsTile = 4096;     // elements per block in the sort's grid-wide partitions
-constexpr int kRsT = 4096;         // elements per block in the key-order radix sort
 __host__ __device__ inline int nms_big_cap(int cap) { return cap / kNmsSegS + 2; }
 __host__ __device__ inline int nms_tile_cap(int cap) { return cap / kNmsTile + nms_big_cap(cap) + 1; }
 constexpr int kNmsCells = 64;      // cells per image axis of the greedy's pick masks
 constexpr int kNmsLevels = 7;      // their sparse-table levels (spans of 1..64 cells)
-__host__ __device__ inline int nms_rs_tiles(int cap) { return (cap + kRsT - 1) / kRsT; }
+// elements per block in the key-order radix sort: small tiles spread a frame's
+// few thousand boxes over more blocks; large ones keep the single-block digit
+// scan short when a model has a million boxes
+__host__ __device__ inline int nms_rs_tile(int cap) { return cap <= (1 << 18) ? 1024 : 4096; }
+__host__ __device__ inline int nms_rs_tiles(int cap) { return (cap + nms_rs_tile(cap) - 1) / nms_rs_tile(cap); }
 // summary bitmap: one bit per word of the alive bitmap
 __host__ __device__ inline int nms_summary_words(int cap) { return ((cap + 31) / 32 + 31) / 32 + 1; }
 __host__ __device__ inline size_t nms_model_words(int cap) {

@@ -20,7 +20,7 @@
 //                 +0, complemented for descending order), indices, the greedy
 //                 state; NaN raises the flag.
 //   four passes of eight bits, three kernels each:
-//     k_rs_count  a block per tile of kRsT keys: the digit histogram of its
+//     k_rs_count  a block per tile of nms_rs_tile(cap) keys: the digit histogram of its
 //                 tile, stored digit-major (H[digit][tile]);
 //     k_rs_scan   a block per model: exclusive scan of H in that order, which
 //                 is each (digit, tile)'s first output position;
@@ -87,8 +87,8 @@ __device__ __forceinline__ void rs_bufs(const Slots &S, int pass, const unsigned
 __global__ void __launch_bounds__(kRsNT) k_rs_count(int pass, int cap, int *si, float *sf) {
   __shared__ int h[256];
   Slots S = slots(si, sf, blockIdx.y, cap);
-  const int D = S.st->D;
-  const int nt = (D + kRsT - 1) / kRsT;
+  const int D = S.st->D, T = nms_rs_tile(cap);
+  const int nt = (D + T - 1) / T;
   const int t = blockIdx.x;
   if (t >= nt) return;
   const unsigned *sk;
@@ -99,7 +99,7 @@ __global__ void __launch_bounds__(kRsNT) k_rs_count(int pass, int cap, int *si, 
   const int shift = 8 * pass;
   for (int d = threadIdx.x; d < 256; d += kRsNT) h[d] = 0;
   __syncthreads();
-  const int e0 = t * kRsT, e1 = min(e0 + kRsT, D);
+  const int e0 = t * T, e1 = min(e0 + T, D);
   for (int e = e0 + threadIdx.x; e < e1; e += kRsNT) atomicAdd(&h[(sk[e] >> shift) & 255u], 1);
   __syncthreads();
   for (int d = threadIdx.x; d < 256; d += kRsNT) S.hist[(size_t)d * nt + t] = h[d];
@@ -116,7 +116,7 @@ __global__ void __launch_bounds__(kRsScanNT) k_rs_scan(int cap, int *si, float *
   Slots S = slots(si, sf, blockIdx.x, cap);
   const int D = S.st->D;
   if (D <= 0) return;
-  const int n = 256 * ((D + kRsT - 1) / kRsT);
+  const int n = 256 * ((D + nms_rs_tile(cap) - 1) / nms_rs_tile(cap));
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   int carry = 0;
   for (int base = 0; base < n; base += kRsScanItems * kRsScanNT) {
@@ -171,8 +171,8 @@ __global__ void __launch_bounds__(kRsNT) k_rs_scatter(int pass, int cap, int *si
   __shared__ int base[256];
   __shared__ int cnt[kRsWarps][256];
   Slots S = slots(si, sf, blockIdx.y, cap);
-  const int D = S.st->D;
-  const int nt = (D + kRsT - 1) / kRsT;
+  const int D = S.st->D, T = nms_rs_tile(cap);
+  const int nt = (D + T - 1) / T;
   const int t = blockIdx.x;
   if (t >= nt) return;
   const unsigned *sk;
@@ -184,7 +184,7 @@ __global__ void __launch_bounds__(kRsNT) k_rs_scatter(int pass, int cap, int *si
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   for (int d = threadIdx.x; d < 256; d += kRsNT) base[d] = S.hist[(size_t)d * nt + t];
   const unsigned lt = (1u << lane) - 1u;
-  for (int e0 = t * kRsT; e0 < min((t + 1) * kRsT, D); e0 += kRsNT) {
+  for (int e0 = t * T; e0 < min((t + 1) * T, D); e0 += kRsNT) {
     for (int k = threadIdx.x; k < kRsWarps * 256; k += kRsNT) (&cnt[0][0])[k] = 0;
     __syncthreads();   // counters clear, base up to date
     const int e = e0 + threadIdx.x;
